@@ -1,0 +1,204 @@
+/*
+ * panostitch.h -- C ABI of the GB300 panorama stitch path.
+ *
+ * The path: per camera frame, apply the exposure / white-balance LUTs, warp
+ * through precomputed dst->src maps with bilinear sampling into an
+ * equirectangular canvas, then blend all cameras with the integer multiband
+ * pipeline (Gaussian pyramids of the seam weights, Laplacian pyramids of the
+ * warped frames, weighted accumulation, normalisation, collapse) and write
+ * 8-bit BGR.
+ *
+ * Every entry point returns an int status (PS_OK or a PS_E* code) and never
+ * throws; ps_last_error() returns the thread-local message of the last
+ * failure.  All work is enqueued on the caller's CUDA stream (NULL = the
+ * legacy default stream); no entry point synchronises the stream unless it
+ * says so.  A ps_render is not thread-safe; distinct renders may be used
+ * from different threads.
+ *
+ * Each declaration names the reference interface it replaces
+ * (xpngzhng/PanoStitcher, path:line).
+ */
+#ifndef PANOSTITCH_H
+#define PANOSTITCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define PS_OK 0
+#define PS_EINVAL 1    /* bad argument / precondition (sizes, formats, counts) */
+#define PS_ENOMEM 2    /* device or host allocation failed, or budget exceeded */
+#define PS_ECUDA 3     /* a CUDA runtime call failed */
+#define PS_ETIMEOUT 4  /* a bounded wait ran out */
+#define PS_ESTATE 5    /* object not prepared / already running / closed */
+
+#define PS_MAX_LEVELS 16   /* getTrueNumLevels cap, source/Blend/MultiBandBlend.cpp:325 */
+#define PS_MAX_CAMS 64     /* cameras per rig */
+
+/* PhotoParam, source/Warp/ZReproject.h:17-50 (same fields, same order,
+   same meaning: image_type 0 rectilinear, 1 full-frame fisheye,
+   2 drum fisheye, 3 circular fisheye; angles in degrees). */
+typedef struct ps_photo_param {
+    int image_type, crop_mode, crop_x, crop_y, crop_width, crop_height;
+    int circle_x, circle_y, circle_r;
+    double hfov, vfov, alpha, beta, gamma, shift_x, shift_y, shear_x, shear_y;
+    double yaw, pitch, roll;
+} ps_photo_param;
+
+/* Pixel formats (B,G,R byte order like cv::Mat CV_8UC3 / CV_8UC4). */
+#define PS_FMT_BGR24 24
+#define PS_FMT_BGR32 32   /* 4th byte ignored on input, written as 0 */
+/* Where an image lives. */
+#define PS_MEM_HOST 0     /* host memory; pinned memory gives async copies */
+#define PS_MEM_DEVICE 1   /* device memory of the current device */
+
+/* An image view: the POD replacement of cv::Mat / cv::cuda::GpuMat. */
+typedef struct ps_image {
+    void* data;
+    long long pitch;     /* bytes between rows */
+    int width, height;
+    int format;          /* PS_FMT_* */
+    int location;        /* PS_MEM_* */
+} ps_image;
+
+/* Thread-local text of the last error ("" if none). */
+const char* ps_last_error(void);
+/* Library version string. */
+const char* ps_version(void);
+
+/* ==== the render: CudaPanoramaRender2 (source/Task/RicohUtil.h:193-220) ==== */
+typedef struct ps_render ps_render;
+
+/* Construct an empty render (CudaPanoramaRender2::CudaPanoramaRender2). */
+int ps_render_create(ps_render** out);
+/* Destroy; NULL is a no-op (~CudaPanoramaRender2). */
+void ps_render_destroy(ps_render* r);
+
+/* CudaPanoramaRender2::prepare (source/Task/RicohUtil.cpp:1091-1205) with the
+   camera parameters passed directly instead of a file path.  Preconditions
+   as the reference: dst_w, dst_h even and dst_h * 2 == dst_w; blend_param
+   (the maximum number of levels) > 0.  high_quality_blend must be 1 (the
+   multiband path; the linear-blend mode is not built).  Seam masks follow
+   the nearest-optical-axis rule.  Synchronises the stream. */
+int ps_render_prepare(ps_render* r, const ps_photo_param* params, int num_params, int high_quality_blend,
+                      int blend_param, int src_w, int src_h, int dst_w, int dst_h, void* stream);
+/* Same, with explicit seam (unique) masks: num_params host arrays of
+   dst_h*dst_w uint8 (non-zero = owned), each a subset of that camera's
+   coverage; they replace getNonIntersectingMasks
+   (source/CudaAccel/CudaMultibandBlend.cpp:570-571). */
+int ps_render_prepare_with_seams(ps_render* r, const ps_photo_param* params, int num_params,
+                                 int high_quality_blend, int blend_param, int src_w, int src_h, int dst_w,
+                                 int dst_h, const uint8_t* const* seam_masks, void* stream);
+
+/* CudaPanoramaRender2::render (source/Task/RicohUtil.cpp:1207-1339).
+   src: num_src camera frames (BGR24 or BGR32, host or device, all src_w x
+   src_h).  luts: NULL (no correction) or num_luts == num_images tables of
+   3*256 bytes (B, G, R), host memory; a malformed count is PS_EINVAL (the
+   reference logs a warning and skips the correction).  dst: a dst_w x dst_h
+   BGR32 or BGR24 image, host or device.  Host src / dst are copied inside
+   the call on the stream (pinned memory keeps the copies asynchronous);
+   device src / dst are read / written in place.  Does not synchronise. */
+int ps_render_render(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,
+                     ps_image* dst, void* stream);
+
+/* Launch the per-frame kernels as one captured CUDA graph (default 1) or as
+   individual launches (0).  No reference counterpart. */
+int ps_render_set_graph(ps_render* r, int enabled);
+
+/* CudaPanoramaRender2::clear / getNumImages (source/Task/RicohUtil.cpp:1341-1361). */
+void ps_render_clear(ps_render* r);
+int ps_render_get_num_images(const ps_render* r);
+
+/* Introspection (no reference counterpart; used by tests and admission). */
+int ps_render_get_num_levels(const ps_render* r);
+int ps_render_is_full_mask(const ps_render* r);
+long long ps_render_resident_bytes(const ps_render* r);
+/* Device-resident frame buffers owned by the render (BGR32, pitch in
+   bytes), one per camera: writing frames there and passing them as device
+   src avoids any copy. */
+int ps_render_get_input_buffer(ps_render* r, int cam, void** data, long long* pitch);
+/* Copies of the prepared state to host memory, for parity checks:
+   what: 0 x map (float, dst_h*dst_w, -1 where invalid), 1 y map (float),
+   2 coverage mask (uint8 0/255), 3 seam mask (uint8 0/255),
+   4 weight pyramid level `level` (int16), 5 alpha pyramid level `level`
+   (int32, the raw 5x5 sum as pyrDown16SC1To32SC1 writes it; level >= 1). */
+int ps_render_export(const ps_render* r, int what, int cam, int level, void* host_out, long long bytes);
+/* Debug copy of the collapsed result at level `level` >= 1 of the last
+   render (int16 x4 per pixel), for bit-exact checks of the pipeline. */
+int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out, long long bytes, void* stream);
+
+/* ==== batched render: several rigs, one frame each, in one launch sequence ==== */
+/* All rigs' work goes into shared persistent launches (one per pyramid step)
+   captured once per batch composition as a CUDA graph.  srcs[k] holds
+   ps_render_get_num_images(renders[k]) frames.  No reference counterpart
+   (the reference renders one rig per call, source/Task/RicohUtil.cpp:1207). */
+int ps_render_batch(ps_render* const* renders, int num_renders, const ps_image* const* srcs,
+                    const uint8_t* const* luts, ps_image* dsts, void* stream);
+
+/* ==== CudaAccel primitives (source/CudaAccel/CudaInterface.h) ==== */
+/* cudaGenerateReprojectMapAndMask (CudaInterface.h:130-131, kernel
+   source/CudaAccel/CudaReproject.cu:81-290): double-precision dst->src
+   maps on the GPU, -1 where invalid, and a 0/255 coverage mask.
+   Device outputs, tightly packed dst_h*dst_w. */
+int ps_generate_reproject_map_and_mask(const ps_photo_param* param, int src_w, int src_h, int dst_w, int dst_h,
+                                       float* xmap, float* ymap, uint8_t* mask, void* stream);
+/* cudaTransform + cudaReprojectTo16S fused (CudaInterface.h:120-121 and
+   :150-151): LUT (3*256 device bytes or NULL) on each source texel, then
+   bilinear interpolation through float maps, written as int16 x4 (B,G,R,0;
+   0 where the map is invalid).  All pointers device; pitches in bytes. */
+int ps_reproject_to_16s(const ps_image* src, const float* xmap, const float* ymap, long long map_pitch,
+                        int dst_w, int dst_h, const uint8_t* lut, int16_t* dst, long long dst_pitch,
+                        void* stream);
+/* getLUT (source/Blend/ExposureColorOptimize.cpp:1217-1223) on the host. */
+int ps_get_lut(double k, uint8_t* lut256);
+
+/* ==== multiband blender: CudaTilingMultibandBlendFast (CudaInterface.h:45-82) ==== */
+typedef struct ps_blender ps_blender;
+int ps_blender_create(ps_blender** out);
+void ps_blender_destroy(ps_blender* b);
+/* prepare(masks, maxLevels, minLength) (source/CudaAccel/CudaMultibandBlend.cpp:
+   549-642): masks = num host uint8 coverage masks (width x height), seams =
+   num host uint8 unique masks (subsets of the masks).  Synchronises. */
+int ps_blender_prepare(ps_blender* b, const uint8_t* const* masks, const uint8_t* const* seams, int num,
+                       int width, int height, int max_levels, int min_length, void* stream);
+/* blend(images, blendImage) (:785-823): num device images of int16 x4
+   (CV_16SC4, values 0..255 in B,G,R as cudaReprojectTo16S writes them) or
+   BGR32 uint8 (CV_8UC4) -> dst (device, BGR32 or BGR24).  A 16-bit value
+   outside 0..255 is PS_EINVAL (checked on the device; the status is read
+   back, so this call synchronises when image_format is 16). */
+int ps_blender_blend(ps_blender* b, const void* const* images, const long long* pitches, int image_format,
+                     ps_image* dst, void* stream);
+int ps_blender_get_num_levels(const ps_blender* b);
+
+/* ==== serving loop: live streams with continuous batching ==== */
+typedef struct ps_server ps_server;
+/* budget_bytes: device memory that resident stream state may occupy
+   (admission control, like the HBM check of source/Task/RicohUtil.cpp:
+   1135-1170).  max_batch: frames per scheduling tick. */
+int ps_server_create(long long budget_bytes, int max_batch, ps_server** out);
+void ps_server_destroy(ps_server* s);
+/* Admit a stream whose rig is described like ps_render_prepare.  Returns
+   PS_ENOMEM (nothing admitted) when its resident bytes would exceed the
+   budget.  *stream_id receives the id. */
+int ps_server_admit(ps_server* s, const ps_photo_param* params, int num_params, int blend_param, int src_w,
+                    int src_h, int dst_w, int dst_h, int* stream_id);
+int ps_server_remove(ps_server* s, int stream_id);
+long long ps_server_resident_bytes(const ps_server* s);
+/* Replay an arrival trace in real time: frame k of the trace arrives at
+   arrival_ns[k] (relative to the start) for stream stream_ids[k], with
+   camera frames srcs[k] (host BGR32, pinned preferred) and luts[k]
+   (num*3*256 or NULL); outputs go to dsts[k] (host BGR32) or nowhere when
+   dsts is NULL.  Blocks until every frame is done, then fills
+   latency_ns[k] (arrival -> output ready) and *wall_ns. */
+int ps_server_run_trace(ps_server* s, int num_frames, const int* stream_ids, const long long* arrival_ns,
+                        const ps_image* const* srcs, const uint8_t* const* luts, ps_image* dsts,
+                        long long* latency_ns, long long* wall_ns);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PANOSTITCH_H */

@@ -1,0 +1,104 @@
+/*
+ * ps_oracle.h -- CPU restatement of PanoStitcher's per-frame stitch path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA
+ * product path in panostitcher_gb300/ is compared against; the product never
+ * links, loads or calls it.  It is also the timed CPU baseline of bench.py.
+ *
+ * Parity status: UNPINNED against the reference binary.  The reference
+ * (xpngzhng/PanoStitcher) cannot be built here: it needs OpenCV 3.0 (incl.
+ * cudaarithm), ticpp, EasyFFmpeg and MSBuild, and its CUDA remap uses texture
+ * references removed in CUDA 12.  It ships no golden vectors and no tests
+ * with assertions.  Every function below restates the cited reference code
+ * line by line in its integer / double semantics; known-answer tests in
+ * tests/ pin the restatement's internal consistency.
+ *
+ * Conventions
+ *   - images are tightly packed row-major; 4-channel int16/int32 images store
+ *     B,G,R,X per pixel (X = channel 3, undefined in the reference and 0 here);
+ *   - masks are uint8 0 / 255;
+ *   - "level" j has size W_j = (W_{j-1}+1)/2, H_j = (H_{j-1}+1)/2.
+ */
+#ifndef PS_ORACLE_H
+#define PS_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* PhotoParam (source/Warp/ZReproject.h:17-50), same field order. */
+typedef struct orc_param {
+    int imageType, cropMode, cropX, cropY, cropWidth, cropHeight;
+    int circleX, circleY, circleR;
+    double hfov, vfov, alpha, beta, gamma, shiftX, shiftY, shearX, shearY;
+    double yaw, pitch, roll;
+} orc_param;
+
+/* Remap (source/Warp/ZReproject.h:91-120). */
+typedef struct orc_remap {
+    int srcImageType;
+    double srcTX, srcTY, destTX, destTY;
+    double scale[2], shear[2], rot[2], rad[6], mt[3][3];
+    double distance, horizontal, vertical;
+} orc_remap;
+
+/* ---- geometry ---------------------------------------------------------- */
+void orc_remap_init(const orc_param* p, int canvasW, int canvasH, int camW, int camH, orc_remap* r);
+void orc_remap_point(const orc_remap* r, double cx, double cy, double* sx, double* sy);
+double orc_remap_axis_angle(const orc_remap* r, double cx, double cy);
+void orc_reproject_map(const orc_param* p, int camW, int camH, int canvasW, int canvasH,
+                       double* map64 /* nullable, 2 per px */, float* xmap, float* ymap, uint8_t* mask);
+void orc_nearest_axis_seams(const orc_param* params, int n, int camW, int camH, int canvasW, int canvasH,
+                            const uint8_t* coverage /* n*W*H */, uint8_t* seams /* n*W*H */);
+void orc_get_lut(double k, uint8_t lut[256]);
+
+/* ---- remap ------------------------------------------------------------- */
+void orc_reproject_bilinear_16s(const uint8_t* src, int srcW, int srcH, long long srcStep, int channels,
+                                const uint8_t* lut /* 3*256 (B,G,R) or NULL */,
+                                const float* xmap, const float* ymap, int dstW, int dstH,
+                                int16_t* dst /* dstW*dstH*4 */);
+void orc_reproject_bilinear_16s_rows(const uint8_t* src, int srcW, int srcH, long long srcStep, int channels,
+                                     const uint8_t* lutted /* unused when NULL */, const float* xmap, const float* ymap,
+                                     int dstW, int row0, int row1, int16_t* dst);
+
+/* ---- pyramid primitives (CudaAccel/CudaPyramid2.cu semantics) ----------- */
+int orc_num_levels(int width, int height, int maxLevels, int minLength);
+void orc_level_sizes(int w, int h, int levels, int* ws, int* hs);
+void orc_pyr_down_16sc1_to_32sc1(const int16_t* src, int sw, int sh, int32_t* dst, int dw, int dh);
+void orc_pyr_down_16sc1_to_16sc1(const int16_t* src, int sw, int sh, int16_t* dst, int dw, int dh);
+void orc_pyr_down_16sc4_masked(const int16_t* src, int sw, int sh, const int32_t* scale,
+                               int16_t* dst, int dw, int dh);
+void orc_pyr_up_16sc4(const int16_t* src, int sw, int sh, int16_t* dst, int dw, int dh);
+void orc_pyr_up_32sc4(const int32_t* src, int sw, int sh, int32_t* dst, int dw, int dh);
+
+/* ---- multiband blend (CudaTilingMultibandBlendFast semantics) ----------- */
+typedef struct orc_blender orc_blender;
+orc_blender* orc_mb_prepare(const uint8_t* masks /* n*W*H coverage */, const uint8_t* seams /* n*W*H */,
+                            int n, int W, int H, int maxLevels, int minLength);
+void orc_mb_free(orc_blender* b);
+int orc_mb_num_levels(const orc_blender* b);
+int orc_mb_full_mask(const orc_blender* b);
+/* copies of prepared pyramids for bit-exact checks */
+void orc_mb_get_alpha(const orc_blender* b, int cam, int level, int32_t* out);
+void orc_mb_get_weight(const orc_blender* b, int cam, int level, int16_t* out);
+/* blend of n int16x4 level-0 images (each W*H*4) into BGR32 (W*H*4, X=0).
+   If level_out != NULL it receives the normalised (pre-collapse) int32x4
+   pyramid followed by the collapsed pyramid, level by level. */
+void orc_mb_blend(orc_blender* b, const int16_t* const* images, uint8_t* dst, int32_t* norm_out, int32_t* coll_out);
+/* same arithmetic, camera pyramids built on nthreads threads */
+void orc_mb_blend_mt(orc_blender* b, const int16_t* const* images, uint8_t* dst, int nthreads);
+
+/* ---- whole render (CPUPanoramaRender / CudaPanoramaRender2 dataflow) ---- */
+/* srcs: n BGR24/BGR32 frames; luts: n*3*256 or NULL; maps: n float x/y maps.
+   Writes BGR32 dst.  nthreads>1 uses the row-parallel remap and the
+   camera-parallel blend. */
+void orc_render(orc_blender* b, const uint8_t* const* srcs, int srcW, int srcH, int channels,
+                const uint8_t* luts, const float* const* xmaps, const float* const* ymaps,
+                uint8_t* dst, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,132 @@
+"""ctypes bindings of libpanostitch.so (the C ABI in include/panostitch.h).
+
+The shared library is built in-tree by ``panostitcher_gb300.build``.  There
+is no fallback: if the library is missing or fails to load, every entry
+point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpanostitch.so")
+
+PS_OK, PS_EINVAL, PS_ENOMEM, PS_ECUDA, PS_ETIMEOUT, PS_ESTATE = 0, 1, 2, 3, 4, 5
+PS_MAX_LEVELS, PS_MAX_CAMS = 16, 64
+PS_FMT_BGR24, PS_FMT_BGR32 = 24, 32
+PS_MEM_HOST, PS_MEM_DEVICE = 0, 1
+EXPORT_XMAP, EXPORT_YMAP, EXPORT_COVERAGE, EXPORT_SEAM, EXPORT_WEIGHT, EXPORT_ALPHA = range(6)
+
+_STATUS_NAMES = {PS_EINVAL: "PS_EINVAL", PS_ENOMEM: "PS_ENOMEM", PS_ECUDA: "PS_ECUDA",
+                 PS_ETIMEOUT: "PS_ETIMEOUT", PS_ESTATE: "PS_ESTATE"}
+
+
+class PsError(RuntimeError):
+    """A non-zero status from the C ABI, with ps_last_error()'s text."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class PhotoParam(C.Structure):
+    """ps_photo_param == PhotoParam (source/Warp/ZReproject.h:17-50)."""
+
+    _fields_ = [(n, C.c_int) for n in ("image_type", "crop_mode", "crop_x", "crop_y", "crop_width",
+                                       "crop_height", "circle_x", "circle_y", "circle_r")] + \
+               [(n, C.c_double) for n in ("hfov", "vfov", "alpha", "beta", "gamma", "shift_x", "shift_y",
+                                          "shear_x", "shear_y", "yaw", "pitch", "roll")]
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "PhotoParam":
+        p = cls()
+        for k, v in d.items():
+            setattr(p, k, v)
+        return p
+
+
+class Image(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("pitch", C.c_longlong), ("width", C.c_int), ("height", C.c_int),
+                ("format", C.c_int), ("location", C.c_int)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+# (name, restype, argtypes)
+_SIGS = [
+    ("ps_last_error", C.c_char_p, []),
+    ("ps_version", C.c_char_p, []),
+    ("ps_render_create", C.c_int, [C.POINTER(C.c_void_p)]),
+    ("ps_render_destroy", None, [C.c_void_p]),
+    ("ps_render_prepare", C.c_int, [C.c_void_p, C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("ps_render_prepare_with_seams", C.c_int, [C.c_void_p, C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int,
+                                               C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p),
+                                               C.c_void_p]),
+    ("ps_render_render", C.c_int, [C.c_void_p, C.POINTER(Image), C.c_int, C.c_void_p, C.c_int,
+                                   C.POINTER(Image), C.c_void_p]),
+    ("ps_render_set_graph", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_render_clear", None, [C.c_void_p]),
+    ("ps_render_get_num_images", C.c_int, [C.c_void_p]),
+    ("ps_render_get_num_levels", C.c_int, [C.c_void_p]),
+    ("ps_render_is_full_mask", C.c_int, [C.c_void_p]),
+    ("ps_render_resident_bytes", C.c_longlong, [C.c_void_p]),
+    ("ps_render_get_input_buffer", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p),
+                                             C.POINTER(C.c_longlong)]),
+    ("ps_render_export", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong]),
+    ("ps_render_export_collapsed", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p]),
+    ("ps_render_batch", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.POINTER(Image)),
+                                  C.POINTER(C.c_void_p), C.POINTER(Image), C.c_void_p]),
+    ("ps_generate_reproject_map_and_mask", C.c_int, [C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,
+                                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ps_reproject_to_16s", C.c_int, [C.POINTER(Image), C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_int,
+                                      C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]),
+    ("ps_get_lut", C.c_int, [C.c_double, C.c_void_p]),
+    ("ps_blender_create", C.c_int, [C.POINTER(C.c_void_p)]),
+    ("ps_blender_destroy", None, [C.c_void_p]),
+    ("ps_blender_prepare", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int,
+                                     C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("ps_blender_blend", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_longlong), C.c_int,
+                                   C.POINTER(Image), C.c_void_p]),
+    ("ps_blender_get_num_levels", C.c_int, [C.c_void_p]),
+    ("ps_server_create", C.c_int, [C.c_longlong, C.c_int, C.POINTER(C.c_void_p)]),
+    ("ps_server_destroy", None, [C.c_void_p]),
+    ("ps_server_admit", C.c_int, [C.c_void_p, C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    ("ps_server_remove", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_server_resident_bytes", C.c_longlong, [C.c_void_p]),
+    ("ps_server_run_trace", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.POINTER(Image)),
+                                      C.POINTER(C.c_void_p), C.POINTER(Image), C.c_void_p, C.c_void_p]),
+]
+
+
+def lib():
+    """Load libpanostitch.so (raises if it was not built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"{LIB_PATH} is missing: run panostitcher_gb300.build.build() first "
+                                   "(there is no CPU fallback)")
+            L = C.CDLL(LIB_PATH)
+            for name, res, args in _SIGS:
+                f = getattr(L, name, None)
+                if f is None:
+                    continue
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != PS_OK:
+        raise PsError(status, lib().ps_last_error().decode(errors="replace"))
+
+
+def exported_symbols():
+    """Names of the C ABI functions this module binds."""
+    return [s[0] for s in _SIGS]

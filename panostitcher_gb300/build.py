@@ -1,0 +1,87 @@
+"""Builds libpanostitch.so in-tree with nvcc for sm_103a (no CMake, no torch).
+
+Each translation unit compiles in parallel into panostitcher_gb300/_build/,
+then nvcc links the shared library next to this file.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libpanostitch.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = {
+    "csrc/ps_kernels.cu": [],
+    "csrc/ps_prepare.cu": ["--fmad=false"],
+    "csrc/ps_rig.cpp": [],
+    "csrc/ps_capi.cpp": [],
+    "csrc/ps_server.cpp": [],
+}
+COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include")]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found")
+    return cand
+
+
+def _stale(out: str, deps) -> bool:
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers():
+    d = os.path.join(HERE, "csrc")
+    hs = [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".h", ".cuh"))]
+    return hs + [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+
+
+def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    cc = nvcc()
+    hdrs = _headers()
+    jobs = []
+    objs = []
+    for src, extra in SOURCES.items():
+        path = os.path.join(HERE, src)
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [path] + hdrs):
+            cmd = [cc] + COMMON + extra + (["-Xptxas", "-v"] if ptxas_info and src.endswith(".cu") else []) + \
+                  ["-c", path, "-o", obj]
+            if src.endswith(".cpp"):
+                cmd[1:1] = ["-x", "cu"] if False else []
+            jobs.append(cmd)
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        return cmd, r
+    with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
+        for cmd, r in ex.map(run, jobs):
+            if verbose or r.returncode != 0 or ptxas_info:
+                sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            if r.returncode != 0:
+                raise RuntimeError(f"nvcc failed on {cmd[-3]}")
+    if force or jobs or not os.path.exists(LIB):
+        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static", "-Xlinker", "-z,defs"] + \
+              ["-lpthread", "-ldl", "-lrt"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("link failed")
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv, force="-f" in sys.argv, ptxas_info="--ptxas" in sys.argv)
+    print(LIB)

@@ -1,0 +1,334 @@
+// ps_capi.cpp -- the extern "C" boundary: validation, status codes, the
+// thread-local error text, and the objects behind the opaque handles.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <set>
+
+#include "ps_rig.h"
+
+using ps::fail;
+
+struct ps_render {
+    ps::Rig rig;
+    std::unique_ptr<ps::Plan> plan;
+    bool useGraph = true;
+};
+
+struct ps_blender {
+    ps::Rig rig;
+    std::unique_ptr<ps::Plan> plan;
+};
+
+namespace {
+
+thread_local std::string t_err;
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        f();
+        return PS_OK;
+    } catch (const ps::Error& e) {
+        t_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        t_err = "host allocation failed";
+        return PS_ENOMEM;
+    } catch (const std::exception& e) {
+        t_err = e.what();
+        return PS_EINVAL;
+    } catch (...) {
+        t_err = "unknown error";
+        return PS_EINVAL;
+    }
+}
+
+inline cudaStream_t toStream(void* s) { return static_cast<cudaStream_t>(s); }
+
+int bpp(int fmt) { return fmt == PS_FMT_BGR24 ? 3 : 4; }
+
+void checkImage(const ps_image* im, int w, int h, const char* what, int idx)
+{
+    if (!im) fail(PS_EINVAL, "%s[%d] is NULL", what, idx);
+    if (!im->data) fail(PS_EINVAL, "%s[%d]: data is NULL", what, idx);
+    if (im->format != PS_FMT_BGR24 && im->format != PS_FMT_BGR32)
+        fail(PS_EINVAL, "%s[%d]: format %d is neither BGR24 nor BGR32", what, idx, im->format);
+    if (im->location != PS_MEM_HOST && im->location != PS_MEM_DEVICE)
+        fail(PS_EINVAL, "%s[%d]: location %d unknown", what, idx, im->location);
+    // source/Task/RicohUtil.cpp:1222-1236
+    if (im->width != w || im->height != h)
+        fail(PS_EINVAL, "%s[%d] size (%d, %d), not equal to (%d, %d)", what, idx, im->width, im->height, w, h);
+    if (im->pitch < (long long)w * bpp(im->format)) fail(PS_EINVAL, "%s[%d]: pitch %lld too small", what, idx, im->pitch);
+    if (im->location == PS_MEM_DEVICE && im->format == PS_FMT_BGR32 &&
+        ((reinterpret_cast<uintptr_t>(im->data) & 3) || (im->pitch & 3)))
+        fail(PS_EINVAL, "%s[%d]: device BGR32 images need 4-byte aligned data and pitch", what, idx);
+}
+
+void checkFrame(const ps::Rig& rig, const ps_image* src, int numSrc, const uint8_t* luts, int numLuts,
+                const ps_image* dst)
+{
+    if (!rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+    if (!rig.hasMaps()) fail(PS_ESTATE, "prepared without camera parameters");
+    if (!src || numSrc != rig.numImages())
+        fail(PS_EINVAL, "%d source images given, %d cameras prepared", numSrc, rig.numImages());
+    for (int i = 0; i < numSrc; i++) {
+        checkImage(&src[i], rig.srcW(), rig.srcH(), "src", i);
+        if (src[i].format != src[0].format) fail(PS_EINVAL, "src[%d]: all sources must share one format", i);
+    }
+    if (luts && numLuts != rig.numImages())
+        fail(PS_EINVAL, "%d look-up tables given, %d cameras prepared (each 3 x 256 bytes)", numLuts, rig.numImages());
+    checkImage(dst, rig.width(), rig.height(), "dst", 0);
+}
+
+// Launch plans of batches, keyed by the rigs they run.
+std::mutex g_planMu;
+std::map<std::vector<ps::Rig*>, std::unique_ptr<ps::Plan>> g_batchPlans;
+
+void purgePlans(const ps::Rig* rig)
+{
+    std::lock_guard<std::mutex> lk(g_planMu);
+    for (auto it = g_batchPlans.begin(); it != g_batchPlans.end();) {
+        if (std::find(it->first.begin(), it->first.end(), rig) != it->first.end()) it = g_batchPlans.erase(it);
+        else ++it;
+    }
+}
+
+}  // namespace
+
+void ps::setLastError(const std::string& msg) { t_err = msg; }
+
+extern "C" {
+
+const char* ps_last_error(void) { return t_err.c_str(); }
+const char* ps_version(void) { return "panostitch-gb300 0.1 (sm_103a)"; }
+
+// ---- render ----------------------------------------------------------------------
+int ps_render_create(ps_render** out)
+{
+    return guarded([&] {
+        if (!out) fail(PS_EINVAL, "out is NULL");
+        *out = new ps_render();
+    });
+}
+
+void ps_render_destroy(ps_render* r)
+{
+    if (!r) return;
+    purgePlans(&r->rig);
+    delete r;
+}
+
+static int prepareRender(ps_render* r, const ps_photo_param* params, int num, int hq, int blendParam, int srcW,
+                         int srcH, int dstW, int dstH, const uint8_t* const* seams, void* stream)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        purgePlans(&r->rig);
+        r->plan.reset();
+        r->rig.clear();
+        if (hq != 1) fail(PS_EINVAL, "high_quality_blend = %d: only the multiband path (1) is built", hq);
+        r->rig.prepareFromParams(params, num, blendParam, srcW, srcH, dstW, dstH, seams, toStream(stream));
+        r->plan.reset(new ps::Plan({&r->rig}));
+    });
+}
+
+int ps_render_prepare(ps_render* r, const ps_photo_param* params, int num_params, int high_quality_blend,
+                      int blend_param, int src_w, int src_h, int dst_w, int dst_h, void* stream)
+{
+    return prepareRender(r, params, num_params, high_quality_blend, blend_param, src_w, src_h, dst_w, dst_h,
+                         nullptr, stream);
+}
+
+int ps_render_prepare_with_seams(ps_render* r, const ps_photo_param* params, int num_params,
+                                 int high_quality_blend, int blend_param, int src_w, int src_h, int dst_w,
+                                 int dst_h, const uint8_t* const* seam_masks, void* stream)
+{
+    if (!seam_masks) {
+        t_err = "seam_masks is NULL";
+        return PS_EINVAL;
+    }
+    return prepareRender(r, params, num_params, high_quality_blend, blend_param, src_w, src_h, dst_w, dst_h,
+                         seam_masks, stream);
+}
+
+int ps_render_render(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,
+                     ps_image* dst, void* stream)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        checkFrame(r->rig, src, num_src, luts, num_luts, dst);
+        if (!r->plan || !r->plan->matches({&r->rig})) r->plan.reset(new ps::Plan({&r->rig}));
+        r->plan->run({ps::FrameInput{src, luts, dst}}, toStream(stream), r->useGraph);
+    });
+}
+
+int ps_render_set_graph(ps_render* r, int enabled)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        r->useGraph = enabled != 0;
+    });
+}
+
+void ps_render_clear(ps_render* r)
+{
+    if (!r) return;
+    purgePlans(&r->rig);
+    r->plan.reset();
+    r->rig.clear();
+}
+
+int ps_render_get_num_images(const ps_render* r) { return r && r->rig.ready() ? r->rig.numImages() : 0; }
+int ps_render_get_num_levels(const ps_render* r) { return r && r->rig.ready() ? r->rig.numLevels() : 0; }
+int ps_render_is_full_mask(const ps_render* r) { return r && r->rig.ready() && r->rig.fullMask() ? 1 : 0; }
+long long ps_render_resident_bytes(const ps_render* r) { return r ? r->rig.residentBytes() : 0; }
+
+int ps_render_get_input_buffer(ps_render* r, int cam, void** data, long long* pitch)
+{
+    return guarded([&] {
+        if (!r || !data || !pitch) fail(PS_EINVAL, "NULL argument");
+        if (!r->rig.ready() || !r->rig.hasMaps()) fail(PS_ESTATE, "not prepared");
+        if (cam < 0 || cam >= r->rig.numImages()) fail(PS_EINVAL, "camera %d out of range", cam);
+        *data = r->rig.inputBuffer(cam);
+        *pitch = r->rig.inputPitch();
+    });
+}
+
+int ps_render_export(const ps_render* r, int what, int cam, int level, void* host_out, long long bytes)
+{
+    return guarded([&] {
+        if (!r || !host_out) fail(PS_EINVAL, "NULL argument");
+        r->rig.exportState(what, cam, level, host_out, bytes);
+    });
+}
+
+int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out, long long bytes, void* stream)
+{
+    return guarded([&] {
+        if (!r || !host_out) fail(PS_EINVAL, "NULL argument");
+        r->rig.exportCollapsed(level, host_out, bytes, toStream(stream));
+    });
+}
+
+// ---- batch ----------------------------------------------------------------------
+int ps_render_batch(ps_render* const* renders, int num_renders, const ps_image* const* srcs,
+                    const uint8_t* const* luts, ps_image* dsts, void* stream)
+{
+    return guarded([&] {
+        if (!renders || !srcs || !dsts || num_renders <= 0) fail(PS_EINVAL, "empty batch");
+        std::vector<ps::Rig*> rigs;
+        std::set<ps_render*> seen;
+        std::vector<ps::FrameInput> in;
+        for (int k = 0; k < num_renders; k++) {
+            ps_render* r = renders[k];
+            if (!r) fail(PS_EINVAL, "render %d is NULL", k);
+            if (!seen.insert(r).second) fail(PS_EINVAL, "render %d appears twice in the batch", k);
+            const uint8_t* lt = luts ? luts[k] : nullptr;
+            checkFrame(r->rig, srcs[k], r->rig.numImages(), lt, r->rig.numImages(), &dsts[k]);
+            rigs.push_back(&r->rig);
+            in.push_back({srcs[k], lt, &dsts[k]});
+        }
+        std::lock_guard<std::mutex> lk(g_planMu);
+        auto& plan = g_batchPlans[rigs];
+        if (!plan || !plan->matches(rigs)) plan.reset(new ps::Plan(rigs));
+        plan->run(in, toStream(stream), true);
+    });
+}
+
+// ---- primitives -----------------------------------------------------------------
+int ps_generate_reproject_map_and_mask(const ps_photo_param* param, int src_w, int src_h, int dst_w, int dst_h,
+                                       float* xmap, float* ymap, uint8_t* mask, void* stream)
+{
+    return guarded([&] {
+        if (!param || !xmap || !ymap || !mask) fail(PS_EINVAL, "NULL argument");
+        if (src_w <= 0 || src_h <= 0 || dst_w <= 0 || dst_h <= 0) fail(PS_EINVAL, "sizes must be positive");
+        if (param->image_type < 0 || param->image_type > 3) fail(PS_EINVAL, "image_type not in 0..3");
+        ps::RemapDev rp;
+        ps::remapInit(*param, dst_w, dst_h, src_w, src_h, rp);
+        ps::DevBuf d(sizeof rp);
+        PS_CUDA(cudaMemcpyAsync(d.get(), &rp, sizeof rp, cudaMemcpyHostToDevice, toStream(stream)));
+        PS_CUDA(ps::launchGenMap(d.as<ps::RemapDev>(), dst_w, dst_h, xmap, ymap, mask, toStream(stream)));
+        PS_CUDA(cudaStreamSynchronize(toStream(stream)));
+    });
+}
+
+int ps_reproject_to_16s(const ps_image* src, const float* xmap, const float* ymap, long long map_pitch, int dst_w,
+                        int dst_h, const uint8_t* lut, int16_t* dst, long long dst_pitch, void* stream)
+{
+    return guarded([&] {
+        if (!src || !xmap || !ymap || !dst) fail(PS_EINVAL, "NULL argument");
+        checkImage(src, src->width, src->height, "src", 0);
+        if (src->location != PS_MEM_DEVICE) fail(PS_EINVAL, "src must be device memory");
+        if (src->width <= 0 || src->height <= 0 || dst_w <= 0 || dst_h <= 0) fail(PS_EINVAL, "empty image");
+        if (map_pitch < (long long)dst_w * 4 || (map_pitch & 3)) fail(PS_EINVAL, "bad map pitch");
+        if (dst_pitch < (long long)dst_w * 8 || (dst_pitch & 7) || (reinterpret_cast<uintptr_t>(dst) & 7))
+            fail(PS_EINVAL, "bad dst pitch / alignment");
+        PS_CUDA(ps::launchReprojectTo16S(static_cast<const uint8_t*>(src->data), src->pitch, src->width, src->height,
+                                         src->format, xmap, ymap, map_pitch, dst_w, dst_h, lut, dst, dst_pitch,
+                                         toStream(stream)));
+    });
+}
+
+int ps_get_lut(double k, uint8_t* lut256)
+{
+    return guarded([&] {
+        if (!lut256) fail(PS_EINVAL, "lut is NULL");
+        if (!(k > 0)) fail(PS_EINVAL, "k = %g must be positive", k);  // CV_Assert(k > 0)
+        for (int i = 0; i < 256; i++) {
+            const double v = std::nearbyint(k * i);
+            lut256[i] = (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v));
+        }
+    });
+}
+
+// ---- blender ----------------------------------------------------------------------
+int ps_blender_create(ps_blender** out)
+{
+    return guarded([&] {
+        if (!out) fail(PS_EINVAL, "out is NULL");
+        *out = new ps_blender();
+    });
+}
+
+void ps_blender_destroy(ps_blender* b) { delete b; }
+
+int ps_blender_prepare(ps_blender* b, const uint8_t* const* masks, const uint8_t* const* seams, int num, int width,
+                       int height, int max_levels, int min_length, void* stream)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        b->plan.reset();
+        b->rig.prepareFromMasks(masks, seams, num, width, height, max_levels, min_length, toStream(stream));
+        b->plan.reset(new ps::Plan({&b->rig}));
+    });
+}
+
+int ps_blender_blend(ps_blender* b, const void* const* images, const long long* pitches, int image_format,
+                     ps_image* dst, void* stream)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        if (!b->rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        if (!images || !pitches) fail(PS_EINVAL, "NULL images");
+        if (image_format != 16 && image_format != 8) fail(PS_EINVAL, "image_format %d is neither 16 nor 8", image_format);
+        const int esz = image_format == 16 ? 8 : 4;
+        for (int i = 0; i < b->rig.numImages(); i++) {
+            if (!images[i]) fail(PS_EINVAL, "image %d is NULL", i);
+            if (pitches[i] < (long long)b->rig.width() * esz || (pitches[i] % esz) ||
+                (reinterpret_cast<uintptr_t>(images[i]) % esz))
+                fail(PS_EINVAL, "image %d: bad pitch or alignment", i);
+        }
+        checkImage(dst, b->rig.width(), b->rig.height(), "dst", 0);
+        b->rig.imagesToLevel0(images, pitches, image_format, toStream(stream));
+        if (!b->plan || !b->plan->matches({&b->rig})) b->plan.reset(new ps::Plan({&b->rig}));
+        b->plan->run({ps::FrameInput{nullptr, nullptr, dst}}, toStream(stream), false);
+    });
+}
+
+int ps_blender_get_num_levels(const ps_blender* b) { return b && b->rig.ready() ? b->rig.numLevels() : 0; }
+
+}  // extern "C"

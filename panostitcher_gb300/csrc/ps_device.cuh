@@ -1,0 +1,114 @@
+// ps_device.cuh -- device-side data layout shared by the stitch kernels.
+//
+// HBM layout of one rig (all cameras share the level geometry):
+//   G[j]   uchar4 Gaussian pyramid of every camera, level j, camera-major,
+//          row pitch lv[j].pitch pixels.  The reference keeps it as int16x4
+//          (CV_16SC4); every value is provably in 0..255 (the level-0 remap
+//          is a convex combination of bytes and each masked pyrDown is a
+//          weighted average of the level below), so one byte per channel is
+//          exact and halves the traffic.
+//   Wt[j]  uint16 seam-weight pyramid (weightPyrs, 0..256), same pitch as G.
+//   Am[j]  uint16 alpha divisor m = alphaPyr / 256 (alphaPyrs is always a
+//          multiple of 256 because its level source is 0/256), level >= 1.
+//   C[j]   short4 collapsed result of level j >= 1 (resultPyr after
+//          normalise + collapse); |value| < 3300 so int16 is exact.
+//   maps   float2 dst->src map, stored tile-compact for the level-0 tiles
+//          that a camera covers (256 pixels per tile, row-major in the tile).
+// Work is described by item lists built at prepare time from the pyramids'
+// supports, so no kernel touches canvas area a camera cannot influence.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/panostitch.h"
+
+namespace ps {
+
+// ---- tiles ------------------------------------------------------------------
+constexpr int kRemapTW = 32, kRemapTH = 8;     // level-0 remap tile (one pixel per thread)
+constexpr int kDownTW = 32, kDownTH = 16;      // pyrDown output tile (two pixels per thread)
+constexpr int kBlendTW = 64, kBlendTH = 8;     // blend tile (two adjacent pixels per thread)
+constexpr int kThreads = 256;
+
+struct LevelDev {
+    int w, h;            // level size
+    int pitch;           // row pitch in pixels of G / Wt / Am / C (multiple of 64)
+    long long camStride; // pixels between cameras in G / Wt / Am
+    uchar4* G;
+    uint16_t* Wt;
+    uint16_t* Am;
+    short4* C;
+};
+
+struct RigDev {
+    int n, L, W, H;
+    int full;                 // union of coverages == whole canvas
+    int srcW, srcH;
+    const float2* maps;       // tile-compact maps of all cameras
+    const uint8_t* unionMask; // level-0 union coverage (0/255), pitch = lv[0].pitch
+    const uint8_t* camLists;  // camera indices referenced by BlendItem::camOff
+    LevelDev lv[PS_MAX_LEVELS + 1];
+};
+
+// Per-frame arguments of one rig in a launch (device resident, rewritten
+// before every launch sequence).
+struct FrameDev {
+    const uint8_t* src[PS_MAX_CAMS];
+    long long srcPitch[PS_MAX_CAMS];
+    int srcFmt;               // PS_FMT_BGR24 / PS_FMT_BGR32
+    int outFmt;
+    uint8_t* out;
+    long long outPitch;
+    const uint8_t* luts;      // n * 768 device bytes (B, G, R tables)
+    int* status;              // device error word (0 = ok)
+};
+
+// Work items (one per tile), resident per rig and built at prepare time.
+struct RemapItem { uint16_t cam, pad; uint16_t tx, ty; uint32_t mapTile; };
+struct DownItem { uint8_t cam, level; uint16_t tx, ty; uint16_t pad; };   // level = output level
+struct BlendItem { uint8_t level, cls; uint16_t tx, ty; uint16_t pad; uint32_t camOff, camCnt; };
+// cls of a level-0 blend tile: 0 uncovered (write zeros), 1 fully covered,
+// 2 partially covered (read the union mask).  Unused above level 0.
+
+// A launch runs the concatenation of segments: `count` items of one rig,
+// numbered from `prefix` in the launch.  Several rigs (a batch, or the
+// frames of a serving tick) share one launch this way.
+struct Segment {
+    const void* items;
+    const RigDev* rig;
+    const FrameDev* frame;
+    int count, prefix;
+};
+
+// Item `it` of a launch -> its segment, scanning forward from a hint (the
+// grid-stride loop visits items in increasing order).
+__device__ __forceinline__ int findSegment(const Segment* segs, int nsegs, int it, int hint)
+{
+    int s = hint;
+    while (s + 1 < nsegs && segs[s + 1].prefix <= it) s++;
+    return s;
+}
+
+// ---- borders: source/CudaAccel/CudaUtil.cuh:6-98 ------------------------------
+// Vertical reflect-101 (BrdColReflect101) and horizontal wrap (BrdRowWrap),
+// restated with the reference's exact index formulas.
+__device__ __forceinline__ int rowLow(int y, int H) { return abs(y) % H; }
+__device__ __forceinline__ int rowHigh(int y, int H) { int last = H - 1; return abs(last - abs(last - y)) % H; }
+__device__ __forceinline__ int colLow(int x, int W) { return x >= 0 ? x : x - ((x - W + 1) / W) * W; }
+__device__ __forceinline__ int colHigh(int x, int W) { return x < W ? x : x % W; }
+// any row index of a pyramid tile -> the row the reference reads
+__device__ __forceinline__ int rowMap(int y, int H) { return y < 0 ? rowLow(y, H) : (y >= H ? rowHigh(y, H) : y); }
+__device__ __forceinline__ int colMap(int x, int W) { return x < 0 ? colLow(x, W) : (x >= W ? colHigh(x, W) : x); }
+
+// ---- packed channel arithmetic -----------------------------------------------
+// A BGRX byte quad splits into two words holding 16-bit lanes:
+//   lo = B | R << 16,  hi = G | X << 16.
+// Sums of up to 256 weighted bytes stay below 65536, so the 5x5 pyramid
+// filters run two channels per 32-bit add with no carry between lanes.
+__device__ __forceinline__ uint2 unpackBytes(uint32_t v)
+{
+    return make_uint2(v & 0x00FF00FFu, (v >> 8) & 0x00FF00FFu);
+}
+
+}  // namespace ps

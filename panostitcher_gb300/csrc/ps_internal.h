@@ -1,0 +1,137 @@
+// ps_internal.h -- host-side internals shared by the library's translation units.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "ps_device.cuh"
+
+namespace ps {
+
+// ---- errors -------------------------------------------------------------------
+// Internal code throws ps::Error; the C ABI converts it to a status code and
+// the thread-local message returned by ps_last_error().
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const char* fmt, ...);
+void setLastError(const std::string& msg);  // the text ps_last_error() returns
+void checkCuda(cudaError_t e, const char* what);
+#define PS_CUDA(call) ::ps::checkCuda((call), #call)
+
+// ---- device memory --------------------------------------------------------------
+// Owning device allocation; every allocation of the library goes through it
+// so resident bytes can be accounted for admission control.
+class DevBuf {
+public:
+    DevBuf() = default;
+    explicit DevBuf(size_t bytes) { alloc(bytes); }
+    ~DevBuf() { reset(); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept
+    {
+        if (this != &o) { reset(); p_ = o.p_; n_ = o.n_; o.p_ = nullptr; o.n_ = 0; }
+        return *this;
+    }
+    void alloc(size_t bytes);
+    void reset();
+    void zero(cudaStream_t st);
+    template <class T> T* as() const { return static_cast<T*>(p_); }
+    void* get() const { return p_; }
+    size_t bytes() const { return n_; }
+
+private:
+    void* p_ = nullptr;
+    size_t n_ = 0;
+};
+
+// Pinned host allocation.
+class HostBuf {
+public:
+    HostBuf() = default;
+    ~HostBuf() { reset(); }
+    HostBuf(const HostBuf&) = delete;
+    HostBuf& operator=(const HostBuf&) = delete;
+    void alloc(size_t bytes);
+    void reset();
+    template <class T> T* as() const { return static_cast<T*>(p_); }
+    size_t bytes() const { return n_; }
+
+private:
+    void* p_ = nullptr;
+    size_t n_ = 0;
+};
+
+// ---- geometry -------------------------------------------------------------------
+// Remap (source/Warp/ZReproject.h:91-120) after init, flattened for the GPU.
+struct RemapDev {
+    int type;                      // PanoTools source type: 0 rectilinear, 2 circular, 3 full-frame fisheye
+    double srcTX, srcTY, destTX, destTY;
+    double scale0, scale1, shear0, shear1, rot0, rot1;
+    double rad[6];
+    double mt[9];
+    double distance, horizontal, vertical;
+    // validity test of getReprojectMapAndMask (source/Warp/ZReproject.cpp:132-219)
+    int camW, camH;
+    int circ;                      // image types 2 / 3: crop rectangle and circle
+    int cropX, cropY, cropW, cropH;
+    double centx, centy, sqrDist;
+};
+
+void remapInit(const ps_photo_param& p, int canvasW, int canvasH, int camW, int camH, RemapDev& out);
+int trueNumLevels(int width, int height, int maxLevels, int minLength);
+
+cudaError_t launchGenMap(const RemapDev* dParam, int W, int H, float* xmap, float* ymap, uint8_t* cov,
+                         cudaStream_t st);
+cudaError_t launchNearestAxisSeams(const RemapDev* dParams, int n, int W, int H, const uint8_t* cov,
+                                   uint8_t* seams, cudaStream_t st);
+
+// ---- prepare-time pyramids --------------------------------------------------------
+// level 0: Wt = seam ? 256 : 0, A (0/256 scratch) = cov ? 256 : 0
+cudaError_t launchInitLevel0(const uint8_t* cov, const uint8_t* seams, int W, int H, long long maskStride,
+                             uint16_t* wt, uint16_t* a0, int pitch, long long camStride, int n,
+                             cudaStream_t st);
+// alpha chain: raw = pyrDown16SC1To32SC1(a_j); am = raw >> 8; a_{j+1} = raw ? 256 : 0
+cudaError_t launchAlphaDown(const uint16_t* aj, int sw, int sh, int spitch, long long sstride, uint16_t* am,
+                            uint16_t* anext, int dw, int dh, int dpitch, long long dstride, int n,
+                            cudaStream_t st);
+// weight chain: Wt_{j+1} = (pyrDown(Wt_j) + 128) >> 8
+cudaError_t launchWeightDown(const uint16_t* wj, int sw, int sh, int spitch, long long sstride, uint16_t* wn,
+                             int dw, int dh, int dpitch, long long dstride, int n, cudaStream_t st);
+// per-tile "any non-zero" flags of a 16-bit or 8-bit plane per camera
+cudaError_t launchTileFlags16(const uint16_t* p, int w, int h, int pitch, long long camStride, int n, int tw,
+                              int th, int tilesX, int tilesY, uint8_t* flags, cudaStream_t st);
+cudaError_t launchTileFlags8(const uint8_t* p, int w, int h, int pitch, long long camStride, int n, int tw,
+                             int th, int tilesX, int tilesY, uint8_t* flags, cudaStream_t st);
+// union coverage (0/255) and per-tile covered-pixel counts
+cudaError_t launchUnion(const uint8_t* cov, int n, int W, int H, long long maskStride, uint8_t* uni, int pitch,
+                        int tw, int th, int tilesX, int* tileCounts, unsigned long long* total,
+                        cudaStream_t st);
+// copy full-canvas maps into tile-compact float2 storage
+cudaError_t launchCompactMaps(const float* xmap, const float* ymap, int W, int H, long long maskStride,
+                              const RemapItem* items, int nitems, float2* maps, cudaStream_t st);
+// int16x4 / uint8x4 images -> uchar4 level 0, checking range and zero outside coverage
+cudaError_t launchImagesToLevel0(const void* const* images, const long long* pitches, int fmt, int n, int W,
+                                 int H, const uint8_t* cov, long long maskStride, uchar4* g0, int pitch,
+                                 long long camStride, int* status, cudaStream_t st);
+
+// ---- per-frame kernels ------------------------------------------------------------
+cudaError_t launchRemap(const Segment* segs, int nsegs, int total, cudaStream_t st);
+cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_t st);
+cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st);
+
+// ---- standalone primitive ---------------------------------------------------------
+cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,
+                                 const float* xmap, const float* ymap, long long mapPitch, int dstW, int dstH,
+                                 const uint8_t* lut, int16_t* dst, long long dstPitch, cudaStream_t st);
+
+}  // namespace ps

@@ -1,0 +1,693 @@
+// ps_rig.cpp -- prepare-time construction of a rig's resident state and the
+// launch plans that stitch frames with it.
+#include "ps_rig.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+
+namespace ps {
+
+static std::atomic<uint64_t> g_generation{1};
+
+[[noreturn]] void fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    throw Error(code, buf);
+}
+
+void checkCuda(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return;
+    cudaGetLastError();  // clear a non-sticky error
+    fail(e == cudaErrorMemoryAllocation ? PS_ENOMEM : PS_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// ---- buffers ---------------------------------------------------------------------
+void DevBuf::alloc(size_t bytes)
+{
+    reset();
+    if (!bytes) return;
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(PS_ENOMEM, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    }
+    p_ = p;
+    n_ = bytes;
+}
+
+void DevBuf::reset()
+{
+    if (p_) cudaFree(p_);
+    p_ = nullptr;
+    n_ = 0;
+}
+
+void DevBuf::zero(cudaStream_t st)
+{
+    if (p_) PS_CUDA(cudaMemsetAsync(p_, 0, n_, st));
+}
+
+void HostBuf::alloc(size_t bytes)
+{
+    reset();
+    if (!bytes) return;
+    void* p = nullptr;
+    const cudaError_t e = cudaMallocHost(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(PS_ENOMEM, "pinned allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    }
+    p_ = p;
+    n_ = bytes;
+}
+
+void HostBuf::reset()
+{
+    if (p_) cudaFreeHost(p_);
+    p_ = nullptr;
+    n_ = 0;
+}
+
+static inline int divUp(int a, int b) { return (a + b - 1) / b; }
+static inline int roundUp(int a, int b) { return divUp(a, b) * b; }
+
+// ---- Rig ---------------------------------------------------------------------------
+void Rig::clear()
+{
+    for (auto& l : lv_) { l.G.reset(); l.Wt.reset(); l.Am.reset(); l.C.reset(); }
+    maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset();
+    imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
+    hRemap_.clear();
+    covBits_.clear();
+    seamBits_.clear();
+    geom_.clear();
+    n_ = W_ = H_ = L_ = full_ = srcW_ = srcH_ = 0;
+    hasMaps_ = false;
+    inPitch_ = 0;
+    gen_ = 0;
+}
+
+void Rig::setGeometry(int n, int W, int H, int L)
+{
+    n_ = n;
+    W_ = W;
+    H_ = H;
+    L_ = L;
+    geom_.resize(L + 1);
+    int w = W, h = H;
+    for (int j = 0; j <= L; j++) {
+        geom_[j] = {w, h, roundUp(w, 64)};
+        w = (w + 1) / 2;  // getPyramidLevelSizes, source/CudaAccel/CudaMultibandBlend.cpp:486-492
+        h = (h + 1) / 2;
+    }
+}
+
+long long Rig::residentBytes() const
+{
+    long long b = 0;
+    for (const auto& l : lv_) b += l.G.bytes() + l.Wt.bytes() + l.Am.bytes() + l.C.bytes();
+    b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
+    b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
+    return b;
+}
+
+static void validateParams(const ps_photo_param* params, int n, int srcW, int srcH, int dstW, int dstH)
+{
+    if (!params || n <= 0) fail(PS_EINVAL, "no camera parameters");
+    if (n > PS_MAX_CAMS) fail(PS_EINVAL, "%d cameras, at most %d supported", n, PS_MAX_CAMS);
+    // source/Task/RicohUtil.cpp:1098-1103
+    if (!((dstW & 1) == 0 && (dstH & 1) == 0 && dstH * 2 == dstW) || dstW <= 0)
+        fail(PS_EINVAL, "dstSize (%d, %d) not qualified: width and height must be even and width == 2 * height",
+             dstW, dstH);
+    if (srcW <= 0 || srcH <= 0) fail(PS_EINVAL, "srcSize (%d, %d) must be positive", srcW, srcH);
+    for (int i = 0; i < n; i++)
+        if (params[i].image_type < 0 || params[i].image_type > 3)
+            fail(PS_EINVAL, "camera %d: image_type %d not in 0..3", i, params[i].image_type);
+}
+
+long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
+                             int dstH)
+{
+    validateParams(params, n, srcW, srcH, dstW, dstH);
+    const int L = std::max(0, trueNumLevels(dstW, dstH, blendParam, 2));
+    long long b = 0;
+    int w = dstW, h = dstH;
+    for (int j = 0; j <= L; j++) {
+        const long long px = (long long)roundUp(w, 64) * h;
+        b += px * n * (4 + 2 + (j ? 2 : 0)) + (j ? px * 8 : 0);
+        w = (w + 1) / 2;
+        h = (h + 1) / 2;
+    }
+    // maps bounded by the full canvas per camera, inputs, output, union mask
+    b += (long long)dstW * dstH * 8 * n + (long long)roundUp(srcW * 4, 256) * srcH * n + (long long)dstW * dstH * 5;
+    return b;
+}
+
+void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
+                            int dstH, const uint8_t* const* seams, cudaStream_t st)
+{
+    clear();
+    validateParams(params, n, srcW, srcH, dstW, dstH);
+    if (blendParam <= 0) fail(PS_EINVAL, "blendParam = %d, should be positive", blendParam);  // RicohUtil.cpp:1105
+    try {
+        // MIN_SIDE_LENGTH = 2, source/Task/RicohUtil.cpp:15
+        setGeometry(n, dstW, dstH, std::max(0, trueNumLevels(dstW, dstH, blendParam, 2)));
+        srcW_ = srcW;
+        srcH_ = srcH;
+        const size_t npx = (size_t)dstW * dstH;
+        DevBuf xmap(n * npx * 4), ymap(n * npx * 4), cov(n * npx), seam(n * npx);
+        std::vector<RemapDev> rp(n);
+        for (int i = 0; i < n; i++) remapInit(params[i], dstW, dstH, srcW, srcH, rp[i]);
+        DevBuf dParams(sizeof(RemapDev) * n);
+        PS_CUDA(cudaMemcpyAsync(dParams.get(), rp.data(), sizeof(RemapDev) * n, cudaMemcpyHostToDevice, st));
+        for (int i = 0; i < n; i++)
+            PS_CUDA(launchGenMap(dParams.as<RemapDev>() + i, dstW, dstH, xmap.as<float>() + i * npx,
+                                 ymap.as<float>() + i * npx, cov.as<uint8_t>() + i * npx, st));
+        if (seams) {
+            for (int i = 0; i < n; i++) {
+                if (!seams[i]) fail(PS_EINVAL, "seam mask %d is NULL", i);
+                PS_CUDA(cudaMemcpyAsync(seam.as<uint8_t>() + i * npx, seams[i], npx, cudaMemcpyHostToDevice, st));
+            }
+        } else {
+            PS_CUDA(launchNearestAxisSeams(dParams.as<RemapDev>(), n, dstW, dstH, cov.as<uint8_t>(),
+                                           seam.as<uint8_t>(), st));
+        }
+        hasMaps_ = true;
+        inPitch_ = roundUp(srcW * 4, 256);
+        inputs_.alloc((size_t)inPitch_ * srcH * n);
+        inputs_.zero(st);
+        output_.alloc(npx * 4);
+        preparePyramids(cov.as<uint8_t>(), seam.as<uint8_t>(), xmap.as<float>(), ymap.as<float>(), st);
+        PS_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        clear();
+        throw;
+    }
+}
+
+void Rig::prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* seams, int n, int W, int H,
+                           int maxLevels, int minLength, cudaStream_t st)
+{
+    clear();
+    // CudaTilingMultibandBlendFast::prepare, source/CudaAccel/CudaMultibandBlend.cpp:549-568
+    if (!masks || !seams || n <= 0) fail(PS_EINVAL, "no masks");
+    if (n > PS_MAX_CAMS) fail(PS_EINVAL, "%d masks, at most %d supported", n, PS_MAX_CAMS);
+    if (W <= 0 || H <= 0) fail(PS_EINVAL, "mask size (%d, %d) must be positive", W, H);
+    for (int i = 0; i < n; i++)
+        if (!masks[i] || !seams[i]) fail(PS_EINVAL, "mask %d is NULL", i);
+    try {
+        setGeometry(n, W, H, std::max(0, trueNumLevels(W, H, maxLevels, minLength)));
+        const size_t npx = (size_t)W * H;
+        covDev_.alloc(n * npx);
+        DevBuf seam(n * npx);
+        for (int i = 0; i < n; i++) {
+            PS_CUDA(cudaMemcpyAsync(covDev_.as<uint8_t>() + i * npx, masks[i], npx, cudaMemcpyHostToDevice, st));
+            PS_CUDA(cudaMemcpyAsync(seam.as<uint8_t>() + i * npx, seams[i], npx, cudaMemcpyHostToDevice, st));
+        }
+        output_.alloc(npx * 4);
+        imgArgs_.alloc((sizeof(void*) + sizeof(long long)) * n);
+        preparePyramids(covDev_.as<uint8_t>(), seam.as<uint8_t>(), nullptr, nullptr, st);
+        PS_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+        clear();
+        throw;
+    }
+}
+
+static void packBits(const std::vector<uint8_t>& in, std::vector<uint8_t>& out)
+{
+    out.assign((in.size() + 7) / 8, 0);
+    for (size_t i = 0; i < in.size(); i++)
+        if (in[i]) out[i >> 3] |= (uint8_t)(1u << (i & 7));
+}
+
+void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* xmap, const float* ymap,
+                          cudaStream_t st)
+{
+    const int n = n_, L = L_, W = W_, H = H_;
+    const size_t npx = (size_t)W * H;
+    // resident pyramids (zeroed: tiles outside a camera's support stay 0)
+    for (int j = 0; j <= L; j++) {
+        const LevelGeom& g = geom_[j];
+        const size_t plane = (size_t)g.pitch * g.h;
+        lv_[j].G.alloc(plane * n * 4);
+        lv_[j].G.zero(st);
+        lv_[j].Wt.alloc(plane * n * 2);
+        lv_[j].Wt.zero(st);
+        if (j > 0) {
+            lv_[j].Am.alloc(plane * n * 2);
+            lv_[j].Am.zero(st);
+            lv_[j].C.alloc(plane * 8);
+            lv_[j].C.zero(st);
+        }
+    }
+    union_.alloc((size_t)geom_[0].pitch * H);
+    union_.zero(st);
+    status_.alloc(sizeof(int));
+    status_.zero(st);
+
+    // weight and alpha pyramids (CudaMultibandBlend.cpp:586-605)
+    {
+        const size_t plane0 = (size_t)geom_[0].pitch * H;
+        DevBuf a0(plane0 * n * 2), a1(plane0 * n * 2);
+        a0.zero(st);
+        a1.zero(st);
+        PS_CUDA(launchInitLevel0(cov, seam, W, H, (long long)npx, lv_[0].Wt.as<uint16_t>(), a0.as<uint16_t>(),
+                                 geom_[0].pitch, (long long)plane0, n, st));
+        uint16_t* cur = a0.as<uint16_t>();
+        uint16_t* nxt = a1.as<uint16_t>();
+        for (int j = 0; j < L; j++) {
+            const LevelGeom& s = geom_[j];
+            const LevelGeom& d = geom_[j + 1];
+            const long long ss = (long long)s.pitch * s.h, ds = (long long)d.pitch * d.h;
+            PS_CUDA(launchAlphaDown(cur, s.w, s.h, s.pitch, ss, lv_[j + 1].Am.as<uint16_t>(), nxt, d.w, d.h, d.pitch,
+                                    ds, n, st));
+            PS_CUDA(launchWeightDown(lv_[j].Wt.as<uint16_t>(), s.w, s.h, s.pitch, ss, lv_[j + 1].Wt.as<uint16_t>(),
+                                     d.w, d.h, d.pitch, ds, n, st));
+            std::swap(cur, nxt);
+        }
+        PS_CUDA(cudaStreamSynchronize(st));
+    }
+
+    // union coverage, per level-0 blend tile counts
+    const int bX0 = divUp(W, kBlendTW), bY0 = divUp(H, kBlendTH);
+    DevBuf tileCounts((size_t)bX0 * bY0 * sizeof(int)), total(sizeof(unsigned long long));
+    total.zero(st);
+    PS_CUDA(launchUnion(cov, n, W, H, (long long)npx, union_.as<uint8_t>(), geom_[0].pitch, kBlendTW, kBlendTH, bX0,
+                        tileCounts.as<int>(), total.as<unsigned long long>(), st));
+
+    // tile activity flags
+    const int rX = divUp(W, kRemapTW), rY = divUp(H, kRemapTH);
+    DevBuf rflags((size_t)n * rX * rY);
+    if (xmap) {
+        rflags.zero(st);
+        PS_CUDA(launchTileFlags8(cov, W, H, W, (long long)npx, n, kRemapTW, kRemapTH, rX, rY, rflags.as<uint8_t>(), st));
+    }
+    std::vector<DevBuf> dflags(L + 1), bflags(L + 1);
+    for (int j = 0; j <= L; j++) {
+        const LevelGeom& g = geom_[j];
+        const long long stride = (long long)g.pitch * g.h;
+        if (j > 0) {
+            const int dX = divUp(g.w, kDownTW), dY = divUp(g.h, kDownTH);
+            dflags[j].alloc((size_t)n * dX * dY);
+            dflags[j].zero(st);
+            PS_CUDA(launchTileFlags16(lv_[j].Am.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kDownTW, kDownTH, dX, dY,
+                                      dflags[j].as<uint8_t>(), st));
+        }
+        const int bX = divUp(g.w, kBlendTW), bY = divUp(g.h, kBlendTH);
+        bflags[j].alloc((size_t)n * bX * bY);
+        bflags[j].zero(st);
+        PS_CUDA(launchTileFlags16(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kBlendTW, kBlendTH, bX, bY,
+                                  bflags[j].as<uint8_t>(), st));
+    }
+    // host copies
+    std::vector<int> hCounts((size_t)bX0 * bY0);
+    unsigned long long hTotal = 0;
+    std::vector<uint8_t> hR(xmap ? rflags.bytes() : 0);
+    std::vector<std::vector<uint8_t>> hD(L + 1), hB(L + 1);
+    PS_CUDA(cudaMemcpyAsync(hCounts.data(), tileCounts.get(), tileCounts.bytes(), cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaMemcpyAsync(&hTotal, total.get(), sizeof hTotal, cudaMemcpyDeviceToHost, st));
+    if (xmap) PS_CUDA(cudaMemcpyAsync(hR.data(), rflags.get(), hR.size(), cudaMemcpyDeviceToHost, st));
+    for (int j = 0; j <= L; j++) {
+        if (j > 0) {
+            hD[j].resize(dflags[j].bytes());
+            PS_CUDA(cudaMemcpyAsync(hD[j].data(), dflags[j].get(), hD[j].size(), cudaMemcpyDeviceToHost, st));
+        }
+        hB[j].resize(bflags[j].bytes());
+        PS_CUDA(cudaMemcpyAsync(hB[j].data(), bflags[j].get(), hB[j].size(), cudaMemcpyDeviceToHost, st));
+    }
+    std::vector<uint8_t> hCov(n * npx), hSeam(n * npx);
+    PS_CUDA(cudaMemcpyAsync(hCov.data(), cov, n * npx, cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaMemcpyAsync(hSeam.data(), seam, n * npx, cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaStreamSynchronize(st));
+    full_ = hTotal == (unsigned long long)npx;  // CudaMultibandBlend.cpp:616-617
+    packBits(hCov, covBits_);
+    packBits(hSeam, seamBits_);
+    hCov.clear();
+    hSeam.clear();
+
+    // work items
+    hRemap_.clear();
+    if (xmap) {
+        uint32_t t = 0;
+        for (int c = 0; c < n; c++)
+            for (int ty = 0; ty < rY; ty++)
+                for (int tx = 0; tx < rX; tx++)
+                    if (hR[((size_t)c * rY + ty) * rX + tx])
+                        hRemap_.push_back({(uint16_t)c, 0, (uint16_t)tx, (uint16_t)ty, t++});
+    }
+    std::vector<DownItem> down;
+    for (int j = 1; j <= L; j++) {
+        const int dX = divUp(geom_[j].w, kDownTW), dY = divUp(geom_[j].h, kDownTH);
+        downOff_[j] = (int)down.size();
+        for (int c = 0; c < n; c++)
+            for (int ty = 0; ty < dY; ty++)
+                for (int tx = 0; tx < dX; tx++)
+                    if (hD[j][((size_t)c * dY + ty) * dX + tx])
+                        down.push_back({(uint8_t)c, (uint8_t)j, (uint16_t)tx, (uint16_t)ty, 0});
+        downCnt_[j] = (int)down.size() - downOff_[j];
+    }
+    std::vector<BlendItem> blend;
+    std::vector<uint8_t> cams;
+    for (int j = 0; j <= L; j++) {
+        const LevelGeom& g = geom_[j];
+        const int bX = divUp(g.w, kBlendTW), bY = divUp(g.h, kBlendTH);
+        blendOff_[j] = (int)blend.size();
+        for (int ty = 0; ty < bY; ty++)
+            for (int tx = 0; tx < bX; tx++) {
+                const uint32_t off = (uint32_t)cams.size();
+                for (int c = 0; c < n; c++)
+                    if (hB[j][((size_t)c * bY + ty) * bX + tx]) cams.push_back((uint8_t)c);
+                uint8_t cls = 0;
+                if (j == 0) {
+                    const int tw = std::min(kBlendTW, g.w - tx * kBlendTW), th = std::min(kBlendTH, g.h - ty * kBlendTH);
+                    const int cnt = hCounts[(size_t)ty * bX0 + tx];
+                    cls = cnt == 0 ? 0 : (cnt == tw * th ? 1 : 2);
+                }
+                blend.push_back({(uint8_t)j, cls, (uint16_t)tx, (uint16_t)ty, 0, off, (uint32_t)cams.size() - off});
+            }
+        blendCnt_[j] = (int)blend.size() - blendOff_[j];
+    }
+    if (cams.empty()) cams.push_back(0);
+    dRemap_.alloc(std::max<size_t>(1, hRemap_.size()) * sizeof(RemapItem));
+    dDown_.alloc(std::max<size_t>(1, down.size()) * sizeof(DownItem));
+    dBlend_.alloc(std::max<size_t>(1, blend.size()) * sizeof(BlendItem));
+    dCams_.alloc(cams.size());
+    if (!hRemap_.empty())
+        PS_CUDA(cudaMemcpyAsync(dRemap_.get(), hRemap_.data(), hRemap_.size() * sizeof(RemapItem),
+                                cudaMemcpyHostToDevice, st));
+    if (!down.empty())
+        PS_CUDA(cudaMemcpyAsync(dDown_.get(), down.data(), down.size() * sizeof(DownItem), cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaMemcpyAsync(dBlend_.get(), blend.data(), blend.size() * sizeof(BlendItem), cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaMemcpyAsync(dCams_.get(), cams.data(), cams.size(), cudaMemcpyHostToDevice, st));
+
+    // tile-compact maps of the covered remap tiles
+    if (xmap && !hRemap_.empty()) {
+        maps_.alloc(hRemap_.size() * kRemapTW * kRemapTH * sizeof(float2));
+        PS_CUDA(launchCompactMaps(xmap, ymap, W, H, (long long)npx, dRemap_.as<RemapItem>(), (int)hRemap_.size(),
+                                  maps_.as<float2>(), st));
+    }
+
+    // device descriptor
+    RigDev d;
+    std::memset(&d, 0, sizeof d);
+    d.n = n;
+    d.L = L;
+    d.W = W;
+    d.H = H;
+    d.full = full_;
+    d.srcW = srcW_;
+    d.srcH = srcH_;
+    d.maps = maps_.as<float2>();
+    d.unionMask = union_.as<uint8_t>();
+    d.camLists = dCams_.as<uint8_t>();
+    for (int j = 0; j <= L; j++) {
+        const LevelGeom& g = geom_[j];
+        d.lv[j].w = g.w;
+        d.lv[j].h = g.h;
+        d.lv[j].pitch = g.pitch;
+        d.lv[j].camStride = (long long)g.pitch * g.h;
+        d.lv[j].G = lv_[j].G.as<uchar4>();
+        d.lv[j].Wt = lv_[j].Wt.as<uint16_t>();
+        d.lv[j].Am = lv_[j].Am.as<uint16_t>();
+        d.lv[j].C = lv_[j].C.as<short4>();
+    }
+    dDesc_.alloc(sizeof(RigDev));
+    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), &d, sizeof d, cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaStreamSynchronize(st));
+    gen_ = g_generation++;
+}
+
+void Rig::imagesToLevel0(const void* const* images, const long long* pitches, int fmt, cudaStream_t st)
+{
+    const size_t n = n_;
+    std::vector<uint8_t> args((sizeof(void*) + sizeof(long long)) * n);
+    std::memcpy(args.data(), images, sizeof(void*) * n);
+    std::memcpy(args.data() + sizeof(void*) * n, pitches, sizeof(long long) * n);
+    PS_CUDA(cudaMemcpyAsync(imgArgs_.get(), args.data(), args.size(), cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaMemsetAsync(status_.get(), 0, sizeof(int), st));
+    const LevelGeom& g = geom_[0];
+    PS_CUDA(launchImagesToLevel0(imgArgs_.as<const void* const>(),
+                                 reinterpret_cast<const long long*>(imgArgs_.as<uint8_t>() + sizeof(void*) * n), fmt,
+                                 n_, W_, H_, covDev_.as<uint8_t>(), (long long)W_ * H_, lv_[0].G.as<uchar4>(), g.pitch,
+                                 (long long)g.pitch * g.h, status_.as<int>(), st));
+    int status = 0;
+    PS_CUDA(cudaMemcpyAsync(&status, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaStreamSynchronize(st));
+    if (status & 1) fail(PS_EINVAL, "an int16 input value lies outside 0..255");
+    if (status & 2) fail(PS_EINVAL, "an input image is non-zero where its coverage mask is zero");
+}
+
+void Rig::exportState(int what, int cam, int level, void* host, long long bytes) const
+{
+    if (!ready()) fail(PS_ESTATE, "not prepared");
+    if (cam < 0 || cam >= n_) fail(PS_EINVAL, "camera %d out of range", cam);
+    const size_t npx = (size_t)W_ * H_;
+    if (what == 0 || what == 1) {
+        if (!hasMaps_) fail(PS_EINVAL, "no maps (prepared from masks)");
+        if ((size_t)bytes < npx * 4) fail(PS_EINVAL, "buffer too small");
+        float* out = static_cast<float*>(host);
+        std::fill(out, out + npx, -1.f);
+        std::vector<float2> m(hRemap_.size() * kRemapTW * kRemapTH);
+        if (!m.empty()) PS_CUDA(cudaMemcpy(m.data(), maps_.get(), m.size() * sizeof(float2), cudaMemcpyDeviceToHost));
+        for (const RemapItem& it : hRemap_) {
+            if (it.cam != cam) continue;
+            for (int k = 0; k < kRemapTW * kRemapTH; k++) {
+                const int x = it.tx * kRemapTW + (k % kRemapTW), y = it.ty * kRemapTH + (k / kRemapTW);
+                if (x < W_ && y < H_) {
+                    const float2 v = m[(size_t)it.mapTile * kRemapTW * kRemapTH + k];
+                    out[(size_t)y * W_ + x] = what == 0 ? v.x : v.y;
+                }
+            }
+        }
+        return;
+    }
+    if (what == 2 || what == 3) {
+        if ((size_t)bytes < npx) fail(PS_EINVAL, "buffer too small");
+        const std::vector<uint8_t>& bits = what == 2 ? covBits_ : seamBits_;
+        uint8_t* out = static_cast<uint8_t*>(host);
+        const size_t base = (size_t)cam * npx;
+        for (size_t i = 0; i < npx; i++) out[i] = (bits[(base + i) >> 3] >> ((base + i) & 7)) & 1 ? 255 : 0;
+        return;
+    }
+    if (what == 4 || what == 5) {
+        if (level < 0 || level > L_ || (what == 5 && level == 0)) fail(PS_EINVAL, "level %d out of range", level);
+        const LevelGeom& g = geom_[level];
+        const size_t cnt = (size_t)g.w * g.h;
+        const size_t esz = what == 4 ? 2 : 4;
+        if ((size_t)bytes < cnt * esz) fail(PS_EINVAL, "buffer too small");
+        std::vector<uint16_t> tmp(cnt);
+        const DevBuf& src = what == 4 ? lv_[level].Wt : lv_[level].Am;
+        PS_CUDA(cudaMemcpy2D(tmp.data(), g.w * 2, src.as<uint16_t>() + (size_t)cam * g.pitch * g.h, g.pitch * 2,
+                             g.w * 2, g.h, cudaMemcpyDeviceToHost));
+        if (what == 4) std::memcpy(host, tmp.data(), cnt * 2);
+        else {
+            int32_t* out = static_cast<int32_t*>(host);
+            for (size_t i = 0; i < cnt; i++) out[i] = (int32_t)tmp[i] * 256;
+        }
+        return;
+    }
+    fail(PS_EINVAL, "unknown export %d", what);
+}
+
+void Rig::exportCollapsed(int level, int16_t* host, long long bytes, cudaStream_t st) const
+{
+    if (!ready()) fail(PS_ESTATE, "not prepared");
+    if (level < 1 || level > L_) fail(PS_EINVAL, "level %d out of range 1..%d", level, L_);
+    const LevelGeom& g = geom_[level];
+    if ((size_t)bytes < (size_t)g.w * g.h * 8) fail(PS_EINVAL, "buffer too small");
+    PS_CUDA(cudaMemcpy2DAsync(host, (size_t)g.w * 8, lv_[level].C.get(), (size_t)g.pitch * 8, (size_t)g.w * 8, g.h,
+                              cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaStreamSynchronize(st));
+}
+
+// ---- Plan ---------------------------------------------------------------------------
+void Plan::dropGraph()
+{
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+}
+
+void Plan::bind(const std::vector<Rig*>& rigs)
+{
+    const int nr = (int)rigs.size();
+    int maxL = 0;
+    for (Rig* r : rigs) {
+        if (!r || !r->ready()) fail(PS_ESTATE, "render not prepared");
+        maxL = std::max(maxL, r->numLevels());
+    }
+    dropGraph();
+    rigs_ = rigs;
+    gens_.clear();
+    for (Rig* r : rigs) gens_.push_back(r->generation());
+    lutOff_.clear();
+    size_t off = sizeof(FrameDev) * nr;
+    for (Rig* r : rigs) {
+        lutOff_.push_back(off);
+        off += (size_t)r->numImages() * 768;
+    }
+    segOff_ = (off + 15) / 16 * 16;
+
+    steps_.clear();
+    segs_.clear();
+    auto addStep = [&](int kind, const std::vector<std::pair<int, std::pair<const void*, int>>>& parts) {
+        Step s{kind, (int)segs_.size(), 0, 0};
+        for (const auto& p : parts) {
+            if (p.second.second <= 0) continue;
+            // frame pointer holds the FrameDev offset until the buffer is known
+            segs_.push_back({p.second.first, rigs[p.first]->deviceDesc(),
+                             reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * p.first), p.second.second, s.total});
+            s.total += p.second.second;
+        }
+        s.nsegs = (int)segs_.size() - s.segOff;
+        if (s.total > 0) steps_.push_back(s);
+    };
+    std::vector<std::pair<int, std::pair<const void*, int>>> parts;
+    for (int r = 0; r < nr; r++) parts.push_back({r, {rigs[r]->remapItems(), rigs[r]->numRemapItems()}});
+    addStep(0, parts);
+    for (int J = 1; J <= maxL; J++) {
+        parts.clear();
+        for (int r = 0; r < nr; r++)
+            if (J <= rigs[r]->numLevels()) parts.push_back({r, {rigs[r]->downItems(J), rigs[r]->numDownItems(J)}});
+        addStep(1, parts);
+    }
+    for (int s = 0; s <= maxL; s++) {
+        parts.clear();
+        for (int r = 0; r < nr; r++) {
+            const int j = rigs[r]->numLevels() - s;
+            if (j >= 0) parts.push_back({r, {rigs[r]->blendItems(j), rigs[r]->numBlendItems(j)}});
+        }
+        addStep(2, parts);
+    }
+    const size_t need = segOff_ + std::max<size_t>(1, segs_.size()) * sizeof(Segment);
+    if (need > dArgs_.bytes()) {
+        if (stageUsed_) PS_CUDA(cudaEventSynchronize(stageDone_));
+        const size_t cap = need + need / 2;
+        dArgs_.alloc(cap);
+        stage_.alloc(cap);
+        stageUsed_ = false;
+    }
+    stageBytes_ = segOff_ + segs_.size() * sizeof(Segment);
+    const uintptr_t base = reinterpret_cast<uintptr_t>(dArgs_.get());
+    for (Segment& sg : segs_) sg.frame = reinterpret_cast<const FrameDev*>(base + reinterpret_cast<uintptr_t>(sg.frame));
+    if (!stageDone_) PS_CUDA(cudaEventCreateWithFlags(&stageDone_, cudaEventDisableTiming));
+}
+
+Plan::~Plan()
+{
+    dropGraph();
+    if (capStream_) cudaStreamDestroy(capStream_);
+    if (stageDone_) cudaEventDestroy(stageDone_);
+}
+
+bool Plan::matches(const std::vector<Rig*>& rigs) const
+{
+    if (rigs.size() != rigs_.size()) return false;
+    for (size_t i = 0; i < rigs.size(); i++)
+        if (rigs[i] != rigs_[i] || rigs[i]->generation() != gens_[i]) return false;
+    return true;
+}
+
+void Plan::launchAll(cudaStream_t st)
+{
+    const Segment* segs = reinterpret_cast<const Segment*>(static_cast<uint8_t*>(dArgs_.get()) + segOff_);
+    for (const Step& s : steps_) {
+        const Segment* p = segs + s.segOff;
+        if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, st));
+        else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, st));
+        else PS_CUDA(launchBlend(p, s.nsegs, s.total, st));
+    }
+}
+
+static int bytesPerPixel(int fmt) { return fmt == PS_FMT_BGR24 ? 3 : 4; }
+
+void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph)
+{
+    if (in.size() != rigs_.size()) fail(PS_EINVAL, "plan input count mismatch");
+    if (stageUsed_) PS_CUDA(cudaEventSynchronize(stageDone_));  // the previous staging copy has been consumed
+    uint8_t* stage = stage_.as<uint8_t>();
+    uint8_t* dArgs = dArgs_.as<uint8_t>();
+    for (size_t r = 0; r < rigs_.size(); r++) {
+        Rig* rig = rigs_[r];
+        const FrameInput& f = in[r];
+        FrameDev fd;
+        std::memset(&fd, 0, sizeof fd);
+        const int n = rig->numImages();
+        if (f.src) {
+            fd.srcFmt = f.src[0].format;
+            for (int i = 0; i < n; i++) {
+                const ps_image& s = f.src[i];
+                if (s.location == PS_MEM_HOST) {
+                    const size_t rowBytes = (size_t)s.width * bytesPerPixel(s.format);
+                    PS_CUDA(cudaMemcpy2DAsync(rig->inputBuffer(i), rig->inputPitch(), s.data, s.pitch, rowBytes,
+                                              s.height, cudaMemcpyHostToDevice, st));
+                    fd.src[i] = rig->inputBuffer(i);
+                    fd.srcPitch[i] = rig->inputPitch();
+                } else {
+                    fd.src[i] = static_cast<const uint8_t*>(s.data);
+                    fd.srcPitch[i] = s.pitch;
+                }
+            }
+        }
+        uint8_t* lut = stage + lutOff_[r];
+        if (f.luts) std::memcpy(lut, f.luts, (size_t)n * 768);
+        else
+            for (int i = 0; i < n * 3; i++)
+                for (int v = 0; v < 256; v++) lut[i * 256 + v] = (uint8_t)v;
+        fd.luts = dArgs + lutOff_[r];
+        const ps_image& d = *f.dst;
+        if (d.location == PS_MEM_HOST) {
+            fd.out = rig->outputBuffer();
+            fd.outPitch = (long long)d.width * bytesPerPixel(d.format);
+        } else {
+            fd.out = static_cast<uint8_t*>(d.data);
+            fd.outPitch = d.pitch;
+        }
+        fd.outFmt = d.format;
+        fd.status = rig->statusWord();
+        std::memcpy(stage + sizeof(FrameDev) * r, &fd, sizeof fd);
+    }
+    if (!segs_.empty()) std::memcpy(stage + segOff_, segs_.data(), segs_.size() * sizeof(Segment));
+    PS_CUDA(cudaMemcpyAsync(dArgs, stage, stageBytes_, cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaEventRecord(stageDone_, st));
+    stageUsed_ = true;
+    if (useGraph) {
+        if (!graph_) {
+            if (!capStream_) PS_CUDA(cudaStreamCreateWithFlags(&capStream_, cudaStreamNonBlocking));
+            cudaGraph_t g = nullptr;
+            PS_CUDA(cudaStreamBeginCapture(capStream_, cudaStreamCaptureModeThreadLocal));
+            try {
+                launchAll(capStream_);
+            } catch (...) {
+                cudaStreamEndCapture(capStream_, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            PS_CUDA(cudaStreamEndCapture(capStream_, &g));
+            const cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
+            cudaGraphDestroy(g);
+            PS_CUDA(e);
+        }
+        PS_CUDA(cudaGraphLaunch(graph_, st));
+    } else {
+        launchAll(st);
+    }
+    for (size_t r = 0; r < rigs_.size(); r++) {
+        const ps_image& d = *in[r].dst;
+        if (d.location == PS_MEM_HOST) {
+            const size_t rowBytes = (size_t)d.width * bytesPerPixel(d.format);
+            PS_CUDA(cudaMemcpy2DAsync(d.data, d.pitch, rigs_[r]->outputBuffer(), rowBytes, rowBytes, d.height,
+                                      cudaMemcpyDeviceToHost, st));
+        }
+    }
+}
+
+}  // namespace ps

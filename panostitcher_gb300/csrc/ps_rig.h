@@ -1,0 +1,134 @@
+// ps_rig.h -- prepared per-rig device state and the launch plans that run it.
+#pragma once
+
+#include <memory>
+
+#include "ps_internal.h"
+
+namespace ps {
+
+struct LevelGeom {
+    int w, h, pitch;
+};
+
+// One prepared rig: pyramids, weights, maps and work lists resident on the
+// device (CudaTilingMultibandBlendFast's state plus the render's maps).
+class Rig {
+public:
+    Rig() = default;
+    ~Rig() = default;
+
+    // CudaPanoramaRender2::prepare: maps + coverage from the camera
+    // parameters, seams by the nearest-axis rule unless given.
+    void prepareFromParams(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
+                           int dstH, const uint8_t* const* seams, cudaStream_t st);
+    // CudaTilingMultibandBlendFast::prepare: coverage + seam masks given.
+    void prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* seams, int n, int W, int H,
+                          int maxLevels, int minLength, cudaStream_t st);
+    void clear();
+
+    bool ready() const { return n_ > 0; }
+    int numImages() const { return n_; }
+    int numLevels() const { return L_; }
+    bool fullMask() const { return full_ != 0; }
+    int width() const { return W_; }
+    int height() const { return H_; }
+    int srcW() const { return srcW_; }
+    int srcH() const { return srcH_; }
+    bool hasMaps() const { return hasMaps_; }
+    uint64_t generation() const { return gen_; }
+    long long residentBytes() const;
+    // resident bytes a rig of this shape would hold (no allocation)
+    static long long estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH,
+                                   int dstW, int dstH);
+
+    uint8_t* inputBuffer(int cam) const { return inputs_.as<uint8_t>() + (size_t)cam * inPitch_ * srcH_; }
+    long long inputPitch() const { return inPitch_; }
+    uint8_t* outputBuffer() const { return output_.as<uint8_t>(); }
+    int* statusWord() const { return status_.as<int>(); }
+
+    void exportState(int what, int cam, int level, void* host, long long bytes) const;
+    void exportCollapsed(int level, int16_t* host, long long bytes, cudaStream_t st) const;
+
+    // building blocks of launch plans
+    const RigDev* deviceDesc() const { return dDesc_.as<RigDev>(); }
+    const RemapItem* remapItems() const { return dRemap_.as<RemapItem>(); }
+    int numRemapItems() const { return (int)hRemap_.size(); }
+    const DownItem* downItems(int level) const { return dDown_.as<DownItem>() + downOff_[level]; }
+    int numDownItems(int level) const { return downCnt_[level]; }
+    const BlendItem* blendItems(int level) const { return dBlend_.as<BlendItem>() + blendOff_[level]; }
+    int numBlendItems(int level) const { return blendCnt_[level]; }
+
+    // blender input: int16x4 / uint8x4 device images -> level 0 (checks)
+    void imagesToLevel0(const void* const* images, const long long* pitches, int fmt, cudaStream_t st);
+
+private:
+    struct LevelBufs {
+        DevBuf G, Wt, Am, C;
+    };
+    void setGeometry(int n, int W, int H, int L);
+    void preparePyramids(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
+                         cudaStream_t st);
+
+    int n_ = 0, W_ = 0, H_ = 0, L_ = 0, full_ = 0, srcW_ = 0, srcH_ = 0;
+    bool hasMaps_ = false;
+    uint64_t gen_ = 0;
+    std::vector<LevelGeom> geom_;
+    LevelBufs lv_[PS_MAX_LEVELS + 1];
+    DevBuf maps_, union_, inputs_, output_, covDev_, status_, imgArgs_;
+    long long inPitch_ = 0;
+    DevBuf dDesc_, dRemap_, dDown_, dBlend_, dCams_;
+    std::vector<RemapItem> hRemap_;
+    int downOff_[PS_MAX_LEVELS + 1] = {}, downCnt_[PS_MAX_LEVELS + 1] = {};
+    int blendOff_[PS_MAX_LEVELS + 1] = {}, blendCnt_[PS_MAX_LEVELS + 1] = {};
+    std::vector<uint8_t> covBits_, seamBits_;  // host copies for exports (1 bit / pixel)
+};
+
+// Per-frame inputs of one rig in a plan.
+struct FrameInput {
+    const ps_image* src;      // numImages images, or nullptr when level 0 is already written
+    const uint8_t* luts;      // n*768 host bytes or nullptr (identity)
+    const ps_image* dst;
+};
+
+// The launch sequence for a set of rigs: one remap launch, one pyrDown
+// launch per level, one blend launch per level; each launch runs the work
+// items of every rig (one segment per rig).  Optionally captured into a CUDA
+// graph on first run.
+class Plan {
+public:
+    Plan() = default;
+    explicit Plan(const std::vector<Rig*>& rigs) { bind(rigs); }
+    ~Plan();
+    Plan(const Plan&) = delete;
+    Plan& operator=(const Plan&) = delete;
+    // (re)build the steps for this set of rigs, reusing buffers when they fit
+    void bind(const std::vector<Rig*>& rigs);
+    // stage frame arguments, upload host inputs, run, download host outputs
+    void run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph);
+    int launchesPerRun() const { return (int)steps_.size(); }
+    bool matches(const std::vector<Rig*>& rigs) const;
+
+private:
+    struct Step {
+        int kind;  // 0 remap, 1 pyrDown, 2 blend
+        int segOff, nsegs, total;
+    };
+    void launchAll(cudaStream_t st);
+    void dropGraph();
+
+    std::vector<Rig*> rigs_;
+    std::vector<uint64_t> gens_;
+    std::vector<Step> steps_;
+    std::vector<Segment> segs_;      // frame pointers already absolute
+    std::vector<size_t> lutOff_;
+    size_t segOff_ = 0, stageBytes_ = 0;
+    DevBuf dArgs_;          // [FrameDev x nr][LUTs][Segment x nseg]
+    HostBuf stage_;         // pinned staging copy of dArgs_
+    cudaGraphExec_t graph_ = nullptr;
+    cudaStream_t capStream_ = nullptr;
+    cudaEvent_t stageDone_ = nullptr;
+    bool stageUsed_ = false;
+};
+
+}  // namespace ps

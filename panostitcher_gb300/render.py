@@ -1,0 +1,256 @@
+"""Host-side mirror of the reference's render interface over the C ABI.
+
+``CudaPanoramaRender2`` keeps the method names, argument meaning and
+bool-returning error behaviour of the reference class
+(source/Task/RicohUtil.h:193-220): ``prepare`` / ``render`` return False and
+record the reason in ``last_error`` (the reference logs it with lprintf).
+Pass ``check=True`` to raise ``PsError`` instead.
+
+Images are numpy uint8 arrays (host memory) or CUDA tensors with a
+``data_ptr()`` (device memory), shaped (H, W, 3) for BGR24 or (H, W, 4) for
+BGR32.  All work runs in libpanostitch.so; nothing here computes pixels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import PhotoParam, Image, PsError, check, lib
+
+
+def _is_device(a) -> bool:
+    return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
+
+
+def as_image(a) -> Image:
+    """ps_image view of a numpy array (host) or a CUDA tensor (device)."""
+    if _is_device(a):
+        assert a.dim() == 3 and a.shape[2] in (3, 4) and a.stride(2) == 1 and a.stride(1) == a.shape[2]
+        return Image(a.data_ptr(), a.stride(0) * a.element_size(), a.shape[1], a.shape[0],
+                     L.PS_FMT_BGR32 if a.shape[2] == 4 else L.PS_FMT_BGR24, L.PS_MEM_DEVICE)
+    assert isinstance(a, np.ndarray) and a.dtype == np.uint8 and a.ndim == 3 and a.shape[2] in (3, 4)
+    assert a.strides[2] == 1 and a.strides[1] == a.shape[2]
+    return Image(a.ctypes.data, a.strides[0], a.shape[1], a.shape[0],
+                 L.PS_FMT_BGR32 if a.shape[2] == 4 else L.PS_FMT_BGR24, L.PS_MEM_HOST)
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return None
+    return getattr(stream, "cuda_stream", stream)
+
+
+def _params(params: Sequence[dict]):
+    arr = (PhotoParam * len(params))(*[PhotoParam.from_dict(p) for p in params])
+    return arr
+
+
+def _luts_arg(luts, n):
+    if luts is None:
+        return None, 0, None
+    a = np.ascontiguousarray(luts, dtype=np.uint8)
+    if a.size % 768:
+        return a, -1, None
+    return a, a.size // 768, a.ctypes.data
+
+
+class CudaPanoramaRender2:
+    """CudaPanoramaRender2 (source/Task/RicohUtil.h:193-220) over libpanostitch."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().ps_render_create(C.byref(h)))
+        self._h = h
+        self.last_error = ""
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().ps_render_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def _status(self, status: int, check_: bool) -> bool:
+        if status == L.PS_OK:
+            return True
+        self.last_error = lib().ps_last_error().decode(errors="replace")
+        if check_:
+            raise PsError(status, self.last_error)
+        return False
+
+    # -- reference methods -------------------------------------------------
+    def prepare(self, params: Sequence[dict], high_quality_blend: int, blend_param: int, src_size, dst_size,
+                seams=None, stream=None, check: bool = False) -> bool:
+        """prepare(params, highQualityBlend, blendParam, srcSize, dstSize); sizes are (w, h)."""
+        arr = _params(params)
+        if seams is None:
+            st = lib().ps_render_prepare(self._h, arr, len(params), high_quality_blend, blend_param,
+                                         src_size[0], src_size[1], dst_size[0], dst_size[1],
+                                         _stream_handle(stream))
+        else:
+            ms = [np.ascontiguousarray(m, np.uint8) for m in seams]
+            ptrs = (C.c_void_p * len(ms))(*[m.ctypes.data for m in ms])
+            st = lib().ps_render_prepare_with_seams(self._h, arr, len(params), high_quality_blend, blend_param,
+                                                    src_size[0], src_size[1], dst_size[0], dst_size[1], ptrs,
+                                                    _stream_handle(stream))
+        return self._status(st, check)
+
+    def render(self, src: Sequence, dst, luts=None, stream=None, check: bool = False) -> bool:
+        """render(src, dst, luts): src frames -> dst canvas (both host or device)."""
+        imgs = (Image * len(src))(*[as_image(s) for s in src])
+        keep, nl, lp = _luts_arg(luts, len(src))
+        d = as_image(dst)
+        st = lib().ps_render_render(self._h, imgs, len(src), lp, nl, C.byref(d), _stream_handle(stream))
+        del keep
+        return self._status(st, check)
+
+    def clear(self) -> None:
+        lib().ps_render_clear(self._h)
+
+    def getNumImages(self) -> int:
+        return lib().ps_render_get_num_images(self._h)
+
+    # -- extras ----------------------------------------------------------------
+    @property
+    def num_levels(self) -> int:
+        return lib().ps_render_get_num_levels(self._h)
+
+    @property
+    def full_mask(self) -> bool:
+        return bool(lib().ps_render_is_full_mask(self._h))
+
+    @property
+    def resident_bytes(self) -> int:
+        return lib().ps_render_resident_bytes(self._h)
+
+    def set_graph(self, enabled: bool) -> None:
+        check(lib().ps_render_set_graph(self._h, int(bool(enabled))))
+
+    def input_buffer(self, cam: int):
+        p, pitch = C.c_void_p(), C.c_longlong()
+        check(lib().ps_render_get_input_buffer(self._h, cam, C.byref(p), C.byref(pitch)))
+        return p.value, pitch.value
+
+    def export(self, what: int, cam: int, level: int, shape, dtype) -> np.ndarray:
+        out = np.empty(shape, dtype)
+        check(lib().ps_render_export(self._h, what, cam, level, out.ctypes.data, out.nbytes))
+        return out
+
+    def maps(self, cam: int, dst_size):
+        W, H = dst_size
+        return (self.export(L.EXPORT_XMAP, cam, 0, (H, W), np.float32),
+                self.export(L.EXPORT_YMAP, cam, 0, (H, W), np.float32))
+
+    def coverage(self, cam: int, dst_size) -> np.ndarray:
+        return self.export(L.EXPORT_COVERAGE, cam, 0, (dst_size[1], dst_size[0]), np.uint8)
+
+    def seam(self, cam: int, dst_size) -> np.ndarray:
+        return self.export(L.EXPORT_SEAM, cam, 0, (dst_size[1], dst_size[0]), np.uint8)
+
+    def collapsed(self, level: int, size) -> np.ndarray:
+        w, h = size
+        out = np.empty((h, w, 4), np.int16)
+        check(lib().ps_render_export_collapsed(self._h, level, out.ctypes.data, out.nbytes, None))
+        return out
+
+
+def render_batch(renders: Sequence[CudaPanoramaRender2], srcs: Sequence[Sequence], dsts: Sequence,
+                 luts: Sequence | None = None, stream=None) -> None:
+    """One launch sequence for several rigs (one frame each)."""
+    k = len(renders)
+    hs = (C.c_void_p * k)(*[r._h.value for r in renders])
+    arrays = [(Image * len(s))(*[as_image(x) for x in s]) for s in srcs]
+    sp = (C.POINTER(Image) * k)(*[C.cast(a, C.POINTER(Image)) for a in arrays])
+    keep = []
+    lp = None
+    if luts is not None:
+        ptrs = []
+        for lt in luts:
+            if lt is None:
+                ptrs.append(None)
+            else:
+                a = np.ascontiguousarray(lt, np.uint8)
+                keep.append(a)
+                ptrs.append(a.ctypes.data)
+        lp = (C.c_void_p * k)(*ptrs)
+    ds = (Image * k)(*[as_image(d) for d in dsts])
+    check(lib().ps_render_batch(hs, k, sp, lp, ds, _stream_handle(stream)))
+
+
+class CudaTilingMultibandBlendFast:
+    """CudaTilingMultibandBlendFast (source/CudaAccel/CudaInterface.h:45-82)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().ps_blender_create(C.byref(h)))
+        self._h = h
+        self.last_error = ""
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().ps_blender_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def prepare(self, masks, seams, max_levels: int, min_length: int = 2, stream=None) -> bool:
+        ms = [np.ascontiguousarray(m, np.uint8) for m in masks]
+        ss = [np.ascontiguousarray(s, np.uint8) for s in seams]
+        H, W = ms[0].shape
+        mp = (C.c_void_p * len(ms))(*[m.ctypes.data for m in ms])
+        sp = (C.c_void_p * len(ss))(*[s.ctypes.data for s in ss])
+        st = lib().ps_blender_prepare(self._h, mp, sp, len(ms), W, H, max_levels, min_length,
+                                      _stream_handle(stream))
+        if st != L.PS_OK:
+            self.last_error = lib().ps_last_error().decode(errors="replace")
+            return False
+        return True
+
+    def blend(self, images, dst, stream=None, check_: bool = True) -> bool:
+        """images: CUDA int16 (H, W, 4) or uint8 (H, W, 4) tensors."""
+        fmt = 16 if images[0].element_size() == 2 else 8
+        ptrs = (C.c_void_p * len(images))(*[t.data_ptr() for t in images])
+        pitches = (C.c_longlong * len(images))(*[t.stride(0) * t.element_size() for t in images])
+        d = as_image(dst)
+        st = lib().ps_blender_blend(self._h, ptrs, pitches, fmt, C.byref(d), _stream_handle(stream))
+        if st != L.PS_OK:
+            self.last_error = lib().ps_last_error().decode(errors="replace")
+            if check_:
+                raise PsError(st, self.last_error)
+            return False
+        return True
+
+    @property
+    def num_levels(self) -> int:
+        return lib().ps_blender_get_num_levels(self._h)
+
+
+def generate_reproject_map_and_mask(param: dict, src_size, dst_size, xmap, ymap, mask, stream=None) -> None:
+    """cudaGenerateReprojectMapAndMask into CUDA tensors (float32, float32, uint8; (H, W))."""
+    p = PhotoParam.from_dict(param)
+    check(lib().ps_generate_reproject_map_and_mask(C.byref(p), src_size[0], src_size[1], dst_size[0],
+                                                   dst_size[1], xmap.data_ptr(), ymap.data_ptr(),
+                                                   mask.data_ptr(), _stream_handle(stream)))
+
+
+def reproject_to_16s(src, xmap, ymap, dst, lut=None, stream=None) -> None:
+    """cudaTransform + cudaReprojectTo16S: CUDA tensors in, int16 (H, W, 4) out."""
+    s = as_image(src)
+    H, W = xmap.shape
+    check(lib().ps_reproject_to_16s(C.byref(s), xmap.data_ptr(), ymap.data_ptr(), xmap.stride(0) * 4, W, H,
+                                    None if lut is None else lut.data_ptr(), dst.data_ptr(),
+                                    dst.stride(0) * dst.element_size(), _stream_handle(stream)))
+
+
+def get_lut(k: float) -> np.ndarray:
+    """getLUT (source/Blend/ExposureColorOptimize.cpp:1217-1223)."""
+    out = np.empty(256, np.uint8)
+    check(lib().ps_get_lut(float(k), out.ctypes.data))
+    return out

@@ -1,0 +1,98 @@
+"""The C ABI library: builds, loads, exports every declared entry point, and
+rejects bad arguments before touching the GPU (CPU only)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import panostitcher_gb300 as P
+from panostitcher_gb300 import _lib as L
+from panostitcher_gb300 import synth as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(ps_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    decl = declared_functions()
+    assert len(decl) >= 25
+    missing = [n for n in sorted(decl) if not hasattr(built_lib, n)]
+    assert not missing, missing
+    # the Python bindings cover the whole ABI
+    assert decl <= set(L.exported_symbols())
+
+
+def test_version_and_empty_error(built_lib):
+    assert b"sm_103a" in built_lib.ps_version()
+
+
+def test_get_lut_host_path(built_lib):
+    assert np.array_equal(P.get_lut(1.0), np.arange(256))
+    assert np.array_equal(P.get_lut(1.17), S.lut_from_gain(1.17))
+    with pytest.raises(P.PsError) as e:
+        P.get_lut(0.0)
+    assert e.value.code == L.PS_EINVAL
+
+
+def _prepare_err(**kw):
+    r = P.CudaPanoramaRender2()
+    cfg = S.rig("c1")
+    args = dict(params=cfg.cams, high_quality_blend=1, blend_param=5, src_size=cfg.src_size,
+                dst_size=cfg.dst_size)
+    args.update(kw)
+    ok = r.prepare(args["params"], args["high_quality_blend"], args["blend_param"], args["src_size"],
+                   args["dst_size"])
+    assert not ok
+    assert r.getNumImages() == 0
+    return r.last_error
+
+
+def test_prepare_preconditions_like_reference(built_lib):
+    # dstSize must be even with width == 2 * height (source/Task/RicohUtil.cpp:1098-1103)
+    assert "not qualified" in _prepare_err(dst_size=(2048, 1000))
+    assert "not qualified" in _prepare_err(dst_size=(2047, 1024 - 0))
+    # blendParam > 0 (:1105-1109)
+    assert "positive" in _prepare_err(blend_param=0)
+    assert "camera" in _prepare_err(params=[])
+    assert "image_type" in _prepare_err(params=[S.photo_param(7, 90.0)])
+    assert "high_quality_blend" in _prepare_err(high_quality_blend=0)
+    assert "srcSize" in _prepare_err(src_size=(0, 10))
+
+
+def test_render_before_prepare_fails(built_lib):
+    r = P.CudaPanoramaRender2()
+    dst = np.zeros((8, 16, 4), np.uint8)
+    assert not r.render([np.zeros((4, 4, 4), np.uint8)], dst)
+    assert "prepare" in r.last_error
+    with pytest.raises(P.PsError) as e:
+        r.render([np.zeros((4, 4, 4), np.uint8)], dst, check=True)
+    assert e.value.code == L.PS_ESTATE
+
+
+def test_blender_prepare_validation(built_lib):
+    b = P.CudaTilingMultibandBlendFast()
+    h = C.c_void_p()
+    assert built_lib.ps_blender_prepare(b._h, None, None, 0, 8, 8, 3, 2, None) == L.PS_EINVAL
+    assert built_lib.ps_blender_blend(b._h, None, None, 16, None, None) == L.PS_ESTATE
+    assert b.num_levels == 0
+
+
+def test_null_handles_are_rejected(built_lib):
+    assert built_lib.ps_render_create(None) == L.PS_EINVAL
+    assert built_lib.ps_render_get_num_images(None) == 0
+    built_lib.ps_render_destroy(None)
+    built_lib.ps_blender_destroy(None)
+    assert built_lib.ps_render_batch(None, 0, None, None, None, None) == L.PS_EINVAL

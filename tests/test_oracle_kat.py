@@ -1,0 +1,176 @@
+"""Known-answer tests pinning the CPU oracle's restatement (CPU only).
+
+The reference ships no golden vectors, so these pin the oracle by
+properties its cited code must have: exact border index formulas, constant
+images through the filters, the single-camera identity of the multiband
+blend, round-half-even LUTs, and the geometry invariants.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from panostitcher_gb300 import synth as S
+
+
+def test_num_levels_matches_getTrueNumLevels(oracle_lib):
+    # min(maxLevels<=16, floor(log2(W/2)), floor(log2(H/2)))
+    assert O.num_levels(4096, 2048, 8) == 8
+    assert O.num_levels(2048, 1024, 5) == 5
+    assert O.num_levels(7680, 3840, 10) == 10
+    assert O.num_levels(64, 32, 16) == 4
+    assert O.num_levels(3, 2, 4) == 0
+    assert O.num_levels(7680, 3840, 100) == 10   # floor(log2(3840 / 2))
+
+
+def test_pyr_down_constant_and_borders(oracle_lib):
+    for (h, w) in [(8, 8), (7, 9), (2, 3), (1, 5), (33, 65)]:
+        a = np.full((h, w), 256, np.int16)
+        s = O.pyr_down_16sc1_to_32sc1(a)
+        assert (s == 256 * 256).all()
+        assert (O.pyr_down_16sc1_to_16sc1(a) == 256).all()
+
+
+def test_pyr_down_wrap_columns(oracle_lib):
+    # a single bright column at x=0 leaks into the last output column via the horizontal wrap
+    a = np.zeros((8, 16), np.int16)
+    a[:, 0] = 256
+    s = O.pyr_down_16sc1_to_32sc1(a)
+    assert s[2, 0] == 6 * 256 * 16          # centre tap 6, column weights sum 16
+    assert s[2, 7] == 1 * 256 * 16          # x = 2*7+2 = 16 wraps to column 0
+
+
+def test_pyr_down_reflect101_rows(oracle_lib):
+    a = np.zeros((8, 8), np.int16)
+    a[1, :] = 256                           # row 1 is row -1's reflection
+    s = O.pyr_down_16sc1_to_32sc1(a)
+    assert s[0, 3] == (4 + 4) * 256 * 16    # taps -1 (-> 1) and +1 with weight 4 each
+
+
+def test_masked_pyr_down_is_floor_of_weighted_mean(oracle_lib):
+    rng = np.random.default_rng(0)
+    img = rng.integers(0, 256, (10, 12, 4)).astype(np.int16)
+    img[..., 3] = 0
+    scale = np.full((5, 6), 256 * 256, np.int32)
+    out = O.pyr_down_16sc4_masked(img, scale)
+    ref = O.pyr_down_16sc1_to_32sc1(np.ascontiguousarray(img[..., 0]))
+    assert np.array_equal(out[..., 0], ref * 256 // (256 * 256))
+    zero = O.pyr_down_16sc4_masked(img, np.zeros((5, 6), np.int32))
+    assert (zero == 0).all()
+
+
+def test_pyr_up_constant(oracle_lib):
+    for (h, w) in [(4, 4), (3, 5), (1, 1), (7, 2)]:
+        a = np.zeros((h, w, 4), np.int16)
+        a[..., :3] = 200
+        for dsz in [(2 * w, 2 * h), (max(1, 2 * w - 1), max(1, 2 * h - 1))]:
+            u = O.pyr_up_16sc4(a, dsz)
+            assert (u[..., :3] == 200).all()
+        b = np.zeros((h, w, 4), np.int32)
+        b[..., :3] = -77
+        assert (O.pyr_up_32sc4(b, (2 * w, 2 * h))[..., :3] == -77).all()
+
+
+def test_blend_single_camera_identity(oracle_lib):
+    rng = np.random.default_rng(3)
+    for (H, W) in [(64, 128), (37, 91)]:
+        img = rng.integers(0, 256, (H, W, 4)).astype(np.int16)
+        img[..., 3] = 0
+        mk = np.full((1, H, W), 255, np.uint8)
+        b = O.Blender(mk, mk, 16)
+        assert b.full_mask
+        out = b.blend([img])
+        assert np.array_equal(out[..., :3], img[..., :3].astype(np.uint8))
+
+
+def test_blend_constant_images(oracle_lib):
+    H, W = 48, 96
+    cov = np.zeros((2, H, W), np.uint8)
+    cov[0][:, :60] = 255
+    cov[1][:, 40:] = 255
+    seams = np.zeros_like(cov)
+    seams[0][:, :50] = 255
+    seams[1][:, 50:] = 255
+    b = O.Blender(cov, seams, 4)
+    imgs = []
+    for i in range(2):
+        im = np.zeros((H, W, 4), np.int16)
+        im[cov[i] > 0, :3] = 123
+        imgs.append(im)
+    out = b.blend(imgs)
+    assert (out[..., :3] == 123).all()
+
+
+def test_blend_uncovered_pixels_are_zero(oracle_lib):
+    H, W = 32, 64
+    cov = np.zeros((1, H, W), np.uint8)
+    cov[0][:, :40] = 255
+    b = O.Blender(cov, cov, 3)
+    assert not b.full_mask
+    im = np.zeros((H, W, 4), np.int16)
+    im[:, :40, :3] = 90
+    out = b.blend([im])
+    assert (out[:, 40:, :3] == 0).all()
+    assert (out[:, :40, :3] == 90).all()
+
+
+def test_lut_round_half_even(oracle_lib):
+    l = O.get_lut(0.5)
+    assert l[1] == 0 and l[3] == 2 and l[5] == 2 and l[255] == 128   # 0.5, 1.5, 2.5, 127.5
+    assert np.array_equal(O.get_lut(1.0), np.arange(256))
+    assert O.get_lut(2.0)[200] == 255
+    for k in (0.8, 1.17, 1.3):
+        assert np.array_equal(O.get_lut(k), S.lut_from_gain(k))
+
+
+def test_bilinear_integer_coordinates_copy(oracle_lib):
+    rng = np.random.default_rng(5)
+    src = rng.integers(0, 256, (20, 30, 4)).astype(np.uint8)
+    yy, xx = np.mgrid[0:20, 0:30].astype(np.float32)
+    out = O.reproject_16s(src, xx, yy)
+    assert np.array_equal(out[..., :3], src[..., :3].astype(np.int16))
+    lut = np.stack([np.arange(256)[::-1]] * 3).astype(np.uint8)
+    inv = O.reproject_16s(src, xx, yy, lut)
+    assert np.array_equal(inv[..., :3], 255 - src[..., :3].astype(np.int16))
+
+
+def test_bilinear_half_pixel_round_half_even(oracle_lib):
+    src = np.zeros((2, 4, 3), np.uint8)
+    src[0, :, 0] = [1, 2, 10, 11]
+    xm = np.array([[0.5, 2.5]], np.float32)
+    ym = np.zeros((1, 2), np.float32)
+    out = O.reproject_16s(src, xm, ym)
+    assert out[0, 0, 0] == 2 and out[0, 1, 0] == 10     # 1.5 -> 2, 10.5 -> 10
+
+
+def test_maps_invalid_sentinel_and_mask(oracle_lib):
+    cfg = S.scaled_rig(S.rig("c2"), 16)
+    xm, ym, mk = O.reproject_map(cfg.cams[0], cfg.src_size, cfg.dst_size)
+    assert ((xm == -1) == (mk == 0)).all() and ((ym == -1) == (mk == 0)).all()
+    v = mk > 0
+    assert (xm[v] >= 0).all() and (xm[v] < cfg.src_size[0]).all()
+    # the yaw-0 rectilinear camera is centred on the canvas centre
+    W, H = cfg.dst_size
+    cx, cy = xm[H // 2, W // 2], ym[H // 2, W // 2]
+    assert abs(cx - cfg.src_size[0] / 2) < 1.0 and abs(cy - cfg.src_size[1] / 2) < 1.0
+
+
+def test_nearest_axis_seams_partition(oracle_lib):
+    cfg = S.scaled_rig(S.rig("c2"), 16)
+    cov = np.stack([O.reproject_map(c, cfg.src_size, cfg.dst_size)[2] for c in cfg.cams])
+    seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov)
+    assert ((seams > 0) <= (cov > 0)).all()
+    assert ((seams > 0).sum(0) == (cov.max(0) > 0)).all()
+    # the c2 rig leaves gaps between the side ring and the pole cameras
+    assert not (cov.max(0) > 0).all()
+
+
+def test_render_mt_equals_st(oracle_lib):
+    cfg = S.scaled_rig(S.rig("c1"), 8)
+    maps = [O.reproject_map(c, cfg.src_size, cfg.dst_size) for c in cfg.cams]
+    cov = np.stack([m[2] for m in maps])
+    seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov)
+    b = O.Blender(cov, seams, cfg.levels)
+    fr = S.FrameSource(cfg).frame(0)
+    a = b.render(fr, S.luts(cfg), [m[0] for m in maps], [m[1] for m in maps], 1)
+    c = b.render(fr, S.luts(cfg), [m[0] for m in maps], [m[1] for m in maps], 3)
+    assert np.array_equal(a, c)
