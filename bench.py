@@ -1,0 +1,497 @@
+#!/usr/bin/env python
+"""Benchmark of the panorama stitch path on GB300.
+
+Headline: stitched output Mpix/s of the plain per-frame path on the
+6-camera rig (6 x 1920x1080 rectilinear, 100 deg -> 4096x2048 equirect,
+8-level multiband blend, per-camera LUT gains), frames resident in HBM.
+The same line carries:
+  e2e         the same metric through the C ABI with pinned host frames in
+              and the host canvas out (H2D + D2H inside the timed region);
+  roofline    the dominant kernel's algorithmic GB/s against the measured
+              HBM copy bandwidth (CUDA events around every launch of a
+              profiled pass over the same workload);
+  batched     four rigs of uneven size per launch sequence (CUDA graph);
+  serve       16 live streams over those rigs, Poisson 30 fps arrivals,
+              continuous batching: p50 / p99 frame latency and Mpix/s;
+  cpu_baseline  the CPU restatement of the reference path on the host cores.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Under torchrun each rank stitches its own replica on its own GPU (weak
+scaling, no collective on the data path); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "stitched output Mpix/s at 4096x2048 (6 cams); p50/p99 frame latency in serve loop"
+WORKLOAD = "6x rectilinear 1920x1080 (100 deg hfov; yaw 0/90/180/270, pitch +-90) -> 4096x2048 equirect, " \
+           "8-level integer multiband blend, per-camera per-channel LUT gains U[0.8,1.2]"
+
+
+# ----------------------------------------------------------------------------- distributed
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world, use_cuda):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("nccl" if use_cuda else "gloo")
+    return dist
+
+
+def reduce_max(value: float, dist=None, device=None) -> float:
+    """Max of a float over all ranks (identity without a process group)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist=None):
+    if dist is not None:
+        dist.barrier()
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms during a timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        loaded = [r[0] for r in rows if r[2] > 200.0] or [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(r[2] for r in rows)}
+
+
+# ----------------------------------------------------------------------------- helpers
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def pinned_copy(a: np.ndarray):
+    import torch
+    t = torch.empty(a.shape, dtype=torch.uint8, pin_memory=True)
+    arr = t.numpy()
+    arr[...] = a
+    return arr, t
+
+
+# ----------------------------------------------------------------------------- our arm
+def run_ours(args, world, rank, local, dist):
+    import torch
+    import panostitcher_gb300 as P
+    from panostitcher_gb300 import build as B
+    from panostitcher_gb300 import synth as S
+
+    B.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg = S.rig("c2")
+    W, H = cfg.dst_size
+    npx = W * H
+    r = P.CudaPanoramaRender2()
+    t = time.perf_counter()
+    r.prepare(cfg.cams, 1, cfg.levels, cfg.src_size, cfg.dst_size, check=True)
+    prepare_s = time.perf_counter() - t
+    fs = S.FrameSource(cfg)
+    pool_host = [fs.frame(k) for k in range(args.pool)]
+    pool_dev = [[torch.from_numpy(f).to(dev) for f in fr] for fr in pool_host]
+    luts = S.luts(cfg)
+    dst = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+
+    # ---- device-resident throughput (CUDA graph per frame)
+    for k in range(args.warmup):
+        r.render(pool_dev[k % args.pool], dst, luts, check=True)
+    torch.cuda.synchronize()
+    barrier(dist)
+    sampler = ClockSampler(local)
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for k in range(args.steps):
+        r.render(pool_dev[k % args.pool], dst, luts, check=True)
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    ms_max = reduce_max(ms, dist, dev)
+    barrier(dist)
+    value = world * args.steps * npx / (ms_max / 1e3) / 1e6
+    out = {"metric": METRIC, "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 5), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
+           "data": f"synthetic: seeded smooth field + per-frame noise, pool of {args.pool} frames in HBM",
+           "gpu_launches": args.steps * r.launches_per_frame,
+           "clocks": clocks}
+    resident = r.resident_bytes
+    out["config"] = {"workload": WORKLOAD, "canvas": [W, H], "cams": cfg.num_cams, "src": list(cfg.src_size),
+                     "levels": r.num_levels, "full_mask": r.full_mask,
+                     "l2": f"inputs larger than L2: {args.pool} distinct 49.8 MB frames cycled, rig state "
+                           f"{resident / 1e6:.0f} MB resident", "parallelism": f"replicas x{world}",
+                     "prepare_s": round(prepare_s, 3)}
+
+    # ---- e2e: pinned host frames in, host canvas out, through the C ABI
+    pinned = []
+    keep = []
+    for fr in pool_host:
+        cams = []
+        for f in fr:
+            a, tt = pinned_copy(f)
+            cams.append(a)
+            keep.append(tt)
+        pinned.append(cams)
+    hdst, hdst_t = pinned_copy(np.zeros((H, W, 4), np.uint8))
+    e2e_steps = args.e2e_steps or args.steps
+    for k in range(2):
+        r.render(pinned[k % args.pool], hdst, luts, check=True)
+    torch.cuda.synchronize()
+    barrier(dist)
+    t = time.perf_counter()
+    for k in range(e2e_steps):
+        r.render(pinned[k % args.pool], hdst, luts, check=True)
+    torch.cuda.synchronize()
+    e2e_s = reduce_max(time.perf_counter() - t, dist, dev)
+    out["e2e"] = {"value": round(world * e2e_steps * npx / e2e_s / 1e6, 3), "unit": "Mpix/s",
+                  "h2d_bytes_per_step": int(sum(f.nbytes for f in pinned[0])),
+                  "d2h_bytes_per_step": int(hdst.nbytes), "steps": e2e_steps,
+                  "path": "ps_render_render, pinned BGR32 host frames -> pinned BGR32 host canvas"}
+
+    # ---- roofline: profiled pass (a CUDA event pair around every launch)
+    r.profile(True)
+    prof_steps = min(args.steps, 30)
+    for k in range(prof_steps):
+        r.render(pool_dev[k % args.pool], dst, luts, check=True)
+    torch.cuda.synchronize()
+    kernels = {}
+    total_ms = 0.0
+    for kind, name in r.KERNELS.items():
+        n, kms, kb = r.profile_read(kind)
+        kernels[name] = {"launches_per_frame": n // prof_steps, "ms_per_frame": kms / prof_steps,
+                         "alg_bytes_per_launch": kb / max(n, 1), "gbs": kb / max(kms, 1e-9) / 1e6}
+        total_ms += kms
+    r.profile(False)
+    for k in kernels.values():
+        k["share"] = round(k["ms_per_frame"] * prof_steps / max(total_ms, 1e-9), 4)
+    dom = max(kernels, key=lambda k: kernels[k]["ms_per_frame"])
+    peak, peak_src = measured_peak()
+    achieved = kernels[dom]["gbs"]
+    traffic = ncu_traffic(dom)
+    out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                       "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                       "traffic": traffic,
+                       "alg_bytes_per_launch": round(kernels[dom]["alg_bytes_per_launch"]),
+                       "frame_alg_bytes": round(r.algorithmic_bytes(4, 4)),
+                       "frame_alg_gbs": round(r.algorithmic_bytes(4, 4) / (ms_max / args.steps) / 1e6, 1)}
+    out["kernels"] = {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                      for k, v in kernels.items()}
+
+    def guarded(fn, *a):
+        try:
+            return fn(*a)
+        except Exception as e:  # an extra leg failing must not lose the headline line
+            return {"error": f"{type(e).__name__}: {e}"}
+
+    if world == 1 and not args.no_batched:
+        out["batched"] = guarded(run_batched, args, dev)
+    if world == 1 and not args.no_serve:
+        out["serve"] = guarded(run_serve, args, dev)
+    if world == 1 and rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = guarded(cpu_baseline, r, cfg, pool_host, luts, args.cpu_seconds)
+    return out
+
+
+def run_batched(args, dev):
+    """Four rigs of uneven size (c3a..c3d) in one launch sequence per tick."""
+    import torch
+    import panostitcher_gb300 as P
+    from panostitcher_gb300 import synth as S
+    names = ["c3a", "c3b", "c3c", "c3d"]
+    cfgs = [S.rig(n) for n in names]
+    renders, pools, luts, dsts = [], [], [], []
+    for c in cfgs:
+        r = P.CudaPanoramaRender2()
+        r.prepare(c.cams, 1, c.levels, c.src_size, c.dst_size, check=True)
+        renders.append(r)
+        fs = S.FrameSource(c)
+        pools.append([[torch.from_numpy(f).to(dev) for f in fs.frame(k)] for k in range(2)])
+        luts.append(S.luts(c))
+        dsts.append(torch.empty((c.dst_size[1], c.dst_size[0], 4), dtype=torch.uint8, device=dev))
+    px = sum(c.canvas_pixels for c in cfgs)
+    steps = max(5, args.steps // 2)
+    res = {"rigs": {n: f"{c.num_cams}x{c.src_size[0]}x{c.src_size[1]} -> {c.dst_size[0]}x{c.dst_size[1]}, "
+                       f"{r.num_levels} levels" for n, c, r in zip(names, cfgs, renders)}, "steps": steps}
+    # batched: one captured graph over all four rigs
+    for k in range(3):
+        P.render_batch(renders, [p[k % 2] for p in pools], dsts, luts)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(steps):
+        P.render_batch(renders, [p[k % 2] for p in pools], dsts, luts)
+    e1.record()
+    torch.cuda.synchronize()
+    bms = e0.elapsed_time(e1)
+    # plain per-frame path on the same rigs: one render per rig per tick, individual launches
+    for r in renders:
+        r.set_graph(False)
+    for k in range(3):
+        for r, p, lt, d in zip(renders, pools, luts, dsts):
+            r.render(p[k % 2], d, lt, check=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for k in range(steps):
+        for r, p, lt, d in zip(renders, pools, luts, dsts):
+            r.render(p[k % 2], d, lt, check=True)
+    e1.record()
+    torch.cuda.synchronize()
+    pms = e0.elapsed_time(e1)
+    res.update({"mpix_s": round(steps * px / (bms / 1e3) / 1e6, 1),
+                "plain_mpix_s": round(steps * px / (pms / 1e3) / 1e6, 1),
+                "ms_per_tick": round(bms / steps, 4), "plain_ms_per_tick": round(pms / steps, 4),
+                "speedup_vs_plain": round(pms / bms, 3)})
+    return res
+
+
+def run_serve(args, dev, seconds=None):
+    """16 live streams over the four batched rigs; Poisson 30 fps arrivals."""
+    from panostitcher_gb300 import synth as S
+    from panostitcher_gb300.serve import StitchServer
+    seconds = seconds or args.serve_seconds
+    names = ["c3a", "c3b", "c3c", "c3d"]
+    cfgs = {n: S.rig(n) for n in names}
+    rng = np.random.default_rng(2024)
+    assign = [names[i] for i in rng.integers(0, 4, 16)]
+    srv = StitchServer(int(120e9), max_batch=16)
+    try:
+        t = time.perf_counter()
+        ids = [srv.admit(cfgs[n].cams, cfgs[n].levels, cfgs[n].src_size, cfgs[n].dst_size) for n in assign]
+        admit_s = time.perf_counter() - t
+        # one pool of two pinned frames per rig type, shared by its streams
+        keep, frames = [], {}
+        for n in names:
+            fs = S.FrameSource(cfgs[n])
+            frames[n] = []
+            for k in range(2):
+                cams = []
+                for f in fs.frame(k):
+                    a, tt = pinned_copy(f)
+                    keep.append(tt)
+                    cams.append(a)
+                frames[n].append(cams)
+        luts = {n: np.ascontiguousarray(S.luts(cfgs[n])) for n in names}
+        events = []
+        for n, sid in zip(assign, ids):
+            if sid is None:
+                continue
+            t = rng.uniform(0, 1 / 30)
+            k = 0
+            while t < seconds:
+                events.append((t, sid, n, k))
+                t += rng.exponential(1 / 30)
+                k += 1
+        events.sort()
+        lat, wall = srv.run_trace([e[1] for e in events], [e[0] for e in events],
+                                  [frames[e[2]][e[3] % 2] for e in events], [luts[e[2]] for e in events], None)
+        lat_ms = lat * 1e3
+        px = sum(cfgs[e[2]].canvas_pixels for e in events)
+        return {"streams": len(assign), "admitted": sum(i is not None for i in ids),
+                "rigs": {n: assign.count(n) for n in names}, "frames": len(events), "seconds": seconds,
+                "p50_ms": round(float(np.percentile(lat_ms, 50)), 3),
+                "p99_ms": round(float(np.percentile(lat_ms, 99)), 3), "max_ms": round(float(lat_ms.max()), 3),
+                "mpix_s": round(px / wall / 1e6, 1), "resident_gb": round(srv.resident_bytes / 1e9, 2),
+                "budget_gb": 120, "admit_s": round(admit_s, 2),
+                "arrivals": "Poisson 30 fps per stream, seeded offsets",
+                "io": "pinned host frames uploaded per frame; outputs kept on the device"}
+    finally:
+        srv.close()
+
+
+def cpu_baseline(r, cfg, pool_host, luts, seconds):
+    """The oracle (CPU restatement of the reference path) on the host cores."""
+    import oracle as O
+    n = cfg.num_cams
+    maps = [r.maps(i, cfg.dst_size) for i in range(n)]
+    cov = np.stack([r.coverage(i, cfg.dst_size) for i in range(n)])
+    seams = np.stack([r.seam(i, cfg.dst_size) for i in range(n)])
+    ob = O.Blender(cov, seams, cfg.levels)
+    threads = os.cpu_count() or 1
+    frames = 0
+    t = time.perf_counter()
+    while True:
+        ob.render(pool_host[frames % len(pool_host)], luts, [m[0] for m in maps], [m[1] for m in maps], threads)
+        frames += 1
+        el = time.perf_counter() - t
+        if el >= seconds:
+            break
+    W, H = cfg.dst_size
+    return {"value": round(frames * W * H / el / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
+            "sample": f"{frames} full frames of the 6-camera 4096x2048 rig (LUT + bilinear remap + multiband "
+                      f"blend) in {el:.1f} s"}
+
+
+# ----------------------------------------------------------------------------- reference arm
+def run_reference(args, world, rank):
+    """The reference path's CPU implementation (the oracle port) on the host cores."""
+    import oracle as O
+    from panostitcher_gb300 import synth as S
+    O.build()
+    cfg = S.rig("c2")
+    W, H = cfg.dst_size
+    n = cfg.num_cams
+    threads = os.cpu_count() or 1
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(n, threads)) as ex:
+        maps = list(ex.map(lambda p: O.reproject_map(p, cfg.src_size, cfg.dst_size), cfg.cams))
+    cov = np.stack([m[2] for m in maps])
+    seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov)
+    ob = O.Blender(cov, seams, cfg.levels)
+    fs = S.FrameSource(cfg)
+    pool = [fs.frame(k) for k in range(2)]
+    luts = S.luts(cfg)
+    run = lambda k: ob.render(pool[k % 2], luts, [m[0] for m in maps], [m[1] for m in maps], threads)
+    budget = args.ref_seconds
+    t = time.perf_counter()
+    run(0)
+    one = time.perf_counter() - t
+    warm = min(args.warmup, 1)
+    for k in range(warm - 1):
+        run(k)
+    steps = max(1, min(args.steps, int(budget / max(one, 1e-3))))
+    t = time.perf_counter()
+    for k in range(steps):
+        run(k)
+    el = time.perf_counter() - t
+    value = steps * W * H / el / 1e6
+    sample = f"{steps} of {args.steps} steps (full 6-camera 4096x2048 frames, {threads} threads), " \
+             f"{warm} warm-up"
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mpix/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
+            "data": "synthetic: seeded smooth field + per-frame noise",
+            "config": {"workload": WORKLOAD, "canvas": [W, H], "cams": n, "levels": ob.levels,
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--pool", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=90.0)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args, world, rank)), flush=True)
+        return 0
+    import torch
+    dist = dist_init(world, torch.cuda.is_available())
+    out = run_ours(args, world, rank, local, dist)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

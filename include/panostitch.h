@@ -131,6 +131,24 @@ int ps_render_export(const ps_render* r, int what, int cam, int level, void* hos
    render (int16 x4 per pixel), for bit-exact checks of the pipeline. */
 int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out, long long bytes, void* stream);
 
+/* Measurement hooks (no reference counterpart).  While profiling is on,
+   renders launch step by step with a CUDA event pair around every launch
+   (no graph); ps_render_profile_read aggregates the finished launches of
+   one kernel kind (0 remap, 1 pyrDown, 2 blend) at one pyramid level
+   (-1 = all levels): launch count, summed device milliseconds and summed
+   algorithmic bytes (each input and output element counted once).
+   Enabling resets the aggregates. */
+int ps_render_profile(ps_render* r, int enable);
+int ps_render_profile_read(ps_render* r, int kind, int level, long long* launches, double* total_ms,
+                           double* bytes);
+/* Kernel launches one render issues. */
+int ps_render_launches_per_frame(const ps_render* r);
+/* Algorithmic bytes of one frame: camera frames (bytes_in_per_px each), the
+   maps of covered canvas pixels (8 B), the non-zero seam weights (2 B) and
+   alpha divisors (4 B) of every level, and the canvas (bytes_out_per_px).
+   Returns < 0 if the render is not prepared. */
+double ps_render_algorithmic_bytes(const ps_render* r, int bytes_in_per_px, int bytes_out_per_px);
+
 /* ==== batched render: several rigs, one frame each, in one launch sequence ==== */
 /* All rigs' work goes into shared persistent launches (one per pyramid step)
    captured once per batch composition as a CUDA graph.  srcs[k] holds

@@ -78,6 +78,11 @@ _SIGS = [
                                              C.POINTER(C.c_longlong)]),
     ("ps_render_export", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong]),
     ("ps_render_export_collapsed", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p]),
+    ("ps_render_profile", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_render_profile_read", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("ps_render_launches_per_frame", C.c_int, [C.c_void_p]),
+    ("ps_render_algorithmic_bytes", C.c_double, [C.c_void_p, C.c_int, C.c_int]),
     ("ps_render_batch", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.POINTER(Image)),
                                   C.POINTER(C.c_void_p), C.POINTER(Image), C.c_void_p]),
     ("ps_generate_reproject_map_and_mask", C.c_int, [C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,

@@ -14,6 +14,7 @@ using ps::fail;
 struct ps_render {
     ps::Rig rig;
     std::unique_ptr<ps::Plan> plan;
+    ps::Profiler prof;
     bool useGraph = true;
 };
 
@@ -162,8 +163,36 @@ int ps_render_render(ps_render* r, const ps_image* src, int num_src, const uint8
         if (!r) fail(PS_EINVAL, "render is NULL");
         checkFrame(r->rig, src, num_src, luts, num_luts, dst);
         if (!r->plan || !r->plan->matches({&r->rig})) r->plan.reset(new ps::Plan({&r->rig}));
-        r->plan->run({ps::FrameInput{src, luts, dst}}, toStream(stream), r->useGraph);
+        r->plan->run({ps::FrameInput{src, luts, dst}}, toStream(stream), r->useGraph, &r->prof);
     });
+}
+
+int ps_render_profile(ps_render* r, int enable)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        r->prof.enable(enable != 0);
+    });
+}
+
+int ps_render_profile_read(ps_render* r, int kind, int level, long long* launches, double* total_ms, double* bytes)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (kind < 0 || kind > 2) fail(PS_EINVAL, "kind %d not in 0..2", kind);
+        r->prof.read(kind, level, launches, total_ms, bytes);
+    });
+}
+
+int ps_render_launches_per_frame(const ps_render* r)
+{
+    return r && r->plan ? r->plan->launchesPerRun() : 0;
+}
+
+double ps_render_algorithmic_bytes(const ps_render* r, int bytes_in_per_px, int bytes_out_per_px)
+{
+    if (!r || !r->rig.ready()) return -1.0;
+    return r->rig.algorithmicBytes(bytes_in_per_px, bytes_out_per_px);
 }
 
 int ps_render_set_graph(ps_render* r, int enabled)

@@ -112,6 +112,9 @@ cudaError_t launchTileFlags16(const uint16_t* p, int w, int h, int pitch, long l
                               int th, int tilesX, int tilesY, uint8_t* flags, cudaStream_t st);
 cudaError_t launchTileFlags8(const uint8_t* p, int w, int h, int pitch, long long camStride, int n, int tw,
                              int th, int tilesX, int tilesY, uint8_t* flags, cudaStream_t st);
+// number of non-zero pixels of a 16-bit plane, all cameras (added to *out)
+cudaError_t launchCountNonzero16(const uint16_t* p, int w, int h, int pitch, long long camStride, int n,
+                                 unsigned long long* out, cudaStream_t st);
 // union coverage (0/255) and per-tile covered-pixel counts
 cudaError_t launchUnion(const uint8_t* cov, int n, int W, int H, long long maskStride, uint8_t* uni, int pitch,
                         int tw, int th, int tilesX, int* tileCounts, unsigned long long* total,

@@ -371,6 +371,24 @@ cudaError_t launchTileFlags8(const uint8_t* p, int w, int h, int pitch, long lon
     return cudaGetLastError();
 }
 
+// number of non-zero pixels of a 16-bit plane over all cameras
+__global__ void k_count_nonzero16(const uint16_t* __restrict__ p, int w, int h, int pitch, long long camStride,
+                                  unsigned long long* out)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, c = blockIdx.z;
+    const int nz = x < w && p[(size_t)c * camStride + (size_t)y * pitch + x] != 0;
+    const int cnt = __syncthreads_count(nz);
+    if (threadIdx.x == 0 && cnt) atomicAdd(out, (unsigned long long)cnt);
+}
+
+cudaError_t launchCountNonzero16(const uint16_t* p, int w, int h, int pitch, long long camStride, int n,
+                                 unsigned long long* out, cudaStream_t st)
+{
+    dim3 grid((w + 127) / 128, h, n);
+    k_count_nonzero16<<<grid, 128, 0, st>>>(p, w, h, pitch, camStride, out);
+    return cudaGetLastError();
+}
+
 // union coverage; one block of tw x th threads per tile counts covered pixels
 __global__ void k_union(const uint8_t* __restrict__ cov, int n, int W, int H, long long maskStride, uint8_t* uni,
                         int pitch, int tilesX, int* tileCounts, unsigned long long* total)

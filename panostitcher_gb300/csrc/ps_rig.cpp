@@ -86,6 +86,10 @@ void Rig::clear()
     maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset();
     imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
     hRemap_.clear();
+    hDown_.clear();
+    hBlend_.clear();
+    hCams_.clear();
+    covCount_ = weightCount_ = alphaCount_ = 0;
     covBits_.clear();
     seamBits_.clear();
     geom_.clear();
@@ -308,6 +312,18 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         PS_CUDA(launchTileFlags16(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kBlendTW, kBlendTH, bX, bY,
                                   bflags[j].as<uint8_t>(), st));
     }
+    DevBuf counts(2 * sizeof(unsigned long long));
+    counts.zero(st);
+    for (int j = 0; j <= L; j++) {
+        const LevelGeom& g = geom_[j];
+        const long long stride = (long long)g.pitch * g.h;
+        PS_CUDA(launchCountNonzero16(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n,
+                                     counts.as<unsigned long long>(), st));
+        if (j > 0)
+            PS_CUDA(launchCountNonzero16(lv_[j].Am.as<uint16_t>(), g.w, g.h, g.pitch, stride, n,
+                                         counts.as<unsigned long long>() + 1, st));
+    }
+    unsigned long long hc[2] = {0, 0};
     // host copies
     std::vector<int> hCounts((size_t)bX0 * bY0);
     unsigned long long hTotal = 0;
@@ -315,6 +331,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     std::vector<std::vector<uint8_t>> hD(L + 1), hB(L + 1);
     PS_CUDA(cudaMemcpyAsync(hCounts.data(), tileCounts.get(), tileCounts.bytes(), cudaMemcpyDeviceToHost, st));
     PS_CUDA(cudaMemcpyAsync(&hTotal, total.get(), sizeof hTotal, cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaMemcpyAsync(hc, counts.get(), sizeof hc, cudaMemcpyDeviceToHost, st));
     if (xmap) PS_CUDA(cudaMemcpyAsync(hR.data(), rflags.get(), hR.size(), cudaMemcpyDeviceToHost, st));
     for (int j = 0; j <= L; j++) {
         if (j > 0) {
@@ -329,6 +346,10 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     PS_CUDA(cudaMemcpyAsync(hSeam.data(), seam, n * npx, cudaMemcpyDeviceToHost, st));
     PS_CUDA(cudaStreamSynchronize(st));
     full_ = hTotal == (unsigned long long)npx;  // CudaMultibandBlend.cpp:616-617
+    weightCount_ = (long long)hc[0];
+    alphaCount_ = (long long)hc[1];
+    covCount_ = 0;
+    for (uint8_t v : hCov) covCount_ += v != 0;
     packBits(hCov, covBits_);
     packBits(hSeam, seamBits_);
     hCov.clear();
@@ -377,6 +398,9 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         blendCnt_[j] = (int)blend.size() - blendOff_[j];
     }
     if (cams.empty()) cams.push_back(0);
+    hDown_ = down;
+    hBlend_ = blend;
+    hCams_ = cams;
     dRemap_.alloc(std::max<size_t>(1, hRemap_.size()) * sizeof(RemapItem));
     dDown_.alloc(std::max<size_t>(1, down.size()) * sizeof(DownItem));
     dBlend_.alloc(std::max<size_t>(1, blend.size()) * sizeof(BlendItem));
@@ -509,6 +533,118 @@ void Rig::exportCollapsed(int level, int16_t* host, long long bytes, cudaStream_
     PS_CUDA(cudaStreamSynchronize(st));
 }
 
+double Rig::stepBytes(int kind, int level) const
+{
+    double b = 0;
+    if (kind == 0) {
+        // map (8 B) in, G0 (4 B) out per tile pixel, every covering camera's frame in once
+        std::vector<char> used(n_, 0);
+        for (const RemapItem& it : hRemap_) {
+            const int tw = std::min(kRemapTW, W_ - it.tx * kRemapTW), th = std::min(kRemapTH, H_ - it.ty * kRemapTH);
+            b += (double)tw * th * 12;
+            used[it.cam] = 1;
+        }
+        for (int c = 0; c < n_; c++)
+            if (used[c]) b += (double)srcW_ * srcH_ * 4;
+        return b;
+    }
+    if (kind == 1) {
+        // per output pixel: 4 input pixels (uchar4), the alpha divisor (2 B), the output (4 B)
+        const LevelGeom& g = geom_[level];
+        for (int k = downOff_[level]; k < downOff_[level] + downCnt_[level]; k++) {
+            const DownItem& it = hDown_[k];
+            const int tw = std::min(kDownTW, g.w - it.tx * kDownTW), th = std::min(kDownTH, g.h - it.ty * kDownTH);
+            b += (double)tw * th * (16 + 2 + 4);
+        }
+        return b;
+    }
+    // blend: per camera in the tile's list weight (2 B) + G_j (4 B) + a quarter of G_{j+1} (1 B);
+    // a quarter of C_{j+1} (2 B); out C_j (8 B) or the canvas (4 B)
+    const LevelGeom& g = geom_[level];
+    for (int k = blendOff_[level]; k < blendOff_[level] + blendCnt_[level]; k++) {
+        const BlendItem& it = hBlend_[k];
+        const int tw = std::min(kBlendTW, g.w - it.tx * kBlendTW), th = std::min(kBlendTH, g.h - it.ty * kBlendTH);
+        if (level == 0 && it.cls == 0) { b += (double)tw * th * 4; continue; }
+        const double perCam = level < L_ ? 7 : 6;
+        b += (double)tw * th * (it.camCnt * perCam + (level < L_ ? 2 : 0) + (level > 0 ? 8 : 4) +
+                                (level == 0 && it.cls == 2 ? 1 : 0));
+    }
+    return b;
+}
+
+double Rig::algorithmicBytes(int bin, int bout) const
+{
+    return (double)n_ * srcW_ * srcH_ * bin + (double)covCount_ * 8 + (double)weightCount_ * 2 +
+           (double)alphaCount_ * 4 + (double)W_ * H_ * bout;
+}
+
+// ---- Profiler -------------------------------------------------------------------------
+Profiler::~Profiler()
+{
+    for (auto& r : recs_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : free_) cudaEventDestroy(e);
+}
+
+void Profiler::enable(bool on)
+{
+    if (on && !on_) {
+        collect();
+        agg_.clear();
+    }
+    on_ = on;
+}
+
+cudaEvent_t Profiler::event()
+{
+    if (!free_.empty()) {
+        cudaEvent_t e = free_.back();
+        free_.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    PS_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void Profiler::record(int kind, int level, double bytes, cudaEvent_t a, cudaEvent_t b)
+{
+    recs_.push_back({kind, level, bytes, a, b});
+}
+
+void Profiler::collect()
+{
+    for (auto& r : recs_) {
+        PS_CUDA(cudaEventSynchronize(r.b));
+        float ms = 0;
+        PS_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        auto key = std::make_pair(r.kind, r.level);
+        auto it = std::find_if(agg_.begin(), agg_.end(), [&](const auto& p) { return p.first == key; });
+        if (it == agg_.end()) { agg_.push_back({key, Agg()}); it = agg_.end() - 1; }
+        it->second.launches++;
+        it->second.ms += ms;
+        it->second.bytes += r.bytes;
+        free_.push_back(r.a);
+        free_.push_back(r.b);
+    }
+    recs_.clear();
+}
+
+void Profiler::read(int kind, int level, long long* launches, double* ms, double* bytes)
+{
+    collect();
+    long long l = 0;
+    double t = 0, b = 0;
+    for (const auto& p : agg_)
+        if (p.first.first == kind && (level < 0 || p.first.second == level)) {
+            l += p.second.launches;
+            t += p.second.ms;
+            b += p.second.bytes;
+        }
+    if (launches) *launches = l;
+    if (ms) *ms = t;
+    if (bytes) *bytes = b;
+}
+
 // ---- Plan ---------------------------------------------------------------------------
 void Plan::dropGraph()
 {
@@ -538,26 +674,30 @@ void Plan::bind(const std::vector<Rig*>& rigs)
 
     steps_.clear();
     segs_.clear();
-    auto addStep = [&](int kind, const std::vector<std::pair<int, std::pair<const void*, int>>>& parts) {
-        Step s{kind, (int)segs_.size(), 0, 0};
+    auto addStep = [&](int kind, const std::vector<std::pair<int, std::pair<const void*, int>>>& parts, int step) {
+        Step s{kind, (int)segs_.size(), 0, 0, -1, 0.0};
         for (const auto& p : parts) {
             if (p.second.second <= 0) continue;
             // frame pointer holds the FrameDev offset until the buffer is known
             segs_.push_back({p.second.first, rigs[p.first]->deviceDesc(),
                              reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * p.first), p.second.second, s.total});
             s.total += p.second.second;
+            const Rig* rg = rigs[p.first];
+            const int lvl = kind == 0 ? 0 : (kind == 1 ? step : rg->numLevels() - step);
+            if (s.level < 0) s.level = lvl;
+            s.bytes += rg->stepBytes(kind, lvl);
         }
         s.nsegs = (int)segs_.size() - s.segOff;
         if (s.total > 0) steps_.push_back(s);
     };
     std::vector<std::pair<int, std::pair<const void*, int>>> parts;
     for (int r = 0; r < nr; r++) parts.push_back({r, {rigs[r]->remapItems(), rigs[r]->numRemapItems()}});
-    addStep(0, parts);
+    addStep(0, parts, 0);
     for (int J = 1; J <= maxL; J++) {
         parts.clear();
         for (int r = 0; r < nr; r++)
             if (J <= rigs[r]->numLevels()) parts.push_back({r, {rigs[r]->downItems(J), rigs[r]->numDownItems(J)}});
-        addStep(1, parts);
+        addStep(1, parts, J);
     }
     for (int s = 0; s <= maxL; s++) {
         parts.clear();
@@ -565,7 +705,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
             const int j = rigs[r]->numLevels() - s;
             if (j >= 0) parts.push_back({r, {rigs[r]->blendItems(j), rigs[r]->numBlendItems(j)}});
         }
-        addStep(2, parts);
+        addStep(2, parts, s);
     }
     const size_t need = segOff_ + std::max<size_t>(1, segs_.size()) * sizeof(Segment);
     if (need > dArgs_.bytes()) {
@@ -596,21 +736,33 @@ bool Plan::matches(const std::vector<Rig*>& rigs) const
     return true;
 }
 
-void Plan::launchAll(cudaStream_t st)
+void Plan::launchAll(cudaStream_t st, Profiler* prof)
 {
     const Segment* segs = reinterpret_cast<const Segment*>(static_cast<uint8_t*>(dArgs_.get()) + segOff_);
     for (const Step& s : steps_) {
         const Segment* p = segs + s.segOff;
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (prof) {
+            a = prof->event();
+            b = prof->event();
+            PS_CUDA(cudaEventRecord(a, st));
+        }
         if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, st));
         else PS_CUDA(launchBlend(p, s.nsegs, s.total, st));
+        if (prof) {
+            PS_CUDA(cudaEventRecord(b, st));
+            prof->record(s.kind, s.level, s.bytes, a, b);
+        }
     }
 }
 
 static int bytesPerPixel(int fmt) { return fmt == PS_FMT_BGR24 ? 3 : 4; }
 
-void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph)
+void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph, Profiler* prof)
 {
+    if (prof && !prof->on()) prof = nullptr;
+    if (prof) useGraph = false;
     if (in.size() != rigs_.size()) fail(PS_EINVAL, "plan input count mismatch");
     if (stageUsed_) PS_CUDA(cudaEventSynchronize(stageDone_));  // the previous staging copy has been consumed
     uint8_t* stage = stage_.as<uint8_t>();
@@ -678,7 +830,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         }
         PS_CUDA(cudaGraphLaunch(graph_, st));
     } else {
-        launchAll(st);
+        launchAll(st, prof);
     }
     for (size_t r = 0; r < rigs_.size(); r++) {
         const ps_image& d = *in[r].dst;

@@ -62,6 +62,14 @@ public:
     // blender input: int16x4 / uint8x4 device images -> level 0 (checks)
     void imagesToLevel0(const void* const* images, const long long* pitches, int fmt, cudaStream_t st);
 
+    // Bytes a step must move at minimum (each input / output element once,
+    // no halo re-reads): kind 0 remap, 1 pyrDown to `level`, 2 blend of `level`.
+    double stepBytes(int kind, int level) const;
+    // Algorithmic bytes of one stitched frame (inputs, maps, weights, alpha
+    // divisors, output; all pyramid levels are intermediate and count 0):
+    //   sum_i Ws*Hs*bin + sum_i C_i*8 + sum_ij K_ij*2 + sum_i,j>=1 A_ij*4 + Wc*Hc*bout
+    double algorithmicBytes(int bin, int bout) const;
+
 private:
     struct LevelBufs {
         DevBuf G, Wt, Am, C;
@@ -82,6 +90,31 @@ private:
     int downOff_[PS_MAX_LEVELS + 1] = {}, downCnt_[PS_MAX_LEVELS + 1] = {};
     int blendOff_[PS_MAX_LEVELS + 1] = {}, blendCnt_[PS_MAX_LEVELS + 1] = {};
     std::vector<uint8_t> covBits_, seamBits_;  // host copies for exports (1 bit / pixel)
+    std::vector<DownItem> hDown_;
+    std::vector<BlendItem> hBlend_;
+    std::vector<uint8_t> hCams_;
+    long long covCount_ = 0, weightCount_ = 0, alphaCount_ = 0;  // non-zero pixels, all cameras / levels
+};
+
+// Per-launch CUDA-event timing of the steps of a plan (non-graph runs only).
+class Profiler {
+public:
+    ~Profiler();
+    void enable(bool on);
+    bool on() const { return on_; }
+    void record(int kind, int level, double bytes, cudaEvent_t a, cudaEvent_t b);
+    cudaEvent_t event();
+    // aggregate of finished launches of (kind, level); level -1 = all levels
+    void read(int kind, int level, long long* launches, double* ms, double* bytes);
+
+private:
+    struct Rec { int kind, level; double bytes; cudaEvent_t a, b; };
+    struct Agg { long long launches = 0; double ms = 0, bytes = 0; };
+    void collect();
+    bool on_ = false;
+    std::vector<Rec> recs_;
+    std::vector<cudaEvent_t> free_;
+    std::vector<std::pair<std::pair<int, int>, Agg>> agg_;
 };
 
 // Per-frame inputs of one rig in a plan.
@@ -105,7 +138,7 @@ public:
     // (re)build the steps for this set of rigs, reusing buffers when they fit
     void bind(const std::vector<Rig*>& rigs);
     // stage frame arguments, upload host inputs, run, download host outputs
-    void run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph);
+    void run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph, Profiler* prof = nullptr);
     int launchesPerRun() const { return (int)steps_.size(); }
     bool matches(const std::vector<Rig*>& rigs) const;
 
@@ -113,8 +146,10 @@ private:
     struct Step {
         int kind;  // 0 remap, 1 pyrDown, 2 blend
         int segOff, nsegs, total;
+        int level;      // level of the first rig in the step
+        double bytes;   // algorithmic bytes of the step (all rigs)
     };
-    void launchAll(cudaStream_t st);
+    void launchAll(cudaStream_t st, Profiler* prof = nullptr);
     void dropGraph();
 
     std::vector<Rig*> rigs_;

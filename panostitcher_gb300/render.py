@@ -131,6 +131,24 @@ class CudaPanoramaRender2:
     def set_graph(self, enabled: bool) -> None:
         check(lib().ps_render_set_graph(self._h, int(bool(enabled))))
 
+    def profile(self, enabled: bool) -> None:
+        check(lib().ps_render_profile(self._h, int(bool(enabled))))
+
+    KERNELS = {0: "k_remap", 1: "k_pyrdown", 2: "k_blend"}
+
+    def profile_read(self, kind: int, level: int = -1):
+        """(launches, total_ms, algorithmic_bytes) of finished profiled launches."""
+        n, ms, b = C.c_longlong(), C.c_double(), C.c_double()
+        check(lib().ps_render_profile_read(self._h, kind, level, C.byref(n), C.byref(ms), C.byref(b)))
+        return n.value, ms.value, b.value
+
+    @property
+    def launches_per_frame(self) -> int:
+        return lib().ps_render_launches_per_frame(self._h)
+
+    def algorithmic_bytes(self, bytes_in_per_px: int = 4, bytes_out_per_px: int = 4) -> float:
+        return lib().ps_render_algorithmic_bytes(self._h, bytes_in_per_px, bytes_out_per_px)
+
     def input_buffer(self, cam: int):
         p, pitch = C.c_void_p(), C.c_longlong()
         check(lib().ps_render_get_input_buffer(self._h, cam, C.byref(p), C.byref(pitch)))
