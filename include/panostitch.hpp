@@ -1,0 +1,120 @@
+// panostitch.hpp -- C++ facade over the C ABI with the reference's class and
+// method names (source/Task/RicohUtil.h:193-220,
+// source/CudaAccel/CudaInterface.h:45-82), so Task-layer call sites switch
+// by changing a type.  Header-only; link with -lpanostitch.
+//
+// Differences from the reference signatures, all forced by OpenCV being
+// absent: images are ps_image views instead of cv::Mat / cv::cuda::GpuMat,
+// camera parameters are passed directly instead of a file path, sizes are
+// panostitch::Size.  Errors return false and keep the message in
+// lastError(), as the reference returns false after lprintf.
+#pragma once
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "panostitch.h"
+
+namespace panostitch {
+
+struct Size {
+    int width = 0, height = 0;
+};
+
+class CudaPanoramaRender2 {
+public:
+    CudaPanoramaRender2() { ps_render_create(&r_); }
+    ~CudaPanoramaRender2() { ps_render_destroy(r_); }
+    CudaPanoramaRender2(const CudaPanoramaRender2&) = delete;
+    CudaPanoramaRender2& operator=(const CudaPanoramaRender2&) = delete;
+
+    // CudaPanoramaRender2::prepare (source/Task/RicohUtil.cpp:1091-1205)
+    bool prepare(const std::vector<ps_photo_param>& params, int highQualityBlend, int blendParam,
+                 const Size& srcSize, const Size& dstSize, void* stream = nullptr)
+    {
+        return ok(ps_render_prepare(r_, params.data(), (int)params.size(), highQualityBlend, blendParam,
+                                    srcSize.width, srcSize.height, dstSize.width, dstSize.height, stream));
+    }
+
+    // CudaPanoramaRender2::render (source/Task/RicohUtil.cpp:1207-1339).  Like
+    // the reference, LUTs that are not numImages x 3 x 256 are skipped with a
+    // warning (:1239-1265) instead of failing the frame.
+    bool render(const std::vector<ps_image>& src, ps_image& dst,
+                const std::vector<std::vector<std::vector<unsigned char>>>& luts = {}, void* stream = nullptr)
+    {
+        const int n = getNumImages();
+        bool correct = (int)luts.size() == n && n > 0;
+        for (size_t i = 0; correct && i < luts.size(); i++) {
+            if (luts[i].size() != 3) correct = false;
+            for (size_t c = 0; correct && c < luts[i].size(); c++)
+                if (luts[i][c].size() != 256) correct = false;
+        }
+        if (!correct && !luts.empty())
+            std::fprintf(stderr, "Warning in render, the non-empty look up tables not satisfied, skip correction\n");
+        std::vector<unsigned char> flat;
+        if (correct) {
+            flat.reserve((size_t)n * 768);
+            for (const auto& cam : luts)
+                for (const auto& ch : cam) flat.insert(flat.end(), ch.begin(), ch.end());
+        }
+        return ok(ps_render_render(r_, src.data(), (int)src.size(), correct ? flat.data() : nullptr,
+                                   correct ? n : 0, &dst, stream));
+    }
+
+    void clear() { ps_render_clear(r_); }
+    int getNumImages() const { return ps_render_get_num_images(r_); }
+    const std::string& lastError() const { return err_; }
+    ps_render* handle() const { return r_; }
+
+private:
+    bool ok(int status)
+    {
+        if (status == PS_OK) return true;
+        err_ = ps_last_error();
+        return false;
+    }
+    ps_render* r_ = nullptr;
+    std::string err_;
+};
+
+// CudaTilingMultibandBlendFast (source/CudaAccel/CudaInterface.h:45-82)
+class CudaTilingMultibandBlendFast {
+public:
+    CudaTilingMultibandBlendFast() { ps_blender_create(&b_); }
+    ~CudaTilingMultibandBlendFast() { ps_blender_destroy(b_); }
+    CudaTilingMultibandBlendFast(const CudaTilingMultibandBlendFast&) = delete;
+    CudaTilingMultibandBlendFast& operator=(const CudaTilingMultibandBlendFast&) = delete;
+
+    // prepare(masks, maxLevels, minLength); seams replace getNonIntersectingMasks
+    bool prepare(const std::vector<const uint8_t*>& masks, const std::vector<const uint8_t*>& seams, int width,
+                 int height, int maxLevels, int minLength, void* stream = nullptr)
+    {
+        if (masks.size() != seams.size()) {
+            err_ = "masks and seams differ in count";
+            return false;
+        }
+        return ok(ps_blender_prepare(b_, masks.data(), seams.data(), (int)masks.size(), width, height, maxLevels,
+                                     minLength, stream));
+    }
+    // blend(images, blendImage): device CV_16SC4 (format 16) or CV_8UC4 (8) images
+    bool blend(const std::vector<const void*>& images, const std::vector<long long>& pitches, int format,
+               ps_image& dst, void* stream = nullptr)
+    {
+        return ok(ps_blender_blend(b_, images.data(), pitches.data(), format, &dst, stream));
+    }
+    int numLevels() const { return ps_blender_get_num_levels(b_); }
+    const std::string& lastError() const { return err_; }
+
+private:
+    bool ok(int status)
+    {
+        if (status == PS_OK) return true;
+        err_ = ps_last_error();
+        return false;
+    }
+    ps_blender* b_ = nullptr;
+    std::string err_;
+};
+
+}  // namespace panostitch

@@ -26,7 +26,7 @@
 namespace ps {
 
 // ---- tiles ------------------------------------------------------------------
-constexpr int kRemapTW = 32, kRemapTH = 8;     // level-0 remap tile (one pixel per thread)
+constexpr int kRemapTW = 32, kRemapTH = 16;    // level-0 remap tile (two pixels per thread)
 constexpr int kDownTW = 32, kDownTH = 16;      // pyrDown output tile (two pixels per thread)
 constexpr int kBlendTW = 64, kBlendTH = 8;     // blend tile (two adjacent pixels per thread)
 constexpr int kThreads = 256;
@@ -47,7 +47,7 @@ struct RigDev {
     int srcW, srcH;
     const float2* maps;       // tile-compact maps of all cameras
     const uint8_t* unionMask; // level-0 union coverage (0/255), pitch = lv[0].pitch
-    const uint8_t* camLists;  // camera indices referenced by BlendItem::camOff
+    const uint8_t* camLists;  // camera indices of blend tiles with more than 8 cameras
     LevelDev lv[PS_MAX_LEVELS + 1];
 };
 
@@ -67,7 +67,10 @@ struct FrameDev {
 // Work items (one per tile), resident per rig and built at prepare time.
 struct RemapItem { uint16_t cam, pad; uint16_t tx, ty; uint32_t mapTile; };
 struct DownItem { uint8_t cam, level; uint16_t tx, ty; uint16_t pad; };   // level = output level
-struct BlendItem { uint8_t level, cls; uint16_t tx, ty; uint16_t pad; uint32_t camOff, camCnt; };
+// A blend tile lists the cameras whose weight touches it: up to 8 inline,
+// more through RigDev::camLists (cams[0..3] then hold the uint32 offset).
+struct alignas(16) BlendItem { uint8_t level, cls, camCnt, pad; uint16_t tx, ty; uint8_t cams[8]; };
+constexpr int kInlineCams = 8;
 // cls of a level-0 blend tile: 0 uncovered (write zeros), 1 fully covered,
 // 2 partially covered (read the union mask).  Unused above level 0.
 
@@ -81,13 +84,23 @@ struct Segment {
     int count, prefix;
 };
 
-// Item `it` of a launch -> its segment, scanning forward from a hint (the
-// grid-stride loop visits items in increasing order).
+#ifdef __CUDACC__
+// Item `it` of a launch -> its segment, scanning forward from a hint (each
+// CTA visits its items in increasing order).
 __device__ __forceinline__ int findSegment(const Segment* segs, int nsegs, int it, int hint)
 {
     int s = hint;
     while (s + 1 < nsegs && segs[s + 1].prefix <= it) s++;
     return s;
+}
+
+// Contiguous chunk of items for this CTA: neighbouring tiles of one camera
+// stay on one SM (source-texel and footprint reuse in L1 / L2).
+__device__ __forceinline__ void itemRange(int total, int& begin, int& end)
+{
+    const int chunk = (total + gridDim.x - 1) / gridDim.x;
+    begin = min(total, (int)blockIdx.x * chunk);
+    end = min(total, begin + chunk);
 }
 
 // ---- borders: source/CudaAccel/CudaUtil.cuh:6-98 ------------------------------
@@ -101,6 +114,26 @@ __device__ __forceinline__ int colHigh(int x, int W) { return x < W ? x : x % W;
 __device__ __forceinline__ int rowMap(int y, int H) { return y < 0 ? rowLow(y, H) : (y >= H ? rowHigh(y, H) : y); }
 __device__ __forceinline__ int colMap(int x, int W) { return x < 0 ? colLow(x, W) : (x >= W ? colHigh(x, W) : x); }
 
+// C truncating division a / d for |a| < 2^21 and 1 <= d < 2^16 given
+// rcp = __frcp_rn(d), exact: the fp32 quotient is within 1 of the true one,
+// and one remainder check fixes it.
+__device__ __forceinline__ int divTrunc(int a, int d, float rcp)
+{
+    const int m = abs(a);
+    int q = (int)__fmul_rz((float)m, rcp);
+    const int r = m - q * d;
+    q += (r >= d) - (r < 0);
+    return a < 0 ? -q : q;
+}
+
+// Programmatic dependent launch: wait until the previous kernel in the
+// stream has completed and its writes are visible (everything before this
+// call may only touch data that kernel does not write).
+__device__ __forceinline__ void waitPrevGrid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Let the next kernel in the stream start launching (its CTAs block in
+// waitPrevGrid until this grid completes).
+__device__ __forceinline__ void allowNextGrid() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // ---- packed channel arithmetic -----------------------------------------------
 // A BGRX byte quad splits into two words holding 16-bit lanes:
 //   lo = B | R << 16,  hi = G | X << 16.
@@ -110,5 +143,6 @@ __device__ __forceinline__ uint2 unpackBytes(uint32_t v)
 {
     return make_uint2(v & 0x00FF00FFu, (v >> 8) & 0x00FF00FFu);
 }
+#endif  // __CUDACC__
 
 }  // namespace ps

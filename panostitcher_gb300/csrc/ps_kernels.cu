@@ -87,19 +87,26 @@ __device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, lo
     return out;
 }
 
-// Level-0 remap over the covered 32x8 tiles of every camera (one pixel per
-// thread; the tile's map is 256 consecutive float2).
+// Level-0 remap over the covered 32x16 tiles of every camera; each thread
+// remaps two pixels (rows ly and ly + 8) so two independent gathers are in
+// flight; the tile's map is 512 consecutive float2.
 __global__ void __launch_bounds__(kThreads) k_remap(const Segment* __restrict__ segs, int nsegs, int total)
 {
     __shared__ uint8_t lut[3 * 256];
     long long loaded = -1;
-    int s = 0;
+    int s = 0, begin, end;
+    itemRange(total, begin, end);
     const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
-    for (int it = blockIdx.x; it < total; it += gridDim.x) {
+    waitPrevGrid();
+    allowNextGrid();
+    for (int it = begin; it < end; it++) {
         s = findSegment(segs, nsegs, it, s);
         const Segment sg = segs[s];
         const RemapItem item = static_cast<const RemapItem*>(sg.items)[it - sg.prefix];
         const FrameDev& F = *sg.frame;
+        const RigDev& R = *sg.rig;
+        const float2* mt = R.maps + (size_t)item.mapTile * (kRemapTW * kRemapTH);
+        const float2 m0 = __ldg(mt + threadIdx.x), m1 = __ldg(mt + threadIdx.x + kThreads);
         const long long key = ((long long)s << 16) | item.cam;
         if (key != loaded) {  // uniform across the block
             __syncthreads();
@@ -108,13 +115,17 @@ __global__ void __launch_bounds__(kThreads) k_remap(const Segment* __restrict__ 
             __syncthreads();
             loaded = key;
         }
-        const RigDev& R = *sg.rig;
-        const int x = item.tx * kRemapTW + lx, y = item.ty * kRemapTH + ly;
-        const float2 m = __ldg(R.maps + (size_t)item.mapTile * (kRemapTW * kRemapTH) + threadIdx.x);
-        if (x >= R.W || y >= R.H) continue;
-        const uint32_t v = remapPixel(m, F.src[item.cam], F.srcPitch[item.cam], F.srcFmt, R.srcW, R.srcH, lut);
+        const int x = item.tx * kRemapTW + lx, y0 = item.ty * kRemapTH + ly, y1 = y0 + 8;
+        const uint8_t* base = F.src[item.cam];
+        const long long pitch = F.srcPitch[item.cam];
+        const uint32_t v0 = remapPixel(m0, base, pitch, F.srcFmt, R.srcW, R.srcH, lut);
+        const uint32_t v1 = remapPixel(m1, base, pitch, F.srcFmt, R.srcW, R.srcH, lut);
         const LevelDev& L0 = R.lv[0];
-        reinterpret_cast<uint32_t*>(L0.G)[(size_t)item.cam * L0.camStride + (size_t)y * L0.pitch + x] = v;
+        uint32_t* G = reinterpret_cast<uint32_t*>(L0.G) + (size_t)item.cam * L0.camStride + x;
+        if (x < R.W) {
+            if (y0 < R.H) G[(size_t)y0 * L0.pitch] = v0;
+            if (y1 < R.H) G[(size_t)y1 * L0.pitch] = v1;
+        }
     }
 }
 
@@ -151,14 +162,20 @@ __global__ void __launch_bounds__(kThreads) k_reproject16s(const uint8_t* __rest
 constexpr int kDInW = 2 * kDownTW + 3;   // 67
 constexpr int kDInH = 2 * kDownTH + 3;   // 35
 
+constexpr int kDLoads = (kDInH * kDInW + kThreads - 1) / kThreads;   // 10 tile elements per thread
+
 __global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict__ segs, int nsegs, int total)
 {
     __shared__ uint32_t s_in[kDInH][kDInW];
     __shared__ uint2 s_v[kDownTH][kDInW];
     __shared__ uint32_t s_magic[257];
     for (int m = threadIdx.x; m < 257; m += kThreads) s_magic[m] = m ? (uint32_t)((16777216u + m - 1) / m) : 0u;
-    int s = 0;
-    for (int it = blockIdx.x; it < total; it += gridDim.x) {
+    int s = 0, begin, end;
+    itemRange(total, begin, end);
+    const int ox = threadIdx.x & 31, oy = threadIdx.x >> 5;
+    waitPrevGrid();
+    allowNextGrid();
+    for (int it = begin; it < end; it++) {
         s = findSegment(segs, nsegs, it, s);
         const Segment sg = segs[s];
         const DownItem item = static_cast<const DownItem*>(sg.items)[it - sg.prefix];
@@ -169,11 +186,29 @@ __global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict_
         const int ox0 = item.tx * kDownTW, oy0 = item.ty * kDownTH;
         const int ix0 = 2 * ox0 - 2, iy0 = 2 * oy0 - 2;
         const uint32_t* G = reinterpret_cast<const uint32_t*>(Ls.G) + (size_t)item.cam * Ls.camStride;
+        // issue every load of the item before the first barrier: the tile and the two divisors
+        const int X = ox0 + ox, Y0 = oy0 + oy, Y1 = Y0 + 8;
+        const size_t o0 = (size_t)item.cam * Ld.camStride + (size_t)Y0 * Ld.pitch + X;
+        const size_t o1 = o0 + (size_t)8 * Ld.pitch;
+        const bool ok0 = X < Ld.w && Y0 < Ld.h, ok1 = X < Ld.w && Y1 < Ld.h;
+        const int m0 = ok0 ? __ldg(Ld.Am + o0) : 0, m1 = ok1 ? __ldg(Ld.Am + o1) : 0;
+        uint32_t v[kDLoads];
+        const bool interior = ix0 >= 0 && iy0 >= 0 && ix0 + kDInW <= sw && iy0 + kDInH <= sh;
+#pragma unroll
+        for (int q = 0; q < kDLoads; q++) {
+            const int k = threadIdx.x + q * kThreads;
+            if (k < kDInH * kDInW) {
+                const int r = k / kDInW, c = k - r * kDInW;
+                const int gy = interior ? iy0 + r : rowMap(iy0 + r, sh);
+                const int gx = interior ? ix0 + c : colMap(ix0 + c, sw);
+                v[q] = __ldg(G + (size_t)gy * Ls.pitch + gx);
+            }
+        }
         __syncthreads();  // the previous item's readers are done with shared memory
-        for (int k = threadIdx.x; k < kDInH * kDInW; k += kThreads) {
-            const int r = k / kDInW, c = k - r * kDInW;
-            const int gy = rowMap(iy0 + r, sh), gx = colMap(ix0 + c, sw);
-            s_in[r][c] = __ldg(G + (size_t)gy * Ls.pitch + gx);
+#pragma unroll
+        for (int q = 0; q < kDLoads; q++) {
+            const int k = threadIdx.x + q * kThreads;
+            if (k < kDInH * kDInW) (&s_in[0][0])[k] = v[q];
         }
         __syncthreads();
         for (int k = threadIdx.x; k < kDownTH * kDInW; k += kThreads) {
@@ -188,31 +223,26 @@ __global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict_
             s_v[r][c] = make_uint2(lo, hi);
         }
         __syncthreads();
-        const int ox = threadIdx.x & 31;
 #pragma unroll
         for (int half = 0; half < 2; half++) {
-            const int oy = (threadIdx.x >> 5) + 8 * half;
+            const int r = oy + 8 * half;
             uint32_t lo = 0, hi = 0;
 #pragma unroll
             for (int t = 0; t < 5; t++) {
-                const uint2 v = s_v[oy][2 * ox + t];
-                lo += c_k5[t] * v.x;
-                hi += c_k5[t] * v.y;
+                const uint2 q = s_v[r][2 * ox + t];
+                lo += c_k5[t] * q.x;
+                hi += c_k5[t] * q.y;
             }
-            const int X = ox0 + ox, Y = oy0 + oy;
-            if (X < Ld.w && Y < Ld.h) {
-                const size_t o = (size_t)item.cam * Ld.camStride + (size_t)Y * Ld.pitch + X;
-                const int m = Ld.Am[o];
-                uint32_t outv = 0;
-                if (m) {
-                    const unsigned long long mg = s_magic[m];
-                    const uint32_t b = (uint32_t)(((lo & 0xFFFFu) * mg) >> 24);
-                    const uint32_t r = (uint32_t)(((lo >> 16) * mg) >> 24);
-                    const uint32_t g = (uint32_t)(((hi & 0xFFFFu) * mg) >> 24);
-                    outv = b | (g << 8) | (r << 16);
-                }
-                reinterpret_cast<uint32_t*>(Ld.G)[o] = outv;
+            const int m = half ? m1 : m0;
+            uint32_t outv = 0;
+            if (m) {
+                const unsigned long long mg = s_magic[m];
+                const uint32_t b = (uint32_t)(((lo & 0xFFFFu) * mg) >> 24);
+                const uint32_t rr = (uint32_t)(((lo >> 16) * mg) >> 24);
+                const uint32_t g = (uint32_t)(((hi & 0xFFFFu) * mg) >> 24);
+                outv = b | (g << 8) | (rr << 16);
             }
+            if (half ? ok1 : ok0) reinterpret_cast<uint32_t*>(Ld.G)[half ? o1 : o0] = outv;
         }
     }
 }
@@ -229,16 +259,37 @@ __global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict_
 //   level 0: out = clamp(C_0, 0, 255), 0 where no camera covers
 //   (convertTo(CV_8U) + setTo(0, maskNot), CudaMultibandBlend.cpp:820-822).
 // A CTA covers a 64x8 tile; thread t owns pixels (2*(t%32), t/32) and the
-// one to its right.  The level j+1 footprint (34x6) is staged in shared
-// memory per camera.
+// one to its right.  Every global load of a tile (the C_{j+1} footprint, the
+// G_{j+1} footprints of two cameras at a time, their weights and G_j pixels) is
+// issued before one barrier, so a tile costs one memory round trip; the next
+// tile's descriptor is prefetched meanwhile.
 // ============================================================================
 constexpr int kFW = kBlendTW / 2 + 2;  // 34
 constexpr int kFH = kBlendTH / 2 + 2;  // 6
+constexpr int kFElems = kFW * kFH;     // 204
+constexpr int kCamsPerPass = 2;
+constexpr int kFLoads = (kCamsPerPass * kFElems + kThreads - 1) / kThreads;  // 4
+constexpr int kMaxSmemSegs = 64;
 
-__global__ void __launch_bounds__(kThreads) k_blend(const Segment* __restrict__ segs, int nsegs, int total)
+// q-th camera of a blend tile (raw 16-byte descriptor)
+__device__ __forceinline__ int tileCam(const uint4& raw, const uint8_t* camLists, int q)
 {
-    __shared__ uint32_t s_g[kFH][kFW];
-    __shared__ int4 s_c[kFH][kFW];
+    if (((raw.x >> 16) & 0xFF) > kInlineCams) return __ldg(camLists + raw.z + q);
+    const uint32_t w = q < 4 ? raw.z : raw.w;
+    return (int)((w >> (8 * (q & 3))) & 0xFF);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total)
+{
+    __shared__ uint32_t s_g[kCamsPerPass * kFElems];
+    __shared__ int4 s_c[kFElems];
+    __shared__ Segment s_segs[kMaxSmemSegs];
+    const Segment* segs = gsegs;
+    if (nsegs <= kMaxSmemSegs) {
+        for (int k = threadIdx.x; k < nsegs; k += kThreads) s_segs[k] = gsegs[k];
+        __syncthreads();
+        segs = s_segs;
+    }
     const int lx = (threadIdx.x & 31) * 2, ly = threadIdx.x >> 5;
     // vertical taps of the zero-inserted upsample for this row's parity:
     // even rows take footprint rows ly/2 .. ly/2+2 with weights 1 6 1,
@@ -247,71 +298,126 @@ __global__ void __launch_bounds__(kThreads) k_blend(const Segment* __restrict__ 
     const int vr0 = evenRow ? ly / 2 : (ly - 1) / 2 + 1;
     // footprint columns: even pixel lx/2 .. lx/2+2 (1 6 1), odd pixel lx/2+1 .. lx/2+2 (4 4)
     const int fc = lx / 2;
+    // interleaved tiles balance the load (uncovered bands are cheap, seams are not)
     int s = 0;
-
+    uint4 nextRaw = make_uint4(0, 0, 0, 0);
+    if ((int)blockIdx.x < total) {
+        s = findSegment(segs, nsegs, blockIdx.x, 0);
+        nextRaw = __ldg(static_cast<const uint4*>(segs[s].items) + (blockIdx.x - segs[s].prefix));
+    }
+    waitPrevGrid();
+    allowNextGrid();
     for (int it = blockIdx.x; it < total; it += gridDim.x) {
-        s = findSegment(segs, nsegs, it, s);
-        const Segment sg = segs[s];
-        const BlendItem item = static_cast<const BlendItem*>(sg.items)[it - sg.prefix];
+        const uint4 raw = nextRaw;
+        const int cs = s;
+        const int nx = it + (int)gridDim.x;
+        if (nx < total) {
+            s = findSegment(segs, nsegs, nx, s);
+            nextRaw = __ldg(static_cast<const uint4*>(segs[s].items) + (nx - segs[s].prefix));
+        }
+        const Segment& sg = segs[cs];
         const RigDev& R = *sg.rig;
-        const int j = item.level;
+        const int j = raw.x & 0xFF, cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
+        const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
         const LevelDev& Lj = R.lv[j];
-        const int x = item.tx * kBlendTW + lx, y = item.ty * kBlendTH + ly;
+        const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
         const bool rowOk = y < Lj.h;
-        const bool active = !(j == 0 && item.cls == 0);
-        const int fx0 = item.tx * (kBlendTW / 2) - 1, fy0 = item.ty * (kBlendTH / 2) - 1;
+        const bool active = !(j == 0 && cls == 0);
+        const bool hasUp = j < R.L;
+        const LevelDev& Lu = R.lv[hasUp ? j + 1 : j];
+        const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
+        const bool interiorU = fx0 >= 0 && fy0 >= 0 && fx0 + kFW <= Lu.w && fy0 + kFH <= Lu.h;
         int r0[3] = {0, 0, 0}, r1[3] = {0, 0, 0};
         int wsum0 = 0, wsum1 = 0;
 
         if (active) {
-            const bool top = j == R.L;
-            const LevelDev& Lu = R.lv[top ? j : j + 1];
-            for (uint32_t ci = 0; ci < item.camCnt; ci++) {
-                const int cam = R.camLists[item.camOff + ci];
-                uint32_t u0lo = 0, u0hi = 0, u1lo = 0, u1hi = 0;
-                if (!top) {
-                    __syncthreads();
-                    const uint32_t* Gu = reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride;
-                    if (threadIdx.x < kFH * kFW) {
-                        const int r = threadIdx.x / kFW, c = threadIdx.x - r * kFW;
-                        const int gy = rowMap(fy0 + r, Lu.h), gx = colMap(fx0 + c, Lu.w);
-                        s_g[r][c] = __ldg(Gu + (size_t)gy * Lu.pitch + gx);
-                    }
-                    __syncthreads();
-                    uint32_t vlo[3], vhi[3];
+            // collapse footprint of C_{j+1}: issued first, staged with the first pass
+            short4 cv = make_short4(0, 0, 0, 0);
+            if (hasUp && threadIdx.x < kFElems) {
+                const int r = threadIdx.x / kFW, c = threadIdx.x - r * kFW;
+                const int gy = interiorU ? fy0 + r : rowMap(fy0 + r, Lu.h);
+                const int gx = interiorU ? fx0 + c : colMap(fx0 + c, Lu.w);
+                cv = Lu.C[(size_t)gy * Lu.pitch + gx];
+            }
+            for (int c0 = 0;; c0 += kCamsPerPass) {
+                const int nc = min(kCamsPerPass, camCnt - c0);
+                uint32_t fv[kFLoads];
+                if (hasUp) {
 #pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        const uint2 a = unpackBytes(s_g[vr0][fc + k]);
-                        const uint2 b = unpackBytes(s_g[vr0 + 1][fc + k]);
-                        if (evenRow) {
-                            const uint2 c = unpackBytes(s_g[vr0 + 2][fc + k]);
-                            vlo[k] = a.x + 6 * b.x + c.x;
-                            vhi[k] = a.y + 6 * b.y + c.y;
-                        } else {
-                            vlo[k] = 4 * (a.x + b.x);
-                            vhi[k] = 4 * (a.y + b.y);
+                    for (int q = 0; q < kFLoads; q++) {
+                        const int k = threadIdx.x + q * kThreads;
+                        if (k < nc * kFElems) {
+                            const int cq = k / kFElems, e = k - cq * kFElems;
+                            const int r = e / kFW, c = e - r * kFW;
+                            const int cam = tileCam(raw, R.camLists, c0 + cq);
+                            const int gy = interiorU ? fy0 + r : rowMap(fy0 + r, Lu.h);
+                            const int gx = interiorU ? fx0 + c : colMap(fx0 + c, Lu.w);
+                            fv[q] = __ldg(reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
+                                          (size_t)gy * Lu.pitch + gx);
                         }
                     }
-                    u0lo = vlo[0] + 6 * vlo[1] + vlo[2];
-                    u0hi = vhi[0] + 6 * vhi[1] + vhi[2];
-                    u1lo = 4 * (vlo[1] + vlo[2]);
-                    u1hi = 4 * (vhi[1] + vhi[2]);
                 }
-                if (rowOk) {
-                    const size_t o = (size_t)cam * Lj.camStride + (size_t)y * Lj.pitch + x;
-                    const uint32_t wpair = __ldg(reinterpret_cast<const uint32_t*>(Lj.Wt + o));
-                    const uint2 gpair = __ldg(reinterpret_cast<const uint2*>(Lj.G + o));
-                    const int w0 = (int)(wpair & 0xFFFFu), w1 = (int)(wpair >> 16);
+                uint32_t wp[kCamsPerPass];
+                uint2 gp[kCamsPerPass];
+#pragma unroll
+                for (int q = 0; q < kCamsPerPass; q++) {
+                    wp[q] = 0;
+                    gp[q] = make_uint2(0, 0);
+                    if (q < nc && rowOk) {
+                        const int cam = tileCam(raw, R.camLists, c0 + q);
+                        const size_t o = (size_t)cam * Lj.camStride + (size_t)y * Lj.pitch + x;
+                        wp[q] = __ldg(reinterpret_cast<const uint32_t*>(Lj.Wt + o));
+                        gp[q] = __ldg(reinterpret_cast<const uint2*>(Lj.G + o));
+                    }
+                }
+                if (hasUp) {
+                    __syncthreads();  // readers of the previous pass / tile are done
+#pragma unroll
+                    for (int q = 0; q < kFLoads; q++) {
+                        const int k = threadIdx.x + q * kThreads;
+                        if (k < nc * kFElems) s_g[k] = fv[q];
+                    }
+                    if (c0 == 0 && threadIdx.x < kFElems) s_c[threadIdx.x] = make_int4(cv.x, cv.y, cv.z, 0);
+                    __syncthreads();
+                }
+#pragma unroll
+                for (int q = 0; q < kCamsPerPass; q++) {
+                    if (q >= nc) break;
+                    uint32_t u0lo = 0, u0hi = 0, u1lo = 0, u1hi = 0;
+                    if (hasUp) {
+                        const uint32_t* g = s_g + q * kFElems;
+                        uint32_t vlo[3], vhi[3];
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            const uint2 a = unpackBytes(g[vr0 * kFW + fc + k]);
+                            const uint2 b = unpackBytes(g[(vr0 + 1) * kFW + fc + k]);
+                            if (evenRow) {
+                                const uint2 c = unpackBytes(g[(vr0 + 2) * kFW + fc + k]);
+                                vlo[k] = a.x + 6 * b.x + c.x;
+                                vhi[k] = a.y + 6 * b.y + c.y;
+                            } else {
+                                vlo[k] = 4 * (a.x + b.x);
+                                vhi[k] = 4 * (a.y + b.y);
+                            }
+                        }
+                        u0lo = vlo[0] + 6 * vlo[1] + vlo[2];
+                        u0hi = vhi[0] + 6 * vhi[1] + vhi[2];
+                        u1lo = 4 * (vlo[1] + vlo[2]);
+                        u1hi = 4 * (vhi[1] + vhi[2]);
+                    }
+                    const int w0 = (int)(wp[q] & 0xFFFFu), w1 = (int)(wp[q] >> 16);
+                    const uint2 gq = gp[q];
                     // L = G - ((U + 32) >> 6), per channel
-                    r0[0] += w0 * ((int)(gpair.x & 0xFF) - (int)(((u0lo & 0xFFFFu) + 32) >> 6));
-                    r0[1] += w0 * ((int)((gpair.x >> 8) & 0xFF) - (int)(((u0hi & 0xFFFFu) + 32) >> 6));
-                    r0[2] += w0 * ((int)((gpair.x >> 16) & 0xFF) - (int)(((u0lo >> 16) + 32) >> 6));
-                    r1[0] += w1 * ((int)(gpair.y & 0xFF) - (int)(((u1lo & 0xFFFFu) + 32) >> 6));
-                    r1[1] += w1 * ((int)((gpair.y >> 8) & 0xFF) - (int)(((u1hi & 0xFFFFu) + 32) >> 6));
-                    r1[2] += w1 * ((int)((gpair.y >> 16) & 0xFF) - (int)(((u1lo >> 16) + 32) >> 6));
+                    r0[0] += w0 * ((int)(gq.x & 0xFF) - (int)(((u0lo & 0xFFFFu) + 32) >> 6));
+                    r0[1] += w0 * ((int)((gq.x >> 8) & 0xFF) - (int)(((u0hi & 0xFFFFu) + 32) >> 6));
+                    r0[2] += w0 * ((int)((gq.x >> 16) & 0xFF) - (int)(((u0lo >> 16) + 32) >> 6));
+                    r1[0] += w1 * ((int)(gq.y & 0xFF) - (int)(((u1lo & 0xFFFFu) + 32) >> 6));
+                    r1[1] += w1 * ((int)((gq.y >> 8) & 0xFF) - (int)(((u1hi & 0xFFFFu) + 32) >> 6));
+                    r1[2] += w1 * ((int)((gq.y >> 16) & 0xFF) - (int)(((u1lo >> 16) + 32) >> 6));
                     wsum0 += w0;
                     wsum1 += w1;
                 }
+                if (c0 + kCamsPerPass >= camCnt) break;
             }
         }
         // normalise
@@ -321,27 +427,19 @@ __global__ void __launch_bounds__(kThreads) k_blend(const Segment* __restrict__ 
             for (int c = 0; c < 3; c++) { n0[c] = (r0[c] + 128) >> 8; n1[c] = (r1[c] + 128) >> 8; }
         } else {
             const int d0 = wsum0 ? wsum0 : 1, d1 = wsum1 ? wsum1 : 1;
+            const float i0 = __frcp_rn((float)d0), i1 = __frcp_rn((float)d1);
 #pragma unroll
-            for (int c = 0; c < 3; c++) { n0[c] = r0[c] / d0; n1[c] = r1[c] / d1; }
+            for (int c = 0; c < 3; c++) { n0[c] = divTrunc(r0[c], d0, i0); n1[c] = divTrunc(r1[c], d1, i1); }
         }
-        // collapse: + pyrUp32(C_{j+1})
-        if (j < R.L && active) {
-            const LevelDev& Lu = R.lv[j + 1];
-            __syncthreads();
-            if (threadIdx.x < kFH * kFW) {
-                const int r = threadIdx.x / kFW, c = threadIdx.x - r * kFW;
-                const int gy = rowMap(fy0 + r, Lu.h), gx = colMap(fx0 + c, Lu.w);
-                const short4 v = Lu.C[(size_t)gy * Lu.pitch + gx];
-                s_c[r][c] = make_int4(v.x, v.y, v.z, 0);
-            }
-            __syncthreads();
+        // collapse: + pyrUp32(C_{j+1}), from the footprint staged above
+        if (hasUp && active) {
             int v[3][3];
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                const int4 a = s_c[vr0][fc + k];
-                const int4 b = s_c[vr0 + 1][fc + k];
+                const int4 a = s_c[vr0 * kFW + fc + k];
+                const int4 b = s_c[(vr0 + 1) * kFW + fc + k];
                 if (evenRow) {
-                    const int4 c = s_c[vr0 + 2][fc + k];
+                    const int4 c = s_c[(vr0 + 2) * kFW + fc + k];
                     v[k][0] = a.x + 6 * b.x + c.x;
                     v[k][1] = a.y + 6 * b.y + c.y;
                     v[k][2] = a.z + 6 * b.z + c.z;
@@ -360,17 +458,22 @@ __global__ void __launch_bounds__(kThreads) k_blend(const Segment* __restrict__ 
         if (!rowOk) continue;
         if (j > 0) {
             short4* Cj = Lj.C + (size_t)y * Lj.pitch + x;
-            if (x < Lj.w) Cj[0] = make_short4((short)n0[0], (short)n0[1], (short)n0[2], 0);
-            if (x + 1 < Lj.w) Cj[1] = make_short4((short)n1[0], (short)n1[1], (short)n1[2], 0);
+            if (x + 1 < Lj.w) {
+                *reinterpret_cast<int4*>(Cj) = make_int4(
+                    (int)((uint32_t)(uint16_t)n0[0] | ((uint32_t)(uint16_t)n0[1] << 16)), (int)(uint32_t)(uint16_t)n0[2],
+                    (int)((uint32_t)(uint16_t)n1[0] | ((uint32_t)(uint16_t)n1[1] << 16)), (int)(uint32_t)(uint16_t)n1[2]);
+            } else if (x < Lj.w) {
+                Cj[0] = make_short4((short)n0[0], (short)n0[1], (short)n0[2], 0);
+            }
         } else {
             const FrameDev& F = *sg.frame;
             uint32_t o0 = 0, o1 = 0;
-            if (item.cls != 0) {
+            if (cls != 0) {
                 o0 = (uint32_t)min(max(n0[0], 0), 255) | ((uint32_t)min(max(n0[1], 0), 255) << 8) |
                      ((uint32_t)min(max(n0[2], 0), 255) << 16);
                 o1 = (uint32_t)min(max(n1[0], 0), 255) | ((uint32_t)min(max(n1[1], 0), 255) << 8) |
                      ((uint32_t)min(max(n1[2], 0), 255) << 16);
-                if (item.cls == 2) {
+                if (cls == 2) {
                     const uint8_t* um = R.unionMask + (size_t)y * Lj.pitch + x;
                     if (!um[0]) o0 = 0;
                     if (x + 1 < Lj.w && !um[1]) o1 = 0;
@@ -419,25 +522,40 @@ static int gridFor(int total, int perSm)
     return total < cap ? total : cap;
 }
 
+// Every per-frame kernel is launched with programmatic stream serialisation,
+// so its prologue overlaps the previous kernel's tail (see waitPrevGrid).
+template <class... Args>
+static cudaError_t launchPdl(void (*kernel)(Args...), int grid, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    k_remap<<<gridFor(total, 8), kThreads, 0, st>>>(segs, nsegs, total);
-    return cudaGetLastError();
+    return launchPdl(k_remap, gridFor(total, 8), st, segs, nsegs, total);
 }
 
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    k_pyrdown<<<gridFor(total, 6), kThreads, 0, st>>>(segs, nsegs, total);
-    return cudaGetLastError();
+    return launchPdl(k_pyrdown, gridFor(total, 6), st, segs, nsegs, total);
 }
 
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    k_blend<<<gridFor(total, 8), kThreads, 0, st>>>(segs, nsegs, total);
-    return cudaGetLastError();
+    return launchPdl(k_blend, gridFor(total, 8), st, segs, nsegs, total);
 }
 
 cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,

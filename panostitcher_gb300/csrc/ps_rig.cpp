@@ -384,16 +384,30 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         blendOff_[j] = (int)blend.size();
         for (int ty = 0; ty < bY; ty++)
             for (int tx = 0; tx < bX; tx++) {
-                const uint32_t off = (uint32_t)cams.size();
+                std::vector<uint8_t> list;
                 for (int c = 0; c < n; c++)
-                    if (hB[j][((size_t)c * bY + ty) * bX + tx]) cams.push_back((uint8_t)c);
+                    if (hB[j][((size_t)c * bY + ty) * bX + tx]) list.push_back((uint8_t)c);
                 uint8_t cls = 0;
                 if (j == 0) {
                     const int tw = std::min(kBlendTW, g.w - tx * kBlendTW), th = std::min(kBlendTH, g.h - ty * kBlendTH);
                     const int cnt = hCounts[(size_t)ty * bX0 + tx];
                     cls = cnt == 0 ? 0 : (cnt == tw * th ? 1 : 2);
                 }
-                blend.push_back({(uint8_t)j, cls, (uint16_t)tx, (uint16_t)ty, 0, off, (uint32_t)cams.size() - off});
+                BlendItem it;
+                std::memset(&it, 0, sizeof it);
+                it.level = (uint8_t)j;
+                it.cls = cls;
+                it.camCnt = (uint8_t)list.size();
+                it.tx = (uint16_t)tx;
+                it.ty = (uint16_t)ty;
+                if (list.size() <= (size_t)kInlineCams) {
+                    for (size_t q = 0; q < list.size(); q++) it.cams[q] = list[q];
+                } else {
+                    const uint32_t off = (uint32_t)cams.size();
+                    std::memcpy(it.cams, &off, sizeof off);
+                    cams.insert(cams.end(), list.begin(), list.end());
+                }
+                blend.push_back(it);
             }
         blendCnt_[j] = (int)blend.size() - blendOff_[j];
     }
