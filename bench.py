@@ -259,6 +259,14 @@ def run_ours(args, world, rank, local, dist):
         kernels[name] = {"launches_per_frame": n // prof_steps, "ms_per_frame": kms / prof_steps,
                          "alg_bytes_per_launch": kb / max(n, 1), "gbs": kb / max(kms, 1e-9) / 1e6}
         total_ms += kms
+    by_level = {}
+    for kind, name in r.KERNELS.items():
+        lv = []
+        for level in range(r.num_levels + 1):
+            n, kms, kb = r.profile_read(kind, level)
+            if n:
+                lv.append([level, round(kms / prof_steps * 1e3, 2), round(kb / max(kms, 1e-9) / 1e6, 1)])
+        by_level[name] = lv
     r.profile(False)
     for k in kernels.values():
         k["share"] = round(k["ms_per_frame"] * prof_steps / max(total_ms, 1e-9), 4)
@@ -274,6 +282,7 @@ def run_ours(args, world, rank, local, dist):
                        "frame_alg_gbs": round(r.algorithmic_bytes(4, 4) / (ms_max / args.steps) / 1e6, 1)}
     out["kernels"] = {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                       for k, v in kernels.items()}
+    out["kernels_by_level"] = {"columns": ["level", "us_per_frame", "alg_GBps"], **by_level}
 
     def guarded(fn, *a):
         try:

@@ -134,7 +134,8 @@ int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out,
 /* Measurement hooks (no reference counterpart).  While profiling is on,
    renders launch step by step with a CUDA event pair around every launch
    (no graph); ps_render_profile_read aggregates the finished launches of
-   one kernel kind (0 remap, 1 pyrDown, 2 blend) at one pyramid level
+   one kernel kind (0 remap, 1 pyrDown, 2 blend, 3 the tail kernel that runs
+   the few-tile top levels, reported at its lowest blend level) at one level
    (-1 = all levels): launch count, summed device milliseconds and summed
    algorithmic bytes (each input and output element counted once).
    Enabling resets the aggregates. */

@@ -179,7 +179,7 @@ int ps_render_profile_read(ps_render* r, int kind, int level, long long* launche
 {
     return guarded([&] {
         if (!r) fail(PS_EINVAL, "render is NULL");
-        if (kind < 0 || kind > 2) fail(PS_EINVAL, "kind %d not in 0..2", kind);
+        if (kind < 0 || kind > 3) fail(PS_EINVAL, "kind %d not in 0..3", kind);
         r->prof.read(kind, level, launches, total_ms, bytes);
     });
 }

@@ -41,6 +41,19 @@ struct LevelDev {
     short4* C;
 };
 
+// Work items (one per tile), resident per rig and built at prepare time.
+struct RemapItem { uint16_t cam, pad; uint16_t tx, ty; uint32_t mapTile; };
+struct DownItem { uint8_t cam, level; uint16_t tx, ty; uint16_t pad; };   // level = output level
+// A blend tile lists the cameras whose weight touches it: up to 8 inline,
+// more through RigDev::camLists (cams[0..3] then hold the uint32 offset).
+struct alignas(16) BlendItem { uint8_t level, cls, camCnt, flags; uint16_t tx, ty; uint8_t cams[8]; };
+constexpr int kInlineCams = 8;
+// flags bit 0: one camera, weight 256 on every pixel of the tile, so the
+// normalised value is the Laplacian itself (R = 256 L, W = 256).
+constexpr int kTileUniform = 1;
+// cls of a level-0 blend tile: 0 uncovered (write zeros), 1 fully covered,
+// 2 partially covered (read the union mask).  Unused above level 0.
+
 struct RigDev {
     int n, L, W, H;
     int full;                 // union of coverages == whole canvas
@@ -49,6 +62,14 @@ struct RigDev {
     const uint8_t* unionMask; // level-0 union coverage (0/255), pitch = lv[0].pitch
     const uint8_t* camLists;  // camera indices of blend tiles with more than 8 cameras
     LevelDev lv[PS_MAX_LEVELS + 1];
+    // work items of every level (used by the tail kernel)
+    const DownItem* downItems;
+    const BlendItem* blendItems;
+    int downOff[PS_MAX_LEVELS + 1], downCnt[PS_MAX_LEVELS + 1];
+    int blendOff[PS_MAX_LEVELS + 1], blendCnt[PS_MAX_LEVELS + 1];
+    // the small top of the pyramid runs in one launch: pyrDown levels
+    // tailDown..L, then blend levels L..tailBlend (L + 1 = none)
+    int tailDown, tailBlend;
 };
 
 // Per-frame arguments of one rig in a launch (device resident, rewritten
@@ -63,16 +84,6 @@ struct FrameDev {
     const uint8_t* luts;      // n * 768 device bytes (B, G, R tables)
     int* status;              // device error word (0 = ok)
 };
-
-// Work items (one per tile), resident per rig and built at prepare time.
-struct RemapItem { uint16_t cam, pad; uint16_t tx, ty; uint32_t mapTile; };
-struct DownItem { uint8_t cam, level; uint16_t tx, ty; uint16_t pad; };   // level = output level
-// A blend tile lists the cameras whose weight touches it: up to 8 inline,
-// more through RigDev::camLists (cams[0..3] then hold the uint32 offset).
-struct alignas(16) BlendItem { uint8_t level, cls, camCnt, pad; uint16_t tx, ty; uint8_t cams[8]; };
-constexpr int kInlineCams = 8;
-// cls of a level-0 blend tile: 0 uncovered (write zeros), 1 fully covered,
-// 2 partially covered (read the union mask).  Unused above level 0.
 
 // A launch runs the concatenation of segments: `count` items of one rig,
 // numbered from `prefix` in the launch.  Several rigs (a batch, or the

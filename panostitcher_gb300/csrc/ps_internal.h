@@ -110,6 +110,8 @@ cudaError_t launchWeightDown(const uint16_t* wj, int sw, int sh, int spitch, lon
 // per-tile "any non-zero" flags of a 16-bit or 8-bit plane per camera
 cudaError_t launchTileFlags16(const uint16_t* p, int w, int h, int pitch, long long camStride, int n, int tw,
                               int th, int tilesX, int tilesY, uint8_t* flags, cudaStream_t st);
+cudaError_t launchTileNot256(const uint16_t* p, int w, int h, int pitch, long long camStride, int n, int tw, int th,
+                             int tilesX, int tilesY, uint8_t* flags, cudaStream_t st);
 cudaError_t launchTileFlags8(const uint8_t* p, int w, int h, int pitch, long long camStride, int n, int tw,
                              int th, int tilesX, int tilesY, uint8_t* flags, cudaStream_t st);
 // number of non-zero pixels of a 16-bit plane, all cameras (added to *out)
@@ -131,6 +133,8 @@ cudaError_t launchImagesToLevel0(const void* const* images, const long long* pit
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, cudaStream_t st);
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_t st);
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st);
+// one cluster per segment: the rig's pyrDown levels tailDown..L and blend levels L..tailBlend
+cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st);
 
 // ---- standalone primitive ---------------------------------------------------------
 cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,

@@ -15,6 +15,7 @@
 // The reference runs the same arithmetic as ~35 launches per camera plus
 // ~36 per frame over full-canvas int16/int32 images
 // (source/CudaAccel/CudaMultibandBlend.cpp:785-823).
+#include "ps_async.cuh"
 #include "ps_device.cuh"
 #include "ps_internal.h"
 
@@ -164,86 +165,106 @@ constexpr int kDInH = 2 * kDownTH + 3;   // 35
 
 constexpr int kDLoads = (kDInH * kDInW + kThreads - 1) / kThreads;   // 10 tile elements per thread
 
+struct DownSmem {
+    uint32_t in[kDInH][kDInW];
+    uint2 v[kDownTH][kDInW];
+    uint32_t magic[257];
+    int rowIdx[kDInH], colIdx[kDInW];  // border index tables of the current tile
+};
+
+__device__ __forceinline__ void initMagic(uint32_t* magic)
+{
+    for (int m = threadIdx.x; m < 257; m += blockDim.x) magic[m] = m ? (uint32_t)((16777216u + m - 1) / m) : 0u;
+}
+
+// One 32x16 output tile of one camera (all kThreads threads of the CTA).
+__device__ __forceinline__ void pyrDownTile(const RigDev& R, const DownItem item, DownSmem& sm)
+{
+    const int ox = threadIdx.x & 31, oy = threadIdx.x >> 5;
+    const LevelDev& Ls = R.lv[item.level - 1];
+    const LevelDev& Ld = R.lv[item.level];
+    const int sw = Ls.w, sh = Ls.h;
+    const int ox0 = item.tx * kDownTW, oy0 = item.ty * kDownTH;
+    const int ix0 = 2 * ox0 - 2, iy0 = 2 * oy0 - 2;
+    const uint32_t* G = reinterpret_cast<const uint32_t*>(Ls.G) + (size_t)item.cam * Ls.camStride;
+    // issue every load of the tile before the first barrier: the input tile and the two divisors
+    const int X = ox0 + ox, Y0 = oy0 + oy, Y1 = Y0 + 8;
+    const size_t o0 = (size_t)item.cam * Ld.camStride + (size_t)Y0 * Ld.pitch + X;
+    const size_t o1 = o0 + (size_t)8 * Ld.pitch;
+    const bool ok0 = X < Ld.w && Y0 < Ld.h, ok1 = X < Ld.w && Y1 < Ld.h;
+    const int m0 = ok0 ? __ldg(Ld.Am + o0) : 0, m1 = ok1 ? __ldg(Ld.Am + o1) : 0;
+    uint32_t v[kDLoads];
+    const bool interior = ix0 >= 0 && iy0 >= 0 && ix0 + kDInW <= sw && iy0 + kDInH <= sh;
+    if (!interior) {
+        // one modulo per row / column instead of two per element
+        if (threadIdx.x < kDInH) sm.rowIdx[threadIdx.x] = rowMap(iy0 + (int)threadIdx.x, sh);
+        else if (threadIdx.x < kDInH + kDInW) sm.colIdx[threadIdx.x - kDInH] = colMap(ix0 + (int)threadIdx.x - kDInH, sw);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < kDLoads; q++) {
+        const int k = threadIdx.x + q * kThreads;
+        if (k < kDInH * kDInW) {
+            const int r = k / kDInW, c = k - r * kDInW;
+            const int gy = interior ? iy0 + r : sm.rowIdx[r];
+            const int gx = interior ? ix0 + c : sm.colIdx[c];
+            v[q] = __ldg(G + (size_t)gy * Ls.pitch + gx);
+        }
+    }
+    __syncthreads();  // the previous tile's readers are done with shared memory
+#pragma unroll
+    for (int q = 0; q < kDLoads; q++) {
+        const int k = threadIdx.x + q * kThreads;
+        if (k < kDInH * kDInW) (&sm.in[0][0])[k] = v[q];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kDownTH * kDInW; k += kThreads) {
+        const int r = k / kDInW, c = k - r * kDInW;
+        uint32_t lo = 0, hi = 0;
+#pragma unroll
+        for (int t = 0; t < 5; t++) {
+            const uint2 p = unpackBytes(sm.in[2 * r + t][c]);
+            lo += c_k5[t] * p.x;
+            hi += c_k5[t] * p.y;
+        }
+        sm.v[r][c] = make_uint2(lo, hi);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        const int r = oy + 8 * half;
+        uint32_t lo = 0, hi = 0;
+#pragma unroll
+        for (int t = 0; t < 5; t++) {
+            const uint2 q = sm.v[r][2 * ox + t];
+            lo += c_k5[t] * q.x;
+            hi += c_k5[t] * q.y;
+        }
+        const int m = half ? m1 : m0;
+        uint32_t outv = 0;
+        if (m) {
+            const unsigned long long mg = sm.magic[m];
+            const uint32_t b = (uint32_t)(((lo & 0xFFFFu) * mg) >> 24);
+            const uint32_t rr = (uint32_t)(((lo >> 16) * mg) >> 24);
+            const uint32_t g = (uint32_t)(((hi & 0xFFFFu) * mg) >> 24);
+            outv = b | (g << 8) | (rr << 16);
+        }
+        if (half ? ok1 : ok0) reinterpret_cast<uint32_t*>(Ld.G)[half ? o1 : o0] = outv;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict__ segs, int nsegs, int total)
 {
-    __shared__ uint32_t s_in[kDInH][kDInW];
-    __shared__ uint2 s_v[kDownTH][kDInW];
-    __shared__ uint32_t s_magic[257];
-    for (int m = threadIdx.x; m < 257; m += kThreads) s_magic[m] = m ? (uint32_t)((16777216u + m - 1) / m) : 0u;
+    __shared__ DownSmem sm;
+    initMagic(sm.magic);
     int s = 0, begin, end;
     itemRange(total, begin, end);
-    const int ox = threadIdx.x & 31, oy = threadIdx.x >> 5;
     waitPrevGrid();
     allowNextGrid();
     for (int it = begin; it < end; it++) {
         s = findSegment(segs, nsegs, it, s);
         const Segment sg = segs[s];
-        const DownItem item = static_cast<const DownItem*>(sg.items)[it - sg.prefix];
-        const RigDev& R = *sg.rig;
-        const LevelDev& Ls = R.lv[item.level - 1];
-        const LevelDev& Ld = R.lv[item.level];
-        const int sw = Ls.w, sh = Ls.h;
-        const int ox0 = item.tx * kDownTW, oy0 = item.ty * kDownTH;
-        const int ix0 = 2 * ox0 - 2, iy0 = 2 * oy0 - 2;
-        const uint32_t* G = reinterpret_cast<const uint32_t*>(Ls.G) + (size_t)item.cam * Ls.camStride;
-        // issue every load of the item before the first barrier: the tile and the two divisors
-        const int X = ox0 + ox, Y0 = oy0 + oy, Y1 = Y0 + 8;
-        const size_t o0 = (size_t)item.cam * Ld.camStride + (size_t)Y0 * Ld.pitch + X;
-        const size_t o1 = o0 + (size_t)8 * Ld.pitch;
-        const bool ok0 = X < Ld.w && Y0 < Ld.h, ok1 = X < Ld.w && Y1 < Ld.h;
-        const int m0 = ok0 ? __ldg(Ld.Am + o0) : 0, m1 = ok1 ? __ldg(Ld.Am + o1) : 0;
-        uint32_t v[kDLoads];
-        const bool interior = ix0 >= 0 && iy0 >= 0 && ix0 + kDInW <= sw && iy0 + kDInH <= sh;
-#pragma unroll
-        for (int q = 0; q < kDLoads; q++) {
-            const int k = threadIdx.x + q * kThreads;
-            if (k < kDInH * kDInW) {
-                const int r = k / kDInW, c = k - r * kDInW;
-                const int gy = interior ? iy0 + r : rowMap(iy0 + r, sh);
-                const int gx = interior ? ix0 + c : colMap(ix0 + c, sw);
-                v[q] = __ldg(G + (size_t)gy * Ls.pitch + gx);
-            }
-        }
-        __syncthreads();  // the previous item's readers are done with shared memory
-#pragma unroll
-        for (int q = 0; q < kDLoads; q++) {
-            const int k = threadIdx.x + q * kThreads;
-            if (k < kDInH * kDInW) (&s_in[0][0])[k] = v[q];
-        }
-        __syncthreads();
-        for (int k = threadIdx.x; k < kDownTH * kDInW; k += kThreads) {
-            const int r = k / kDInW, c = k - r * kDInW;
-            uint32_t lo = 0, hi = 0;
-#pragma unroll
-            for (int t = 0; t < 5; t++) {
-                const uint2 p = unpackBytes(s_in[2 * r + t][c]);
-                lo += c_k5[t] * p.x;
-                hi += c_k5[t] * p.y;
-            }
-            s_v[r][c] = make_uint2(lo, hi);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int half = 0; half < 2; half++) {
-            const int r = oy + 8 * half;
-            uint32_t lo = 0, hi = 0;
-#pragma unroll
-            for (int t = 0; t < 5; t++) {
-                const uint2 q = s_v[r][2 * ox + t];
-                lo += c_k5[t] * q.x;
-                hi += c_k5[t] * q.y;
-            }
-            const int m = half ? m1 : m0;
-            uint32_t outv = 0;
-            if (m) {
-                const unsigned long long mg = s_magic[m];
-                const uint32_t b = (uint32_t)(((lo & 0xFFFFu) * mg) >> 24);
-                const uint32_t rr = (uint32_t)(((lo >> 16) * mg) >> 24);
-                const uint32_t g = (uint32_t)(((hi & 0xFFFFu) * mg) >> 24);
-                outv = b | (g << 8) | (rr << 16);
-            }
-            if (half ? ok1 : ok0) reinterpret_cast<uint32_t*>(Ld.G)[half ? o1 : o0] = outv;
-        }
+        pyrDownTile(*sg.rig, static_cast<const DownItem*>(sg.items)[it - sg.prefix], sm);
     }
 }
 
@@ -258,18 +279,43 @@ __global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict_
 //                                     CudaMultibandBlend.cpp:220-231
 //   level 0: out = clamp(C_0, 0, 255), 0 where no camera covers
 //   (convertTo(CV_8U) + setTo(0, maskNot), CudaMultibandBlend.cpp:820-822).
-// A CTA covers a 64x8 tile; thread t owns pixels (2*(t%32), t/32) and the
-// one to its right.  Every global load of a tile (the C_{j+1} footprint, the
-// G_{j+1} footprints of two cameras at a time, their weights and G_j pixels) is
-// issued before one barrier, so a tile costs one memory round trip; the next
-// tile's descriptor is prefetched meanwhile.
+// A tile whose only camera has weight 256 on every pixel has N = L exactly
+// (R = 256 L, W = 256; (256 L + 128) >> 8 = L), so it skips the weights.
+//
+// A tile is 64x8 canvas pixels; consumer thread t (of 256) owns pixels
+// (2*(t%32), t/32) and the one to its right.  Work flows through a 3-stage
+// shared-memory ring of "units" (a tile and up to two of its cameras).  A
+// dedicated producer warp stages each unit with bulk asynchronous copies of
+// whole rows -- the cameras' G_j and weight rows, their G_{j+1} footprint
+// rows and, with a tile's last unit, the C_{j+1} footprint rows -- completing
+// on the stage's "full" mbarrier; the eight consumer warps compute from
+// shared memory and release the stage on its "empty" mbarrier.  Tiles whose
+// footprints cross the canvas border (horizontal wrap, vertical
+// reflect-101) are staged by the consumers with the reference's index
+// mapping.
 // ============================================================================
-constexpr int kFW = kBlendTW / 2 + 2;  // 34
-constexpr int kFH = kBlendTH / 2 + 2;  // 6
+constexpr int kFW = kBlendTW / 2 + 2;  // 34: footprint columns fx0 .. fx0+33
+constexpr int kFH = kBlendTH / 2 + 2;  // 6:  footprint rows    fy0 .. fy0+5
 constexpr int kFElems = kFW * kFH;     // 204
-constexpr int kCamsPerPass = 2;
-constexpr int kFLoads = (kCamsPerPass * kFElems + kThreads - 1) / kThreads;  // 4
+constexpr int kBStages = 3;
+constexpr int kCamsPerUnit = 2;
+constexpr int kFpW = 40;   // staged footprint row: columns fx0-3 .. fx0+36 (16-byte aligned start)
+constexpr int kCfW = 36;   // staged collapse footprint row: columns fx0-1 .. fx0+34
 constexpr int kMaxSmemSegs = 64;
+constexpr int kConsumers = kThreads;          // 8 warps
+constexpr int kBlendThreads = kConsumers + 32;  // + the producer warp
+
+struct alignas(16) BlendStage {
+    uint32_t gj[kCamsPerUnit][kBlendTH][kBlendTW];  // G_j, uchar4
+    uint16_t w[kCamsPerUnit][kBlendTH][kBlendTW];   // weights
+    uint32_t fp[kCamsPerUnit][kFH][kFpW];           // G_{j+1} footprint
+    uint2 cf[kFH][kCfW];                            // C_{j+1} footprint (short4 bits)
+};
+
+struct UnitInfo {
+    uint4 raw;
+    int seg, chunk, valid, staged;  // staged: copies issued by the producer
+};
 
 // q-th camera of a blend tile (raw 16-byte descriptor)
 __device__ __forceinline__ int tileCam(const uint4& raw, const uint8_t* camLists, int q)
@@ -279,227 +325,432 @@ __device__ __forceinline__ int tileCam(const uint4& raw, const uint8_t* camLists
     return (int)((w >> (8 * (q & 3))) & 0xFF);
 }
 
-__global__ void __launch_bounds__(kThreads, 4) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total)
+__device__ __forceinline__ int unitChunks(const uint4& raw)
 {
-    __shared__ uint32_t s_g[kCamsPerPass * kFElems];
-    __shared__ int4 s_c[kFElems];
-    __shared__ Segment s_segs[kMaxSmemSegs];
-    const Segment* segs = gsegs;
-    if (nsegs <= kMaxSmemSegs) {
-        for (int k = threadIdx.x; k < nsegs; k += kThreads) s_segs[k] = gsegs[k];
-        __syncthreads();
-        segs = s_segs;
+    const int cnt = (raw.x >> 16) & 0xFF;
+    return cnt <= kCamsPerUnit ? 1 : (cnt + kCamsPerUnit - 1) / kCamsPerUnit;
+}
+
+struct BlendAcc {
+    int r0[3], r1[3];
+    int wsum0, wsum1;
+};
+
+// Stage one unit with index-mapped loads (border tiles; every tile of the
+// tail kernel).  Threads 0..kConsumers-1; the caller synchronises.
+// fRow / fCol: footprint index tables (kFH / kFW ints) filled here; sync is
+// the barrier over the calling threads.
+template <class Sync>
+__device__ __forceinline__ void stageUnitDirect(BlendStage& S, const RigDev& R, const uint4& raw, int chunk, int* fRow,
+                                                int* fCol, Sync sync)
+{
+    const int lx = (threadIdx.x & 31) * 2, ly = threadIdx.x >> 5;
+    const int j = raw.x & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
+    const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
+    const LevelDev& Lj = R.lv[j];
+    const bool hasUp = j < R.L;
+    const LevelDev& Lu = R.lv[hasUp ? j + 1 : j];
+    const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
+    const int c0 = chunk * kCamsPerUnit;
+    const int nc = max(0, min(kCamsPerUnit, camCnt - c0));
+    const bool last = chunk == unitChunks(raw) - 1;
+    const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
+    for (int q = 0; q < nc; q++) {
+        const int cam = tileCam(raw, R.camLists, c0 + q);
+        uint2 g = make_uint2(0, 0);
+        uint32_t w = 0;
+        if (y < Lj.h) {
+            const size_t o = (size_t)cam * Lj.camStride + (size_t)y * Lj.pitch + x;
+            g = __ldg(reinterpret_cast<const uint2*>(Lj.G + o));
+            w = __ldg(reinterpret_cast<const uint32_t*>(Lj.Wt + o));
+        }
+        *reinterpret_cast<uint2*>(&S.gj[q][ly][lx]) = g;
+        *reinterpret_cast<uint32_t*>(&S.w[q][ly][lx]) = w;
     }
+    if (hasUp) {
+        if (threadIdx.x < kFH) fRow[threadIdx.x] = rowMap(fy0 + (int)threadIdx.x, Lu.h);
+        else if (threadIdx.x < kFH + kFW) fCol[threadIdx.x - kFH] = colMap(fx0 + (int)threadIdx.x - kFH, Lu.w);
+        sync();
+        for (int k = threadIdx.x; k < nc * kFElems; k += kConsumers) {
+            const int q = k / kFElems, e = k - q * kFElems;
+            const int r = e / kFW, c = e - r * kFW;
+            const int cam = tileCam(raw, R.camLists, c0 + q);
+            S.fp[q][r][c + 3] = __ldg(reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
+                                      (size_t)fRow[r] * Lu.pitch + fCol[c]);
+        }
+        if (last && threadIdx.x < kFElems) {
+            const int r = threadIdx.x / kFW, c = threadIdx.x - r * kFW;
+            S.cf[r][c + 1] = *reinterpret_cast<const uint2*>(Lu.C + (size_t)fRow[r] * Lu.pitch + fCol[c]);
+        }
+    }
+}
+
+// Accumulate one unit from its stage; at a tile's last unit normalise,
+// collapse and store.  Threads 0..kConsumers-1.  staged: the unit came from
+// the bulk copies (weights absent for uniform tiles).
+__device__ __forceinline__ void computeUnit(const BlendStage& S, const RigDev& R, const FrameDev& F, const uint4& raw,
+                                            int chunk, bool staged, BlendAcc& acc)
+{
     const int lx = (threadIdx.x & 31) * 2, ly = threadIdx.x >> 5;
     // vertical taps of the zero-inserted upsample for this row's parity:
     // even rows take footprint rows ly/2 .. ly/2+2 with weights 1 6 1,
     // odd rows (ly+1)/2 .. (ly+1)/2+1 with weights 4 4
     const bool evenRow = (ly & 1) == 0;
     const int vr0 = evenRow ? ly / 2 : (ly - 1) / 2 + 1;
-    // footprint columns: even pixel lx/2 .. lx/2+2 (1 6 1), odd pixel lx/2+1 .. lx/2+2 (4 4)
+    // footprint columns: even pixel fc .. fc+2 (1 6 1), odd pixel fc+1 .. fc+2 (4 4)
     const int fc = lx / 2;
-    // interleaved tiles balance the load (uncovered bands are cheap, seams are not)
-    int s = 0;
-    uint4 nextRaw = make_uint4(0, 0, 0, 0);
-    if ((int)blockIdx.x < total) {
-        s = findSegment(segs, nsegs, blockIdx.x, 0);
-        nextRaw = __ldg(static_cast<const uint4*>(segs[s].items) + (blockIdx.x - segs[s].prefix));
+    const int j = raw.x & 0xFF, cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
+    const bool uni = ((raw.x >> 24) & kTileUniform) != 0;
+    const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
+    const LevelDev& Lj = R.lv[j];
+    const bool hasUp = j < R.L;
+    const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
+    const bool rowOk = y < Lj.h;
+    const bool active = !(j == 0 && cls == 0);
+    const int c0 = chunk * kCamsPerUnit;
+    const int nc = max(0, min(kCamsPerUnit, camCnt - c0));
+    const bool first = chunk == 0, last = chunk == unitChunks(raw) - 1;
+    const bool fast = uni && staged;  // weights were not staged
+    if (first) {
+        acc.r0[0] = acc.r0[1] = acc.r0[2] = acc.r1[0] = acc.r1[1] = acc.r1[2] = 0;
+        acc.wsum0 = acc.wsum1 = 0;
     }
+    if (active) {
+        for (int q = 0; q < nc; q++) {
+            uint32_t u0lo = 0, u0hi = 0, u1lo = 0, u1hi = 0;
+            if (hasUp) {
+                const uint32_t* g = &S.fp[q][0][0] + 3;
+                uint32_t vlo[3], vhi[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const uint2 a = unpackBytes(g[vr0 * kFpW + fc + k]);
+                    const uint2 b = unpackBytes(g[(vr0 + 1) * kFpW + fc + k]);
+                    if (evenRow) {
+                        const uint2 c = unpackBytes(g[(vr0 + 2) * kFpW + fc + k]);
+                        vlo[k] = a.x + 6 * b.x + c.x;
+                        vhi[k] = a.y + 6 * b.y + c.y;
+                    } else {
+                        vlo[k] = 4 * (a.x + b.x);
+                        vhi[k] = 4 * (a.y + b.y);
+                    }
+                }
+                u0lo = vlo[0] + 6 * vlo[1] + vlo[2];
+                u0hi = vhi[0] + 6 * vhi[1] + vhi[2];
+                u1lo = 4 * (vlo[1] + vlo[2]);
+                u1hi = 4 * (vhi[1] + vhi[2]);
+            }
+            const uint2 gq = *reinterpret_cast<const uint2*>(&S.gj[q][ly][lx]);
+            // L = G - ((U + 32) >> 6), per channel
+            const int l0b = (int)(gq.x & 0xFF) - (int)(((u0lo & 0xFFFFu) + 32) >> 6);
+            const int l0g = (int)((gq.x >> 8) & 0xFF) - (int)(((u0hi & 0xFFFFu) + 32) >> 6);
+            const int l0r = (int)((gq.x >> 16) & 0xFF) - (int)(((u0lo >> 16) + 32) >> 6);
+            const int l1b = (int)(gq.y & 0xFF) - (int)(((u1lo & 0xFFFFu) + 32) >> 6);
+            const int l1g = (int)((gq.y >> 8) & 0xFF) - (int)(((u1hi & 0xFFFFu) + 32) >> 6);
+            const int l1r = (int)((gq.y >> 16) & 0xFF) - (int)(((u1lo >> 16) + 32) >> 6);
+            if (fast) {
+                acc.r0[0] = l0b; acc.r0[1] = l0g; acc.r0[2] = l0r;
+                acc.r1[0] = l1b; acc.r1[1] = l1g; acc.r1[2] = l1r;
+            } else {
+                const uint32_t wq = *reinterpret_cast<const uint32_t*>(&S.w[q][ly][lx]);
+                const int w0 = (int)(wq & 0xFFFFu), w1 = (int)(wq >> 16);
+                acc.r0[0] += w0 * l0b; acc.r0[1] += w0 * l0g; acc.r0[2] += w0 * l0r;
+                acc.r1[0] += w1 * l1b; acc.r1[1] += w1 * l1g; acc.r1[2] += w1 * l1r;
+                acc.wsum0 += w0;
+                acc.wsum1 += w1;
+            }
+        }
+    }
+    if (!last) return;
+    int n0[3], n1[3];
+    if (fast) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) { n0[c] = acc.r0[c]; n1[c] = acc.r1[c]; }
+    } else if (R.full) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) { n0[c] = (acc.r0[c] + 128) >> 8; n1[c] = (acc.r1[c] + 128) >> 8; }
+    } else {
+        const int d0 = acc.wsum0 ? acc.wsum0 : 1, d1 = acc.wsum1 ? acc.wsum1 : 1;
+        const float i0 = __frcp_rn((float)d0), i1 = __frcp_rn((float)d1);
+#pragma unroll
+        for (int c = 0; c < 3; c++) { n0[c] = divTrunc(acc.r0[c], d0, i0); n1[c] = divTrunc(acc.r1[c], d1, i1); }
+    }
+    // collapse: + pyrUp32(C_{j+1})
+    if (hasUp && active) {
+        const uint2* cf = &S.cf[0][0] + 1;
+        int v[3][3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint2 a = cf[vr0 * kCfW + fc + k], b = cf[(vr0 + 1) * kCfW + fc + k];
+            const int ax = (short)(a.x & 0xFFFF), ay = (short)(a.x >> 16), az = (short)(a.y & 0xFFFF);
+            const int bx = (short)(b.x & 0xFFFF), by = (short)(b.x >> 16), bz = (short)(b.y & 0xFFFF);
+            if (evenRow) {
+                const uint2 c = cf[(vr0 + 2) * kCfW + fc + k];
+                v[k][0] = ax + 6 * bx + (short)(c.x & 0xFFFF);
+                v[k][1] = ay + 6 * by + (short)(c.x >> 16);
+                v[k][2] = az + 6 * bz + (short)(c.y & 0xFFFF);
+            } else {
+                v[k][0] = 4 * (ax + bx);
+                v[k][1] = 4 * (ay + by);
+                v[k][2] = 4 * (az + bz);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            n0[c] += (v[0][c] + 6 * v[1][c] + v[2][c] + 32) >> 6;
+            n1[c] += (4 * (v[1][c] + v[2][c]) + 32) >> 6;
+        }
+    }
+    if (!rowOk) return;
+    if (j > 0) {
+        short4* Cj = Lj.C + (size_t)y * Lj.pitch + x;
+        if (x + 1 < Lj.w) {
+            *reinterpret_cast<int4*>(Cj) =
+                make_int4((int)((uint32_t)(uint16_t)n0[0] | ((uint32_t)(uint16_t)n0[1] << 16)),
+                          (int)(uint32_t)(uint16_t)n0[2],
+                          (int)((uint32_t)(uint16_t)n1[0] | ((uint32_t)(uint16_t)n1[1] << 16)),
+                          (int)(uint32_t)(uint16_t)n1[2]);
+        } else if (x < Lj.w) {
+            Cj[0] = make_short4((short)n0[0], (short)n0[1], (short)n0[2], 0);
+        }
+        return;
+    }
+    uint32_t o0 = 0, o1 = 0;
+    if (cls != 0) {
+        o0 = (uint32_t)min(max(n0[0], 0), 255) | ((uint32_t)min(max(n0[1], 0), 255) << 8) |
+             ((uint32_t)min(max(n0[2], 0), 255) << 16);
+        o1 = (uint32_t)min(max(n1[0], 0), 255) | ((uint32_t)min(max(n1[1], 0), 255) << 8) |
+             ((uint32_t)min(max(n1[2], 0), 255) << 16);
+        if (cls == 2) {
+            const uint8_t* um = R.unionMask + (size_t)y * Lj.pitch + x;
+            if (!um[0]) o0 = 0;
+            if (x + 1 < Lj.w && !um[1]) o1 = 0;
+        }
+    }
+    uint8_t* orow = F.out + (size_t)y * F.outPitch;
+    if (F.outFmt == PS_FMT_BGR32) {
+        if (x + 1 < Lj.w && ((reinterpret_cast<uintptr_t>(orow) & 7) == 0)) {
+            reinterpret_cast<uint2*>(orow)[x / 2] = make_uint2(o0, o1);
+        } else {
+            if (x < Lj.w) reinterpret_cast<uint32_t*>(orow)[x] = o0;
+            if (x + 1 < Lj.w) reinterpret_cast<uint32_t*>(orow)[x + 1] = o1;
+        }
+    } else {
+        if (x < Lj.w) {
+            orow[3 * x] = o0 & 0xFF;
+            orow[3 * x + 1] = (o0 >> 8) & 0xFF;
+            orow[3 * x + 2] = (o0 >> 16) & 0xFF;
+        }
+        if (x + 1 < Lj.w) {
+            orow[3 * x + 3] = o1 & 0xFF;
+            orow[3 * x + 4] = (o1 >> 8) & 0xFF;
+            orow[3 * x + 5] = (o1 >> 16) & 0xFF;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlendThreads, 3) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total)
+{
+    __shared__ BlendStage st[kBStages];
+    __shared__ UnitInfo info[kBStages];
+    __shared__ uint64_t full[kBStages], empty[kBStages];
+    __shared__ Segment s_segs[kMaxSmemSegs];
+    __shared__ int s_timeout;
+    __shared__ int fRow[kFH], fCol[kFW];
+    const Segment* segs = gsegs;
+    if (nsegs <= kMaxSmemSegs) {
+        for (int k = threadIdx.x; k < nsegs; k += kBlendThreads) s_segs[k] = gsegs[k];
+        segs = s_segs;
+    }
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kBStages; k++) {
+            mbarInit(&full[k], 1);
+            mbarInit(&empty[k], kConsumers / 32);
+        }
+        s_timeout = 0;
+    }
+    __syncthreads();
     waitPrevGrid();
     allowNextGrid();
-    for (int it = blockIdx.x; it < total; it += gridDim.x) {
-        const uint4 raw = nextRaw;
-        const int cs = s;
-        const int nx = it + (int)gridDim.x;
-        if (nx < total) {
-            s = findSegment(segs, nsegs, nx, s);
-            nextRaw = __ldg(static_cast<const uint4*>(segs[s].items) + (nx - segs[s].prefix));
-        }
-        const Segment& sg = segs[cs];
-        const RigDev& R = *sg.rig;
-        const int j = raw.x & 0xFF, cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
-        const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
-        const LevelDev& Lj = R.lv[j];
-        const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
-        const bool rowOk = y < Lj.h;
-        const bool active = !(j == 0 && cls == 0);
-        const bool hasUp = j < R.L;
-        const LevelDev& Lu = R.lv[hasUp ? j + 1 : j];
-        const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
-        const bool interiorU = fx0 >= 0 && fy0 >= 0 && fx0 + kFW <= Lu.w && fy0 + kFH <= Lu.h;
-        int r0[3] = {0, 0, 0}, r1[3] = {0, 0, 0};
-        int wsum0 = 0, wsum1 = 0;
+    const int lane = threadIdx.x & 31;
 
-        if (active) {
-            // collapse footprint of C_{j+1}: issued first, staged with the first pass
-            short4 cv = make_short4(0, 0, 0, 0);
-            if (hasUp && threadIdx.x < kFElems) {
-                const int r = threadIdx.x / kFW, c = threadIdx.x - r * kFW;
-                const int gy = interiorU ? fy0 + r : rowMap(fy0 + r, Lu.h);
-                const int gx = interiorU ? fx0 + c : colMap(fx0 + c, Lu.w);
-                cv = Lu.C[(size_t)gy * Lu.pitch + gx];
+    if (threadIdx.x >= kConsumers) {
+        // ---------------- producer warp ----------------
+        int it = blockIdx.x, chunk = 0, seg = 0;
+        uint4 raw = make_uint4(0, 0, 0, 0);
+        bool valid = it < total;
+        if (valid) {
+            seg = findSegment(segs, nsegs, it, 0);
+            raw = __ldg(static_cast<const uint4*>(segs[seg].items) + (it - segs[seg].prefix));
+        }
+        for (int u = 0;; u++) {
+            const int stg = u % kBStages;
+            if (u >= kBStages && !mbarWait(&empty[stg], ((u / kBStages) - 1) & 1)) s_timeout = 1;
+            UnitInfo ui;
+            ui.raw = raw;
+            ui.seg = seg;
+            ui.chunk = chunk;
+            ui.valid = valid;
+            ui.staged = 0;
+            int nc = 0, cb = 8, j = 0, tx = 0, ty = 0, nCopies = 0;
+            bool hasUp = false, last = false, uni = false;
+            const RigDev* R = nullptr;
+            if (valid) {
+                R = segs[seg].rig;
+                j = raw.x & 0xFF;
+                const int cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
+                uni = ((raw.x >> 24) & kTileUniform) != 0;
+                tx = raw.y & 0xFFFF;
+                ty = raw.y >> 16;
+                hasUp = j < R->L;
+                const LevelDev& Lj = R->lv[j];
+                const LevelDev& Lu = R->lv[hasUp ? j + 1 : j];
+                nc = max(0, min(kCamsPerUnit, camCnt - chunk * kCamsPerUnit));
+                last = chunk == unitChunks(raw) - 1;
+                const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
+                const bool rowsIn = (ty + 1) * kBlendTH <= Lj.h;
+                const bool fpIn = !hasUp || (fx0 - 3 >= 0 && fx0 - 3 + kFpW <= Lu.w && fy0 >= 0 && fy0 + kFH <= Lu.h);
+                const bool active = !(j == 0 && cls == 0);
+                if (active && rowsIn && fpIn && (nc > 0 || (hasUp && last))) {
+                    ui.staged = 1;
+                    cb = 8 + (uni ? 0 : 8) + (hasUp ? kFH : 0);
+                    nCopies = nc * cb + (hasUp && last ? kFH : 0);
+                }
             }
-            for (int c0 = 0;; c0 += kCamsPerPass) {
-                const int nc = min(kCamsPerPass, camCnt - c0);
-                uint32_t fv[kFLoads];
-                if (hasUp) {
-#pragma unroll
-                    for (int q = 0; q < kFLoads; q++) {
-                        const int k = threadIdx.x + q * kThreads;
-                        if (k < nc * kFElems) {
-                            const int cq = k / kFElems, e = k - cq * kFElems;
-                            const int r = e / kFW, c = e - r * kFW;
-                            const int cam = tileCam(raw, R.camLists, c0 + cq);
-                            const int gy = interiorU ? fy0 + r : rowMap(fy0 + r, Lu.h);
-                            const int gx = interiorU ? fx0 + c : colMap(fx0 + c, Lu.w);
-                            fv[q] = __ldg(reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
-                                          (size_t)gy * Lu.pitch + gx);
+            fenceProxyAsync();
+            if (lane == 0) info[stg] = ui;
+            if (ui.staged) {
+                const LevelDev& Lj = R->lv[j];
+                const LevelDev& Lu = R->lv[hasUp ? j + 1 : j];
+                if (lane == 0) {
+                    const uint32_t bytes = nc * (kBlendTH * kBlendTW * 4 + (uni ? 0 : kBlendTH * kBlendTW * 2) +
+                                                 (hasUp ? kFH * kFpW * 4 : 0)) +
+                                           (hasUp && last ? kFH * kCfW * 8 : 0);
+                    mbarArriveExpectTx(&full[stg], bytes);
+                }
+                __syncwarp();
+                const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
+                for (int k = lane; k < nCopies; k += 32) {
+                    if (k < nc * cb) {
+                        const int q = k / cb;
+                        int r = k - q * cb;
+                        const int cam = tileCam(raw, R->camLists, chunk * kCamsPerUnit + q);
+                        if (r < 8) {
+                            bulkCopy(&st[stg].gj[q][r][0],
+                                     Lj.G + (size_t)cam * Lj.camStride + (size_t)(ty * kBlendTH + r) * Lj.pitch +
+                                         tx * kBlendTW,
+                                     kBlendTW * 4, &full[stg]);
+                            continue;
                         }
-                    }
-                }
-                uint32_t wp[kCamsPerPass];
-                uint2 gp[kCamsPerPass];
-#pragma unroll
-                for (int q = 0; q < kCamsPerPass; q++) {
-                    wp[q] = 0;
-                    gp[q] = make_uint2(0, 0);
-                    if (q < nc && rowOk) {
-                        const int cam = tileCam(raw, R.camLists, c0 + q);
-                        const size_t o = (size_t)cam * Lj.camStride + (size_t)y * Lj.pitch + x;
-                        wp[q] = __ldg(reinterpret_cast<const uint32_t*>(Lj.Wt + o));
-                        gp[q] = __ldg(reinterpret_cast<const uint2*>(Lj.G + o));
-                    }
-                }
-                if (hasUp) {
-                    __syncthreads();  // readers of the previous pass / tile are done
-#pragma unroll
-                    for (int q = 0; q < kFLoads; q++) {
-                        const int k = threadIdx.x + q * kThreads;
-                        if (k < nc * kFElems) s_g[k] = fv[q];
-                    }
-                    if (c0 == 0 && threadIdx.x < kFElems) s_c[threadIdx.x] = make_int4(cv.x, cv.y, cv.z, 0);
-                    __syncthreads();
-                }
-#pragma unroll
-                for (int q = 0; q < kCamsPerPass; q++) {
-                    if (q >= nc) break;
-                    uint32_t u0lo = 0, u0hi = 0, u1lo = 0, u1hi = 0;
-                    if (hasUp) {
-                        const uint32_t* g = s_g + q * kFElems;
-                        uint32_t vlo[3], vhi[3];
-#pragma unroll
-                        for (int k = 0; k < 3; k++) {
-                            const uint2 a = unpackBytes(g[vr0 * kFW + fc + k]);
-                            const uint2 b = unpackBytes(g[(vr0 + 1) * kFW + fc + k]);
-                            if (evenRow) {
-                                const uint2 c = unpackBytes(g[(vr0 + 2) * kFW + fc + k]);
-                                vlo[k] = a.x + 6 * b.x + c.x;
-                                vhi[k] = a.y + 6 * b.y + c.y;
-                            } else {
-                                vlo[k] = 4 * (a.x + b.x);
-                                vhi[k] = 4 * (a.y + b.y);
+                        r -= 8;
+                        if (!uni) {
+                            if (r < 8) {
+                                bulkCopy(&st[stg].w[q][r][0],
+                                         Lj.Wt + (size_t)cam * Lj.camStride + (size_t)(ty * kBlendTH + r) * Lj.pitch +
+                                             tx * kBlendTW,
+                                         kBlendTW * 2, &full[stg]);
+                                continue;
                             }
+                            r -= 8;
                         }
-                        u0lo = vlo[0] + 6 * vlo[1] + vlo[2];
-                        u0hi = vhi[0] + 6 * vhi[1] + vhi[2];
-                        u1lo = 4 * (vlo[1] + vlo[2]);
-                        u1hi = 4 * (vhi[1] + vhi[2]);
+                        bulkCopy(&st[stg].fp[q][r][0],
+                                 Lu.G + (size_t)cam * Lu.camStride + (size_t)(fy0 + r) * Lu.pitch + (fx0 - 3), kFpW * 4,
+                                 &full[stg]);
+                    } else {
+                        const int r = k - nc * cb;
+                        bulkCopy(&st[stg].cf[r][0], Lu.C + (size_t)(fy0 + r) * Lu.pitch + (fx0 - 1), kCfW * 8,
+                                 &full[stg]);
                     }
-                    const int w0 = (int)(wp[q] & 0xFFFFu), w1 = (int)(wp[q] >> 16);
-                    const uint2 gq = gp[q];
-                    // L = G - ((U + 32) >> 6), per channel
-                    r0[0] += w0 * ((int)(gq.x & 0xFF) - (int)(((u0lo & 0xFFFFu) + 32) >> 6));
-                    r0[1] += w0 * ((int)((gq.x >> 8) & 0xFF) - (int)(((u0hi & 0xFFFFu) + 32) >> 6));
-                    r0[2] += w0 * ((int)((gq.x >> 16) & 0xFF) - (int)(((u0lo >> 16) + 32) >> 6));
-                    r1[0] += w1 * ((int)(gq.y & 0xFF) - (int)(((u1lo & 0xFFFFu) + 32) >> 6));
-                    r1[1] += w1 * ((int)((gq.y >> 8) & 0xFF) - (int)(((u1hi & 0xFFFFu) + 32) >> 6));
-                    r1[2] += w1 * ((int)((gq.y >> 16) & 0xFF) - (int)(((u1lo >> 16) + 32) >> 6));
-                    wsum0 += w0;
-                    wsum1 += w1;
                 }
-                if (c0 + kCamsPerPass >= camCnt) break;
+            } else if (lane == 0) {
+                mbarArrive(&full[stg]);
             }
-        }
-        // normalise
-        int n0[3], n1[3];
-        if (R.full) {
-#pragma unroll
-            for (int c = 0; c < 3; c++) { n0[c] = (r0[c] + 128) >> 8; n1[c] = (r1[c] + 128) >> 8; }
-        } else {
-            const int d0 = wsum0 ? wsum0 : 1, d1 = wsum1 ? wsum1 : 1;
-            const float i0 = __frcp_rn((float)d0), i1 = __frcp_rn((float)d1);
-#pragma unroll
-            for (int c = 0; c < 3; c++) { n0[c] = divTrunc(r0[c], d0, i0); n1[c] = divTrunc(r1[c], d1, i1); }
-        }
-        // collapse: + pyrUp32(C_{j+1}), from the footprint staged above
-        if (hasUp && active) {
-            int v[3][3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const int4 a = s_c[vr0 * kFW + fc + k];
-                const int4 b = s_c[(vr0 + 1) * kFW + fc + k];
-                if (evenRow) {
-                    const int4 c = s_c[(vr0 + 2) * kFW + fc + k];
-                    v[k][0] = a.x + 6 * b.x + c.x;
-                    v[k][1] = a.y + 6 * b.y + c.y;
-                    v[k][2] = a.z + 6 * b.z + c.z;
-                } else {
-                    v[k][0] = 4 * (a.x + b.x);
-                    v[k][1] = 4 * (a.y + b.y);
-                    v[k][2] = 4 * (a.z + b.z);
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                n0[c] += (v[0][c] + 6 * v[1][c] + v[2][c] + 32) >> 6;
-                n1[c] += (4 * (v[1][c] + v[2][c]) + 32) >> 6;
-            }
-        }
-        if (!rowOk) continue;
-        if (j > 0) {
-            short4* Cj = Lj.C + (size_t)y * Lj.pitch + x;
-            if (x + 1 < Lj.w) {
-                *reinterpret_cast<int4*>(Cj) = make_int4(
-                    (int)((uint32_t)(uint16_t)n0[0] | ((uint32_t)(uint16_t)n0[1] << 16)), (int)(uint32_t)(uint16_t)n0[2],
-                    (int)((uint32_t)(uint16_t)n1[0] | ((uint32_t)(uint16_t)n1[1] << 16)), (int)(uint32_t)(uint16_t)n1[2]);
-            } else if (x < Lj.w) {
-                Cj[0] = make_short4((short)n0[0], (short)n0[1], (short)n0[2], 0);
-            }
-        } else {
-            const FrameDev& F = *sg.frame;
-            uint32_t o0 = 0, o1 = 0;
-            if (cls != 0) {
-                o0 = (uint32_t)min(max(n0[0], 0), 255) | ((uint32_t)min(max(n0[1], 0), 255) << 8) |
-                     ((uint32_t)min(max(n0[2], 0), 255) << 16);
-                o1 = (uint32_t)min(max(n1[0], 0), 255) | ((uint32_t)min(max(n1[1], 0), 255) << 8) |
-                     ((uint32_t)min(max(n1[2], 0), 255) << 16);
-                if (cls == 2) {
-                    const uint8_t* um = R.unionMask + (size_t)y * Lj.pitch + x;
-                    if (!um[0]) o0 = 0;
-                    if (x + 1 < Lj.w && !um[1]) o1 = 0;
-                }
-            }
-            uint8_t* orow = F.out + (size_t)y * F.outPitch;
-            if (F.outFmt == PS_FMT_BGR32) {
-                if (x + 1 < Lj.w && ((reinterpret_cast<uintptr_t>(orow) & 7) == 0)) {
-                    reinterpret_cast<uint2*>(orow)[x / 2] = make_uint2(o0, o1);
-                } else {
-                    if (x < Lj.w) reinterpret_cast<uint32_t*>(orow)[x] = o0;
-                    if (x + 1 < Lj.w) reinterpret_cast<uint32_t*>(orow)[x + 1] = o1;
-                }
+            if (!valid) break;  // the terminal unit is out
+            if (chunk + 1 < unitChunks(raw)) {
+                chunk++;
             } else {
-                if (x < Lj.w) {
-                    orow[3 * x] = o0 & 0xFF;
-                    orow[3 * x + 1] = (o0 >> 8) & 0xFF;
-                    orow[3 * x + 2] = (o0 >> 16) & 0xFF;
-                }
-                if (x + 1 < Lj.w) {
-                    orow[3 * x + 3] = o1 & 0xFF;
-                    orow[3 * x + 4] = (o1 >> 8) & 0xFF;
-                    orow[3 * x + 5] = (o1 >> 16) & 0xFF;
+                chunk = 0;
+                it += gridDim.x;
+                valid = it < total;
+                if (valid) {
+                    seg = findSegment(segs, nsegs, it, seg);
+                    raw = __ldg(static_cast<const uint4*>(segs[seg].items) + (it - segs[seg].prefix));
                 }
             }
         }
+        return;
+    }
+
+    // ---------------- consumer warps ----------------
+    BlendAcc acc;
+    for (int u = 0;; u++) {
+        const int stg = u % kBStages;
+        if (!mbarWait(&full[stg], (u / kBStages) & 1)) s_timeout = 1;
+        const UnitInfo ui = info[stg];
+        if (!ui.valid) break;
+        const Segment& sg = segs[ui.seg];
+        const RigDev& R = *sg.rig;
+        const bool active = !((ui.raw.x & 0xFF) == 0 && ((ui.raw.x >> 8) & 0xFF) == 0);
+        if (active && !ui.staged) {
+            stageUnitDirect(st[stg], R, ui.raw, ui.chunk, fRow, fCol, [] { namedBarrier(1, kConsumers); });
+            namedBarrier(1, kConsumers);
+        }
+        computeUnit(st[stg], R, *sg.frame, ui.raw, ui.chunk, ui.staged != 0, acc);
+        if (active && !ui.staged) fenceProxyAsync();  // our stage writes precede later bulk copies into it
+        __syncwarp();
+        if (lane == 0) mbarArrive(&empty[stg]);  // this warp is done with the stage
+    }
+    if (s_timeout && threadIdx.x == 0 && nsegs > 0 && segs[0].frame->status) atomicOr(segs[0].frame->status, 4);
+}
+
+// ============================================================================
+// k_tail: the small top of the pyramid of each rig in one launch.  A cluster
+// of 16 CTAs (8 where 16 cannot be co-scheduled) owns one rig: it runs pyrDown levels tailDown..L and
+// then blend levels L..tailBlend, spreading each level's tiles over its
+// CTAs, with a cluster barrier (release / acquire, so the level's global
+// writes are visible to the whole cluster) between levels.  These levels
+// hold few tiles, so separate launches would cost mostly launch latency.
+// ============================================================================
+constexpr int kTailCluster = 8;       // portable cluster size
+constexpr int kTailClusterWide = 16;  // used when the GPU can co-schedule it
+
+__device__ __forceinline__ void clusterSync()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ segs, int nsegs, int cluster)
+{
+    __shared__ union {
+        DownSmem down;
+        BlendStage blend;
+    } sm;
+    __shared__ int fRow[kFH], fCol[kFW];
+    const int rig = blockIdx.x / cluster, rank = blockIdx.x % cluster;
+    initMagic(sm.down.magic);
+    waitPrevGrid();
+    allowNextGrid();
+    if (rig >= nsegs) return;  // never: the grid is nsegs clusters
+    const Segment& sg = segs[rig];
+    const RigDev& R = *sg.rig;
+    for (int J = R.tailDown; J <= R.L; J++) {
+        const DownItem* items = R.downItems + R.downOff[J];
+        for (int k = rank; k < R.downCnt[J]; k += cluster) pyrDownTile(R, items[k], sm.down);
+        clusterSync();
+    }
+    BlendAcc acc;
+    for (int j = R.L; j >= R.tailBlend; j--) {
+        const BlendItem* items = R.blendItems + R.blendOff[j];
+        for (int k = rank; k < R.blendCnt[j]; k += cluster) {
+            const uint4 raw = *reinterpret_cast<const uint4*>(items + k);
+            const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
+            for (int chunk = 0; chunk < unitChunks(raw); chunk++) {
+                __syncthreads();  // readers of the previous unit are done
+                if (active) stageUnitDirect(sm.blend, R, raw, chunk, fRow, fCol, [] { __syncthreads(); });
+                __syncthreads();
+                computeUnit(sm.blend, R, *sg.frame, raw, chunk, false, acc);
+            }
+        }
+        clusterSync();
     }
 }
 
@@ -525,11 +776,11 @@ static int gridFor(int total, int perSm)
 // Every per-frame kernel is launched with programmatic stream serialisation,
 // so its prologue overlaps the previous kernel's tail (see waitPrevGrid).
 template <class... Args>
-static cudaError_t launchPdl(void (*kernel)(Args...), int grid, cudaStream_t st, Args... args)
+static cudaError_t launchPdl(void (*kernel)(Args...), int grid, int block, cudaStream_t st, Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kThreads);
+    cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
@@ -543,19 +794,64 @@ static cudaError_t launchPdl(void (*kernel)(Args...), int grid, cudaStream_t st,
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_remap, gridFor(total, 8), st, segs, nsegs, total);
+    return launchPdl(k_remap, gridFor(total, 8), kThreads, st, segs, nsegs, total);
 }
 
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_pyrdown, gridFor(total, 6), st, segs, nsegs, total);
+    return launchPdl(k_pyrdown, gridFor(total, 6), kThreads, st, segs, nsegs, total);
 }
 
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_blend, gridFor(total, 8), st, segs, nsegs, total);
+    return launchPdl(k_blend, gridFor(total, 3), kBlendThreads, st, segs, nsegs, total);
+}
+
+static int tailClusterSize()
+{
+    static int size = 0;
+    if (size) return size;
+    size = kTailCluster;
+    if (cudaFuncSetAttribute(k_tail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kTailClusterWide);
+        cfg.blockDim = dim3(kThreads);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kTailClusterWide;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, k_tail, &cfg) == cudaSuccess && clusters >= 1)
+            size = kTailClusterWide;
+    }
+    cudaGetLastError();
+    return size;
+}
+
+cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st)
+{
+    if (nsegs <= 0) return cudaSuccess;
+    const int cluster = tailClusterSize();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nsegs * cluster);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 2;
+    return cudaLaunchKernelEx(&cfg, k_tail, segs, nsegs, cluster);
 }
 
 cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,

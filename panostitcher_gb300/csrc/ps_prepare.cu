@@ -363,6 +363,24 @@ cudaError_t launchTileFlags16(const uint16_t* p, int w, int h, int pitch, long l
     return cudaGetLastError();
 }
 
+// per-tile "some pixel differs from 256" flags of a weight plane
+__global__ void k_tile_not256(const uint16_t* __restrict__ p, int w, int h, int pitch, long long camStride, int tw,
+                              int th, int tilesX, int tilesY, uint8_t* flags)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, c = blockIdx.z;
+    if (x >= w) return;
+    if (p[(size_t)c * camStride + (size_t)y * pitch + x] != 256)
+        flags[((size_t)c * tilesY + y / th) * tilesX + x / tw] = 1;
+}
+
+cudaError_t launchTileNot256(const uint16_t* p, int w, int h, int pitch, long long camStride, int n, int tw, int th,
+                             int tilesX, int tilesY, uint8_t* flags, cudaStream_t st)
+{
+    dim3 grid((w + 127) / 128, h, n);
+    k_tile_not256<<<grid, 128, 0, st>>>(p, w, h, pitch, camStride, tw, th, tilesX, tilesY, flags);
+    return cudaGetLastError();
+}
+
 cudaError_t launchTileFlags8(const uint8_t* p, int w, int h, int pitch, long long camStride, int n, int tw,
                              int th, int tilesX, int tilesY, uint8_t* flags, cudaStream_t st)
 {

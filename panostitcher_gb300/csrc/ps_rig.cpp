@@ -89,6 +89,8 @@ void Rig::clear()
     hDown_.clear();
     hBlend_.clear();
     hCams_.clear();
+    tailDown_ = tailBlend_ = 1;
+    for (int j = 0; j <= PS_MAX_LEVELS; j++) downOff_[j] = downCnt_[j] = blendOff_[j] = blendCnt_[j] = 0;
     covCount_ = weightCount_ = alphaCount_ = 0;
     covBits_.clear();
     seamBits_.clear();
@@ -295,7 +297,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         rflags.zero(st);
         PS_CUDA(launchTileFlags8(cov, W, H, W, (long long)npx, n, kRemapTW, kRemapTH, rX, rY, rflags.as<uint8_t>(), st));
     }
-    std::vector<DevBuf> dflags(L + 1), bflags(L + 1);
+    std::vector<DevBuf> dflags(L + 1), bflags(L + 1), uflags(L + 1);
     for (int j = 0; j <= L; j++) {
         const LevelGeom& g = geom_[j];
         const long long stride = (long long)g.pitch * g.h;
@@ -309,6 +311,10 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         const int bX = divUp(g.w, kBlendTW), bY = divUp(g.h, kBlendTH);
         bflags[j].alloc((size_t)n * bX * bY);
         bflags[j].zero(st);
+        uflags[j].alloc((size_t)n * bX * bY);
+        uflags[j].zero(st);
+        PS_CUDA(launchTileNot256(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kBlendTW, kBlendTH, bX, bY,
+                                 uflags[j].as<uint8_t>(), st));
         PS_CUDA(launchTileFlags16(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kBlendTW, kBlendTH, bX, bY,
                                   bflags[j].as<uint8_t>(), st));
     }
@@ -328,7 +334,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     std::vector<int> hCounts((size_t)bX0 * bY0);
     unsigned long long hTotal = 0;
     std::vector<uint8_t> hR(xmap ? rflags.bytes() : 0);
-    std::vector<std::vector<uint8_t>> hD(L + 1), hB(L + 1);
+    std::vector<std::vector<uint8_t>> hD(L + 1), hB(L + 1), hU(L + 1);
     PS_CUDA(cudaMemcpyAsync(hCounts.data(), tileCounts.get(), tileCounts.bytes(), cudaMemcpyDeviceToHost, st));
     PS_CUDA(cudaMemcpyAsync(&hTotal, total.get(), sizeof hTotal, cudaMemcpyDeviceToHost, st));
     PS_CUDA(cudaMemcpyAsync(hc, counts.get(), sizeof hc, cudaMemcpyDeviceToHost, st));
@@ -340,6 +346,8 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         }
         hB[j].resize(bflags[j].bytes());
         PS_CUDA(cudaMemcpyAsync(hB[j].data(), bflags[j].get(), hB[j].size(), cudaMemcpyDeviceToHost, st));
+        hU[j].resize(uflags[j].bytes());
+        PS_CUDA(cudaMemcpyAsync(hU[j].data(), uflags[j].get(), hU[j].size(), cudaMemcpyDeviceToHost, st));
     }
     std::vector<uint8_t> hCov(n * npx), hSeam(n * npx);
     PS_CUDA(cudaMemcpyAsync(hCov.data(), cov, n * npx, cudaMemcpyDeviceToHost, st));
@@ -398,6 +406,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
                 it.level = (uint8_t)j;
                 it.cls = cls;
                 it.camCnt = (uint8_t)list.size();
+                if (list.size() == 1 && !hU[j][((size_t)list[0] * bY + ty) * bX + tx]) it.flags |= kTileUniform;
                 it.tx = (uint16_t)tx;
                 it.ty = (uint16_t)ty;
                 if (list.size() <= (size_t)kInlineCams) {
@@ -415,6 +424,12 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     hDown_ = down;
     hBlend_ = blend;
     hCams_ = cams;
+    // levels with few tiles (from the top down) go to the tail kernel
+    const int kTailMaxItems = 32;
+    tailDown_ = L + 1;
+    while (tailDown_ > 1 && downCnt_[tailDown_ - 1] <= kTailMaxItems) tailDown_--;
+    tailBlend_ = L + 1;
+    while (tailBlend_ > 0 && blendCnt_[tailBlend_ - 1] <= kTailMaxItems) tailBlend_--;
     dRemap_.alloc(std::max<size_t>(1, hRemap_.size()) * sizeof(RemapItem));
     dDown_.alloc(std::max<size_t>(1, down.size()) * sizeof(DownItem));
     dBlend_.alloc(std::max<size_t>(1, blend.size()) * sizeof(BlendItem));
@@ -447,6 +462,16 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     d.maps = maps_.as<float2>();
     d.unionMask = union_.as<uint8_t>();
     d.camLists = dCams_.as<uint8_t>();
+    d.downItems = dDown_.as<DownItem>();
+    d.blendItems = dBlend_.as<BlendItem>();
+    for (int j = 0; j <= L; j++) {
+        d.downOff[j] = downOff_[j];
+        d.downCnt[j] = downCnt_[j];
+        d.blendOff[j] = blendOff_[j];
+        d.blendCnt[j] = blendCnt_[j];
+    }
+    d.tailDown = tailDown_;
+    d.tailBlend = tailBlend_;
     for (int j = 0; j <= L; j++) {
         const LevelGeom& g = geom_[j];
         d.lv[j].w = g.w;
@@ -550,6 +575,11 @@ void Rig::exportCollapsed(int level, int16_t* host, long long bytes, cudaStream_
 double Rig::stepBytes(int kind, int level) const
 {
     double b = 0;
+    if (kind == 3) {
+        for (int J = tailDown_; J <= L_; J++) b += stepBytes(1, J);
+        for (int j = tailBlend_; j <= L_; j++) b += stepBytes(2, j);
+        return b;
+    }
     if (kind == 0) {
         // map (8 B) in, G0 (4 B) out per tile pixel, every covering camera's frame in once
         std::vector<char> used(n_, 0);
@@ -697,7 +727,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
                              reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * p.first), p.second.second, s.total});
             s.total += p.second.second;
             const Rig* rg = rigs[p.first];
-            const int lvl = kind == 0 ? 0 : (kind == 1 ? step : rg->numLevels() - step);
+            const int lvl = kind == 0 ? 0 : (kind == 1 ? step : rg->tailBlend() - 1 - step);
             if (s.level < 0) s.level = lvl;
             s.bytes += rg->stepBytes(kind, lvl);
         }
@@ -710,13 +740,29 @@ void Plan::bind(const std::vector<Rig*>& rigs)
     for (int J = 1; J <= maxL; J++) {
         parts.clear();
         for (int r = 0; r < nr; r++)
-            if (J <= rigs[r]->numLevels()) parts.push_back({r, {rigs[r]->downItems(J), rigs[r]->numDownItems(J)}});
+            if (J < rigs[r]->tailDown()) parts.push_back({r, {rigs[r]->downItems(J), rigs[r]->numDownItems(J)}});
         addStep(1, parts, J);
     }
-    for (int s = 0; s <= maxL; s++) {
+    {
+        // the tail: one cluster per rig that has one (segment count 1)
+        Step s{3, (int)segs_.size(), 0, 0, -1, 0.0};
+        for (int r = 0; r < nr; r++) {
+            if (!rigs[r]->hasTail()) continue;
+            segs_.push_back({nullptr, rigs[r]->deviceDesc(), reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * r), 1,
+                             s.total});
+            s.total += 1;
+            if (s.level < 0) s.level = rigs[r]->tailBlend();
+            s.bytes += rigs[r]->stepBytes(3, 0);
+        }
+        s.nsegs = (int)segs_.size() - s.segOff;
+        if (s.total > 0) steps_.push_back(s);
+    }
+    int maxB = 0;
+    for (Rig* r : rigs) maxB = std::max(maxB, r->tailBlend());
+    for (int s = 0; s < maxB; s++) {
         parts.clear();
         for (int r = 0; r < nr; r++) {
-            const int j = rigs[r]->numLevels() - s;
+            const int j = rigs[r]->tailBlend() - 1 - s;
             if (j >= 0) parts.push_back({r, {rigs[r]->blendItems(j), rigs[r]->numBlendItems(j)}});
         }
         addStep(2, parts, s);
@@ -763,7 +809,8 @@ void Plan::launchAll(cudaStream_t st, Profiler* prof)
         }
         if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, st));
-        else PS_CUDA(launchBlend(p, s.nsegs, s.total, st));
+        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, st));
+        else PS_CUDA(launchTail(p, s.nsegs, st));
         if (prof) {
             PS_CUDA(cudaEventRecord(b, st));
             prof->record(s.kind, s.level, s.bytes, a, b);

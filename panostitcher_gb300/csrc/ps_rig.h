@@ -58,6 +58,10 @@ public:
     int numDownItems(int level) const { return downCnt_[level]; }
     const BlendItem* blendItems(int level) const { return dBlend_.as<BlendItem>() + blendOff_[level]; }
     int numBlendItems(int level) const { return blendCnt_[level]; }
+    // pyrDown levels tailDown()..L and blend levels L..tailBlend() run in the tail kernel
+    int tailDown() const { return tailDown_; }
+    int tailBlend() const { return tailBlend_; }
+    bool hasTail() const { return tailDown_ <= L_ || tailBlend_ <= L_; }
 
     // blender input: int16x4 / uint8x4 device images -> level 0 (checks)
     void imagesToLevel0(const void* const* images, const long long* pitches, int fmt, cudaStream_t st);
@@ -89,6 +93,7 @@ private:
     std::vector<RemapItem> hRemap_;
     int downOff_[PS_MAX_LEVELS + 1] = {}, downCnt_[PS_MAX_LEVELS + 1] = {};
     int blendOff_[PS_MAX_LEVELS + 1] = {}, blendCnt_[PS_MAX_LEVELS + 1] = {};
+    int tailDown_ = 1, tailBlend_ = 1;
     std::vector<uint8_t> covBits_, seamBits_;  // host copies for exports (1 bit / pixel)
     std::vector<DownItem> hDown_;
     std::vector<BlendItem> hBlend_;
@@ -144,7 +149,7 @@ public:
 
 private:
     struct Step {
-        int kind;  // 0 remap, 1 pyrDown, 2 blend
+        int kind;  // 0 remap, 1 pyrDown, 2 blend, 3 tail
         int segOff, nsegs, total;
         int level;      // level of the first rig in the step
         double bytes;   // algorithmic bytes of the step (all rigs)

@@ -134,7 +134,7 @@ class CudaPanoramaRender2:
     def profile(self, enabled: bool) -> None:
         check(lib().ps_render_profile(self._h, int(bool(enabled))))
 
-    KERNELS = {0: "k_remap", 1: "k_pyrdown", 2: "k_blend"}
+    KERNELS = {0: "k_remap", 1: "k_pyrdown", 2: "k_blend", 3: "k_tail"}
 
     def profile_read(self, kind: int, level: int = -1):
         """(launches, total_ms, algorithmic_bytes) of finished profiled launches."""

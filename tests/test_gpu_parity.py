@@ -250,3 +250,16 @@ def test_blender_rejects_bad_inputs(cuda):
     outside[0, 20, 1] = 5      # non-zero where the coverage mask is 0
     with pytest.raises(P.PsError):
         b.blend([outside], out)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_render_full_size_bit_exact(cuda, oracle_lib, name):
+    """The benchmark rigs at full size: every kernel path (bulk-copied interior
+    tiles, border tiles, uniform tiles, the tail kernel) against the oracle."""
+    import os
+    cfg = S.rig(name)
+    p = Prepared(cfg)
+    frames = p.frames.frame(9)
+    ref = p.oracle_render(frames, p.luts, nthreads=os.cpu_count() or 4)
+    got = p.product_render(frames, p.luts)
+    assert np.array_equal(got[..., :3], ref[..., :3]), diff_histogram(got[..., :3], ref[..., :3])
