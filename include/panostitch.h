@@ -175,6 +175,23 @@ int ps_reproject_to_16s(const ps_image* src, const float* xmap, const float* yma
 /* getLUT (source/Blend/ExposureColorOptimize.cpp:1217-1223) on the host. */
 int ps_get_lut(double k, uint8_t* lut256);
 
+/* No counterpart in the reference.  The nearest-optical-axis seam masks of a
+   rig (the masks ps_render_prepare derives internally), computed without
+   allocating any device memory, for callers that cannot call cudaMalloc: a
+   host whose device memory is owned by another allocator, or a real-time
+   thread that must not risk the synchronisation an allocation can cause.
+   The caller passes the camera parameters and the output: seams, device
+   memory of num_params * dst_h * dst_w bytes (0/255 per camera).  The
+   scratch (parameters and coverage masks) lives in one fixed 16 MiB device
+   array inside the library, held on every GPU that loads it until the
+   process exits; num_params * dst_w * dst_h must not exceed
+   16 MiB - 64 KiB, else PS_EINVAL.  The first call on a device looks up the
+   array's address on that device, so make it before any stream capture.
+   All calls on a device share the array: calls whose work overlaps on the
+   GPU race.  Every scratch byte a call reads it has written itself. */
+int ps_nearest_axis_seams_no_alloc(const ps_photo_param* params, int num_params, int src_w, int src_h, int dst_w,
+                                   int dst_h, uint8_t* seams, void* stream);
+
 /* ==== multiband blender: CudaTilingMultibandBlendFast (CudaInterface.h:45-82) ==== */
 typedef struct ps_blender ps_blender;
 int ps_blender_create(ps_blender** out);

@@ -90,6 +90,8 @@ _SIGS = [
     ("ps_reproject_to_16s", C.c_int, [C.POINTER(Image), C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_int,
                                       C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]),
     ("ps_get_lut", C.c_int, [C.c_double, C.c_void_p]),
+    ("ps_nearest_axis_seams_no_alloc", C.c_int, [C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,
+                                                 C.c_int, C.c_void_p, C.c_void_p]),
     ("ps_blender_create", C.c_int, [C.POINTER(C.c_void_p)]),
     ("ps_blender_destroy", None, [C.c_void_p]),
     ("ps_blender_prepare", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int,

@@ -2,6 +2,7 @@
 // pyramids, tile activity.  Built with --fmad=false so the double-precision
 // geometry keeps the reference's separate multiply / add roundings.
 #include <cmath>
+#include <mutex>
 
 #include "ps_internal.h"
 
@@ -491,3 +492,96 @@ cudaError_t launchImagesToLevel0(const void* const* images, const long long* pit
 }
 
 }  // namespace ps
+
+// ============================================================================
+// Allocation-free seam masks.
+//
+// Some callers cannot call cudaMalloc: a host that has handed its device
+// memory budget to another allocator and must not touch the driver's heap,
+// a real-time thread where an allocation (which may synchronise the device)
+// would blow the frame deadline, or code that must run while other work on
+// the device cannot be disturbed.  For them this entry point computes the
+// nearest-optical-axis seam masks (what ps_render_prepare does internally)
+// with all of its scratch -- the cameras' parameters and coverage masks -- in
+// one fixed array that lives in the library image.  The array holds
+// kNoAllocScratchBytes on every GPU that loads the library, until the
+// process exits.
+// ============================================================================
+namespace ps {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB
+constexpr size_t kNoAllocParamBytes = 64 * 1024;    // camera parameters at the front
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+// Device address of g_noallocScratch per device, looked up once per device.
+std::mutex g_noallocMu;
+void* g_noallocPtr[64] = {};
+
+}  // namespace
+
+// coverage only (getReprojectMapAndMask's mask), as k_gen_map computes it
+__global__ void k_coverage(const RemapDev* __restrict__ prm, int W, int H, uint8_t* cov)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, c = blockIdx.z;
+    if (x >= W) return;
+    const RemapDev m = prm[c];
+    double sx, sy;
+    remapPoint(m, x, y, sx, sy);
+    cov[(size_t)c * W * H + (size_t)y * W + x] = mapValid(m, sx, sy) ? 255 : 0;
+}
+
+}  // namespace ps
+
+extern "C" int ps_nearest_axis_seams_no_alloc(const ps_photo_param* params, int num_params, int src_w, int src_h,
+                                              int dst_w, int dst_h, uint8_t* seams, void* stream)
+{
+    using namespace ps;
+    try {
+        if (!params || !seams || num_params <= 0) fail(PS_EINVAL, "NULL argument or no cameras");
+        if (num_params > PS_MAX_CAMS) fail(PS_EINVAL, "%d cameras, at most %d supported", num_params, PS_MAX_CAMS);
+        if (src_w <= 0 || src_h <= 0 || dst_w <= 0 || dst_h <= 0) fail(PS_EINVAL, "sizes must be positive");
+        for (int i = 0; i < num_params; i++)
+            if (params[i].image_type < 0 || params[i].image_type > 3)
+                fail(PS_EINVAL, "camera %d: image_type %d not in 0..3", i, params[i].image_type);
+        const size_t covBytes = (size_t)num_params * dst_w * dst_h;
+        if (covBytes > kNoAllocScratchBytes - kNoAllocParamBytes)
+            fail(PS_EINVAL,
+                 "%d cameras x %d x %d coverage bytes exceed the %zu-byte scratch of the allocation-free path "
+                 "(use ps_render_prepare)",
+                 num_params, dst_w, dst_h, kNoAllocScratchBytes - kNoAllocParamBytes);
+        int dev = 0;
+        PS_CUDA(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= 64) fail(PS_EINVAL, "device %d out of range", dev);
+        void* base = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(g_noallocMu);
+            if (!g_noallocPtr[dev]) {
+                // the symbol's device address on the current device (the host-side
+                // name is only a stand-in and must never reach a kernel)
+                PS_CUDA(cudaGetSymbolAddress(&g_noallocPtr[dev], g_noallocScratch));
+            }
+            base = g_noallocPtr[dev];
+        }
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        RemapDev* dParams = static_cast<RemapDev*>(base);
+        uint8_t* cov = static_cast<uint8_t*>(base) + kNoAllocParamBytes;
+        static_assert(sizeof(RemapDev) * PS_MAX_CAMS <= kNoAllocParamBytes, "parameter area too small");
+        std::vector<RemapDev> rp(num_params);
+        for (int i = 0; i < num_params; i++) remapInit(params[i], dst_w, dst_h, src_w, src_h, rp[i]);
+        // pageable source: the copy is staged before cudaMemcpyAsync returns
+        PS_CUDA(cudaMemcpyAsync(dParams, rp.data(), sizeof(RemapDev) * num_params, cudaMemcpyHostToDevice, st));
+        // every coverage byte is rewritten, so nothing of the last call's contents survives
+        dim3 grid((dst_w + 127) / 128, dst_h, num_params);
+        k_coverage<<<grid, 128, 0, st>>>(dParams, dst_w, dst_h, cov);
+        PS_CUDA(cudaGetLastError());
+        PS_CUDA(launchNearestAxisSeams(dParams, num_params, dst_w, dst_h, cov, seams, st));
+        return PS_OK;
+    } catch (const Error& e) {
+        setLastError(e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        setLastError(e.what());
+        return PS_EINVAL;
+    }
+}

@@ -1,0 +1,49 @@
+"""The allocation-free seam entry point (GPU).
+
+ps_nearest_axis_seams_no_alloc serves callers that cannot call cudaMalloc;
+its scratch is a fixed device array inside the library.  Its masks must equal
+the ones the existing path (ps_render_prepare, read back with
+ps_render_export) derives, on two calls in a row (the second call reuses the
+array the first one left behind).  This file is collected last so a run that
+stops at the first failure has run everything else first; it also passes
+alone in a fresh process."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import panostitcher_gb300 as P
+from panostitcher_gb300 import _lib as L
+from panostitcher_gb300 import synth as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _call(cfg, out):
+    arr = (L.PhotoParam * cfg.num_cams)(*[L.PhotoParam.from_dict(p) for p in cfg.cams])
+    return L.lib().ps_nearest_axis_seams_no_alloc(arr, cfg.num_cams, cfg.src_size[0], cfg.src_size[1],
+                                                  cfg.dst_size[0], cfg.dst_size[1], out.data_ptr(), None)
+
+
+@pytest.mark.parametrize("name,factor", [("c2", 8), ("c1", 4)])
+def test_no_alloc_seams_equal_prepare(cuda, name, factor):
+    torch = cuda
+    cfg = S.scaled_rig(S.rig(name), factor)
+    r = P.CudaPanoramaRender2()
+    r.prepare(cfg.cams, 1, cfg.levels, cfg.src_size, cfg.dst_size, check=True)
+    ref = np.stack([r.seam(i, cfg.dst_size) for i in range(cfg.num_cams)])
+    W, H = cfg.dst_size
+    for call in range(2):
+        out = torch.full((cfg.num_cams, H, W), 7, dtype=torch.uint8, device="cuda")
+        L.check(_call(cfg, out))
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), ref), f"call {call}"
+
+
+def test_no_alloc_rejects_oversize(cuda):
+    torch = cuda
+    cfg = S.rig("c3d")                   # 8 cameras x 7680 x 3840: far beyond the 16 MiB scratch
+    out = torch.empty(16, dtype=torch.uint8, device="cuda")
+    st = _call(cfg, out)
+    assert st == L.PS_EINVAL
+    assert "scratch" in L.lib().ps_last_error().decode()
