@@ -38,8 +38,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "stitched output Mpix/s at 4096x2048 (6 cams); p50/p99 frame latency in serve loop"
-WORKLOAD = "6x rectilinear 1920x1080 (100 deg hfov; yaw 0/90/180/270, pitch +-90) -> 4096x2048 equirect, " \
-           "8-level integer multiband blend, per-camera per-channel LUT gains U[0.8,1.2]"
+METRICS = {"c2": METRIC, "c5": "stitched output Mpix/s at 7680x3840 (8 cams)"}
+WORKLOADS = {
+    "c2": "6x rectilinear 1920x1080 (100 deg hfov; yaw 0/90/180/270, pitch +-90) -> 4096x2048 equirect, "
+          "8-level integer multiband blend, per-camera per-channel LUT gains U[0.8,1.2]",
+    "c5": "8x rectilinear 3840x2160 (120 deg hfov; yaw every 45 deg) -> 7680x3840 equirect, 10-level integer "
+          "multiband blend, per-camera per-channel LUT gains U[0.7,1.3], noise +-20",
+}
+WORKLOAD = WORKLOADS["c2"]
 
 
 # ----------------------------------------------------------------------------- distributed
@@ -175,7 +181,7 @@ def run_ours(args, world, rank, local, dist):
     B.build()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    cfg = S.rig("c2")
+    cfg = S.rig(args.workload)
     W, H = cfg.dst_size
     npx = W * H
     r = P.CudaPanoramaRender2()
@@ -207,17 +213,18 @@ def run_ours(args, world, rank, local, dist):
     ms_max = reduce_max(ms, dist, dev)
     barrier(dist)
     value = aggregate_mpix(world, args.steps, npx, ms_max)
-    out = {"metric": METRIC, "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+    out = {"metric": METRICS[args.workload], "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 5), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
            "data": f"synthetic: seeded smooth field + per-frame noise, pool of {args.pool} frames in HBM",
            "gpu_launches": args.steps * r.launches_per_frame,
            "clocks": clocks}
     resident = r.resident_bytes
-    out["config"] = {"workload": WORKLOAD, "canvas": [W, H], "cams": cfg.num_cams, "src": list(cfg.src_size),
-                     "levels": r.num_levels, "full_mask": r.full_mask,
-                     "l2": f"inputs larger than L2: {args.pool} distinct 49.8 MB frames cycled, rig state "
-                           f"{resident / 1e6:.0f} MB resident", "parallelism": f"replicas x{world}",
+    frame_mb = sum(f.nbytes for f in pool_host[0]) / 1e6
+    out["config"] = {"workload": WORKLOADS[args.workload], "canvas": [W, H], "cams": cfg.num_cams,
+                     "src": list(cfg.src_size), "levels": r.num_levels, "full_mask": r.full_mask,
+                     "l2": f"inputs larger than L2: {args.pool} distinct {frame_mb:.1f} MB frames cycled, "
+                           f"rig state {resident / 1e6:.0f} MB resident", "parallelism": f"replicas x{world}",
                      "prepare_s": round(prepare_s, 3)}
 
     # ---- e2e: pinned host frames in, host canvas out, through the C ABI
@@ -290,9 +297,9 @@ def run_ours(args, world, rank, local, dist):
         except Exception as e:  # an extra leg failing must not lose the headline line
             return {"error": f"{type(e).__name__}: {e}"}
 
-    if world == 1 and not args.no_batched:
+    if world == 1 and not args.no_batched and args.workload == "c2":
         out["batched"] = guarded(run_batched, args, dev)
-    if world == 1 and not args.no_serve:
+    if world == 1 and not args.no_serve and args.workload == "c2":
         out["serve"] = guarded(run_serve, args, dev)
     if world == 1 and rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = guarded(cpu_baseline, r, cfg, pool_host, luts, args.cpu_seconds)
@@ -424,8 +431,8 @@ def cpu_baseline(r, cfg, pool_host, luts, seconds):
             break
     W, H = cfg.dst_size
     return {"value": round(frames * W * H / el / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
-            "sample": f"{frames} full frames of the 6-camera 4096x2048 rig (LUT + bilinear remap + multiband "
-                      f"blend) in {el:.1f} s"}
+            "sample": f"{frames} full frames of the {cfg.num_cams}-camera {W}x{H} rig (LUT + bilinear remap + "
+                      f"multiband blend) in {el:.1f} s"}
 
 
 # ----------------------------------------------------------------------------- reference arm
@@ -482,6 +489,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--pool", type=int, default=4)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
