@@ -253,6 +253,24 @@ def run_ours(args, world, rank, local, dist):
                   "d2h_bytes_per_step": int(hdst.nbytes), "steps": e2e_steps,
                   "path": "ps_render_render, pinned BGR32 host frames -> pinned BGR32 host canvas"}
 
+    # ---- e2e with the encoder handoff: NV12 planes downloaded (the Task layer's render + cvt + download)
+    hy, hy_t = pinned_copy(np.zeros((H, W), np.uint8))
+    huv, huv_t = pinned_copy(np.zeros((H // 2, W), np.uint8))
+    for k in range(2):
+        r.render_yuv(pinned[k % args.pool], [hy, huv], luts, P.PS_FMT_NV12, check=True)
+    torch.cuda.synchronize()
+    barrier(dist)
+    t = time.perf_counter()
+    for k in range(e2e_steps):
+        r.render_yuv(pinned[k % args.pool], [hy, huv], luts, P.PS_FMT_NV12, check=True)
+    torch.cuda.synchronize()
+    nv12_s = reduce_max(time.perf_counter() - t, dist, dev)
+    out["e2e_nv12"] = {"value": round(world * e2e_steps * npx / nv12_s / 1e6, 3), "unit": "Mpix/s",
+                       "h2d_bytes_per_step": int(sum(f.nbytes for f in pinned[0])),
+                       "d2h_bytes_per_step": int(hy.nbytes + huv.nbytes), "steps": e2e_steps,
+                       "path": "ps_render_render_yuv, pinned BGR32 host frames -> pinned NV12 host planes "
+                               "(conversion fused into the level-0 blend)"}
+
     # ---- roofline: profiled pass (a CUDA event pair around every launch)
     r.profile(True)
     prof_steps = min(args.steps, 30)

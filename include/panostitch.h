@@ -65,6 +65,21 @@ typedef struct ps_image {
     int location;        /* PS_MEM_* */
 } ps_image;
 
+/* Planar encoder formats (BT.601 studio range, the encoders' inputs in
+   source/Task/PanoramaLocalDiskTask.cpp:2054-2076). */
+#define PS_FMT_YUV420P 420  /* planes: Y (w x h), U (w/2 x h/2), V (w/2 x h/2) */
+#define PS_FMT_NV12 12      /* planes: Y (w x h), interleaved U,V (w bytes x h/2) */
+
+/* A planar frame view: the replacement of the Y / U / V (or Y / UV)
+   GpuMats and the encoder's host planes. */
+typedef struct ps_planar_image {
+    void* planes[3];        /* Y, U, V (YUV420P) or Y, UV, unused (NV12) */
+    long long pitches[3];   /* bytes between rows of each plane */
+    int width, height;      /* luma size; both even */
+    int format;             /* PS_FMT_YUV420P or PS_FMT_NV12 */
+    int location;           /* PS_MEM_* (all planes alike) */
+} ps_planar_image;
+
 /* Thread-local text of the last error ("" if none). */
 const char* ps_last_error(void);
 /* Library version string. */
@@ -104,6 +119,17 @@ int ps_render_prepare_with_seams(ps_render* r, const ps_photo_param* params, int
    device src / dst are read / written in place.  Does not synchronise. */
 int ps_render_render(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,
                      ps_image* dst, void* stream);
+
+/* CudaPanoramaRender2::render followed by the encoder handoff
+   cvtBGR32ToYUV420P / cvtBGR32ToNV12 and the planes' download
+   (source/CudaAccel/ImageProc.cu:44-160, called at
+   source/Task/PanoramaLocalDiskTask.cpp:2054-2076), in one call: the
+   conversion is fused into the level-0 blend store, so the BGR canvas is
+   never written.  The planes are byte-identical to converting the
+   ps_render_render BGR32 output.  dst: dst_w x dst_h, host or device.  Does
+   not synchronise. */
+int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,
+                         const ps_planar_image* dst, void* stream);
 
 /* Launch the per-frame kernels as one captured CUDA graph (default 1) or as
    individual launches (0).  No reference counterpart. */
@@ -174,6 +200,11 @@ int ps_reproject_to_16s(const ps_image* src, const float* xmap, const float* yma
                         void* stream);
 /* getLUT (source/Blend/ExposureColorOptimize.cpp:1217-1223) on the host. */
 int ps_get_lut(double k, uint8_t* lut256);
+/* cvtBGR32ToYUV420P / cvtBGR32ToNV12 (source/CudaAccel/ImageProc.cu:97-160):
+   a device BGR32 image to device planes of the same (even) size.  Y per
+   pixel; U and V per 2x2 block from its left column, as the reference
+   computes them. */
+int ps_cvt_bgr32_to_yuv(const ps_image* src, const ps_planar_image* dst, void* stream);
 
 /* No counterpart in the reference.  The nearest-optical-axis seam masks of a
    rig (the masks ps_render_prepare derives internally), computed without

@@ -43,23 +43,21 @@ public:
     bool render(const std::vector<ps_image>& src, ps_image& dst,
                 const std::vector<std::vector<std::vector<unsigned char>>>& luts = {}, void* stream = nullptr)
     {
-        const int n = getNumImages();
-        bool correct = (int)luts.size() == n && n > 0;
-        for (size_t i = 0; correct && i < luts.size(); i++) {
-            if (luts[i].size() != 3) correct = false;
-            for (size_t c = 0; correct && c < luts[i].size(); c++)
-                if (luts[i][c].size() != 256) correct = false;
-        }
-        if (!correct && !luts.empty())
-            std::fprintf(stderr, "Warning in render, the non-empty look up tables not satisfied, skip correction\n");
         std::vector<unsigned char> flat;
-        if (correct) {
-            flat.reserve((size_t)n * 768);
-            for (const auto& cam : luts)
-                for (const auto& ch : cam) flat.insert(flat.end(), ch.begin(), ch.end());
-        }
+        const bool correct = flattenLuts(luts, flat);
         return ok(ps_render_render(r_, src.data(), (int)src.size(), correct ? flat.data() : nullptr,
-                                   correct ? n : 0, &dst, stream));
+                                   correct ? getNumImages() : 0, &dst, stream));
+    }
+
+    // render followed by the encoder handoff (cvtBGR32ToYUV420P / cvtBGR32ToNV12
+    // and the planes' download, source/Task/PanoramaLocalDiskTask.cpp:2054-2076)
+    bool renderYuv(const std::vector<ps_image>& src, const ps_planar_image& dst,
+                   const std::vector<std::vector<std::vector<unsigned char>>>& luts = {}, void* stream = nullptr)
+    {
+        std::vector<unsigned char> flat;
+        const bool correct = flattenLuts(luts, flat);
+        return ok(ps_render_render_yuv(r_, src.data(), (int)src.size(), correct ? flat.data() : nullptr,
+                                       correct ? getNumImages() : 0, &dst, stream));
     }
 
     void clear() { ps_render_clear(r_); }
@@ -73,6 +71,27 @@ private:
         if (status == PS_OK) return true;
         err_ = ps_last_error();
         return false;
+    }
+    // The reference's LUT check (source/Task/RicohUtil.cpp:1239-1265): a
+    // malformed non-empty set is skipped with a warning.
+    bool flattenLuts(const std::vector<std::vector<std::vector<unsigned char>>>& luts,
+                     std::vector<unsigned char>& flat) const
+    {
+        const int n = getNumImages();
+        bool correct = (int)luts.size() == n && n > 0;
+        for (size_t i = 0; correct && i < luts.size(); i++) {
+            if (luts[i].size() != 3) correct = false;
+            for (size_t c = 0; correct && c < luts[i].size(); c++)
+                if (luts[i][c].size() != 256) correct = false;
+        }
+        if (!correct && !luts.empty())
+            std::fprintf(stderr, "Warning in render, the non-empty look up tables not satisfied, skip correction\n");
+        if (correct) {
+            flat.reserve((size_t)n * 768);
+            for (const auto& cam : luts)
+                for (const auto& ch : cam) flat.insert(flat.end(), ch.begin(), ch.end());
+        }
+        return correct;
     }
     ps_render* r_ = nullptr;
     std::string err_;

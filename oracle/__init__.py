@@ -94,6 +94,8 @@ def lib():
             L.orc_mb_blend.argtypes = [vp, vp, vp, vp, vp]
             L.orc_mb_blend_mt.argtypes = [vp, vp, vp, C.c_int]
             L.orc_render.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int]
+            L.orc_bgr32_to_yuv.argtypes = [vp, C.c_longlong, C.c_int, C.c_int, C.c_int, vp, C.c_longlong, vp,
+                                           C.c_longlong, vp, C.c_longlong]
             _lib = L
     return _lib
 
@@ -136,6 +138,28 @@ def get_lut(k: float) -> np.ndarray:
     out = np.empty(256, np.uint8)
     lib().orc_get_lut(float(k), _ptr(out))
     return out
+
+
+# ------------------------------------------------------------------- encoder handoff
+FMT_YUV420P = 420
+FMT_NV12 = 12
+
+
+def bgr32_to_yuv(bgr: np.ndarray, fmt: int = FMT_YUV420P):
+    """BGR32 HxWx4 -> (Y, U, V) planes (YUV420P) or (Y, UV) planes (NV12)."""
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    H, W, chn = bgr.shape
+    if chn != 4 or H % 2 or W % 2:
+        raise ValueError("BGR32 image with even width and height expected")
+    y = np.empty((H, W), np.uint8)
+    if fmt == FMT_NV12:
+        uv = np.empty((H // 2, W), np.uint8)
+        lib().orc_bgr32_to_yuv(_ptr(bgr), W * 4, W, H, fmt, _ptr(y), W, _ptr(uv), W, None, 0)
+        return y, uv
+    u = np.empty((H // 2, W // 2), np.uint8)
+    v = np.empty((H // 2, W // 2), np.uint8)
+    lib().orc_bgr32_to_yuv(_ptr(bgr), W * 4, W, H, FMT_YUV420P, _ptr(y), W, _ptr(u), W // 2, _ptr(v), W // 2)
+    return y, u, v
 
 
 # ------------------------------------------------------------------- remap

@@ -888,3 +888,52 @@ void orc_render(orc_blender* b, const uint8_t* const* srcs, int srcW, int srcH, 
     free(tmp);
     free(imgs);
 }
+
+/* ---- encoder handoff: BGR32 -> YUV420P / NV12 ------------------------------
+ * source/CudaAccel/ImageProc.cu:44-95 (cvtBGRToYUV2x2Block) over 2x2 blocks
+ * (:97-117).  BT.601 coefficients scaled by 2^20, +0.5 rounding and the
+ * 16 / 128 offsets folded in; every sum is non-negative, so >> is a floor.
+ * Luma per pixel; chroma of a block from its left column only (top-left and
+ * bottom-left pixels), averaged by one extra shift.
+ */
+static int yuv_clamp(int v) { return v < 0 ? 0 : (v > 255 ? 255 : v); }
+
+static int yuv_y(const uint8_t* p)
+{
+    return yuv_clamp((269484 * p[2] + 528482 * p[1] + 102760 * p[0] + (1 << 19) + (16 << 20)) >> 20);
+}
+
+static void yuv_uv_sums(const uint8_t* p, int* su, int* sv)
+{
+    *su = -155188 * p[2] - 305135 * p[1] + 460324 * p[0] + (1 << 19) + (128 << 20);
+    *sv = 460324 * p[2] - 385875 * p[1] - 74448 * p[0] + (1 << 19) + (128 << 20);
+}
+
+void orc_bgr32_to_yuv(const uint8_t* bgr, long long bgrStep, int w, int h, int fmt, uint8_t* y, long long yStep,
+                      uint8_t* u, long long uStep, uint8_t* v, long long vStep)
+{
+    for (int by = 0; by < h / 2; by++) {
+        const uint8_t* top = bgr + (size_t)(2 * by) * bgrStep;
+        const uint8_t* bot = top + bgrStep;
+        uint8_t* yt = y + (size_t)(2 * by) * yStep;
+        uint8_t* yb = yt + yStep;
+        for (int bx = 0; bx < w / 2; bx++) {
+            const int x = 2 * bx;
+            yt[x] = (uint8_t)yuv_y(top + 4 * x);
+            yt[x + 1] = (uint8_t)yuv_y(top + 4 * x + 4);
+            yb[x] = (uint8_t)yuv_y(bot + 4 * x);
+            yb[x + 1] = (uint8_t)yuv_y(bot + 4 * x + 4);
+            int u0, v0, u1, v1;
+            yuv_uv_sums(top + 4 * x, &u0, &v0);
+            yuv_uv_sums(bot + 4 * x, &u1, &v1);
+            const uint8_t cu = (uint8_t)yuv_clamp((u0 + u1) >> 21), cv = (uint8_t)yuv_clamp((v0 + v1) >> 21);
+            if (fmt == 12) {
+                u[(size_t)by * uStep + x] = cu;
+                u[(size_t)by * uStep + x + 1] = cv;
+            } else {
+                u[(size_t)by * uStep + bx] = cu;
+                v[(size_t)by * vStep + bx] = cv;
+            }
+        }
+    }
+}

@@ -98,6 +98,13 @@ void orc_render(orc_blender* b, const uint8_t* const* srcs, int srcW, int srcH, 
                 const uint8_t* luts, const float* const* xmaps, const float* const* ymaps,
                 uint8_t* dst, int nthreads);
 
+/* ---- encoder handoff --------------------------------------------------- */
+/* cvtBGR32ToYUV420P / cvtBGR32ToNV12 (source/CudaAccel/ImageProc.cu:44-160):
+   BT.601 studio range in 20-bit fixed point.  fmt 420: planes y, u, v;
+   fmt 12 (NV12): planes y, uv (v unused).  w, h even. */
+void orc_bgr32_to_yuv(const uint8_t* bgr, long long bgrStep, int w, int h, int fmt, uint8_t* y, long long yStep,
+                      uint8_t* u, long long uStep, uint8_t* v, long long vStep);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "libpanostitch.so")
 PS_OK, PS_EINVAL, PS_ENOMEM, PS_ECUDA, PS_ETIMEOUT, PS_ESTATE = 0, 1, 2, 3, 4, 5
 PS_MAX_LEVELS, PS_MAX_CAMS = 16, 64
 PS_FMT_BGR24, PS_FMT_BGR32 = 24, 32
+PS_FMT_YUV420P, PS_FMT_NV12 = 420, 12
 PS_MEM_HOST, PS_MEM_DEVICE = 0, 1
 EXPORT_XMAP, EXPORT_YMAP, EXPORT_COVERAGE, EXPORT_SEAM, EXPORT_WEIGHT, EXPORT_ALPHA = range(6)
 
@@ -52,6 +53,13 @@ class Image(C.Structure):
                 ("format", C.c_int), ("location", C.c_int)]
 
 
+class PlanarImage(C.Structure):
+    """ps_planar_image: Y / U / V (YUV420P) or Y / UV (NV12) planes."""
+
+    _fields_ = [("planes", C.c_void_p * 3), ("pitches", C.c_longlong * 3), ("width", C.c_int),
+                ("height", C.c_int), ("format", C.c_int), ("location", C.c_int)]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -68,6 +76,8 @@ _SIGS = [
                                                C.c_void_p]),
     ("ps_render_render", C.c_int, [C.c_void_p, C.POINTER(Image), C.c_int, C.c_void_p, C.c_int,
                                    C.POINTER(Image), C.c_void_p]),
+    ("ps_render_render_yuv", C.c_int, [C.c_void_p, C.POINTER(Image), C.c_int, C.c_void_p, C.c_int,
+                                       C.POINTER(PlanarImage), C.c_void_p]),
     ("ps_render_set_graph", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_clear", None, [C.c_void_p]),
     ("ps_render_get_num_images", C.c_int, [C.c_void_p]),
@@ -90,6 +100,7 @@ _SIGS = [
     ("ps_reproject_to_16s", C.c_int, [C.POINTER(Image), C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_int,
                                       C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]),
     ("ps_get_lut", C.c_int, [C.c_double, C.c_void_p]),
+    ("ps_cvt_bgr32_to_yuv", C.c_int, [C.POINTER(Image), C.POINTER(PlanarImage), C.c_void_p]),
     ("ps_nearest_axis_seams_no_alloc", C.c_int, [C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,
                                                  C.c_int, C.c_void_p, C.c_void_p]),
     ("ps_blender_create", C.c_int, [C.POINTER(C.c_void_p)]),

@@ -85,6 +85,26 @@ void checkFrame(const ps::Rig& rig, const ps_image* src, int numSrc, const uint8
     checkImage(dst, rig.width(), rig.height(), "dst", 0);
 }
 
+// A planar YUV420P / NV12 view of w x h (both even).
+void checkPlanar(const ps_planar_image* im, int w, int h, const char* what)
+{
+    if (!im) fail(PS_EINVAL, "%s is NULL", what);
+    if (im->format != PS_FMT_YUV420P && im->format != PS_FMT_NV12)
+        fail(PS_EINVAL, "%s: format %d is neither YUV420P nor NV12", what, im->format);
+    if (im->location != PS_MEM_HOST && im->location != PS_MEM_DEVICE)
+        fail(PS_EINVAL, "%s: location %d unknown", what, im->location);
+    if (im->width != w || im->height != h)
+        fail(PS_EINVAL, "%s size (%d, %d), not equal to (%d, %d)", what, im->width, im->height, w, h);
+    // CV_Assert((rows & 1) == 0 && (cols & 1) == 0), ImageProc.cu:123,143
+    if (w <= 0 || h <= 0 || (w & 1) || (h & 1)) fail(PS_EINVAL, "%s: size (%d, %d) must be positive and even", what, w, h);
+    const int planes = im->format == PS_FMT_NV12 ? 2 : 3;
+    const long long minPitch[3] = {w, im->format == PS_FMT_NV12 ? w : w / 2, w / 2};
+    for (int k = 0; k < planes; k++) {
+        if (!im->planes[k]) fail(PS_EINVAL, "%s: plane %d is NULL", what, k);
+        if (im->pitches[k] < minPitch[k]) fail(PS_EINVAL, "%s: plane %d pitch %lld too small", what, k, im->pitches[k]);
+    }
+}
+
 // Launch plans of batches, keyed by the rigs they run.
 std::mutex g_planMu;
 std::map<std::vector<ps::Rig*>, std::unique_ptr<ps::Plan>> g_batchPlans;
@@ -195,6 +215,21 @@ double ps_render_algorithmic_bytes(const ps_render* r, int bytes_in_per_px, int 
     return r->rig.algorithmicBytes(bytes_in_per_px, bytes_out_per_px);
 }
 
+int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,
+                         const ps_planar_image* dst, void* stream)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (!r->rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        checkPlanar(dst, r->rig.width(), r->rig.height(), "dst");
+        ps_image probe = {dst->planes[0], (long long)r->rig.width() * 4, r->rig.width(), r->rig.height(),
+                          PS_FMT_BGR32, PS_MEM_DEVICE};  // only for the shared source / LUT checks
+        checkFrame(r->rig, src, num_src, luts, num_luts, &probe);
+        if (!r->plan || !r->plan->matches({&r->rig})) r->plan.reset(new ps::Plan({&r->rig}));
+        r->plan->run({ps::FrameInput{src, luts, nullptr, dst}}, toStream(stream), r->useGraph, &r->prof);
+    });
+}
+
 int ps_render_set_graph(ps_render* r, int enabled)
 {
     return guarded([&] {
@@ -299,6 +334,22 @@ int ps_reproject_to_16s(const ps_image* src, const float* xmap, const float* yma
         PS_CUDA(ps::launchReprojectTo16S(static_cast<const uint8_t*>(src->data), src->pitch, src->width, src->height,
                                          src->format, xmap, ymap, map_pitch, dst_w, dst_h, lut, dst, dst_pitch,
                                          toStream(stream)));
+    });
+}
+
+int ps_cvt_bgr32_to_yuv(const ps_image* src, const ps_planar_image* dst, void* stream)
+{
+    return guarded([&] {
+        if (!src || !dst) fail(PS_EINVAL, "NULL argument");
+        checkImage(src, src->width, src->height, "src", 0);
+        if (src->format != PS_FMT_BGR32) fail(PS_EINVAL, "src must be BGR32");  // CV_8UC4, ImageProc.cu:123
+        if (src->location != PS_MEM_DEVICE) fail(PS_EINVAL, "src must be device memory");
+        checkPlanar(dst, src->width, src->height, "dst");
+        if (dst->location != PS_MEM_DEVICE) fail(PS_EINVAL, "dst must be device memory");
+        PS_CUDA(ps::launchCvtYuv(static_cast<const uint8_t*>(src->data), src->pitch, src->width, src->height,
+                                 dst->format, static_cast<uint8_t*>(dst->planes[0]), dst->pitches[0],
+                                 static_cast<uint8_t*>(dst->planes[1]), dst->pitches[1],
+                                 static_cast<uint8_t*>(dst->planes[2]), dst->pitches[2], toStream(stream)));
     });
 }
 

@@ -13,7 +13,7 @@
 //   C[j]   short4 collapsed result of level j >= 1 (resultPyr after
 //          normalise + collapse); |value| < 3300 so int16 is exact.
 //   maps   float2 dst->src map, stored tile-compact for the level-0 tiles
-//          that a camera covers (256 pixels per tile, row-major in the tile).
+//          that a camera covers (512 pixels per 32x16 tile, row-major in the tile).
 // Work is described by item lists built at prepare time from the pyramids'
 // supports, so no kernel touches canvas area a camera cannot influence.
 #pragma once
@@ -78,9 +78,13 @@ struct FrameDev {
     const uint8_t* src[PS_MAX_CAMS];
     long long srcPitch[PS_MAX_CAMS];
     int srcFmt;               // PS_FMT_BGR24 / PS_FMT_BGR32
-    int outFmt;
-    uint8_t* out;
+    int outFmt;               // PS_FMT_BGR24 / BGR32 / YUV420P / NV12
+    uint8_t* out;             // BGR canvas, or the Y plane
     long long outPitch;
+    uint8_t* outU;            // YUV420P: U plane; NV12: interleaved UV plane
+    uint8_t* outV;            // YUV420P: V plane
+    long long outCPitch;      // pitch of the U (or UV) plane
+    long long outVPitch;      // pitch of the V plane
     const uint8_t* luts;      // n * 768 device bytes (B, G, R tables)
     int* status;              // device error word (0 = ok)
 };

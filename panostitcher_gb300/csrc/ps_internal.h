@@ -136,9 +136,12 @@ cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t 
 // one cluster per segment: the rig's pyrDown levels tailDown..L and blend levels L..tailBlend
 cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st);
 
-// ---- standalone primitive ---------------------------------------------------------
+// ---- standalone primitives -------------------------------------------------------
 cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,
                                  const float* xmap, const float* ymap, long long mapPitch, int dstW, int dstH,
                                  const uint8_t* lut, int16_t* dst, long long dstPitch, cudaStream_t st);
+// BGR32 -> YUV420P (u, v planes) or NV12 (u = the UV plane, v unused); w, h even
+cudaError_t launchCvtYuv(const uint8_t* src, long long srcPitch, int w, int h, int fmt, uint8_t* y, long long yPitch,
+                         uint8_t* u, long long uPitch, uint8_t* v, long long vPitch, cudaStream_t st);
 
 }  // namespace ps

@@ -15,6 +15,8 @@
 // The reference runs the same arithmetic as ~35 launches per camera plus
 // ~36 per frame over full-canvas int16/int32 images
 // (source/CudaAccel/CudaMultibandBlend.cpp:785-823).
+#include <algorithm>
+
 #include "ps_async.cuh"
 #include "ps_device.cuh"
 #include "ps_internal.h"
@@ -304,6 +306,7 @@ constexpr int kCfW = 36;   // staged collapse footprint row: columns fx0-1 .. fx
 constexpr int kMaxSmemSegs = 64;
 constexpr int kConsumers = kThreads;          // 8 warps
 constexpr int kBlendThreads = kConsumers + 32;  // + the producer warp
+constexpr int kConsumersYuv = kConsumers / 2;   // one chroma hand-over slot per odd-row thread
 
 struct alignas(16) BlendStage {
     uint32_t gj[kCamsPerUnit][kBlendTH][kBlendTW];  // G_j, uchar4
@@ -312,10 +315,113 @@ struct alignas(16) BlendStage {
     uint2 cf[kFH][kCfW];                            // C_{j+1} footprint (short4 bits)
 };
 
+// What the consumers need of a unit besides its stage: the level geometry
+// and the frame's output, resolved once per unit (in k_blend by the
+// producer warp, so the consumers read it from shared memory).
+struct UnitGeo {
+    int w, h, pitch, full, hasUp, outFmt;
+    short4* C;              // collapsed result of the unit's level (j >= 1)
+    const uint8_t* um;      // union mask (level 0, partially covered tiles)
+    uint8_t* out;           // BGR canvas or Y plane
+    uint8_t* outU;          // U (YUV420P) or UV (NV12) plane
+    uint8_t* outV;          // V plane (YUV420P)
+    long long outPitch, outCPitch, outVPitch;
+};
+
+__device__ __forceinline__ void fillGeo(UnitGeo& g, const RigDev& R, const FrameDev& F, int j)
+{
+    const LevelDev& Lj = R.lv[j];
+    g.w = Lj.w;
+    g.h = Lj.h;
+    g.pitch = Lj.pitch;
+    g.full = R.full;
+    g.hasUp = j < R.L;
+    g.outFmt = F.outFmt;
+    g.C = Lj.C;
+    g.um = R.unionMask;
+    g.out = F.out;
+    g.outU = F.outU;
+    g.outV = F.outV;
+    g.outPitch = F.outPitch;
+    g.outCPitch = F.outCPitch;
+    g.outVPitch = F.outVPitch;
+}
+
 struct UnitInfo {
     uint4 raw;
     int seg, chunk, valid, staged;  // staged: copies issued by the producer
+    UnitGeo geo;
 };
+
+// ---- BT.601 studio-range conversion (cvtBGRToYUV2x2Block,
+// ImageProc.cu:44-95): 20-bit fixed point, Y = 16 + ..., chroma = 128 + ...
+// These are the standard BT.601 coefficients scaled by 2^20; the chroma of
+// a 2x2 block is the mean of its left column's two pixels.
+constexpr int kYR = 269484, kYG = 528482, kYB = 102760;
+constexpr int kUR = -155188, kUG = -305135, kUB = 460324;
+constexpr int kVR = 460324, kVG = -385875, kVB = -74448;
+constexpr int kYuvShift = 20;
+constexpr int kYuvHalf = 1 << (kYuvShift - 1);
+constexpr int kYOff = (16 << kYuvShift) + kYuvHalf;
+constexpr int kCOff = (128 << kYuvShift) + kYuvHalf;
+
+__device__ __forceinline__ int clamp255(int v) { return min(max(v, 0), 255); }
+
+__device__ __forceinline__ uint32_t yuvLuma(uint32_t bgr)
+{
+    const int b = bgr & 0xFF, g = (bgr >> 8) & 0xFF, r = (bgr >> 16) & 0xFF;
+    return (uint32_t)clamp255((kYR * r + kYG * g + kYB * b + kYOff) >> kYuvShift);
+}
+
+// Unshifted chroma sums of one pixel (both are non-negative).
+__device__ __forceinline__ int2 yuvChromaSums(uint32_t bgr)
+{
+    const int b = bgr & 0xFF, g = (bgr >> 8) & 0xFF, r = (bgr >> 16) & 0xFF;
+    return make_int2(kUR * r + kUG * g + kUB * b + kCOff, kVR * r + kVG * g + kVB * b + kCOff);
+}
+
+// Level-0 store of a consumer thread's pixel pair as Y and, for even rows,
+// the block's U and V.  The block's lower-left pixel belongs to the next
+// consumer warp, so odd rows hand their chroma sums over through xch (two
+// alternating halves of 128 int2, so one barrier per tile suffices).
+// Every consumer thread must call this for the unit (it contains a barrier).
+template <class Sync>
+__device__ __forceinline__ void storeYuv(const UnitGeo& G, int x, int y, bool inside, uint32_t o0, uint32_t o1,
+                                         int2* xch, int& parity, Sync sync)
+{
+    const int lane = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    int2* buf = xch + parity * (kConsumersYuv);
+    parity ^= 1;
+    const int2 c = yuvChromaSums(o0);
+    if (ly & 1) buf[(ly >> 1) * 32 + lane] = c;
+    sync();
+    if (!inside) return;
+    uint8_t* yrow = G.out + (size_t)y * G.outPitch + x;
+    const uint32_t y0 = yuvLuma(o0), y1 = yuvLuma(o1);
+    if ((reinterpret_cast<uintptr_t>(yrow) & 1) == 0) {
+        *reinterpret_cast<uint16_t*>(yrow) = (uint16_t)(y0 | (y1 << 8));
+    } else {
+        yrow[0] = (uint8_t)y0;
+        yrow[1] = (uint8_t)y1;
+    }
+    if (ly & 1) return;
+    const int2 d = buf[(ly >> 1) * 32 + lane];
+    const uint8_t u = (uint8_t)clamp255((c.x + d.x) >> (kYuvShift + 1));
+    const uint8_t v = (uint8_t)clamp255((c.y + d.y) >> (kYuvShift + 1));
+    const size_t cy = (size_t)(y >> 1);
+    if (G.outFmt == PS_FMT_NV12) {
+        uint8_t* p = G.outU + cy * G.outCPitch + x;
+        if ((reinterpret_cast<uintptr_t>(p) & 1) == 0) {
+            *reinterpret_cast<uint16_t*>(p) = (uint16_t)(u | (v << 8));
+        } else {
+            p[0] = u;
+            p[1] = v;
+        }
+    } else {
+        G.outU[cy * G.outCPitch + (x >> 1)] = u;
+        G.outV[cy * G.outVPitch + (x >> 1)] = v;
+    }
+}
 
 // q-th camera of a blend tile (raw 16-byte descriptor)
 __device__ __forceinline__ int tileCam(const uint4& raw, const uint8_t* camLists, int q)
@@ -334,6 +440,7 @@ __device__ __forceinline__ int unitChunks(const uint4& raw)
 struct BlendAcc {
     int r0[3], r1[3];
     int wsum0, wsum1;
+    int parity = 0;  // half of the chroma hand-over buffer in use
 };
 
 // Stage one unit with index-mapped loads (border tiles; every tile of the
@@ -386,10 +493,12 @@ __device__ __forceinline__ void stageUnitDirect(BlendStage& S, const RigDev& R, 
 }
 
 // Accumulate one unit from its stage; at a tile's last unit normalise,
-// collapse and store.  Threads 0..kConsumers-1.  staged: the unit came from
-// the bulk copies (weights absent for uniform tiles).
-__device__ __forceinline__ void computeUnit(const BlendStage& S, const RigDev& R, const FrameDev& F, const uint4& raw,
-                                            int chunk, bool staged, BlendAcc& acc)
+// collapse and store.  Threads 0..kConsumers-1, all of them (a YUV store
+// synchronises them with sync()).  staged: the unit came from the bulk
+// copies (weights absent for uniform tiles).
+template <class Sync>
+__device__ __forceinline__ void computeUnit(const BlendStage& S, const UnitGeo& G, const uint4& raw, int chunk,
+                                            bool staged, BlendAcc& acc, int2* xch, Sync sync)
 {
     const int lx = (threadIdx.x & 31) * 2, ly = threadIdx.x >> 5;
     // vertical taps of the zero-inserted upsample for this row's parity:
@@ -402,10 +511,9 @@ __device__ __forceinline__ void computeUnit(const BlendStage& S, const RigDev& R
     const int j = raw.x & 0xFF, cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
     const bool uni = ((raw.x >> 24) & kTileUniform) != 0;
     const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
-    const LevelDev& Lj = R.lv[j];
-    const bool hasUp = j < R.L;
+    const bool hasUp = G.hasUp != 0;
     const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
-    const bool rowOk = y < Lj.h;
+    const bool rowOk = y < G.h;
     const bool active = !(j == 0 && cls == 0);
     const int c0 = chunk * kCamsPerUnit;
     const int nc = max(0, min(kCamsPerUnit, camCnt - c0));
@@ -465,7 +573,7 @@ __device__ __forceinline__ void computeUnit(const BlendStage& S, const RigDev& R
     if (fast) {
 #pragma unroll
         for (int c = 0; c < 3; c++) { n0[c] = acc.r0[c]; n1[c] = acc.r1[c]; }
-    } else if (R.full) {
+    } else if (G.full) {
 #pragma unroll
         for (int c = 0; c < 3; c++) { n0[c] = (acc.r0[c] + 128) >> 8; n1[c] = (acc.r1[c] + 128) >> 8; }
     } else {
@@ -500,47 +608,54 @@ __device__ __forceinline__ void computeUnit(const BlendStage& S, const RigDev& R
             n1[c] += (4 * (v[1][c] + v[2][c]) + 32) >> 6;
         }
     }
-    if (!rowOk) return;
     if (j > 0) {
-        short4* Cj = Lj.C + (size_t)y * Lj.pitch + x;
-        if (x + 1 < Lj.w) {
+        if (!rowOk) return;
+        short4* Cj = G.C + (size_t)y * G.pitch + x;
+        if (x + 1 < G.w) {
             *reinterpret_cast<int4*>(Cj) =
                 make_int4((int)((uint32_t)(uint16_t)n0[0] | ((uint32_t)(uint16_t)n0[1] << 16)),
                           (int)(uint32_t)(uint16_t)n0[2],
                           (int)((uint32_t)(uint16_t)n1[0] | ((uint32_t)(uint16_t)n1[1] << 16)),
                           (int)(uint32_t)(uint16_t)n1[2]);
-        } else if (x < Lj.w) {
+        } else if (x < G.w) {
             Cj[0] = make_short4((short)n0[0], (short)n0[1], (short)n0[2], 0);
         }
         return;
     }
     uint32_t o0 = 0, o1 = 0;
-    if (cls != 0) {
+    if (cls != 0 && rowOk) {
         o0 = (uint32_t)min(max(n0[0], 0), 255) | ((uint32_t)min(max(n0[1], 0), 255) << 8) |
              ((uint32_t)min(max(n0[2], 0), 255) << 16);
         o1 = (uint32_t)min(max(n1[0], 0), 255) | ((uint32_t)min(max(n1[1], 0), 255) << 8) |
              ((uint32_t)min(max(n1[2], 0), 255) << 16);
         if (cls == 2) {
-            const uint8_t* um = R.unionMask + (size_t)y * Lj.pitch + x;
+            const uint8_t* um = G.um + (size_t)y * G.pitch + x;
             if (!um[0]) o0 = 0;
-            if (x + 1 < Lj.w && !um[1]) o1 = 0;
+            if (x + 1 < G.w && !um[1]) o1 = 0;
         }
     }
-    uint8_t* orow = F.out + (size_t)y * F.outPitch;
-    if (F.outFmt == PS_FMT_BGR32) {
-        if (x + 1 < Lj.w && ((reinterpret_cast<uintptr_t>(orow) & 7) == 0)) {
+    if (G.outFmt == PS_FMT_YUV420P || G.outFmt == PS_FMT_NV12) {
+        // widths and heights are even, so a pixel pair and a 2x2 block are
+        // inside or outside the canvas together
+        storeYuv(G, x, y, rowOk && x < G.w, o0, o1, xch, acc.parity, sync);
+        return;
+    }
+    if (!rowOk) return;
+    uint8_t* orow = G.out + (size_t)y * G.outPitch;
+    if (G.outFmt == PS_FMT_BGR32) {
+        if (x + 1 < G.w && ((reinterpret_cast<uintptr_t>(orow) & 7) == 0)) {
             reinterpret_cast<uint2*>(orow)[x / 2] = make_uint2(o0, o1);
         } else {
-            if (x < Lj.w) reinterpret_cast<uint32_t*>(orow)[x] = o0;
-            if (x + 1 < Lj.w) reinterpret_cast<uint32_t*>(orow)[x + 1] = o1;
+            if (x < G.w) reinterpret_cast<uint32_t*>(orow)[x] = o0;
+            if (x + 1 < G.w) reinterpret_cast<uint32_t*>(orow)[x + 1] = o1;
         }
     } else {
-        if (x < Lj.w) {
+        if (x < G.w) {
             orow[3 * x] = o0 & 0xFF;
             orow[3 * x + 1] = (o0 >> 8) & 0xFF;
             orow[3 * x + 2] = (o0 >> 16) & 0xFF;
         }
-        if (x + 1 < Lj.w) {
+        if (x + 1 < G.w) {
             orow[3 * x + 3] = o1 & 0xFF;
             orow[3 * x + 4] = (o1 >> 8) & 0xFF;
             orow[3 * x + 5] = (o1 >> 16) & 0xFF;
@@ -548,7 +663,7 @@ __device__ __forceinline__ void computeUnit(const BlendStage& S, const RigDev& R
     }
 }
 
-__global__ void __launch_bounds__(kBlendThreads, 3) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total)
+__global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total)
 {
     __shared__ BlendStage st[kBStages];
     __shared__ UnitInfo info[kBStages];
@@ -556,6 +671,7 @@ __global__ void __launch_bounds__(kBlendThreads, 3) k_blend(const Segment* __res
     __shared__ Segment s_segs[kMaxSmemSegs];
     __shared__ int s_timeout;
     __shared__ int fRow[kFH], fCol[kFW];
+    __shared__ int2 xch[2 * kConsumersYuv];
     const Segment* segs = gsegs;
     if (nsegs <= kMaxSmemSegs) {
         for (int k = threadIdx.x; k < nsegs; k += kBlendThreads) s_segs[k] = gsegs[k];
@@ -597,6 +713,7 @@ __global__ void __launch_bounds__(kBlendThreads, 3) k_blend(const Segment* __res
             if (valid) {
                 R = segs[seg].rig;
                 j = raw.x & 0xFF;
+                if (lane == 0) fillGeo(ui.geo, *R, *segs[seg].frame, j);
                 const int cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
                 uni = ((raw.x >> 24) & kTileUniform) != 0;
                 tx = raw.y & 0xFFFF;
@@ -685,17 +802,18 @@ __global__ void __launch_bounds__(kBlendThreads, 3) k_blend(const Segment* __res
     for (int u = 0;; u++) {
         const int stg = u % kBStages;
         if (!mbarWait(&full[stg], (u / kBStages) & 1)) s_timeout = 1;
-        const UnitInfo ui = info[stg];
+        const UnitInfo& ui = info[stg];  // rewritten only after this warp releases the stage
+        const uint4 raw = ui.raw;
         if (!ui.valid) break;
-        const Segment& sg = segs[ui.seg];
-        const RigDev& R = *sg.rig;
-        const bool active = !((ui.raw.x & 0xFF) == 0 && ((ui.raw.x >> 8) & 0xFF) == 0);
-        if (active && !ui.staged) {
-            stageUnitDirect(st[stg], R, ui.raw, ui.chunk, fRow, fCol, [] { namedBarrier(1, kConsumers); });
+        const int chunk = ui.chunk;
+        const bool staged = ui.staged != 0;
+        const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
+        if (active && !staged) {
+            stageUnitDirect(st[stg], *segs[ui.seg].rig, raw, chunk, fRow, fCol, [] { namedBarrier(1, kConsumers); });
             namedBarrier(1, kConsumers);
         }
-        computeUnit(st[stg], R, *sg.frame, ui.raw, ui.chunk, ui.staged != 0, acc);
-        if (active && !ui.staged) fenceProxyAsync();  // our stage writes precede later bulk copies into it
+        computeUnit(st[stg], ui.geo, raw, chunk, staged, acc, xch, [] { namedBarrier(2, kConsumers); });
+        if (active && !staged) fenceProxyAsync();  // our stage writes precede later bulk copies into it
         __syncwarp();
         if (lane == 0) mbarArrive(&empty[stg]);  // this warp is done with the stage
     }
@@ -725,6 +843,7 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
         BlendStage blend;
     } sm;
     __shared__ int fRow[kFH], fCol[kFW];
+    __shared__ int2 xch[2 * kConsumersYuv];
     const int rig = blockIdx.x / cluster, rank = blockIdx.x % cluster;
     initMagic(sm.down.magic);
     waitPrevGrid();
@@ -740,6 +859,8 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
     BlendAcc acc;
     for (int j = R.L; j >= R.tailBlend; j--) {
         const BlendItem* items = R.blendItems + R.blendOff[j];
+        UnitGeo geo;
+        fillGeo(geo, R, *sg.frame, j);
         for (int k = rank; k < R.blendCnt[j]; k += cluster) {
             const uint4 raw = *reinterpret_cast<const uint4*>(items + k);
             const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
@@ -747,10 +868,48 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
                 __syncthreads();  // readers of the previous unit are done
                 if (active) stageUnitDirect(sm.blend, R, raw, chunk, fRow, fCol, [] { __syncthreads(); });
                 __syncthreads();
-                computeUnit(sm.blend, R, *sg.frame, raw, chunk, false, acc);
+                computeUnit(sm.blend, geo, raw, chunk, false, acc, xch, [] { __syncthreads(); });
             }
         }
         clusterSync();
+    }
+}
+
+// ============================================================================
+// k_cvt_yuv: standalone BGR32 -> YUV420P / NV12 of a device image
+// (cvtBGR32ToYUV420P / cvtBGR32ToNV12, ImageProc.cu:97-160).  One thread per
+// 2x2 block, consecutive threads on consecutive blocks of a block row.
+// ============================================================================
+__global__ void __launch_bounds__(kThreads) k_cvt_yuv(const uint8_t* __restrict__ src, long long srcPitch, int w,
+                                                      int h, int fmt, uint8_t* __restrict__ py, long long yPitch,
+                                                      uint8_t* __restrict__ pu, long long uPitch,
+                                                      uint8_t* __restrict__ pv, long long vPitch)
+{
+    const int bw = w >> 1, bh = h >> 1;
+    const long long total = (long long)bw * bh;
+    for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < total;
+         b += (long long)gridDim.x * blockDim.x) {
+        const int by = (int)(b / bw), bx = (int)(b - (long long)by * bw);
+        const int x = bx * 2, y = by * 2;
+        const uint32_t* r0 = reinterpret_cast<const uint32_t*>(src + (size_t)y * srcPitch) + x;
+        const uint32_t* r1 = reinterpret_cast<const uint32_t*>(src + (size_t)(y + 1) * srcPitch) + x;
+        const uint32_t p00 = r0[0], p01 = r0[1], p10 = r1[0], p11 = r1[1];
+        uint8_t* y0 = py + (size_t)y * yPitch + x;
+        uint8_t* y1 = y0 + yPitch;
+        y0[0] = (uint8_t)yuvLuma(p00);
+        y0[1] = (uint8_t)yuvLuma(p01);
+        y1[0] = (uint8_t)yuvLuma(p10);
+        y1[1] = (uint8_t)yuvLuma(p11);
+        const int2 c0 = yuvChromaSums(p00), c1 = yuvChromaSums(p10);
+        const uint8_t u = (uint8_t)clamp255((c0.x + c1.x) >> (kYuvShift + 1));
+        const uint8_t v = (uint8_t)clamp255((c0.y + c1.y) >> (kYuvShift + 1));
+        if (fmt == PS_FMT_NV12) {
+            pu[(size_t)by * uPitch + x] = u;
+            pu[(size_t)by * uPitch + x + 1] = v;
+        } else {
+            pu[(size_t)by * uPitch + bx] = u;
+            pv[(size_t)by * vPitch + bx] = v;
+        }
     }
 }
 
@@ -806,7 +965,7 @@ cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_blend, gridFor(total, 3), kBlendThreads, st, segs, nsegs, total);
+    return launchPdl(k_blend, gridFor(total, 4), kBlendThreads, st, segs, nsegs, total);
 }
 
 static int tailClusterSize()
@@ -852,6 +1011,16 @@ cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st)
     cfg.attrs = attr;
     cfg.numAttrs = 2;
     return cudaLaunchKernelEx(&cfg, k_tail, segs, nsegs, cluster);
+}
+
+cudaError_t launchCvtYuv(const uint8_t* src, long long srcPitch, int w, int h, int fmt, uint8_t* y, long long yPitch,
+                         uint8_t* u, long long uPitch, uint8_t* v, long long vPitch, cudaStream_t st)
+{
+    const long long blocks = (long long)(w / 2) * (h / 2);
+    if (blocks <= 0) return cudaSuccess;
+    const int grid = (int)std::min<long long>((blocks + kThreads - 1) / kThreads, (long long)smCount() * 8);
+    k_cvt_yuv<<<grid, kThreads, 0, st>>>(src, srcPitch, w, h, fmt, y, yPitch, u, uPitch, v, vPitch);
+    return cudaGetLastError();
 }
 
 cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,

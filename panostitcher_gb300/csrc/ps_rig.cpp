@@ -856,15 +856,36 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
             for (int i = 0; i < n * 3; i++)
                 for (int v = 0; v < 256; v++) lut[i * 256 + v] = (uint8_t)v;
         fd.luts = dArgs + lutOff_[r];
-        const ps_image& d = *f.dst;
-        if (d.location == PS_MEM_HOST) {
-            fd.out = rig->outputBuffer();
-            fd.outPitch = (long long)d.width * bytesPerPixel(d.format);
+        if (f.ydst) {
+            const ps_planar_image& d = *f.ydst;
+            if (d.location == PS_MEM_HOST) {  // planes staged tightly in the output buffer, then downloaded
+                const size_t luma = (size_t)d.width * d.height;
+                fd.out = rig->outputBuffer();
+                fd.outPitch = d.width;
+                fd.outU = fd.out + luma;
+                fd.outCPitch = d.format == PS_FMT_NV12 ? d.width : d.width / 2;
+                fd.outV = fd.outU + luma / 4;
+                fd.outVPitch = d.width / 2;
+            } else {
+                fd.out = static_cast<uint8_t*>(d.planes[0]);
+                fd.outPitch = d.pitches[0];
+                fd.outU = static_cast<uint8_t*>(d.planes[1]);
+                fd.outCPitch = d.pitches[1];
+                fd.outV = static_cast<uint8_t*>(d.planes[2]);
+                fd.outVPitch = d.pitches[2];
+            }
+            fd.outFmt = d.format;
         } else {
-            fd.out = static_cast<uint8_t*>(d.data);
-            fd.outPitch = d.pitch;
+            const ps_image& d = *f.dst;
+            if (d.location == PS_MEM_HOST) {
+                fd.out = rig->outputBuffer();
+                fd.outPitch = (long long)d.width * bytesPerPixel(d.format);
+            } else {
+                fd.out = static_cast<uint8_t*>(d.data);
+                fd.outPitch = d.pitch;
+            }
+            fd.outFmt = d.format;
         }
-        fd.outFmt = d.format;
         fd.status = rig->statusWord();
         std::memcpy(stage + sizeof(FrameDev) * r, &fd, sizeof fd);
     }
@@ -894,6 +915,23 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         launchAll(st, prof);
     }
     for (size_t r = 0; r < rigs_.size(); r++) {
+        if (in[r].ydst) {
+            const ps_planar_image& d = *in[r].ydst;
+            if (d.location != PS_MEM_HOST) continue;
+            const uint8_t* out = rigs_[r]->outputBuffer();
+            const size_t w = d.width, h = d.height, luma = w * h;
+            PS_CUDA(cudaMemcpy2DAsync(d.planes[0], d.pitches[0], out, w, w, h, cudaMemcpyDeviceToHost, st));
+            if (d.format == PS_FMT_NV12) {
+                PS_CUDA(cudaMemcpy2DAsync(d.planes[1], d.pitches[1], out + luma, w, w, h / 2, cudaMemcpyDeviceToHost,
+                                          st));
+            } else {
+                PS_CUDA(cudaMemcpy2DAsync(d.planes[1], d.pitches[1], out + luma, w / 2, w / 2, h / 2,
+                                          cudaMemcpyDeviceToHost, st));
+                PS_CUDA(cudaMemcpy2DAsync(d.planes[2], d.pitches[2], out + luma + luma / 4, w / 2, w / 2, h / 2,
+                                          cudaMemcpyDeviceToHost, st));
+            }
+            continue;
+        }
         const ps_image& d = *in[r].dst;
         if (d.location == PS_MEM_HOST) {
             const size_t rowBytes = (size_t)d.width * bytesPerPixel(d.format);

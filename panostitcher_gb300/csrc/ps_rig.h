@@ -126,7 +126,8 @@ private:
 struct FrameInput {
     const ps_image* src;      // numImages images, or nullptr when level 0 is already written
     const uint8_t* luts;      // n*768 host bytes or nullptr (identity)
-    const ps_image* dst;
+    const ps_image* dst;      // BGR canvas, or nullptr when ydst is given
+    const ps_planar_image* ydst = nullptr;  // YUV420P / NV12 planes instead of dst
 };
 
 // The launch sequence for a set of rigs: one remap launch, one pyrDown

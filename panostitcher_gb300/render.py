@@ -18,7 +18,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib as L
-from ._lib import PhotoParam, Image, PsError, check, lib
+from ._lib import PhotoParam, Image, PlanarImage, PsError, check, lib
 
 
 def _is_device(a) -> bool:
@@ -35,6 +35,37 @@ def as_image(a) -> Image:
     assert a.strides[2] == 1 and a.strides[1] == a.shape[2]
     return Image(a.ctypes.data, a.strides[0], a.shape[1], a.shape[0],
                  L.PS_FMT_BGR32 if a.shape[2] == 4 else L.PS_FMT_BGR24, L.PS_MEM_HOST)
+
+
+def as_planar(planes: Sequence, fmt: int) -> PlanarImage:
+    """ps_planar_image view of (Y, U, V) or (Y, UV) 2-D uint8 planes, all numpy
+    (host) or all CUDA tensors (device); the luma plane sets the size."""
+    want = 2 if fmt == L.PS_FMT_NV12 else 3
+    if len(planes) != want:
+        raise ValueError(f"{want} planes expected for format {fmt}")
+    dev = _is_device(planes[0])
+    ptrs, pitches = [], []
+    for p in planes:
+        if _is_device(p) != dev:
+            raise ValueError("planes must all be host arrays or all CUDA tensors")
+        if dev:
+            assert p.dim() == 2 and p.stride(1) == 1 and p.element_size() == 1
+            ptrs.append(p.data_ptr())
+            pitches.append(p.stride(0))
+        else:
+            assert isinstance(p, np.ndarray) and p.dtype == np.uint8 and p.ndim == 2 and p.strides[1] == 1
+            ptrs.append(p.ctypes.data)
+            pitches.append(p.strides[0])
+    while len(ptrs) < 3:
+        ptrs.append(None)
+        pitches.append(0)
+    im = PlanarImage()
+    im.planes[:] = ptrs
+    im.pitches[:] = pitches
+    im.height, im.width = int(planes[0].shape[0]), int(planes[0].shape[1])
+    im.format = fmt
+    im.location = L.PS_MEM_DEVICE if dev else L.PS_MEM_HOST
+    return im
 
 
 def _stream_handle(stream):
@@ -106,6 +137,17 @@ class CudaPanoramaRender2:
         keep, nl, lp = _luts_arg(luts, len(src))
         d = as_image(dst)
         st = lib().ps_render_render(self._h, imgs, len(src), lp, nl, C.byref(d), _stream_handle(stream))
+        del keep
+        return self._status(st, check)
+
+    def render_yuv(self, src: Sequence, planes: Sequence, luts=None, fmt: int = L.PS_FMT_YUV420P, stream=None,
+                   check: bool = False) -> bool:
+        """render + cvtBGR32ToYUV420P / cvtBGR32ToNV12 + download in one call: planes
+        are (Y, U, V) or (Y, UV), host arrays or CUDA tensors."""
+        imgs = (Image * len(src))(*[as_image(s) for s in src])
+        keep, nl, lp = _luts_arg(luts, len(src))
+        d = as_planar(planes, fmt)
+        st = lib().ps_render_render_yuv(self._h, imgs, len(src), lp, nl, C.byref(d), _stream_handle(stream))
         del keep
         return self._status(st, check)
 
@@ -265,6 +307,14 @@ def reproject_to_16s(src, xmap, ymap, dst, lut=None, stream=None) -> None:
     check(lib().ps_reproject_to_16s(C.byref(s), xmap.data_ptr(), ymap.data_ptr(), xmap.stride(0) * 4, W, H,
                                     None if lut is None else lut.data_ptr(), dst.data_ptr(),
                                     dst.stride(0) * dst.element_size(), _stream_handle(stream)))
+
+
+def cvt_bgr32_to_yuv(src, planes: Sequence, fmt: int = L.PS_FMT_YUV420P, stream=None) -> None:
+    """cvtBGR32ToYUV420P / cvtBGR32ToNV12 (ImageProc.cu:120-160): a BGR32 CUDA tensor
+    to (Y, U, V) or (Y, UV) CUDA tensor planes."""
+    s = as_image(src)
+    d = as_planar(planes, fmt)
+    check(lib().ps_cvt_bgr32_to_yuv(C.byref(s), C.byref(d), _stream_handle(stream)))
 
 
 def get_lut(k: float) -> np.ndarray:

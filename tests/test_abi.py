@@ -96,3 +96,23 @@ def test_null_handles_are_rejected(built_lib):
     built_lib.ps_render_destroy(None)
     built_lib.ps_blender_destroy(None)
     assert built_lib.ps_render_batch(None, 0, None, None, None, None) == L.PS_EINVAL
+
+
+def test_yuv_entry_points_validate_before_the_gpu(built_lib):
+    r = P.CudaPanoramaRender2()
+    y = np.zeros((64, 128), np.uint8)
+    u = np.zeros((32, 64), np.uint8)
+    v = np.zeros((32, 64), np.uint8)
+    frames = [np.zeros((8, 8, 4), np.uint8)]
+    assert not r.render_yuv(frames, [y, u, v])
+    assert "prepare" in r.last_error
+    im = P.as_image(np.zeros((4, 6, 4), np.uint8))
+    pl = P.as_planar([np.zeros((4, 6), np.uint8), np.zeros((2, 6), np.uint8)], P.PS_FMT_NV12)
+    assert built_lib.ps_cvt_bgr32_to_yuv(C.byref(im), C.byref(pl), None) == L.PS_EINVAL  # host source
+    pl.format = 77
+    im.location = L.PS_MEM_DEVICE
+    assert built_lib.ps_cvt_bgr32_to_yuv(C.byref(im), C.byref(pl), None) == L.PS_EINVAL  # unknown format
+    assert "format" in built_lib.ps_last_error().decode()
+    pl.format = P.PS_FMT_NV12
+    pl.height = 5
+    assert built_lib.ps_cvt_bgr32_to_yuv(C.byref(im), C.byref(pl), None) == L.PS_EINVAL  # size mismatch

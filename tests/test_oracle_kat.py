@@ -174,3 +174,42 @@ def test_render_mt_equals_st(oracle_lib):
     a = b.render(fr, S.luts(cfg), [m[0] for m in maps], [m[1] for m in maps], 1)
     c = b.render(fr, S.luts(cfg), [m[0] for m in maps], [m[1] for m in maps], 3)
     assert np.array_equal(a, c)
+
+
+# ---- encoder handoff (cvtBGR32ToYUV420P / NV12, ImageProc.cu:44-160) -------
+@pytest.mark.parametrize("bgr,yuv", [
+    ((0, 0, 0), (16, 128, 128)),        # black: studio-range floor
+    ((255, 255, 255), (235, 128, 128)),  # white: studio-range ceiling
+    ((0, 0, 255), (82, 90, 240)),        # red
+    ((0, 255, 0), (145, 54, 34)),        # green
+    ((255, 0, 0), (41, 240, 110)),       # blue
+    ((128, 128, 128), (126, 128, 128)),
+])
+def test_yuv_known_answers(oracle_lib, bgr, yuv):
+    img = np.zeros((2, 2, 4), np.uint8)
+    img[..., :3] = bgr
+    y, u, v = O.bgr32_to_yuv(img)
+    assert (y == yuv[0]).all() and u[0, 0] == yuv[1] and v[0, 0] == yuv[2]
+    # within one step of the real-valued BT.601 definition
+    r, g, b = bgr[2], bgr[1], bgr[0]
+    ref = (16 + (65.481 * r + 128.553 * g + 24.966 * b) / 255, 128 + (-37.797 * r - 74.203 * g + 112 * b) / 255,
+           128 + (112 * r - 93.786 * g - 18.214 * b) / 255)
+    assert all(abs(a - e) <= 1 for a, e in zip(yuv, ref))
+
+
+def test_yuv_chroma_from_left_column_and_nv12_interleave(oracle_lib):
+    rng = np.random.default_rng(5)
+    img = rng.integers(0, 256, (6, 10, 4), dtype=np.uint8)
+    y, u, v = O.bgr32_to_yuv(img)
+    y2, uv = O.bgr32_to_yuv(img, O.FMT_NV12)
+    assert np.array_equal(y, y2)
+    assert np.array_equal(uv[:, 0::2], u) and np.array_equal(uv[:, 1::2], v)
+    # the right column of every 2x2 block does not affect chroma
+    img2 = img.copy()
+    img2[:, 1::2, :3] = rng.integers(0, 256, img2[:, 1::2, :3].shape, dtype=np.uint8)
+    _, u2, v2 = O.bgr32_to_yuv(img2)
+    assert np.array_equal(u, u2) and np.array_equal(v, v2)
+    # the 4th byte is ignored
+    img3 = img.copy()
+    img3[..., 3] = 255 - img3[..., 3]
+    assert all(np.array_equal(a, b) for a, b in zip(O.bgr32_to_yuv(img3), (y, u, v)))
