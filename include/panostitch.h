@@ -98,7 +98,8 @@ void ps_render_destroy(ps_render* r);
    as the reference: dst_w, dst_h even and dst_h * 2 == dst_w; blend_param
    (the maximum number of levels) > 0.  high_quality_blend must be 1 (the
    multiband path; the linear-blend mode is not built).  Seam masks follow
-   the nearest-optical-axis rule.  Synchronises the stream. */
+   the rule set by ps_render_set_seam_rule (by default the nearest optical
+   axis).  Synchronises the stream. */
 int ps_render_prepare(ps_render* r, const ps_photo_param* params, int num_params, int high_quality_blend,
                       int blend_param, int src_w, int src_h, int dst_w, int dst_h, void* stream);
 /* Same, with explicit seam (unique) masks: num_params host arrays of
@@ -130,6 +131,17 @@ int ps_render_render(ps_render* r, const ps_image* src, int num_src, const uint8
    not synchronise. */
 int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,
                          const ps_planar_image* dst, void* stream);
+
+/* Seam (unique mask) rule of the next prepare without explicit seams:
+   PS_SEAMS_NEAREST_AXIS (default) gives each covered pixel to the camera
+   whose optical axis is nearest; PS_SEAMS_DISTANCE is the reference's
+   getNonIntersectingMasks (source/Blend/Mask.cpp:376-398, called at
+   source/CudaAccel/CudaMultibandBlend.cpp:570-571), which splits overlaps
+   by the L1 distance to each coverage border.  Any other value is
+   PS_EINVAL. */
+#define PS_SEAMS_NEAREST_AXIS 0
+#define PS_SEAMS_DISTANCE 1
+int ps_render_set_seam_rule(ps_render* r, int rule);
 
 /* Launch the per-frame kernels as one captured CUDA graph (default 1) or as
    individual launches (0).  No reference counterpart. */
@@ -200,6 +212,18 @@ int ps_reproject_to_16s(const ps_image* src, const float* xmap, const float* yma
                         void* stream);
 /* getLUT (source/Blend/ExposureColorOptimize.cpp:1217-1223) on the host. */
 int ps_get_lut(double k, uint8_t* lut256);
+/* getNonIntersectingMasks (source/Blend/Mask.cpp:376-398): num device
+   coverage masks (width x height each, non-zero = covered, packed one after
+   another) -> num device 0/255 unique masks (same layout): a partition of
+   the union of the coverage in which camera i, in index order, takes the
+   pixels where its own L1 distance to an uncovered pixel exceeds that of
+   the union taken before it.  Allocates scratch; synchronises. */
+int ps_non_intersecting_masks(const uint8_t* masks, int num, int width, int height, uint8_t* out, void* stream);
+/* cv::distanceTransform(mask, dist, CV_DIST_L1, 3) on the device: the exact
+   L1 distance of every pixel to the nearest zero pixel of the mask, as
+   int32; a mask without zero pixels gives values >= 2^28.  Device
+   pointers, tightly packed. */
+int ps_distance_transform_l1(const uint8_t* mask, int width, int height, int32_t* dist, void* stream);
 /* cvtBGR32ToYUV420P / cvtBGR32ToNV12 (source/CudaAccel/ImageProc.cu:97-160):
    a device BGR32 image to device planes of the same (even) size.  Y per
    pixel; U and V per 2x2 block from its left column, as the reference
@@ -229,7 +253,9 @@ int ps_blender_create(ps_blender** out);
 void ps_blender_destroy(ps_blender* b);
 /* prepare(masks, maxLevels, minLength) (source/CudaAccel/CudaMultibandBlend.cpp:
    549-642): masks = num host uint8 coverage masks (width x height), seams =
-   num host uint8 unique masks (subsets of the masks).  Synchronises. */
+   num host uint8 unique masks (subsets of the masks), or NULL to derive them
+   from the masks with getNonIntersectingMasks as the reference does
+   (:570-571).  Synchronises. */
 int ps_blender_prepare(ps_blender* b, const uint8_t* const* masks, const uint8_t* const* seams, int num,
                        int width, int height, int max_levels, int min_length, void* stream);
 /* blend(images, blendImage) (:785-823): num device images of int16 x4

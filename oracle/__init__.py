@@ -94,6 +94,8 @@ def lib():
             L.orc_mb_blend.argtypes = [vp, vp, vp, vp, vp]
             L.orc_mb_blend_mt.argtypes = [vp, vp, vp, C.c_int]
             L.orc_render.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int]
+            L.orc_distance_transform_l1.argtypes = [vp, C.c_int, C.c_int, vp]
+            L.orc_non_intersecting_masks.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
             L.orc_bgr32_to_yuv.argtypes = [vp, C.c_longlong, C.c_int, C.c_int, C.c_int, vp, C.c_longlong, vp,
                                            C.c_longlong, vp, C.c_longlong]
             _lib = L
@@ -137,6 +139,28 @@ def nearest_axis_seams(params, cam_size, canvas_size, coverage: np.ndarray) -> n
 def get_lut(k: float) -> np.ndarray:
     out = np.empty(256, np.uint8)
     lib().orc_get_lut(float(k), _ptr(out))
+    return out
+
+
+# ------------------------------------------------------------------- reference seams
+DT_FAR = 1 << 28
+
+
+def distance_transform_l1(mask: np.ndarray) -> np.ndarray:
+    """L1 distance of every pixel to the nearest zero pixel (int32; DT_FAR + d without zeros)."""
+    m = np.ascontiguousarray(mask, np.uint8)
+    H, W = m.shape
+    out = np.empty((H, W), np.int32)
+    lib().orc_distance_transform_l1(_ptr(m), W, H, _ptr(out))
+    return out
+
+
+def non_intersecting_masks(masks: np.ndarray) -> np.ndarray:
+    """getNonIntersectingMasks: (n, H, W) coverage -> (n, H, W) 0/255 unique masks."""
+    m = np.ascontiguousarray(masks, np.uint8)
+    n, H, W = m.shape
+    out = np.empty_like(m)
+    lib().orc_non_intersecting_masks(_ptr(m), n, W, H, _ptr(out))
     return out
 
 

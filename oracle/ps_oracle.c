@@ -937,3 +937,67 @@ void orc_bgr32_to_yuv(const uint8_t* bgr, long long bgrStep, int w, int h, int f
         }
     }
 }
+
+/* ---- getNonIntersectingMasks (source/Blend/Mask.cpp:376-398) ---------------
+ * Distance transform: OpenCV 3.0's cv::distanceTransform with CV_DIST_L1 and
+ * a 3x3 mask is a two-pass chamfer (forward: up-left, up, up-right, left;
+ * backward: down-right, down, down-left, right) with step 1 for horizontal /
+ * vertical and 2 for diagonal neighbours, which yields the exact L1 distance
+ * to the nearest zero pixel.  Outside the image counts as far away.
+ */
+void orc_distance_transform_l1(const uint8_t* mask, int W, int H, int32_t* d)
+{
+    const int32_t far = ORC_DT_FAR;
+#define DT_AT(y, x) (((y) < 0 || (y) >= H || (x) < 0 || (x) >= W) ? far : d[(size_t)(y) * W + (x)])
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            size_t o = (size_t)y * W + x;
+            if (!mask[o]) {
+                d[o] = 0;
+                continue;
+            }
+            int32_t v = DT_AT(y - 1, x - 1) + 2, t;
+            if ((t = DT_AT(y - 1, x) + 1) < v) v = t;
+            if ((t = DT_AT(y - 1, x + 1) + 2) < v) v = t;
+            if ((t = DT_AT(y, x - 1) + 1) < v) v = t;
+            d[o] = v;
+        }
+    for (int y = H - 1; y >= 0; y--)
+        for (int x = W - 1; x >= 0; x--) {
+            size_t o = (size_t)y * W + x;
+            int32_t v = d[o], t;
+            if (v <= 1) continue;
+            if ((t = DT_AT(y + 1, x + 1) + 2) < v) v = t;
+            if ((t = DT_AT(y + 1, x) + 1) < v) v = t;
+            if ((t = DT_AT(y + 1, x - 1) + 2) < v) v = t;
+            if ((t = DT_AT(y, x + 1) + 1) < v) v = t;
+            d[o] = v;
+        }
+#undef DT_AT
+}
+
+void orc_non_intersecting_masks(const uint8_t* masks, int n, int W, int H, uint8_t* out)
+{
+    const size_t npx = (size_t)W * H;
+    uint8_t* uni = (uint8_t*)malloc(npx);
+    int32_t* dist = (int32_t*)malloc(npx * sizeof(int32_t));
+    int32_t* cur = (int32_t*)malloc(npx * sizeof(int32_t));
+    for (int i = 0; i < n; i++)
+        for (size_t p = 0; p < npx; p++) out[i * npx + p] = masks[i * npx + p] ? 255 : 0;
+    memcpy(uni, out, npx);
+    for (int i = 1; i < n; i++) {
+        orc_distance_transform_l1(uni, W, H, dist);
+        orc_distance_transform_l1(out + i * npx, W, H, cur);
+        for (size_t p = 0; p < npx; p++) {
+            const uint8_t take = cur[p] > dist[p] ? 255 : 0;
+            out[i * npx + p] = take;
+            if (take) {
+                for (int j = 0; j < i; j++) out[j * npx + p] = 0;
+                uni[p] = 255;
+            }
+        }
+    }
+    free(uni);
+    free(dist);
+    free(cur);
+}

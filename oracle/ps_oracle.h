@@ -98,6 +98,17 @@ void orc_render(orc_blender* b, const uint8_t* const* srcs, int srcW, int srcH, 
                 const uint8_t* luts, const float* const* xmaps, const float* const* ymaps,
                 uint8_t* dst, int nthreads);
 
+/* ---- reference seams: getNonIntersectingMasks (source/Blend/Mask.cpp:376-398) */
+/* L1 distance of every pixel of an 8-bit mask to its nearest zero pixel, by
+   the two-pass 3x3 chamfer with unit horizontal / vertical and diagonal 2
+   steps (cv::distanceTransform(src, dst, CV_DIST_L1, 3)); pixels outside
+   the image are not zeros.  A mask without any zero pixel gets ORC_DT_FAR
+   plus the chamfer distance to the image border everywhere. */
+#define ORC_DT_FAR (1 << 28)
+void orc_distance_transform_l1(const uint8_t* mask, int W, int H, int32_t* dist);
+/* masks: n W*H 0/non-zero coverage masks; out: n W*H 0/255 unique masks. */
+void orc_non_intersecting_masks(const uint8_t* masks, int n, int W, int H, uint8_t* out);
+
 /* ---- encoder handoff --------------------------------------------------- */
 /* cvtBGR32ToYUV420P / cvtBGR32ToNV12 (source/CudaAccel/ImageProc.cu:44-160):
    BT.601 studio range in 20-bit fixed point.  fmt 420: planes y, u, v;

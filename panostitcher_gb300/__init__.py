@@ -5,12 +5,14 @@ equirectangular canvas; then the integer multiband blend of all cameras down
 to 8-bit BGR.  The kernels live in libpanostitch.so (built in-tree by
 ``panostitcher_gb300.build``); this package only binds and drives them.
 """
-from ._lib import PsError, PhotoParam, Image, PlanarImage, lib, PS_FMT_YUV420P, PS_FMT_NV12  # noqa: F401
+from ._lib import (PsError, PhotoParam, Image, PlanarImage, lib, PS_FMT_YUV420P, PS_FMT_NV12,  # noqa: F401
+                   PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE)
 from .render import (CudaPanoramaRender2, CudaTilingMultibandBlendFast, render_batch,  # noqa: F401
                      generate_reproject_map_and_mask, reproject_to_16s, get_lut, as_image, as_planar,
-                     cvt_bgr32_to_yuv)
+                     cvt_bgr32_to_yuv, non_intersecting_masks, distance_transform_l1)
 
 __all__ = ["CudaPanoramaRender2", "CudaTilingMultibandBlendFast", "render_batch",
            "generate_reproject_map_and_mask", "reproject_to_16s", "get_lut", "as_image", "as_planar",
-           "cvt_bgr32_to_yuv", "PsError", "PhotoParam", "Image", "PlanarImage", "lib", "PS_FMT_YUV420P",
-           "PS_FMT_NV12"]
+           "cvt_bgr32_to_yuv", "non_intersecting_masks", "distance_transform_l1", "PsError", "PhotoParam",
+           "Image", "PlanarImage", "lib", "PS_FMT_YUV420P", "PS_FMT_NV12", "PS_SEAMS_NEAREST_AXIS",
+           "PS_SEAMS_DISTANCE"]

@@ -17,6 +17,7 @@ PS_OK, PS_EINVAL, PS_ENOMEM, PS_ECUDA, PS_ETIMEOUT, PS_ESTATE = 0, 1, 2, 3, 4, 5
 PS_MAX_LEVELS, PS_MAX_CAMS = 16, 64
 PS_FMT_BGR24, PS_FMT_BGR32 = 24, 32
 PS_FMT_YUV420P, PS_FMT_NV12 = 420, 12
+PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE = 0, 1
 PS_MEM_HOST, PS_MEM_DEVICE = 0, 1
 EXPORT_XMAP, EXPORT_YMAP, EXPORT_COVERAGE, EXPORT_SEAM, EXPORT_WEIGHT, EXPORT_ALPHA = range(6)
 
@@ -78,6 +79,7 @@ _SIGS = [
                                    C.POINTER(Image), C.c_void_p]),
     ("ps_render_render_yuv", C.c_int, [C.c_void_p, C.POINTER(Image), C.c_int, C.c_void_p, C.c_int,
                                        C.POINTER(PlanarImage), C.c_void_p]),
+    ("ps_render_set_seam_rule", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_set_graph", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_clear", None, [C.c_void_p]),
     ("ps_render_get_num_images", C.c_int, [C.c_void_p]),
@@ -100,6 +102,8 @@ _SIGS = [
     ("ps_reproject_to_16s", C.c_int, [C.POINTER(Image), C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_int,
                                       C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]),
     ("ps_get_lut", C.c_int, [C.c_double, C.c_void_p]),
+    ("ps_non_intersecting_masks", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    ("ps_distance_transform_l1", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     ("ps_cvt_bgr32_to_yuv", C.c_int, [C.POINTER(Image), C.POINTER(PlanarImage), C.c_void_p]),
     ("ps_nearest_axis_seams_no_alloc", C.c_int, [C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,
                                                  C.c_int, C.c_void_p, C.c_void_p]),

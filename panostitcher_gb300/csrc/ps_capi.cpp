@@ -16,6 +16,7 @@ struct ps_render {
     std::unique_ptr<ps::Plan> plan;
     ps::Profiler prof;
     bool useGraph = true;
+    int seamRule = PS_SEAMS_NEAREST_AXIS;
 };
 
 struct ps_blender {
@@ -152,7 +153,8 @@ static int prepareRender(ps_render* r, const ps_photo_param* params, int num, in
         r->plan.reset();
         r->rig.clear();
         if (hq != 1) fail(PS_EINVAL, "high_quality_blend = %d: only the multiband path (1) is built", hq);
-        r->rig.prepareFromParams(params, num, blendParam, srcW, srcH, dstW, dstH, seams, toStream(stream));
+        r->rig.prepareFromParams(params, num, blendParam, srcW, srcH, dstW, dstH, seams, toStream(stream),
+                                 r->seamRule);
         r->plan.reset(new ps::Plan({&r->rig}));
     });
 }
@@ -227,6 +229,15 @@ int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const u
         checkFrame(r->rig, src, num_src, luts, num_luts, &probe);
         if (!r->plan || !r->plan->matches({&r->rig})) r->plan.reset(new ps::Plan({&r->rig}));
         r->plan->run({ps::FrameInput{src, luts, nullptr, dst}}, toStream(stream), r->useGraph, &r->prof);
+    });
+}
+
+int ps_render_set_seam_rule(ps_render* r, int rule)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (rule != PS_SEAMS_NEAREST_AXIS && rule != PS_SEAMS_DISTANCE) fail(PS_EINVAL, "unknown seam rule %d", rule);
+        r->seamRule = rule;
     });
 }
 
@@ -334,6 +345,29 @@ int ps_reproject_to_16s(const ps_image* src, const float* xmap, const float* yma
         PS_CUDA(ps::launchReprojectTo16S(static_cast<const uint8_t*>(src->data), src->pitch, src->width, src->height,
                                          src->format, xmap, ymap, map_pitch, dst_w, dst_h, lut, dst, dst_pitch,
                                          toStream(stream)));
+    });
+}
+
+int ps_non_intersecting_masks(const uint8_t* masks, int num, int width, int height, uint8_t* out, void* stream)
+{
+    return guarded([&] {
+        if (!masks || !out) fail(PS_EINVAL, "NULL argument");
+        if (num <= 0 || num > PS_MAX_CAMS) fail(PS_EINVAL, "%d masks, 1..%d supported", num, PS_MAX_CAMS);
+        if (width <= 0 || height <= 0) fail(PS_EINVAL, "mask size (%d, %d) must be positive", width, height);
+        const size_t npx = (size_t)width * height;
+        ps::DevBuf uni(npx), dUni(npx * 4), dCam(npx * 4);
+        PS_CUDA(ps::launchNonIntersectingMasks(masks, num, width, height, out, uni.as<uint8_t>(), dUni.as<int32_t>(),
+                                               dCam.as<int32_t>(), toStream(stream)));
+        PS_CUDA(cudaStreamSynchronize(toStream(stream)));
+    });
+}
+
+int ps_distance_transform_l1(const uint8_t* mask, int width, int height, int32_t* dist, void* stream)
+{
+    return guarded([&] {
+        if (!mask || !dist) fail(PS_EINVAL, "NULL argument");
+        if (width <= 0 || height <= 0) fail(PS_EINVAL, "mask size (%d, %d) must be positive", width, height);
+        PS_CUDA(ps::launchDistanceTransformL1(mask, width, height, dist, toStream(stream)));
     });
 }
 

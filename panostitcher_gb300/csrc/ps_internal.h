@@ -94,6 +94,12 @@ cudaError_t launchGenMap(const RemapDev* dParam, int W, int H, float* xmap, floa
                          cudaStream_t st);
 cudaError_t launchNearestAxisSeams(const RemapDev* dParams, int n, int W, int H, const uint8_t* cov,
                                    uint8_t* seams, cudaStream_t st);
+// getNonIntersectingMasks: n W*H coverage masks -> n 0/255 unique masks.
+// Scratch: uni W*H bytes, dUni and dCam W*H int32 each.
+cudaError_t launchNonIntersectingMasks(const uint8_t* cov, int n, int W, int H, uint8_t* out, uint8_t* uni,
+                                       int32_t* dUni, int32_t* dCam, cudaStream_t st);
+// exact L1 distance of every pixel to the nearest zero pixel (>= 2^28 when there is none)
+cudaError_t launchDistanceTransformL1(const uint8_t* mask, int W, int H, int32_t* dist, cudaStream_t st);
 
 // ---- prepare-time pyramids --------------------------------------------------------
 // level 0: Wt = seam ? 256 : 0, A (0/256 scratch) = cov ? 256 : 0

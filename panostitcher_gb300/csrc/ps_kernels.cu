@@ -57,35 +57,45 @@ __device__ __noinline__ int bilinearExact(double x, double y, int x0, int y0, in
     return min(max(v, 0), 255);
 }
 
-// Returns B | G << 8 | R << 16 (0 where the map is invalid).
+// Exact float of a byte without a conversion instruction: 2^23 + b has b in
+// its low mantissa bits.
+__device__ __forceinline__ float byteToFloat(uint32_t b) { return __int_as_float(0x4B000000u | b) - 8388608.f; }
+
+// Returns B | G << 8 | R << 16 (0 where the map is invalid).  Integer parts
+// and roundings use float additions at 2^23 scale (round toward zero for
+// the floor of a non-negative coordinate, round to nearest even for the
+// result), which keeps the conversion unit out of the inner loop.
 __device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, long long pitch, int fmt, int sw,
                                                int sh, const uint8_t* lut)
 {
     if (!(m.x >= 0.f && m.y >= 0.f && m.x < (float)sw && m.y < (float)sh)) return 0;
-    const int x0 = (int)m.x, y0 = (int)m.y;
+    const float tx = __fadd_rz(m.x, 8388608.f), ty = __fadd_rz(m.y, 8388608.f);  // 2^23 + floor
+    const int x0 = __float_as_int(tx) - 0x4B000000, y0 = __float_as_int(ty) - 0x4B000000;
     const int x1 = min(x0 + 1, sw - 1), y1 = min(y0 + 1, sh - 1);
     const uint8_t* r0 = base + (size_t)y0 * pitch;
     const uint8_t* r1 = base + (size_t)y1 * pitch;
     const uint32_t t00 = loadTexel(r0, x0, fmt), t01 = loadTexel(r0, x1, fmt);
     const uint32_t t10 = loadTexel(r1, x0, fmt), t11 = loadTexel(r1, x1, fmt);
-    const float fx = m.x - (float)x0, fy = m.y - (float)y0;
+    const float fx = m.x - (tx - 8388608.f), fy = m.y - (ty - 8388608.f);  // exact
     const float gx = 1.f - fx, gy = 1.f - fy;
     const float w00 = gx * gy, w01 = fx * gy, w10 = gx * fy, w11 = fx * fy;
     uint32_t out = 0;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        const int s = 8 * c;
-        const int p00 = lut[c * 256 + ((t00 >> s) & 0xFF)];
-        const int p01 = lut[c * 256 + ((t01 >> s) & 0xFF)];
-        const int p10 = lut[c * 256 + ((t10 >> s) & 0xFF)];
-        const int p11 = lut[c * 256 + ((t11 >> s) & 0xFF)];
-        const float r = fmaf((float)p11, w11, fmaf((float)p10, w10, fmaf((float)p01, w01, (float)p00 * w00)));
-        int v;
-        if (fabsf(r - floorf(r) - 0.5f) < 2e-4f)
+        const uint32_t sel = 0x4440u | (uint32_t)c;  // byte c, zero-extended
+        const int p00 = lut[c * 256 + __byte_perm(t00, 0, sel)];
+        const int p01 = lut[c * 256 + __byte_perm(t01, 0, sel)];
+        const int p10 = lut[c * 256 + __byte_perm(t10, 0, sel)];
+        const int p11 = lut[c * 256 + __byte_perm(t11, 0, sel)];
+        const float r = fmaf(byteToFloat(p11), w11,
+                             fmaf(byteToFloat(p10), w10, fmaf(byteToFloat(p01), w01, byteToFloat(p00) * w00)));
+        // r lies in [-1e-4, 255 + 1e-4]; 1.5 * 2^23 + r rounds r to the
+        // nearest integer, ties to even, in the low mantissa bits
+        const float t = r + 12582912.f;
+        int v = __float_as_int(t) - 0x4B400000;
+        if (fabsf(r - (t - 12582912.f)) > 0.4998f)  // within 2e-4 of a tie: exact recompute
             v = bilinearExact((double)m.x, (double)m.y, x0, y0, p00, p01, p10, p11);
-        else
-            v = min(max(__float2int_rn(r), 0), 255);
-        out |= (uint32_t)v << s;
+        out |= (uint32_t)v << (8 * c);
     }
     return out;
 }
@@ -179,7 +189,18 @@ __device__ __forceinline__ void initMagic(uint32_t* magic)
     for (int m = threadIdx.x; m < 257; m += blockDim.x) magic[m] = m ? (uint32_t)((16777216u + m - 1) / m) : 0u;
 }
 
+// Loads of pyramid levels.  A level written earlier in the same launch (the
+// tail kernel's levels) is read through L2 (ld.global.cg); one written by an
+// earlier launch may use the read-only path.
+template <bool kFresh, class T>
+__device__ __forceinline__ T ldLevel(const T* p)
+{
+    if constexpr (kFresh) return __ldcg(p);
+    else return __ldg(p);
+}
+
 // One 32x16 output tile of one camera (all kThreads threads of the CTA).
+template <bool kFresh>
 __device__ __forceinline__ void pyrDownTile(const RigDev& R, const DownItem item, DownSmem& sm)
 {
     const int ox = threadIdx.x & 31, oy = threadIdx.x >> 5;
@@ -210,7 +231,7 @@ __device__ __forceinline__ void pyrDownTile(const RigDev& R, const DownItem item
             const int r = k / kDInW, c = k - r * kDInW;
             const int gy = interior ? iy0 + r : sm.rowIdx[r];
             const int gx = interior ? ix0 + c : sm.colIdx[c];
-            v[q] = __ldg(G + (size_t)gy * Ls.pitch + gx);
+            v[q] = ldLevel<kFresh>(G + (size_t)gy * Ls.pitch + gx);
         }
     }
     __syncthreads();  // the previous tile's readers are done with shared memory
@@ -266,7 +287,7 @@ __global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict_
     for (int it = begin; it < end; it++) {
         s = findSegment(segs, nsegs, it, s);
         const Segment sg = segs[s];
-        pyrDownTile(*sg.rig, static_cast<const DownItem*>(sg.items)[it - sg.prefix], sm);
+        pyrDownTile<false>(*sg.rig, static_cast<const DownItem*>(sg.items)[it - sg.prefix], sm);
     }
 }
 
@@ -447,7 +468,7 @@ struct BlendAcc {
 // tail kernel).  Threads 0..kConsumers-1; the caller synchronises.
 // fRow / fCol: footprint index tables (kFH / kFW ints) filled here; sync is
 // the barrier over the calling threads.
-template <class Sync>
+template <bool kFresh, class Sync>
 __device__ __forceinline__ void stageUnitDirect(BlendStage& S, const RigDev& R, const uint4& raw, int chunk, int* fRow,
                                                 int* fCol, Sync sync)
 {
@@ -468,7 +489,7 @@ __device__ __forceinline__ void stageUnitDirect(BlendStage& S, const RigDev& R, 
         uint32_t w = 0;
         if (y < Lj.h) {
             const size_t o = (size_t)cam * Lj.camStride + (size_t)y * Lj.pitch + x;
-            g = __ldg(reinterpret_cast<const uint2*>(Lj.G + o));
+            g = ldLevel<kFresh>(reinterpret_cast<const uint2*>(Lj.G + o));
             w = __ldg(reinterpret_cast<const uint32_t*>(Lj.Wt + o));
         }
         *reinterpret_cast<uint2*>(&S.gj[q][ly][lx]) = g;
@@ -482,12 +503,12 @@ __device__ __forceinline__ void stageUnitDirect(BlendStage& S, const RigDev& R, 
             const int q = k / kFElems, e = k - q * kFElems;
             const int r = e / kFW, c = e - r * kFW;
             const int cam = tileCam(raw, R.camLists, c0 + q);
-            S.fp[q][r][c + 3] = __ldg(reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
+            S.fp[q][r][c + 3] = ldLevel<kFresh>(reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
                                       (size_t)fRow[r] * Lu.pitch + fCol[c]);
         }
         if (last && threadIdx.x < kFElems) {
             const int r = threadIdx.x / kFW, c = threadIdx.x - r * kFW;
-            S.cf[r][c + 1] = *reinterpret_cast<const uint2*>(Lu.C + (size_t)fRow[r] * Lu.pitch + fCol[c]);
+            S.cf[r][c + 1] = ldLevel<kFresh>(reinterpret_cast<const uint2*>(Lu.C + (size_t)fRow[r] * Lu.pitch + fCol[c]));
         }
     }
 }
@@ -809,7 +830,8 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
         const bool staged = ui.staged != 0;
         const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
         if (active && !staged) {
-            stageUnitDirect(st[stg], *segs[ui.seg].rig, raw, chunk, fRow, fCol, [] { namedBarrier(1, kConsumers); });
+            stageUnitDirect<false>(st[stg], *segs[ui.seg].rig, raw, chunk, fRow, fCol,
+                                   [] { namedBarrier(1, kConsumers); });
             namedBarrier(1, kConsumers);
         }
         computeUnit(st[stg], ui.geo, raw, chunk, staged, acc, xch, [] { namedBarrier(2, kConsumers); });
@@ -853,7 +875,7 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
     const RigDev& R = *sg.rig;
     for (int J = R.tailDown; J <= R.L; J++) {
         const DownItem* items = R.downItems + R.downOff[J];
-        for (int k = rank; k < R.downCnt[J]; k += cluster) pyrDownTile(R, items[k], sm.down);
+        for (int k = rank; k < R.downCnt[J]; k += cluster) pyrDownTile<true>(R, items[k], sm.down);
         clusterSync();
     }
     BlendAcc acc;
@@ -866,7 +888,7 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
             const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
             for (int chunk = 0; chunk < unitChunks(raw); chunk++) {
                 __syncthreads();  // readers of the previous unit are done
-                if (active) stageUnitDirect(sm.blend, R, raw, chunk, fRow, fCol, [] { __syncthreads(); });
+                if (active) stageUnitDirect<true>(sm.blend, R, raw, chunk, fRow, fCol, [] { __syncthreads(); });
                 __syncthreads();
                 computeUnit(sm.blend, geo, raw, chunk, false, acc, xch, [] { __syncthreads(); });
             }

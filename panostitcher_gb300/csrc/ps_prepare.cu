@@ -1,6 +1,8 @@
 // ps_prepare.cu -- prepare-time kernels: geometry, seams, weight / alpha
 // pyramids, tile activity.  Built with --fmad=false so the double-precision
 // geometry keeps the reference's separate multiply / add roundings.
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <mutex>
 
@@ -267,6 +269,134 @@ cudaError_t launchNearestAxisSeams(const RemapDev* dParams, int n, int W, int H,
     dim3 grid((W + 127) / 128, H);
     k_seams<<<grid, 128, 0, st>>>(dParams, n, W, H, cov, seams);
     return cudaGetLastError();
+}
+
+// ============================================================================
+// Reference seams: getNonIntersectingMasks (source/Blend/Mask.cpp:376-398).
+// Camera 0 starts with its whole coverage; camera i (i = 1..n-1) takes the
+// pixels where the L1 distance to the nearest zero of its own coverage
+// exceeds that of the union taken so far, and earlier cameras lose them.
+// The L1 distance transform (cv::distanceTransform, CV_DIST_L1, 3x3 mask) is
+// computed exactly and separably: the distance along the row to the nearest
+// zero (block-wide scans of the last / first zero), then
+// d(x, y) = min_y' |y - y'| + r(x, y') by a downward and an upward sweep of
+// every column.  Pixels outside the image are not zeros; an image without
+// any zero pixel gets kDtFar or more everywhere, above every finite
+// distance, which is all the comparisons need.
+// ============================================================================
+constexpr int kDtFar = 1 << 28;
+constexpr int kDtThreads = 256;
+
+__global__ void __launch_bounds__(kDtThreads) k_dt_rows(const uint8_t* __restrict__ mask, int W, int32_t* __restrict__ dist)
+{
+    __shared__ int sLast[kDtThreads], sFirst[kDtThreads];
+    const int t = threadIdx.x;
+    const uint8_t* m = mask + (size_t)blockIdx.x * W;
+    int32_t* d = dist + (size_t)blockIdx.x * W;
+    const int per = (W + kDtThreads - 1) / kDtThreads;
+    const int x0 = min(W, t * per), x1 = min(W, x0 + per);
+    int last = -1, first = INT_MAX;
+    for (int x = x0; x < x1; x++)
+        if (!m[x]) {
+            if (first == INT_MAX) first = x;
+            last = x;
+        }
+    sLast[t] = last;
+    sFirst[t] = first;
+    __syncthreads();
+    // inclusive prefix max of the last zeros, suffix min of the first zeros
+    for (int off = 1; off < kDtThreads; off <<= 1) {
+        const int a = t >= off ? sLast[t - off] : -1;
+        const int b = t + off < kDtThreads ? sFirst[t + off] : INT_MAX;
+        __syncthreads();
+        sLast[t] = max(sLast[t], a);
+        sFirst[t] = min(sFirst[t], b);
+        __syncthreads();
+    }
+    int L = t > 0 ? sLast[t - 1] : -1;
+    for (int x = x0; x < x1; x++) {
+        if (!m[x]) L = x;
+        d[x] = L < 0 ? kDtFar : x - L;
+    }
+    int R = t + 1 < kDtThreads ? sFirst[t + 1] : INT_MAX;
+    for (int x = x1 - 1; x >= x0; x--) {
+        if (!m[x]) R = x;
+        if (R != INT_MAX) d[x] = min(d[x], R - x);
+    }
+}
+
+__global__ void k_dt_cols(int32_t* __restrict__ dist, int W, int H)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    int32_t* c = dist + x;
+    int prev = kDtFar;
+    for (int y = 0; y < H; y++) {
+        const int v = min(c[(size_t)y * W], prev + 1);
+        c[(size_t)y * W] = v;
+        prev = v;
+    }
+    prev = kDtFar;
+    for (int y = H - 1; y >= 0; y--) {
+        const int v = min(c[(size_t)y * W], prev + 1);
+        c[(size_t)y * W] = v;
+        prev = v;
+    }
+}
+
+static cudaError_t distanceTransformL1(const uint8_t* mask, int W, int H, int32_t* dist, cudaStream_t st)
+{
+    k_dt_rows<<<H, kDtThreads, 0, st>>>(mask, W, dist);
+    k_dt_cols<<<(W + 127) / 128, 128, 0, st>>>(dist, W, H);
+    return cudaGetLastError();
+}
+
+__global__ void k_seam_init(const uint8_t* __restrict__ cov, long long total, long long npx, uint8_t* out,
+                            uint8_t* uni)
+{
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total; p += (long long)gridDim.x * blockDim.x) {
+        const uint8_t v = cov[p] ? 255 : 0;
+        out[p] = v;
+        if (p < npx) uni[p] = v;
+    }
+}
+
+__global__ void k_seam_take(const int32_t* __restrict__ dCam, const int32_t* __restrict__ dUni, long long npx, int i,
+                            uint8_t* out, uint8_t* uni)
+{
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+        const bool take = dCam[p] > dUni[p];
+        out[(size_t)i * npx + p] = take ? 255 : 0;
+        if (take) {
+            for (int j = 0; j < i; j++) out[(size_t)j * npx + p] = 0;
+            uni[p] = 255;
+        }
+    }
+}
+
+cudaError_t launchNonIntersectingMasks(const uint8_t* cov, int n, int W, int H, uint8_t* out, uint8_t* uni,
+                                       int32_t* dUni, int32_t* dCam, cudaStream_t st)
+{
+    const long long npx = (long long)W * H;
+    const int grid = (int)std::min<long long>((npx * n + 255) / 256, 4096);
+    k_seam_init<<<grid, 256, 0, st>>>(cov, npx * n, npx, out, uni);
+    cudaError_t e = cudaGetLastError();
+    for (int i = 1; i < n && e == cudaSuccess; i++) {
+        e = distanceTransformL1(uni, W, H, dUni, st);
+        if (e == cudaSuccess) e = distanceTransformL1(out + (size_t)i * npx, W, H, dCam, st);
+        if (e == cudaSuccess) {
+            k_seam_take<<<(int)std::min<long long>((npx + 255) / 256, 4096), 256, 0, st>>>(dCam, dUni, npx, i, out,
+                                                                                          uni);
+            e = cudaGetLastError();
+        }
+    }
+    return e;
+}
+
+// Standalone distance transform (tests and callers of the primitive).
+cudaError_t launchDistanceTransformL1(const uint8_t* mask, int W, int H, int32_t* dist, cudaStream_t st)
+{
+    return distanceTransformL1(mask, W, H, dist, st);
 }
 
 // ============================================================================

@@ -157,8 +157,18 @@ long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam
     return b;
 }
 
+// getNonIntersectingMasks of n device coverage masks into seam (device).
+static void distanceSeams(const uint8_t* cov, int n, int W, int H, uint8_t* seam, cudaStream_t st)
+{
+    const size_t npx = (size_t)W * H;
+    DevBuf uni(npx), dUni(npx * 4), dCam(npx * 4);
+    PS_CUDA(launchNonIntersectingMasks(cov, n, W, H, seam, uni.as<uint8_t>(), dUni.as<int32_t>(), dCam.as<int32_t>(),
+                                       st));
+    PS_CUDA(cudaStreamSynchronize(st));  // before the scratch is freed
+}
+
 void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
-                            int dstH, const uint8_t* const* seams, cudaStream_t st)
+                            int dstH, const uint8_t* const* seams, cudaStream_t st, int seamRule)
 {
     clear();
     validateParams(params, n, srcW, srcH, dstW, dstH);
@@ -182,6 +192,8 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
                 if (!seams[i]) fail(PS_EINVAL, "seam mask %d is NULL", i);
                 PS_CUDA(cudaMemcpyAsync(seam.as<uint8_t>() + i * npx, seams[i], npx, cudaMemcpyHostToDevice, st));
             }
+        } else if (seamRule == PS_SEAMS_DISTANCE) {
+            distanceSeams(cov.as<uint8_t>(), n, dstW, dstH, seam.as<uint8_t>(), st);
         } else {
             PS_CUDA(launchNearestAxisSeams(dParams.as<RemapDev>(), n, dstW, dstH, cov.as<uint8_t>(),
                                            seam.as<uint8_t>(), st));
@@ -204,11 +216,11 @@ void Rig::prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* se
 {
     clear();
     // CudaTilingMultibandBlendFast::prepare, source/CudaAccel/CudaMultibandBlend.cpp:549-568
-    if (!masks || !seams || n <= 0) fail(PS_EINVAL, "no masks");
+    if (!masks || n <= 0) fail(PS_EINVAL, "no masks");
     if (n > PS_MAX_CAMS) fail(PS_EINVAL, "%d masks, at most %d supported", n, PS_MAX_CAMS);
     if (W <= 0 || H <= 0) fail(PS_EINVAL, "mask size (%d, %d) must be positive", W, H);
     for (int i = 0; i < n; i++)
-        if (!masks[i] || !seams[i]) fail(PS_EINVAL, "mask %d is NULL", i);
+        if (!masks[i] || (seams && !seams[i])) fail(PS_EINVAL, "mask %d is NULL", i);
     try {
         setGeometry(n, W, H, std::max(0, trueNumLevels(W, H, maxLevels, minLength)));
         const size_t npx = (size_t)W * H;
@@ -216,8 +228,11 @@ void Rig::prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* se
         DevBuf seam(n * npx);
         for (int i = 0; i < n; i++) {
             PS_CUDA(cudaMemcpyAsync(covDev_.as<uint8_t>() + i * npx, masks[i], npx, cudaMemcpyHostToDevice, st));
-            PS_CUDA(cudaMemcpyAsync(seam.as<uint8_t>() + i * npx, seams[i], npx, cudaMemcpyHostToDevice, st));
+            if (seams)
+                PS_CUDA(cudaMemcpyAsync(seam.as<uint8_t>() + i * npx, seams[i], npx, cudaMemcpyHostToDevice, st));
         }
+        // CudaMultibandBlend.cpp:570-571
+        if (!seams) distanceSeams(covDev_.as<uint8_t>(), n, W, H, seam.as<uint8_t>(), st);
         output_.alloc(npx * 4);
         imgArgs_.alloc((sizeof(void*) + sizeof(long long)) * n);
         preparePyramids(covDev_.as<uint8_t>(), seam.as<uint8_t>(), nullptr, nullptr, st);

@@ -19,10 +19,11 @@ public:
     ~Rig() = default;
 
     // CudaPanoramaRender2::prepare: maps + coverage from the camera
-    // parameters, seams by the nearest-axis rule unless given.
+    // parameters; seams given, or derived by seamRule (PS_SEAMS_*).
     void prepareFromParams(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
-                           int dstH, const uint8_t* const* seams, cudaStream_t st);
-    // CudaTilingMultibandBlendFast::prepare: coverage + seam masks given.
+                           int dstH, const uint8_t* const* seams, cudaStream_t st, int seamRule = PS_SEAMS_NEAREST_AXIS);
+    // CudaTilingMultibandBlendFast::prepare: coverage masks given; seams
+    // given, or getNonIntersectingMasks of the coverage when seams is NULL.
     void prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* seams, int n, int W, int H,
                           int maxLevels, int minLength, cudaStream_t st);
     void clear();

@@ -131,6 +131,10 @@ class CudaPanoramaRender2:
                                                     _stream_handle(stream))
         return self._status(st, check)
 
+    def set_seam_rule(self, rule: int) -> None:
+        """PS_SEAMS_NEAREST_AXIS (default) or PS_SEAMS_DISTANCE (getNonIntersectingMasks); next prepare."""
+        check(lib().ps_render_set_seam_rule(self._h, rule))
+
     def render(self, src: Sequence, dst, luts=None, stream=None, check: bool = False) -> bool:
         """render(src, dst, luts): src frames -> dst canvas (both host or device)."""
         imgs = (Image * len(src))(*[as_image(s) for s in src])
@@ -260,12 +264,13 @@ class CudaTilingMultibandBlendFast:
                 pass
             self._h = None
 
-    def prepare(self, masks, seams, max_levels: int, min_length: int = 2, stream=None) -> bool:
+    def prepare(self, masks, seams=None, max_levels: int = 16, min_length: int = 2, stream=None) -> bool:
+        """prepare(masks, maxLevels, minLength); seams None derives them as the reference does."""
         ms = [np.ascontiguousarray(m, np.uint8) for m in masks]
-        ss = [np.ascontiguousarray(s, np.uint8) for s in seams]
+        ss = None if seams is None else [np.ascontiguousarray(s, np.uint8) for s in seams]
         H, W = ms[0].shape
         mp = (C.c_void_p * len(ms))(*[m.ctypes.data for m in ms])
-        sp = (C.c_void_p * len(ss))(*[s.ctypes.data for s in ss])
+        sp = None if ss is None else (C.c_void_p * len(ss))(*[s.ctypes.data for s in ss])
         st = lib().ps_blender_prepare(self._h, mp, sp, len(ms), W, H, max_levels, min_length,
                                       _stream_handle(stream))
         if st != L.PS_OK:
@@ -307,6 +312,20 @@ def reproject_to_16s(src, xmap, ymap, dst, lut=None, stream=None) -> None:
     check(lib().ps_reproject_to_16s(C.byref(s), xmap.data_ptr(), ymap.data_ptr(), xmap.stride(0) * 4, W, H,
                                     None if lut is None else lut.data_ptr(), dst.data_ptr(),
                                     dst.stride(0) * dst.element_size(), _stream_handle(stream)))
+
+
+def non_intersecting_masks(masks, out, stream=None) -> None:
+    """getNonIntersectingMasks: (n, H, W) uint8 CUDA tensor -> (n, H, W) 0/255 CUDA tensor."""
+    n, H, W = masks.shape
+    assert masks.is_contiguous() and out.is_contiguous() and tuple(out.shape) == (n, H, W)
+    check(lib().ps_non_intersecting_masks(masks.data_ptr(), n, W, H, out.data_ptr(), _stream_handle(stream)))
+
+
+def distance_transform_l1(mask, dist, stream=None) -> None:
+    """cv::distanceTransform(mask, dist, CV_DIST_L1, 3): uint8 (H, W) -> int32 (H, W) CUDA tensors."""
+    H, W = mask.shape
+    assert mask.is_contiguous() and dist.is_contiguous()
+    check(lib().ps_distance_transform_l1(mask.data_ptr(), W, H, dist.data_ptr(), _stream_handle(stream)))
 
 
 def cvt_bgr32_to_yuv(src, planes: Sequence, fmt: int = L.PS_FMT_YUV420P, stream=None) -> None:

@@ -213,3 +213,43 @@ def test_yuv_chroma_from_left_column_and_nv12_interleave(oracle_lib):
     img3 = img.copy()
     img3[..., 3] = 255 - img3[..., 3]
     assert all(np.array_equal(a, b) for a, b in zip(O.bgr32_to_yuv(img3), (y, u, v)))
+
+
+# ---- reference seams (getNonIntersectingMasks, Mask.cpp:376-398) ----------
+def test_distance_transform_is_exact_l1(oracle_lib):
+    rng = np.random.default_rng(11)
+    for _ in range(40):
+        H, W = rng.integers(1, 14, 2)
+        m = (rng.random((H, W)) < rng.uniform(0.2, 1.0)).astype(np.uint8) * 255
+        d = O.distance_transform_l1(m)
+        zeros = np.argwhere(m == 0)
+        if len(zeros) == 0:
+            assert (d >= O.DT_FAR).all()
+            continue
+        yy, xx = np.mgrid[0:H, 0:W]
+        brute = np.min(np.abs(yy[..., None] - zeros[:, 0]) + np.abs(xx[..., None] - zeros[:, 1]), axis=-1)
+        assert np.array_equal(d, brute)
+
+
+def test_non_intersecting_masks_split_overlaps_by_distance(oracle_lib):
+    m = np.zeros((2, 20, 40), np.uint8)
+    m[0, :, :25] = 255
+    m[1, :, 15:] = 255
+    u = O.non_intersecting_masks(m)
+    # in the overlap (columns 15..24) column c goes to camera 1 where its distance to
+    # camera 1's uncovered columns (c - 14) exceeds camera 0's (25 - c): c >= 20
+    assert (u[0][:, :20] == 255).all() and (u[0][:, 20:] == 0).all()
+    assert (u[1][:, 20:] == 255).all() and (u[1][:, :20] == 0).all()
+
+
+def test_non_intersecting_masks_partition_random(oracle_lib):
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 3, 5):
+        m = np.zeros((n, 24, 48), np.uint8)
+        for i in range(n):
+            y0, x0 = rng.integers(0, 12), rng.integers(0, 30)
+            m[i, y0:y0 + rng.integers(4, 14), x0:x0 + rng.integers(6, 20)] = 255
+        u = O.non_intersecting_masks(m)
+        assert ((u > 0) <= (m > 0)).all()
+        assert ((u > 0).sum(0) == (m.max(0) > 0)).all()
+        assert set(np.unique(u)) <= {0, 255}
