@@ -10,6 +10,7 @@ The same line carries:
   roofline    the dominant kernel's algorithmic GB/s against the measured
               HBM copy bandwidth (CUDA events around every launch of a
               profiled pass over the same workload);
+  linear_blend  the linear-blend render mode (highQualityBlend 0) on the same rig;
   batched     four rigs of uneven size per launch sequence (CUDA graph);
   serve       16 live streams over those rigs, Poisson 30 fps arrivals,
               continuous batching: p50 / p99 frame latency and Mpix/s;
@@ -281,11 +282,15 @@ def run_ours(args, world, rank, local, dist):
     total_ms = 0.0
     for kind, name in r.KERNELS.items():
         n, kms, kb = r.profile_read(kind)
+        if n == 0:
+            continue
         kernels[name] = {"launches_per_frame": n // prof_steps, "ms_per_frame": kms / prof_steps,
                          "alg_bytes_per_launch": kb / max(n, 1), "gbs": kb / max(kms, 1e-9) / 1e6}
         total_ms += kms
     by_level = {}
     for kind, name in r.KERNELS.items():
+        if name not in kernels:
+            continue
         lv = []
         for level in range(r.num_levels + 1):
             n, kms, kb = r.profile_read(kind, level)
@@ -315,6 +320,8 @@ def run_ours(args, world, rank, local, dist):
         except Exception as e:  # an extra leg failing must not lose the headline line
             return {"error": f"{type(e).__name__}: {e}"}
 
+    if world == 1 and not args.no_linear:
+        out["linear_blend"] = guarded(run_linear, args, dev)
     if world == 1 and not args.no_batched and args.workload == "c2":
         out["batched"] = guarded(run_batched, args, dev)
     if world == 1 and not args.no_serve and args.workload == "c2":
@@ -322,6 +329,39 @@ def run_ours(args, world, rank, local, dist):
     if world == 1 and rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = guarded(cpu_baseline, r, cfg, pool_host, luts, args.cpu_seconds)
     return out
+
+
+def run_linear(args, dev):
+    """The linear-blend render mode on the same rig: weights feathered with a radius of 5% of the
+    canvas width (as CudaPanoramaRender prepares them), fp32 weighted accumulation."""
+    import torch
+    import panostitcher_gb300 as P
+    from panostitcher_gb300 import synth as S
+    cfg = S.rig(args.workload)
+    W, H = cfg.dst_size
+    radius = int(W * 0.05)
+    r = P.CudaPanoramaRender2()
+    t = time.perf_counter()
+    r.prepare(cfg.cams, 0, radius, cfg.src_size, cfg.dst_size, check=True)
+    prep = time.perf_counter() - t
+    fs = S.FrameSource(cfg)
+    pool = [[torch.from_numpy(f).to(dev) for f in fs.frame(k)] for k in range(2)]
+    luts = S.luts(cfg)
+    dst = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+    for k in range(5):
+        r.render(pool[k % 2], dst, luts, check=True)
+    torch.cuda.synchronize()
+    steps = max(10, args.steps // 2)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(steps):
+        r.render(pool[k % 2], dst, luts, check=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"mpix_s": round(W * H / ms / 1e3, 1), "ms_per_frame": round(ms, 4), "radius": radius,
+            "launches_per_frame": r.launches_per_frame, "prepare_s": round(prep, 3), "steps": steps,
+            "frame_alg_gbs": round(r.algorithmic_bytes(4, 4) / ms / 1e6, 1)}
 
 
 def run_batched(args, dev):
@@ -513,6 +553,7 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-linear", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args(argv)

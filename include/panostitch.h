@@ -96,8 +96,14 @@ void ps_render_destroy(ps_render* r);
 /* CudaPanoramaRender2::prepare (source/Task/RicohUtil.cpp:1091-1205) with the
    camera parameters passed directly instead of a file path.  Preconditions
    as the reference: dst_w, dst_h even and dst_h * 2 == dst_w; blend_param
-   (the maximum number of levels) > 0.  high_quality_blend must be 1 (the
-   multiband path; the linear-blend mode is not built).  Seam masks follow
+   > 0.  high_quality_blend non-zero prepares the multiband path with
+   blend_param the maximum number of levels; 0 prepares the linear-blend
+   path (RicohUtil.cpp:1174-1193): blend_param (<= 1024) is the radius of the
+   Gaussian that feathers the seam masks into per-camera weights
+   (getWeightsLinearBlend32F, source/Blend/LinearBlend.cpp:136-151), and
+   render accumulates the weighted warped frames in fp32
+   (cudaReprojectWeightedAccumulateTo32F + convertTo, RicohUtil.cpp:1269-1286;
+   BGR output only).  Seam masks follow
    the rule set by ps_render_set_seam_rule (by default the nearest optical
    axis).  Synchronises the stream. */
 int ps_render_prepare(ps_render* r, const ps_photo_param* params, int num_params, int high_quality_blend,
@@ -163,7 +169,8 @@ int ps_render_get_input_buffer(ps_render* r, int cam, void** data, long long* pi
    what: 0 x map (float, dst_h*dst_w, -1 where invalid), 1 y map (float),
    2 coverage mask (uint8 0/255), 3 seam mask (uint8 0/255),
    4 weight pyramid level `level` (int16), 5 alpha pyramid level `level`
-   (int32, the raw 5x5 sum as pyrDown16SC1To32SC1 writes it; level >= 1). */
+   (int32, the raw 5x5 sum as pyrDown16SC1To32SC1 writes it; level >= 1),
+   6 linear-blend weight (float, linear-blend mode). */
 int ps_render_export(const ps_render* r, int what, int cam, int level, void* host_out, long long bytes);
 /* Debug copy of the collapsed result at level `level` >= 1 of the last
    render (int16 x4 per pixel), for bit-exact checks of the pipeline. */
@@ -173,9 +180,10 @@ int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out,
    renders launch step by step with a CUDA event pair around every launch
    (no graph); ps_render_profile_read aggregates the finished launches of
    one kernel kind (0 remap, 1 pyrDown, 2 blend, 3 the tail kernel that runs
-   the few-tile top levels, reported at its lowest blend level) at one level
-   (-1 = all levels): launch count, summed device milliseconds and summed
-   algorithmic bytes (each input and output element counted once).
+   the few-tile top levels, reported at its lowest blend level, 4 the
+   linear-blend render) at one level (-1 = all levels): launch count, summed
+   device milliseconds and summed algorithmic bytes (each input and output
+   element counted once).
    Enabling resets the aggregates. */
 int ps_render_profile(ps_render* r, int enable);
 int ps_render_profile_read(ps_render* r, int kind, int level, long long* launches, double* total_ms,

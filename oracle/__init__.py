@@ -94,6 +94,9 @@ def lib():
             L.orc_mb_blend.argtypes = [vp, vp, vp, vp, vp]
             L.orc_mb_blend_mt.argtypes = [vp, vp, vp, C.c_int]
             L.orc_render.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int]
+            L.orc_linear_weights.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
+            L.orc_linear_render.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int,
+                                            vp]
             L.orc_distance_transform_l1.argtypes = [vp, C.c_int, C.c_int, vp]
             L.orc_non_intersecting_masks.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
             L.orc_bgr32_to_yuv.argtypes = [vp, C.c_longlong, C.c_int, C.c_int, C.c_int, vp, C.c_longlong, vp,
@@ -162,6 +165,33 @@ def non_intersecting_masks(masks: np.ndarray) -> np.ndarray:
     out = np.empty_like(m)
     lib().orc_non_intersecting_masks(_ptr(m), n, W, H, _ptr(out))
     return out
+
+
+# ------------------------------------------------------------------- linear blend
+def linear_weights(coverage: np.ndarray, seams: np.ndarray, radius: int) -> np.ndarray:
+    """getWeightsLinearBlend32F over given masks: (n, H, W) float32 weights."""
+    cov = np.ascontiguousarray(coverage, np.uint8)
+    sm = np.ascontiguousarray(seams, np.uint8)
+    n, H, W = cov.shape
+    out = np.empty((n, H, W), np.float32)
+    lib().orc_linear_weights(_ptr(cov), _ptr(sm), n, W, H, int(radius), _ptr(out))
+    return out
+
+
+def linear_render(srcs, luts, xmaps, ymaps, weights: np.ndarray) -> np.ndarray:
+    """The linear-blend render (BGR32 (H, W, 4))."""
+    srcs = [np.ascontiguousarray(s, np.uint8) for s in srcs]
+    n = len(srcs)
+    sh, sw, chn = srcs[0].shape
+    H, W = xmaps[0].shape
+    xs = [np.ascontiguousarray(m, np.float32) for m in xmaps]
+    ys = [np.ascontiguousarray(m, np.float32) for m in ymaps]
+    w = np.ascontiguousarray(weights, np.float32)
+    lt = None if luts is None else np.ascontiguousarray(luts, np.uint8)
+    dst = np.empty((H, W, 4), np.uint8)
+    lib().orc_linear_render(_ptr_array(srcs), sw, sh, chn, None if lt is None else _ptr(lt), _ptr_array(xs),
+                            _ptr_array(ys), _ptr(w), n, W, H, _ptr(dst))
+    return dst
 
 
 # ------------------------------------------------------------------- encoder handoff

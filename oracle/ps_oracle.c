@@ -1001,3 +1001,123 @@ void orc_non_intersecting_masks(const uint8_t* masks, int n, int W, int H, uint8
     free(dist);
     free(cur);
 }
+
+/* ---- linear blend --------------------------------------------------------
+ * Weights: getWeightsLinearBlend32F (source/Blend/LinearBlend.cpp:136-151).
+ * cv::GaussianBlur(unique, dist, Size(2r+1, 2r+1), r/3., r/3.) on an 8-bit
+ * mask: cv::getGaussianKernel's terms exp(-x^2 / (2 sigma^2)) are stored as
+ * float, normalised by their (double) sum into float, scaled by 2^8 and
+ * rounded to integers; rows then columns are filtered with the integer taps
+ * (border reflect-101, repeated for radii beyond the image), and the
+ * 2^16-scaled sum is rounded and saturated to 8 bits.  cv::bitwise_and with
+ * the 0/255 coverage keeps the blurred value where covered.  calcWeights32F
+ * (:78-120): where two or more cameras are non-zero, w_k = d_k * (1 / sum),
+ * one fp32 reciprocal and one product; where exactly one is, 1.
+ */
+static void linear_taps(int r, int* q)
+{
+    const int n = 2 * r + 1;
+    const double sigma = r / 3.0, scale2X = -0.5 / (sigma * sigma);
+    float* f = (float*)malloc(sizeof(float) * (size_t)n);
+    double sum = 0;
+    for (int i = 0; i < n; i++) {
+        const double x = i - (n - 1) * 0.5;
+        f[i] = (float)exp(scale2X * x * x);
+        sum += f[i];
+    }
+    sum = 1. / sum;
+    for (int i = 0; i < n; i++) {
+        const float k = (float)(f[i] * sum);
+        q[i] = (int)nearbyint((double)k * 256.0);
+    }
+    free(f);
+}
+
+static int reflect101_index(int p, int len)
+{
+    if (len == 1) return 0;
+    while (p < 0 || p >= len) p = p < 0 ? -p : 2 * len - 2 - p;
+    return p;
+}
+
+void orc_linear_weights(const uint8_t* cov, const uint8_t* seams, int n, int W, int H, int r, float* w)
+{
+    const size_t npx = (size_t)W * H;
+    int* q = (int*)malloc(sizeof(int) * (size_t)(2 * r + 1));
+    linear_taps(r, q);
+    int32_t* rows = (int32_t*)malloc(sizeof(int32_t) * npx);
+    uint8_t* dist = (uint8_t*)malloc(npx * (size_t)n);
+    for (int c = 0; c < n; c++) {
+        const uint8_t* s = seams + (size_t)c * npx;
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                int acc = 0;
+                for (int k = 0; k <= 2 * r; k++) acc += q[k] * (s[(size_t)y * W + reflect101_index(x + k - r, W)] ? 255 : 0);
+                rows[(size_t)y * W + x] = acc;
+            }
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                long long acc = 0;
+                for (int k = 0; k <= 2 * r; k++) acc += (long long)q[k] * rows[(size_t)reflect101_index(y + k - r, H) * W + x];
+                long long v = (acc + (1 << 15)) >> 16;
+                if (v < 0) v = 0;
+                if (v > 255) v = 255;
+                const size_t o = (size_t)c * npx + (size_t)y * W + x;
+                dist[o] = (uint8_t)v & (cov[o] ? 255 : 0);
+            }
+    }
+    for (size_t p = 0; p < npx; p++) {
+        float sum = 0.f;
+        int count = 0, last = 0;
+        for (int k = 0; k < n; k++) {
+            const int d = dist[(size_t)k * npx + p];
+            sum += (float)d;
+            if (d) {
+                count++;
+                last = k;
+            }
+        }
+        const float inv = count > 1 ? 1.0f / sum : 0.f;
+        for (int k = 0; k < n; k++) {
+            float v = 0.f;
+            if (count > 1) v = (float)dist[(size_t)k * npx + p] * inv;
+            else if (count == 1 && k == last) v = 1.f;
+            w[(size_t)k * npx + p] = v;
+        }
+    }
+    free(q);
+    free(rows);
+    free(dist);
+}
+
+void orc_linear_render(const uint8_t* const* srcs, int srcW, int srcH, int channels, const uint8_t* luts,
+                       const float* const* xmaps, const float* const* ymaps, const float* weights, int n, int W,
+                       int H, uint8_t* dst)
+{
+    const size_t npx = (size_t)W * H;
+    float* acc = (float*)calloc(npx * 3, sizeof(float));
+    int16_t* img = (int16_t*)malloc(sizeof(int16_t) * 4 * npx);
+    for (int i = 0; i < n; i++) {
+        orc_reproject_bilinear_16s(srcs[i], srcW, srcH, (long long)srcW * channels, channels,
+                                   luts ? luts + (size_t)i * 768 : NULL, xmaps[i], ymaps[i], W, H, img);
+        const float* wi = weights + (size_t)i * npx;
+        for (size_t p = 0; p < npx; p++) {
+            /* reprojectWeightedAccumulateTo32F adds only where the map is valid */
+            const float x = xmaps[i][p], y = ymaps[i][p];
+            if (!(x >= 0 && y >= 0 && x < srcW && y < srcH)) continue;
+            for (int c = 0; c < 3; c++) {
+                const float prod = (float)img[4 * p + c] * wi[p];
+                acc[3 * p + c] = acc[3 * p + c] + prod;
+            }
+        }
+    }
+    for (size_t p = 0; p < npx; p++) {
+        for (int c = 0; c < 3; c++) {
+            const float v = nearbyintf(acc[3 * p + c]);
+            dst[4 * p + c] = (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v));
+        }
+        dst[4 * p + 3] = 0;
+    }
+    free(acc);
+    free(img);
+}

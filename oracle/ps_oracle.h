@@ -109,6 +109,22 @@ void orc_distance_transform_l1(const uint8_t* mask, int W, int H, int32_t* dist)
 /* masks: n W*H 0/non-zero coverage masks; out: n W*H 0/255 unique masks. */
 void orc_non_intersecting_masks(const uint8_t* masks, int n, int W, int H, uint8_t* out);
 
+/* ---- linear blend (highQualityBlend == 0) -------------------------------- */
+/* getWeightsLinearBlend32F (source/Blend/LinearBlend.cpp:136-151) over given
+   coverage and unique masks (n W*H each, 0/non-zero): Gaussian blur of
+   radius r (2r+1 taps, sigma r/3, reflect-101) of each unique mask in 8-bit
+   fixed point, AND coverage, then calcWeights32F (:78-120).  weights: n W*H
+   floats. */
+void orc_linear_weights(const uint8_t* coverage, const uint8_t* seams, int n, int W, int H, int r, float* weights);
+/* The linear-blend render: per camera LUT + double bilinear remap to bytes,
+   then accum += byte * weight in fp32 in camera order, then round half to
+   even and saturate (RicohUtil.cpp:1269-1286 with the CPU
+   reprojectWeightedAccumulateTo32F, source/Warp/ZReproject.cpp:606-633).
+   Writes BGR32 dst (W*H*4). */
+void orc_linear_render(const uint8_t* const* srcs, int srcW, int srcH, int channels, const uint8_t* luts,
+                       const float* const* xmaps, const float* const* ymaps, const float* weights, int n, int W,
+                       int H, uint8_t* dst);
+
 /* ---- encoder handoff --------------------------------------------------- */
 /* cvtBGR32ToYUV420P / cvtBGR32ToNV12 (source/CudaAccel/ImageProc.cu:44-160):
    BT.601 studio range in 20-bit fixed point.  fmt 420: planes y, u, v;

@@ -19,7 +19,7 @@ PS_FMT_BGR24, PS_FMT_BGR32 = 24, 32
 PS_FMT_YUV420P, PS_FMT_NV12 = 420, 12
 PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE = 0, 1
 PS_MEM_HOST, PS_MEM_DEVICE = 0, 1
-EXPORT_XMAP, EXPORT_YMAP, EXPORT_COVERAGE, EXPORT_SEAM, EXPORT_WEIGHT, EXPORT_ALPHA = range(6)
+EXPORT_XMAP, EXPORT_YMAP, EXPORT_COVERAGE, EXPORT_SEAM, EXPORT_WEIGHT, EXPORT_ALPHA, EXPORT_LINEAR_WEIGHT = range(7)
 
 _STATUS_NAMES = {PS_EINVAL: "PS_EINVAL", PS_ENOMEM: "PS_ENOMEM", PS_ECUDA: "PS_ECUDA",
                  PS_ETIMEOUT: "PS_ETIMEOUT", PS_ESTATE: "PS_ESTATE"}

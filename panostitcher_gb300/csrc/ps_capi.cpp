@@ -152,9 +152,9 @@ static int prepareRender(ps_render* r, const ps_photo_param* params, int num, in
         purgePlans(&r->rig);
         r->plan.reset();
         r->rig.clear();
-        if (hq != 1) fail(PS_EINVAL, "high_quality_blend = %d: only the multiband path (1) is built", hq);
+        // source/Task/RicohUtil.cpp:1120-1193: non-zero = multiband, 0 = linear blend
         r->rig.prepareFromParams(params, num, blendParam, srcW, srcH, dstW, dstH, seams, toStream(stream),
-                                 r->seamRule);
+                                 r->seamRule, hq != 0);
         r->plan.reset(new ps::Plan({&r->rig}));
     });
 }
@@ -201,7 +201,7 @@ int ps_render_profile_read(ps_render* r, int kind, int level, long long* launche
 {
     return guarded([&] {
         if (!r) fail(PS_EINVAL, "render is NULL");
-        if (kind < 0 || kind > 3) fail(PS_EINVAL, "kind %d not in 0..3", kind);
+        if (kind < 0 || kind > 4) fail(PS_EINVAL, "kind %d not in 0..4", kind);
         r->prof.read(kind, level, launches, total_ms, bytes);
     });
 }
@@ -223,6 +223,7 @@ int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const u
     return guarded([&] {
         if (!r) fail(PS_EINVAL, "render is NULL");
         if (!r->rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        if (r->rig.linear()) fail(PS_EINVAL, "the linear-blend mode writes BGR only; use ps_cvt_bgr32_to_yuv");
         checkPlanar(dst, r->rig.width(), r->rig.height(), "dst");
         ps_image probe = {dst->planes[0], (long long)r->rig.width() * 4, r->rig.width(), r->rig.height(),
                           PS_FMT_BGR32, PS_MEM_DEVICE};  // only for the shared source / LUT checks

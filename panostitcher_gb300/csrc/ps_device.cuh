@@ -53,6 +53,9 @@ constexpr int kInlineCams = 8;
 constexpr int kTileUniform = 1;
 // cls of a level-0 blend tile: 0 uncovered (write zeros), 1 fully covered,
 // 2 partially covered (read the union mask).  Unused above level 0.
+// Linear-blend mode: one item per 32x16 canvas tile, naming the run
+// [first, first + count) of remap items (cameras in index order) covering it.
+struct LinearItem { uint16_t tx, ty; uint32_t first, count; };
 
 struct RigDev {
     int n, L, W, H;
@@ -70,6 +73,10 @@ struct RigDev {
     // the small top of the pyramid runs in one launch: pyrDown levels
     // tailDown..L, then blend levels L..tailBlend (L + 1 = none)
     int tailDown, tailBlend;
+    // linear-blend mode: the remap items (tile-major) and their weights,
+    // 512 floats per item in the layout of the maps
+    const RemapItem* remapItems;
+    const float* linWeights;
 };
 
 // Per-frame arguments of one rig in a launch (device resident, rewritten

@@ -98,6 +98,12 @@ cudaError_t launchNearestAxisSeams(const RemapDev* dParams, int n, int W, int H,
 // Scratch: uni W*H bytes, dUni and dCam W*H int32 each.
 cudaError_t launchNonIntersectingMasks(const uint8_t* cov, int n, int W, int H, uint8_t* out, uint8_t* uni,
                                        int32_t* dUni, int32_t* dCam, cudaStream_t st);
+// Linear-blend weights of n cameras (taps: 2r+1 fixed-point Gaussian taps on
+// the device), full-canvas into wFull and tile-compact (items) into wCompact.
+// Scratch: rowsScratch n*W*H int32, distScratch n*W*H bytes.
+cudaError_t launchLinearWeights(const uint8_t* seam, const uint8_t* cov, int n, int W, int H, const int* taps, int r,
+                                int32_t* rowsScratch, uint8_t* distScratch, float* wFull, const RemapItem* items,
+                                int nitems, float* wCompact, cudaStream_t st);
 // exact L1 distance of every pixel to the nearest zero pixel (>= 2^28 when there is none)
 cudaError_t launchDistanceTransformL1(const uint8_t* mask, int W, int H, int32_t* dist, cudaStream_t st);
 
@@ -141,6 +147,8 @@ cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st);
 // one cluster per segment: the rig's pyrDown levels tailDown..L and blend levels L..tailBlend
 cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st);
+// linear-blend mode: LinearItems of every segment; maxCams sizes the LUT stage
+cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams, cudaStream_t st);
 
 // ---- standalone primitives -------------------------------------------------------
 cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,

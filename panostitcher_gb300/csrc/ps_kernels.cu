@@ -142,6 +142,81 @@ __global__ void __launch_bounds__(kThreads) k_remap(const Segment* __restrict__ 
     }
 }
 
+// ============================================================================
+// k_linear: the linear-blend render (highQualityBlend == 0, CudaPanoramaRender2::
+// render, source/Task/RicohUtil.cpp:1269-1286): per canvas pixel
+//   accum = sum over cameras, in index order, of remap_i * w_i
+// in fp32 with one rounded product and one rounded sum per camera
+// (reprojectWeightedAccumulateTo32F, source/Warp/ZReproject.cpp:606-633),
+// then convertTo(CV_8U): round half to even, saturate.  One 32x16 canvas
+// tile per item (all tiles are items, so uncovered tiles are written 0);
+// each thread two pixels (rows ly and ly + 8).  The LUTs of all cameras of
+// the current rig are staged in shared memory.
+// ============================================================================
+__device__ __forceinline__ void storeBgr(const FrameDev& F, int x, int y, uint32_t v)
+{
+    uint8_t* row = F.out + (size_t)y * F.outPitch;
+    if (F.outFmt == PS_FMT_BGR32) {
+        reinterpret_cast<uint32_t*>(row)[x] = v;
+    } else {
+        row[3 * x] = v & 0xFF;
+        row[3 * x + 1] = (v >> 8) & 0xFF;
+        row[3 * x + 2] = (v >> 16) & 0xFF;
+    }
+}
+
+__device__ __forceinline__ uint32_t roundSaturate3(const float* a)
+{
+    uint32_t v = 0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) v |= (uint32_t)min(max(__float2int_rn(a[c]), 0), 255) << (8 * c);
+    return v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_linear(const Segment* __restrict__ segs, int nsegs, int total)
+{
+    extern __shared__ uint8_t luts[];  // 768 bytes per camera of the current rig
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    int s = 0, loaded = -1;
+    waitPrevGrid();
+    allowNextGrid();
+    for (int it = blockIdx.x; it < total; it += gridDim.x) {  // uniform across the CTA
+        s = findSegment(segs, nsegs, it, s);
+        const Segment& sg = segs[s];
+        const RigDev& R = *sg.rig;
+        const FrameDev& F = *sg.frame;
+        if (s != loaded) {
+            __syncthreads();
+            for (int k = threadIdx.x; k < R.n * 768; k += kThreads) luts[k] = __ldg(F.luts + k);
+            __syncthreads();
+            loaded = s;
+        }
+        const LinearItem item = static_cast<const LinearItem*>(sg.items)[it - sg.prefix];
+        float a0[3] = {0.f, 0.f, 0.f}, a1[3] = {0.f, 0.f, 0.f};
+        for (uint32_t q = 0; q < item.count; q++) {
+            const RemapItem ri = R.remapItems[item.first + q];
+            const size_t base = (size_t)ri.mapTile * (kRemapTW * kRemapTH) + threadIdx.x;
+            const float2 m0 = __ldg(R.maps + base), m1 = __ldg(R.maps + base + kThreads);
+            const float w0 = __ldg(R.linWeights + base), w1 = __ldg(R.linWeights + base + kThreads);
+            const uint8_t* src = F.src[ri.cam];
+            const long long pitch = F.srcPitch[ri.cam];
+            const uint8_t* lut = luts + ri.cam * 768;
+            const uint32_t v0 = remapPixel(m0, src, pitch, F.srcFmt, R.srcW, R.srcH, lut);
+            const uint32_t v1 = remapPixel(m1, src, pitch, F.srcFmt, R.srcW, R.srcH, lut);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                a0[c] = __fadd_rn(a0[c], __fmul_rn(byteToFloat((v0 >> (8 * c)) & 0xFF), w0));
+                a1[c] = __fadd_rn(a1[c], __fmul_rn(byteToFloat((v1 >> (8 * c)) & 0xFF), w1));
+            }
+        }
+        const int x = item.tx * kRemapTW + lx, y0 = item.ty * kRemapTH + ly, y1 = y0 + 8;
+        if (x < R.W) {
+            if (y0 < R.H) storeBgr(F, x, y0, roundSaturate3(a0));
+            if (y1 < R.H) storeBgr(F, x, y1, roundSaturate3(a1));
+        }
+    }
+}
+
 // Standalone cudaReprojectTo16S with an optional LUT: full-canvas maps,
 // int16x4 output (B, G, R, 0).
 __global__ void __launch_bounds__(kThreads) k_reproject16s(const uint8_t* __restrict__ src, long long srcPitch,
@@ -982,6 +1057,22 @@ cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_
 {
     if (total <= 0) return cudaSuccess;
     return launchPdl(k_pyrdown, gridFor(total, 6), kThreads, st, segs, nsegs, total);
+}
+
+cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams, cudaStream_t st)
+{
+    if (total <= 0) return cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(gridFor(total, 8));
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = (size_t)maxCams * 768;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_linear, segs, nsegs, total);
 }
 
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st)

@@ -585,6 +585,101 @@ cudaError_t launchCompactMaps(const float* xmap, const float* ymap, int W, int H
     return cudaGetLastError();
 }
 
+// ============================================================================
+// Linear-blend weights: getWeightsLinearBlend32F (source/Blend/LinearBlend.cpp:
+// 136-151) and calcWeights32F (:78-120).  Per camera, the 0/255 seam mask is
+// blurred by a (2r+1)-tap Gaussian (sigma r/3) with cv::GaussianBlur's
+// default reflect-101 border, in 8-bit fixed point (row and column taps
+// scaled by 2^8, the 2^16-scaled sum rounded and saturated), ANDed with the
+// 0/255 coverage; at each pixel the blurred values then become weights:
+// d_k / sum_k d_k (fp32, one reciprocal, one product) where two or more
+// cameras are non-zero, 1 where exactly one is.
+// ============================================================================
+// reflect-101 index with repeated reflection (cv::borderInterpolate)
+__device__ __forceinline__ int reflect101(int p, int len)
+{
+    if (len == 1) return 0;
+    while (p < 0 || p >= len) p = p < 0 ? -p : 2 * len - 2 - p;
+    return p;
+}
+
+// grid (H, n): one CTA per row of one camera; the row is staged with its
+// reflected borders in shared memory (W + 2r bytes).
+__global__ void k_gauss_rows(const uint8_t* __restrict__ seam, int W, int H, const int* __restrict__ taps, int r,
+                             int32_t* __restrict__ rows)
+{
+    extern __shared__ uint8_t ext[];
+    const int y = blockIdx.x, c = blockIdx.y;
+    const uint8_t* src = seam + ((size_t)c * H + y) * W;
+    for (int k = threadIdx.x; k < W + 2 * r; k += blockDim.x) ext[k] = src[reflect101(k - r, W)] ? 255 : 0;
+    __syncthreads();
+    int32_t* out = rows + ((size_t)c * H + y) * W;
+    for (int x = threadIdx.x; x < W; x += blockDim.x) {
+        int acc = 0;
+        for (int k = 0; k <= 2 * r; k++) acc += __ldg(taps + k) * ext[x + k];
+        out[x] = acc;
+    }
+}
+
+// grid (ceil(W / 128), H, n): the column pass, rounding, saturation and the
+// AND with the coverage.
+__global__ void k_gauss_cols(const int32_t* __restrict__ rows, const uint8_t* __restrict__ cov, int W, int H,
+                             const int* __restrict__ taps, int r, uint8_t* __restrict__ dist)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, c = blockIdx.z;
+    if (x >= W) return;
+    const int32_t* col = rows + (size_t)c * H * W + x;
+    long long acc = 0;
+    for (int k = 0; k <= 2 * r; k++) acc += (long long)__ldg(taps + k) * col[(size_t)reflect101(y + k - r, H) * W];
+    const long long v = (acc + (1 << 15)) >> 16;
+    const size_t o = ((size_t)c * H + y) * W + x;
+    dist[o] = cov[o] ? (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v)) : 0;
+}
+
+__global__ void k_linear_weights(const uint8_t* __restrict__ dist, int n, long long npx, float* __restrict__ w)
+{
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+        float sum = 0.f;
+        int count = 0, last = 0;
+        for (int k = 0; k < n; k++) {
+            const int d = dist[(size_t)k * npx + p];
+            sum = __fadd_rn(sum, (float)d);
+            if (d) {
+                count++;
+                last = k;
+            }
+        }
+        const float inv = count > 1 ? __fdiv_rn(1.f, sum) : 0.f;
+        for (int k = 0; k < n; k++) {
+            float v = 0.f;
+            if (count > 1) v = __fmul_rn((float)dist[(size_t)k * npx + p], inv);
+            else if (count == 1 && k == last) v = 1.f;
+            w[(size_t)k * npx + p] = v;
+        }
+    }
+}
+
+__global__ void k_compact_weights(const float* __restrict__ w, int W, int H, long long npx,
+                                  const RemapItem* __restrict__ items, float* out)
+{
+    const RemapItem it = items[blockIdx.x];
+    const int x = it.tx * kRemapTW + (threadIdx.x & 31), y = it.ty * kRemapTH + (threadIdx.x >> 5);
+    out[(size_t)it.mapTile * (kRemapTW * kRemapTH) + threadIdx.x] =
+        (x < W && y < H) ? w[(size_t)it.cam * npx + (size_t)y * W + x] : 0.f;
+}
+
+cudaError_t launchLinearWeights(const uint8_t* seam, const uint8_t* cov, int n, int W, int H, const int* taps, int r,
+                                int32_t* rowsScratch, uint8_t* distScratch, float* wFull, const RemapItem* items,
+                                int nitems, float* wCompact, cudaStream_t st)
+{
+    const long long npx = (long long)W * H;
+    k_gauss_rows<<<dim3(H, n), 256, W + 2 * r, st>>>(seam, W, H, taps, r, rowsScratch);
+    k_gauss_cols<<<dim3((W + 127) / 128, H, n), 128, 0, st>>>(rowsScratch, cov, W, H, taps, r, distScratch);
+    k_linear_weights<<<(int)std::min<long long>((npx + 255) / 256, 8192), 256, 0, st>>>(distScratch, n, npx, wFull);
+    if (nitems > 0) k_compact_weights<<<nitems, kRemapTW * kRemapTH, 0, st>>>(wFull, W, H, npx, items, wCompact);
+    return cudaGetLastError();
+}
+
 // Blender input images -> uchar4 level 0.  status bit 1: a 16-bit value
 // outside 0..255; bit 2: a non-zero pixel where the coverage mask is 0 (the
 // multiband blend needs zeros there, source/Warp/ZReproject.cpp:200-208).

@@ -3,6 +3,7 @@
 #include "ps_rig.h"
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -10,6 +11,34 @@
 namespace ps {
 
 static std::atomic<uint64_t> g_generation{1};
+
+// Largest Gaussian radius of the linear-blend weights (2r+1 taps per pass).
+constexpr int kMaxLinearRadius = 1024;
+
+// Fixed-point taps of a (2r+1)-tap Gaussian with sigma r/3: the kernel of
+// cv::getGaussianKernel(2r+1, r/3, CV_32F) (exp in double, each term and
+// the normalised term stored as float) scaled by 2^8 and rounded to the
+// nearest integer, ties to even.
+static std::vector<int> gaussTaps(int r)
+{
+    const int n = 2 * r + 1;
+    const double sigma = r / 3.0;  // source/Blend/LinearBlend.cpp:142
+    const double scale2X = -0.5 / (sigma * sigma);
+    std::vector<float> f(n);
+    double sum = 0;
+    for (int i = 0; i < n; i++) {
+        const double x = i - (n - 1) * 0.5;
+        f[i] = (float)std::exp(scale2X * x * x);
+        sum += f[i];
+    }
+    sum = 1. / sum;
+    std::vector<int> q(n);
+    for (int i = 0; i < n; i++) {
+        const float k = (float)(f[i] * sum);
+        q[i] = (int)std::nearbyint((double)k * 256.0);
+    }
+    return q;
+}
 
 [[noreturn]] void fail(int code, const char* fmt, ...)
 {
@@ -96,7 +125,10 @@ void Rig::clear()
     seamBits_.clear();
     geom_.clear();
     n_ = W_ = H_ = L_ = full_ = srcW_ = srcH_ = 0;
-    hasMaps_ = false;
+    hasMaps_ = linear_ = false;
+    numLinear_ = 0;
+    dLinear_.reset();
+    linW_.reset();
     inPitch_ = 0;
     gen_ = 0;
 }
@@ -122,6 +154,7 @@ long long Rig::residentBytes() const
     for (const auto& l : lv_) b += l.G.bytes() + l.Wt.bytes() + l.Am.bytes() + l.C.bytes();
     b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
     b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
+    b += dLinear_.bytes() + linW_.bytes();
     return b;
 }
 
@@ -168,14 +201,16 @@ static void distanceSeams(const uint8_t* cov, int n, int W, int H, uint8_t* seam
 }
 
 void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
-                            int dstH, const uint8_t* const* seams, cudaStream_t st, int seamRule)
+                            int dstH, const uint8_t* const* seams, cudaStream_t st, int seamRule, int highQuality)
 {
     clear();
     validateParams(params, n, srcW, srcH, dstW, dstH);
     if (blendParam <= 0) fail(PS_EINVAL, "blendParam = %d, should be positive", blendParam);  // RicohUtil.cpp:1105
+    if (!highQuality && blendParam > kMaxLinearRadius)
+        fail(PS_EINVAL, "blendParam = %d, the linear-blend radius is at most %d", blendParam, kMaxLinearRadius);
     try {
         // MIN_SIDE_LENGTH = 2, source/Task/RicohUtil.cpp:15
-        setGeometry(n, dstW, dstH, std::max(0, trueNumLevels(dstW, dstH, blendParam, 2)));
+        setGeometry(n, dstW, dstH, highQuality ? std::max(0, trueNumLevels(dstW, dstH, blendParam, 2)) : 0);
         srcW_ = srcW;
         srcH_ = srcH;
         const size_t npx = (size_t)dstW * dstH;
@@ -203,7 +238,8 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
         inputs_.alloc((size_t)inPitch_ * srcH * n);
         inputs_.zero(st);
         output_.alloc(npx * 4);
-        preparePyramids(cov.as<uint8_t>(), seam.as<uint8_t>(), xmap.as<float>(), ymap.as<float>(), st);
+        if (highQuality) preparePyramids(cov.as<uint8_t>(), seam.as<uint8_t>(), xmap.as<float>(), ymap.as<float>(), st);
+        else prepareLinear(cov.as<uint8_t>(), seam.as<uint8_t>(), xmap.as<float>(), ymap.as<float>(), blendParam, st);
         PS_CUDA(cudaStreamSynchronize(st));
     } catch (...) {
         clear();
@@ -504,6 +540,94 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     gen_ = g_generation++;
 }
 
+void Rig::prepareLinear(const uint8_t* cov, const uint8_t* seam, const float* xmap, const float* ymap, int radius,
+                        cudaStream_t st)
+{
+    const int n = n_, W = W_, H = H_;
+    const size_t npx = (size_t)W * H;
+    linear_ = true;
+    status_.alloc(sizeof(int));
+    status_.zero(st);
+    // the 32x16 tiles each camera covers
+    const int rX = divUp(W, kRemapTW), rY = divUp(H, kRemapTH);
+    DevBuf rflags((size_t)n * rX * rY);
+    rflags.zero(st);
+    PS_CUDA(launchTileFlags8(cov, W, H, W, (long long)npx, n, kRemapTW, kRemapTH, rX, rY, rflags.as<uint8_t>(), st));
+    std::vector<uint8_t> hR(rflags.bytes()), hCov(n * npx), hSeam(n * npx);
+    PS_CUDA(cudaMemcpyAsync(hR.data(), rflags.get(), hR.size(), cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaMemcpyAsync(hCov.data(), cov, n * npx, cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaMemcpyAsync(hSeam.data(), seam, n * npx, cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaStreamSynchronize(st));
+    covCount_ = 0;
+    std::vector<uint8_t> any(npx, 0);
+    for (size_t c = 0; c < (size_t)n; c++)
+        for (size_t p = 0; p < npx; p++)
+            if (hCov[c * npx + p]) {
+                covCount_++;
+                any[p] = 1;
+            }
+    full_ = std::all_of(any.begin(), any.end(), [](uint8_t v) { return v != 0; });
+    packBits(hCov, covBits_);
+    packBits(hSeam, seamBits_);
+
+    // work items: every canvas tile, with the covering cameras' remap items (index order)
+    hRemap_.clear();
+    std::vector<LinearItem> lin;
+    lin.reserve((size_t)rX * rY);
+    uint32_t t = 0;
+    for (int ty = 0; ty < rY; ty++)
+        for (int tx = 0; tx < rX; tx++) {
+            const uint32_t first = (uint32_t)hRemap_.size();
+            for (int c = 0; c < n; c++)
+                if (hR[((size_t)c * rY + ty) * rX + tx]) hRemap_.push_back({(uint16_t)c, 0, (uint16_t)tx, (uint16_t)ty, t++});
+            lin.push_back({(uint16_t)tx, (uint16_t)ty, first, (uint32_t)hRemap_.size() - first});
+        }
+    numLinear_ = (int)lin.size();
+    dRemap_.alloc(std::max<size_t>(1, hRemap_.size()) * sizeof(RemapItem));
+    dLinear_.alloc(lin.size() * sizeof(LinearItem));
+    if (!hRemap_.empty())
+        PS_CUDA(cudaMemcpyAsync(dRemap_.get(), hRemap_.data(), hRemap_.size() * sizeof(RemapItem),
+                                cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaMemcpyAsync(dLinear_.get(), lin.data(), lin.size() * sizeof(LinearItem), cudaMemcpyHostToDevice, st));
+    const size_t tiles = std::max<size_t>(1, hRemap_.size());
+    maps_.alloc(tiles * kRemapTW * kRemapTH * sizeof(float2));
+    linW_.alloc(tiles * kRemapTW * kRemapTH * sizeof(float));
+    if (!hRemap_.empty())
+        PS_CUDA(launchCompactMaps(xmap, ymap, W, H, (long long)npx, dRemap_.as<RemapItem>(), (int)hRemap_.size(),
+                                  maps_.as<float2>(), st));
+    // weights (getWeightsLinearBlend32F)
+    const std::vector<int> taps = gaussTaps(radius);
+    DevBuf dTaps(taps.size() * sizeof(int));
+    PS_CUDA(cudaMemcpyAsync(dTaps.get(), taps.data(), dTaps.bytes(), cudaMemcpyHostToDevice, st));
+    {
+        DevBuf rows(n * npx * 4), dist(n * npx), wFull(n * npx * 4);
+        PS_CUDA(launchLinearWeights(seam, cov, n, W, H, dTaps.as<int>(), radius, rows.as<int32_t>(), dist.as<uint8_t>(),
+                                    wFull.as<float>(), dRemap_.as<RemapItem>(), (int)hRemap_.size(), linW_.as<float>(),
+                                    st));
+        PS_CUDA(cudaStreamSynchronize(st));
+    }
+    RigDev d;
+    std::memset(&d, 0, sizeof d);
+    d.n = n;
+    d.W = W;
+    d.H = H;
+    d.full = full_;
+    d.srcW = srcW_;
+    d.srcH = srcH_;
+    d.maps = maps_.as<float2>();
+    d.remapItems = dRemap_.as<RemapItem>();
+    d.linWeights = linW_.as<float>();
+    d.tailDown = d.tailBlend = 1;
+    d.lv[0].w = W;
+    d.lv[0].h = H;
+    d.lv[0].pitch = geom_[0].pitch;
+    dDesc_.alloc(sizeof(RigDev));
+    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), &d, sizeof d, cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaStreamSynchronize(st));
+    tailDown_ = tailBlend_ = 1;  // no pyramid
+    gen_ = g_generation++;
+}
+
 void Rig::imagesToLevel0(const void* const* images, const long long* pitches, int fmt, cudaStream_t st)
 {
     const size_t n = n_;
@@ -556,7 +680,24 @@ void Rig::exportState(int what, int cam, int level, void* host, long long bytes)
         for (size_t i = 0; i < npx; i++) out[i] = (bits[(base + i) >> 3] >> ((base + i) & 7)) & 1 ? 255 : 0;
         return;
     }
+    if (what == 6) {  // linear-blend weights (float per pixel, 0 outside the camera's tiles)
+        if (!linear_) fail(PS_EINVAL, "no linear-blend weights (multiband mode)");
+        if ((size_t)bytes < npx * 4) fail(PS_EINVAL, "buffer too small");
+        float* out = static_cast<float*>(host);
+        std::fill(out, out + npx, 0.f);
+        std::vector<float> w(hRemap_.size() * kRemapTW * kRemapTH);
+        if (!w.empty()) PS_CUDA(cudaMemcpy(w.data(), linW_.get(), w.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        for (const RemapItem& it : hRemap_) {
+            if (it.cam != cam) continue;
+            for (int k = 0; k < kRemapTW * kRemapTH; k++) {
+                const int x = it.tx * kRemapTW + (k % kRemapTW), y = it.ty * kRemapTH + (k / kRemapTW);
+                if (x < W_ && y < H_) out[(size_t)y * W_ + x] = w[(size_t)it.mapTile * kRemapTW * kRemapTH + k];
+            }
+        }
+        return;
+    }
     if (what == 4 || what == 5) {
+        if (linear_) fail(PS_EINVAL, "no pyramids (linear-blend mode)");
         if (level < 0 || level > L_ || (what == 5 && level == 0)) fail(PS_EINVAL, "level %d out of range", level);
         const LevelGeom& g = geom_[level];
         const size_t cnt = (size_t)g.w * g.h;
@@ -590,6 +731,18 @@ void Rig::exportCollapsed(int level, int16_t* host, long long bytes, cudaStream_
 double Rig::stepBytes(int kind, int level) const
 {
     double b = 0;
+    if (kind == 4) {
+        // map (8 B) and weight (4 B) per covered tile pixel, every covering frame once, the canvas out
+        std::vector<char> used(n_, 0);
+        for (const RemapItem& it : hRemap_) {
+            const int tw = std::min(kRemapTW, W_ - it.tx * kRemapTW), th = std::min(kRemapTH, H_ - it.ty * kRemapTH);
+            b += (double)tw * th * 12;
+            used[it.cam] = 1;
+        }
+        for (int c = 0; c < n_; c++)
+            if (used[c]) b += (double)srcW_ * srcH_ * 4;
+        return b + (double)W_ * H_ * 4;
+    }
     if (kind == 3) {
         for (int J = tailDown_; J <= L_; J++) b += stepBytes(1, J);
         for (int j = tailBlend_; j <= L_; j++) b += stepBytes(2, j);
@@ -633,6 +786,8 @@ double Rig::stepBytes(int kind, int level) const
 
 double Rig::algorithmicBytes(int bin, int bout) const
 {
+    if (linear_)  // frames in, map (8 B) and weight (4 B) per covered pixel, canvas out
+        return (double)n_ * srcW_ * srcH_ * bin + (double)covCount_ * 12 + (double)W_ * H_ * bout;
     return (double)n_ * srcW_ * srcH_ * bin + (double)covCount_ * 8 + (double)weightCount_ * 2 +
            (double)alphaCount_ * 4 + (double)W_ * H_ * bout;
 }
@@ -733,6 +888,8 @@ void Plan::bind(const std::vector<Rig*>& rigs)
 
     steps_.clear();
     segs_.clear();
+    maxCams_ = 0;
+    for (Rig* r : rigs) maxCams_ = std::max(maxCams_, r->numImages());
     auto addStep = [&](int kind, const std::vector<std::pair<int, std::pair<const void*, int>>>& parts, int step) {
         Step s{kind, (int)segs_.size(), 0, 0, -1, 0.0};
         for (const auto& p : parts) {
@@ -742,7 +899,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
                              reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * p.first), p.second.second, s.total});
             s.total += p.second.second;
             const Rig* rg = rigs[p.first];
-            const int lvl = kind == 0 ? 0 : (kind == 1 ? step : rg->tailBlend() - 1 - step);
+            const int lvl = kind == 0 || kind == 4 ? 0 : (kind == 1 ? step : rg->tailBlend() - 1 - step);
             if (s.level < 0) s.level = lvl;
             s.bytes += rg->stepBytes(kind, lvl);
         }
@@ -750,7 +907,12 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         if (s.total > 0) steps_.push_back(s);
     };
     std::vector<std::pair<int, std::pair<const void*, int>>> parts;
-    for (int r = 0; r < nr; r++) parts.push_back({r, {rigs[r]->remapItems(), rigs[r]->numRemapItems()}});
+    for (int r = 0; r < nr; r++)
+        if (rigs[r]->linear()) parts.push_back({r, {rigs[r]->linearItems(), rigs[r]->numLinearItems()}});
+    addStep(4, parts, 0);
+    parts.clear();
+    for (int r = 0; r < nr; r++)
+        if (!rigs[r]->linear()) parts.push_back({r, {rigs[r]->remapItems(), rigs[r]->numRemapItems()}});
     addStep(0, parts, 0);
     for (int J = 1; J <= maxL; J++) {
         parts.clear();
@@ -762,7 +924,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         // the tail: one cluster per rig that has one (segment count 1)
         Step s{3, (int)segs_.size(), 0, 0, -1, 0.0};
         for (int r = 0; r < nr; r++) {
-            if (!rigs[r]->hasTail()) continue;
+            if (rigs[r]->linear() || !rigs[r]->hasTail()) continue;
             segs_.push_back({nullptr, rigs[r]->deviceDesc(), reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * r), 1,
                              s.total});
             s.total += 1;
@@ -773,10 +935,12 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         if (s.total > 0) steps_.push_back(s);
     }
     int maxB = 0;
-    for (Rig* r : rigs) maxB = std::max(maxB, r->tailBlend());
+    for (Rig* r : rigs)
+        if (!r->linear()) maxB = std::max(maxB, r->tailBlend());
     for (int s = 0; s < maxB; s++) {
         parts.clear();
         for (int r = 0; r < nr; r++) {
+            if (rigs[r]->linear()) continue;
             const int j = rigs[r]->tailBlend() - 1 - s;
             if (j >= 0) parts.push_back({r, {rigs[r]->blendItems(j), rigs[r]->numBlendItems(j)}});
         }
@@ -825,7 +989,8 @@ void Plan::launchAll(cudaStream_t st, Profiler* prof)
         if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, st));
         else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, st));
-        else PS_CUDA(launchTail(p, s.nsegs, st));
+        else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, st));
+        else PS_CUDA(launchLinear(p, s.nsegs, s.total, maxCams_, st));
         if (prof) {
             PS_CUDA(cudaEventRecord(b, st));
             prof->record(s.kind, s.level, s.bytes, a, b);

@@ -20,8 +20,11 @@ public:
 
     // CudaPanoramaRender2::prepare: maps + coverage from the camera
     // parameters; seams given, or derived by seamRule (PS_SEAMS_*).
+    // highQuality 0 prepares the linear-blend mode, with blendParam the
+    // Gaussian radius of the weights (RicohUtil.cpp:1174-1193).
     void prepareFromParams(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
-                           int dstH, const uint8_t* const* seams, cudaStream_t st, int seamRule = PS_SEAMS_NEAREST_AXIS);
+                           int dstH, const uint8_t* const* seams, cudaStream_t st, int seamRule = PS_SEAMS_NEAREST_AXIS,
+                           int highQuality = 1);
     // CudaTilingMultibandBlendFast::prepare: coverage masks given; seams
     // given, or getNonIntersectingMasks of the coverage when seams is NULL.
     void prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* seams, int n, int W, int H,
@@ -37,6 +40,9 @@ public:
     int srcW() const { return srcW_; }
     int srcH() const { return srcH_; }
     bool hasMaps() const { return hasMaps_; }
+    bool linear() const { return linear_; }
+    const LinearItem* linearItems() const { return dLinear_.as<LinearItem>(); }
+    int numLinearItems() const { return numLinear_; }
     uint64_t generation() const { return gen_; }
     long long residentBytes() const;
     // resident bytes a rig of this shape would hold (no allocation)
@@ -68,7 +74,8 @@ public:
     void imagesToLevel0(const void* const* images, const long long* pitches, int fmt, cudaStream_t st);
 
     // Bytes a step must move at minimum (each input / output element once,
-    // no halo re-reads): kind 0 remap, 1 pyrDown to `level`, 2 blend of `level`.
+    // no halo re-reads): kind 0 remap, 1 pyrDown to `level`, 2 blend of
+    // `level`, 3 the tail, 4 the linear-blend render.
     double stepBytes(int kind, int level) const;
     // Algorithmic bytes of one stitched frame (inputs, maps, weights, alpha
     // divisors, output; all pyramid levels are intermediate and count 0):
@@ -82,9 +89,13 @@ private:
     void setGeometry(int n, int W, int H, int L);
     void preparePyramids(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
                          cudaStream_t st);
+    void prepareLinear(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
+                       int radius, cudaStream_t st);
 
     int n_ = 0, W_ = 0, H_ = 0, L_ = 0, full_ = 0, srcW_ = 0, srcH_ = 0;
-    bool hasMaps_ = false;
+    bool hasMaps_ = false, linear_ = false;
+    int numLinear_ = 0;
+    DevBuf dLinear_, linW_;
     uint64_t gen_ = 0;
     std::vector<LevelGeom> geom_;
     LevelBufs lv_[PS_MAX_LEVELS + 1];
@@ -151,7 +162,7 @@ public:
 
 private:
     struct Step {
-        int kind;  // 0 remap, 1 pyrDown, 2 blend, 3 tail
+        int kind;  // 0 remap, 1 pyrDown, 2 blend, 3 tail, 4 linear-blend render
         int segOff, nsegs, total;
         int level;      // level of the first rig in the step
         double bytes;   // algorithmic bytes of the step (all rigs)
@@ -165,6 +176,7 @@ private:
     std::vector<Segment> segs_;      // frame pointers already absolute
     std::vector<size_t> lutOff_;
     size_t segOff_ = 0, stageBytes_ = 0;
+    int maxCams_ = 0;
     DevBuf dArgs_;          // [FrameDev x nr][LUTs][Segment x nseg]
     HostBuf stage_;         // pinned staging copy of dArgs_
     cudaGraphExec_t graph_ = nullptr;

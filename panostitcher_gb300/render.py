@@ -180,7 +180,7 @@ class CudaPanoramaRender2:
     def profile(self, enabled: bool) -> None:
         check(lib().ps_render_profile(self._h, int(bool(enabled))))
 
-    KERNELS = {0: "k_remap", 1: "k_pyrdown", 2: "k_blend", 3: "k_tail"}
+    KERNELS = {0: "k_remap", 1: "k_pyrdown", 2: "k_blend", 3: "k_tail", 4: "k_linear"}
 
     def profile_read(self, kind: int, level: int = -1):
         """(launches, total_ms, algorithmic_bytes) of finished profiled launches."""
@@ -212,6 +212,10 @@ class CudaPanoramaRender2:
 
     def coverage(self, cam: int, dst_size) -> np.ndarray:
         return self.export(L.EXPORT_COVERAGE, cam, 0, (dst_size[1], dst_size[0]), np.uint8)
+
+    def linear_weight(self, cam: int, dst_size) -> np.ndarray:
+        """Linear-blend mode: the camera's float weight per canvas pixel."""
+        return self.export(L.EXPORT_LINEAR_WEIGHT, cam, 0, (dst_size[1], dst_size[0]), np.float32)
 
     def seam(self, cam: int, dst_size) -> np.ndarray:
         return self.export(L.EXPORT_SEAM, cam, 0, (dst_size[1], dst_size[0]), np.uint8)

@@ -68,7 +68,8 @@ def test_prepare_preconditions_like_reference(built_lib):
     assert "positive" in _prepare_err(blend_param=0)
     assert "camera" in _prepare_err(params=[])
     assert "image_type" in _prepare_err(params=[S.photo_param(7, 90.0)])
-    assert "high_quality_blend" in _prepare_err(high_quality_blend=0)
+    # linear-blend mode: the Gaussian radius is bounded
+    assert "radius" in _prepare_err(high_quality_blend=0, blend_param=5000)
     assert "srcSize" in _prepare_err(src_size=(0, 10))
 
 

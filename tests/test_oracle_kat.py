@@ -253,3 +253,35 @@ def test_non_intersecting_masks_partition_random(oracle_lib):
         assert ((u > 0) <= (m > 0)).all()
         assert ((u > 0).sum(0) == (m.max(0) > 0)).all()
         assert set(np.unique(u)) <= {0, 255}
+
+
+# ---- linear blend (getWeightsLinearBlend32F + weighted accumulate) --------
+def test_linear_weights_partition_of_unity(oracle_lib):
+    cov = np.zeros((3, 24, 48), np.uint8)
+    cov[0, :, :30] = 255
+    cov[1, :, 18:] = 255
+    cov[2, 4:20, 10:40] = 255
+    seams = O.non_intersecting_masks(cov)
+    for r in (1, 4, 9, 30):
+        w = O.linear_weights(cov, seams, r)
+        covered = cov.max(0) > 0
+        s = w.sum(0)
+        assert np.abs(s[covered] - 1).max() < 1e-6
+        assert (s[~covered] == 0).all()
+        assert (w[cov == 0] == 0).all()
+
+
+def test_linear_render_identity_kat(oracle_lib):
+    # two cameras with identical warped content: the weighted sum is the content
+    H, W = 16, 32
+    src = np.random.default_rng(0).integers(0, 256, (H, W, 4), dtype=np.uint8)
+    yy, xx = np.mgrid[0:H, 0:W].astype(np.float32)
+    cov = np.full((2, H, W), 255, np.uint8)
+    cov[0, :, 24:] = 0
+    cov[1, :, :8] = 0
+    seams = O.non_intersecting_masks(cov)
+    w = O.linear_weights(cov, seams, 3)
+    xm = [np.where(cov[i] > 0, xx, -1).astype(np.float32) for i in range(2)]
+    ym = [np.where(cov[i] > 0, yy, -1).astype(np.float32) for i in range(2)]
+    out = O.linear_render([src, src], None, xm, ym, w)
+    assert np.array_equal(out[..., :3], src[..., :3]) and (out[..., 3] == 0).all()
