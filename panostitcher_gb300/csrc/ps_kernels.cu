@@ -61,32 +61,50 @@ __device__ __noinline__ int bilinearExact(double x, double y, int x0, int y0, in
 // its low mantissa bits.
 __device__ __forceinline__ float byteToFloat(uint32_t b) { return __int_as_float(0x4B000000u | b) - 8388608.f; }
 
-// Returns B | G << 8 | R << 16 (0 where the map is invalid).  Integer parts
-// and roundings use float additions at 2^23 scale (round toward zero for
-// the floor of a non-negative coordinate, round to nearest even for the
-// result), which keeps the conversion unit out of the inner loop.
-__device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, long long pitch, int fmt, int sw,
-                                               int sh, const uint8_t* lut)
+// The remap of one pixel: the texel fetch and the LUT + bilinear finish.
+struct RemapTap {
+    uint32_t t00, t01, t10, t11;  // texels (x0,y0) (x1,y0) (x0,y1) (x1,y1)
+    float fx, fy;                 // fractional coordinates
+    int x0, y0;                   // -1: the map is invalid here
+};
+
+// Integer parts use a float addition at 2^23 scale (round toward zero: the
+// floor of a non-negative coordinate), which keeps the conversion unit out
+// of the inner loop.
+__device__ __forceinline__ void remapFetch(float2 m, const uint8_t* base, long long pitch, int fmt, int sw, int sh,
+                                           RemapTap& p)
 {
-    if (!(m.x >= 0.f && m.y >= 0.f && m.x < (float)sw && m.y < (float)sh)) return 0;
+    p.x0 = -1;
+    if (!(m.x >= 0.f && m.y >= 0.f && m.x < (float)sw && m.y < (float)sh)) return;
     const float tx = __fadd_rz(m.x, 8388608.f), ty = __fadd_rz(m.y, 8388608.f);  // 2^23 + floor
     const int x0 = __float_as_int(tx) - 0x4B000000, y0 = __float_as_int(ty) - 0x4B000000;
     const int x1 = min(x0 + 1, sw - 1), y1 = min(y0 + 1, sh - 1);
     const uint8_t* r0 = base + (size_t)y0 * pitch;
     const uint8_t* r1 = base + (size_t)y1 * pitch;
-    const uint32_t t00 = loadTexel(r0, x0, fmt), t01 = loadTexel(r0, x1, fmt);
-    const uint32_t t10 = loadTexel(r1, x0, fmt), t11 = loadTexel(r1, x1, fmt);
-    const float fx = m.x - (tx - 8388608.f), fy = m.y - (ty - 8388608.f);  // exact
-    const float gx = 1.f - fx, gy = 1.f - fy;
-    const float w00 = gx * gy, w01 = fx * gy, w10 = gx * fy, w11 = fx * fy;
+    p.t00 = loadTexel(r0, x0, fmt);
+    p.t01 = loadTexel(r0, x1, fmt);
+    p.t10 = loadTexel(r1, x0, fmt);
+    p.t11 = loadTexel(r1, x1, fmt);
+    p.fx = m.x - (tx - 8388608.f);  // exact
+    p.fy = m.y - (ty - 8388608.f);
+    p.x0 = x0;
+    p.y0 = y0;
+}
+
+// Returns B | G << 8 | R << 16 (0 where the map is invalid).
+__device__ __forceinline__ uint32_t remapFinish(const RemapTap& p, float2 m, const uint8_t* lut)
+{
+    if (p.x0 < 0) return 0;
+    const float gx = 1.f - p.fx, gy = 1.f - p.fy;
+    const float w00 = gx * gy, w01 = p.fx * gy, w10 = gx * p.fy, w11 = p.fx * p.fy;
     uint32_t out = 0;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const uint32_t sel = 0x4440u | (uint32_t)c;  // byte c, zero-extended
-        const int p00 = lut[c * 256 + __byte_perm(t00, 0, sel)];
-        const int p01 = lut[c * 256 + __byte_perm(t01, 0, sel)];
-        const int p10 = lut[c * 256 + __byte_perm(t10, 0, sel)];
-        const int p11 = lut[c * 256 + __byte_perm(t11, 0, sel)];
+        const int p00 = lut[c * 256 + __byte_perm(p.t00, 0, sel)];
+        const int p01 = lut[c * 256 + __byte_perm(p.t01, 0, sel)];
+        const int p10 = lut[c * 256 + __byte_perm(p.t10, 0, sel)];
+        const int p11 = lut[c * 256 + __byte_perm(p.t11, 0, sel)];
         const float r = fmaf(byteToFloat(p11), w11,
                              fmaf(byteToFloat(p10), w10, fmaf(byteToFloat(p01), w01, byteToFloat(p00) * w00)));
         // r lies in [-1e-4, 255 + 1e-4]; 1.5 * 2^23 + r rounds r to the
@@ -94,51 +112,105 @@ __device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, lo
         const float t = r + 12582912.f;
         int v = __float_as_int(t) - 0x4B400000;
         if (fabsf(r - (t - 12582912.f)) > 0.4998f)  // within 2e-4 of a tie: exact recompute
-            v = bilinearExact((double)m.x, (double)m.y, x0, y0, p00, p01, p10, p11);
+            v = bilinearExact((double)m.x, (double)m.y, p.x0, p.y0, p00, p01, p10, p11);
         out |= (uint32_t)v << (8 * c);
     }
     return out;
 }
 
+__device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, long long pitch, int fmt, int sw,
+                                               int sh, const uint8_t* lut)
+{
+    RemapTap p;
+    remapFetch(m, base, pitch, fmt, sw, sh, p);
+    return remapFinish(p, m, lut);
+}
+
 // Level-0 remap over the covered 32x16 tiles of every camera; each thread
 // remaps two pixels (rows ly and ly + 8) so two independent gathers are in
-// flight; the tile's map is 512 consecutive float2.
-__global__ void __launch_bounds__(kThreads) k_remap(const Segment* __restrict__ segs, int nsegs, int total)
+// flight; the tile's map is 512 consecutive float2.  A CTA walks a
+// contiguous run of items (camera-major, so the camera rarely changes): the
+// camera's constants and LUT are reloaded only when it does, and the next
+// item's map is loaded before the current item's gathers.
+struct RemapSeg {
+    const RemapItem* items;
+    int prefix, end;
+    const RigDev* R;
+    const FrameDev* F;
+};
+
+__device__ __forceinline__ RemapSeg remapSeg(const Segment* segs, int nsegs, int s, int total)
+{
+    const Segment& sg = segs[s];
+    return {static_cast<const RemapItem*>(sg.items), sg.prefix, s + 1 < nsegs ? segs[s + 1].prefix : total, sg.rig,
+            sg.frame};
+}
+
+__global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict__ segs, int nsegs, int total)
 {
     __shared__ uint8_t lut[3 * 256];
-    long long loaded = -1;
-    int s = 0, begin, end;
+    int begin, end;
     itemRange(total, begin, end);
     const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
     waitPrevGrid();
     allowNextGrid();
+    if (begin >= end) return;
+    int s = findSegment(segs, nsegs, begin, 0);
+    RemapSeg cur = remapSeg(segs, nsegs, s, total);
+    RemapItem item = cur.items[begin - cur.prefix];
+    const float2* mt = cur.R->maps + (size_t)item.mapTile * (kRemapTW * kRemapTH);
+    float2 m0 = __ldg(mt + threadIdx.x), m1 = __ldg(mt + threadIdx.x + kThreads);
+    // constants of the loaded camera
+    int camSeg = -1, cam = -1;
+    const uint8_t* base = nullptr;
+    long long pitch = 0;
+    int fmt = 0, sw = 0, sh = 0, W = 0, H = 0, gpitch = 0;
+    uint32_t* G = nullptr;
     for (int it = begin; it < end; it++) {
-        s = findSegment(segs, nsegs, it, s);
-        const Segment sg = segs[s];
-        const RemapItem item = static_cast<const RemapItem*>(sg.items)[it - sg.prefix];
-        const FrameDev& F = *sg.frame;
-        const RigDev& R = *sg.rig;
-        const float2* mt = R.maps + (size_t)item.mapTile * (kRemapTW * kRemapTH);
-        const float2 m0 = __ldg(mt + threadIdx.x), m1 = __ldg(mt + threadIdx.x + kThreads);
-        const long long key = ((long long)s << 16) | item.cam;
-        if (key != loaded) {  // uniform across the block
+        if (item.cam != cam || s != camSeg) {  // uniform across the block
+            const FrameDev& F = *cur.F;
+            const RigDev& R = *cur.R;
+            cam = item.cam;
+            camSeg = s;
+            base = F.src[cam];
+            pitch = F.srcPitch[cam];
+            fmt = F.srcFmt;
+            sw = R.srcW;
+            sh = R.srcH;
+            W = R.W;
+            H = R.H;
+            gpitch = R.lv[0].pitch;
+            G = reinterpret_cast<uint32_t*>(R.lv[0].G) + (size_t)cam * R.lv[0].camStride;
             __syncthreads();
-            const uint8_t* src = F.luts + item.cam * 768;
+            const uint8_t* src = F.luts + cam * 768;
             for (int k = threadIdx.x; k < 768; k += kThreads) lut[k] = __ldg(src + k);
             __syncthreads();
-            loaded = key;
         }
+        // the next item and its map
+        RemapItem nitem = item;
+        float2 n0 = m0, n1 = m1;
+        const int sCur = s;
+        if (it + 1 < end) {
+            if (it + 1 >= cur.end) {
+                s = findSegment(segs, nsegs, it + 1, s);
+                cur = remapSeg(segs, nsegs, s, total);
+            }
+            nitem = cur.items[it + 1 - cur.prefix];
+            const float2* nt = cur.R->maps + (size_t)nitem.mapTile * (kRemapTW * kRemapTH);
+            n0 = __ldg(nt + threadIdx.x);
+            n1 = __ldg(nt + threadIdx.x + kThreads);
+        }
+        const uint32_t v0 = remapPixel(m0, base, pitch, fmt, sw, sh, lut);
+        const uint32_t v1 = remapPixel(m1, base, pitch, fmt, sw, sh, lut);
         const int x = item.tx * kRemapTW + lx, y0 = item.ty * kRemapTH + ly, y1 = y0 + 8;
-        const uint8_t* base = F.src[item.cam];
-        const long long pitch = F.srcPitch[item.cam];
-        const uint32_t v0 = remapPixel(m0, base, pitch, F.srcFmt, R.srcW, R.srcH, lut);
-        const uint32_t v1 = remapPixel(m1, base, pitch, F.srcFmt, R.srcW, R.srcH, lut);
-        const LevelDev& L0 = R.lv[0];
-        uint32_t* G = reinterpret_cast<uint32_t*>(L0.G) + (size_t)item.cam * L0.camStride + x;
-        if (x < R.W) {
-            if (y0 < R.H) G[(size_t)y0 * L0.pitch] = v0;
-            if (y1 < R.H) G[(size_t)y1 * L0.pitch] = v1;
+        if (x < W) {
+            if (y0 < H) G[(size_t)y0 * gpitch + x] = v0;
+            if (y1 < H) G[(size_t)y1 * gpitch + x] = v1;
         }
+        (void)sCur;
+        item = nitem;
+        m0 = n0;
+        m1 = n1;
     }
 }
 
@@ -249,14 +321,19 @@ __global__ void __launch_bounds__(kThreads) k_reproject16s(const uint8_t* __rest
 // ============================================================================
 constexpr int kDInW = 2 * kDownTW + 3;   // 67
 constexpr int kDInH = 2 * kDownTH + 3;   // 35
+constexpr int kDInP = kDInW + 1;         // 68: row stride of the staged tile (16-byte aligned rows)
 
-constexpr int kDLoads = (kDInH * kDInW + kThreads - 1) / kThreads;   // 10 tile elements per thread
+constexpr int kDLoads = (kDInH * kDInW + kThreads - 1) / kThreads;   // 10 tile elements per thread (border tiles)
+constexpr int kDRows = (kDInH + 7) / 8;                               // 5 tile rows per warp (interior tiles)
 
+// The input tile is staged unpacked: element (r, c) holds the B|R and G|0
+// 16-bit lane pairs of the uchar4, so the filter passes add two channels per
+// 32-bit operation without unpacking every tap.
 struct DownSmem {
-    uint32_t in[kDInH][kDInW];
-    uint2 v[kDownTH][kDInW];
+    uint2 in[kDInH][kDInP];
+    uint2 v[kDownTH][kDInP];
     uint32_t magic[257];
-    int rowIdx[kDInH], colIdx[kDInW];  // border index tables of the current tile
+    int rowIdx[2][kDInH], colIdx[2][kDInW];  // border index tables, double-buffered across tiles
 };
 
 __device__ __forceinline__ void initMagic(uint32_t* magic)
@@ -274,63 +351,90 @@ __device__ __forceinline__ T ldLevel(const T* p)
     else return __ldg(p);
 }
 
-// One 32x16 output tile of one camera (all kThreads threads of the CTA).
+// The input tile of a 32x16 output tile of one camera, read into registers
+// (thread t holds elements t, t + 256, ... of the 35x67 tile in row-major
+// order), and the output's two alpha divisors.
+struct DownRegs {
+    uint32_t v[3 * kDRows];  // interior: per warp row, two elements + one of the last three; border: kDLoads elements
+    int m0, m1;
+};
+
+__device__ __forceinline__ bool downInterior(const RigDev& R, const DownItem& item)
+{
+    const LevelDev& Ls = R.lv[item.level - 1];
+    const int ix0 = 2 * item.tx * kDownTW - 2, iy0 = 2 * item.ty * kDownTH - 2;
+    return ix0 >= 0 && iy0 >= 0 && ix0 + kDInW <= Ls.w && iy0 + kDInH <= Ls.h;
+}
+
+// Border tiles: the row / column index tables (threads 0..101), read after
+// the caller's next barrier.
+__device__ __forceinline__ void downTables(const RigDev& R, const DownItem& item, int* rowIdx, int* colIdx)
+{
+    const LevelDev& Ls = R.lv[item.level - 1];
+    const int ix0 = 2 * item.tx * kDownTW - 2, iy0 = 2 * item.ty * kDownTH - 2;
+    if (threadIdx.x < kDInH) rowIdx[threadIdx.x] = rowMap(iy0 + (int)threadIdx.x, Ls.h);
+    else if (threadIdx.x < kDInH + kDInW) colIdx[threadIdx.x - kDInH] = colMap(ix0 + (int)threadIdx.x - kDInH, Ls.w);
+}
+
 template <bool kFresh>
-__device__ __forceinline__ void pyrDownTile(const RigDev& R, const DownItem item, DownSmem& sm)
+__device__ __forceinline__ void downLoad(const RigDev& R, const DownItem& item, bool interior, const int* rowIdx,
+                                         const int* colIdx, DownRegs& g)
 {
     const int ox = threadIdx.x & 31, oy = threadIdx.x >> 5;
     const LevelDev& Ls = R.lv[item.level - 1];
     const LevelDev& Ld = R.lv[item.level];
-    const int sw = Ls.w, sh = Ls.h;
     const int ox0 = item.tx * kDownTW, oy0 = item.ty * kDownTH;
     const int ix0 = 2 * ox0 - 2, iy0 = 2 * oy0 - 2;
     const uint32_t* G = reinterpret_cast<const uint32_t*>(Ls.G) + (size_t)item.cam * Ls.camStride;
-    // issue every load of the tile before the first barrier: the input tile and the two divisors
     const int X = ox0 + ox, Y0 = oy0 + oy, Y1 = Y0 + 8;
     const size_t o0 = (size_t)item.cam * Ld.camStride + (size_t)Y0 * Ld.pitch + X;
     const size_t o1 = o0 + (size_t)8 * Ld.pitch;
-    const bool ok0 = X < Ld.w && Y0 < Ld.h, ok1 = X < Ld.w && Y1 < Ld.h;
-    const int m0 = ok0 ? __ldg(Ld.Am + o0) : 0, m1 = ok1 ? __ldg(Ld.Am + o1) : 0;
-    uint32_t v[kDLoads];
-    const bool interior = ix0 >= 0 && iy0 >= 0 && ix0 + kDInW <= sw && iy0 + kDInH <= sh;
-    if (!interior) {
-        // one modulo per row / column instead of two per element
-        if (threadIdx.x < kDInH) sm.rowIdx[threadIdx.x] = rowMap(iy0 + (int)threadIdx.x, sh);
-        else if (threadIdx.x < kDInH + kDInW) sm.colIdx[threadIdx.x - kDInH] = colMap(ix0 + (int)threadIdx.x - kDInH, sw);
-        __syncthreads();
+    g.m0 = X < Ld.w && Y0 < Ld.h ? __ldg(Ld.Am + o0) : 0;
+    g.m1 = X < Ld.w && Y1 < Ld.h ? __ldg(Ld.Am + o1) : 0;
+    if (interior) {
+        // warp w loads tile rows w, w + 8, ...: columns 2*lane, 2*lane + 1 as one 8-byte load
+        // (ix0 is even and rows are 256-byte aligned), lanes 0..2 also column 64 + lane
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const uint32_t* row0 = G + (size_t)(iy0 + w) * Ls.pitch + ix0;
+#pragma unroll
+        for (int i = 0; i < kDRows; i++) {
+            if (w + 8 * i < kDInH) {
+                const uint32_t* row = row0 + (size_t)(8 * i) * Ls.pitch;
+                const uint2 a = ldLevel<kFresh>(reinterpret_cast<const uint2*>(row) + lane);
+                g.v[3 * i] = a.x;
+                g.v[3 * i + 1] = a.y;
+                g.v[3 * i + 2] = lane < kDInW - 64 ? ldLevel<kFresh>(row + 64 + lane) : 0u;
+            }
+        }
+        return;
     }
 #pragma unroll
     for (int q = 0; q < kDLoads; q++) {
         const int k = threadIdx.x + q * kThreads;
         if (k < kDInH * kDInW) {
             const int r = k / kDInW, c = k - r * kDInW;
-            const int gy = interior ? iy0 + r : sm.rowIdx[r];
-            const int gx = interior ? ix0 + c : sm.colIdx[c];
-            v[q] = ldLevel<kFresh>(G + (size_t)gy * Ls.pitch + gx);
+            g.v[q] = ldLevel<kFresh>(G + (size_t)rowIdx[r] * Ls.pitch + colIdx[c]);
         }
     }
-    __syncthreads();  // the previous tile's readers are done with shared memory
-#pragma unroll
-    for (int q = 0; q < kDLoads; q++) {
-        const int k = threadIdx.x + q * kThreads;
-        if (k < kDInH * kDInW) (&sm.in[0][0])[k] = v[q];
-    }
-    __syncthreads();
+}
+
+// Filter the staged tile: the caller has written it to sm.in and
+// synchronised.  Ends with the outputs stored.
+__device__ __forceinline__ void downCompute(const RigDev& R, const DownItem& item, const DownRegs& g, DownSmem& sm)
+{
+    const int ox = threadIdx.x & 31, oy = threadIdx.x >> 5;
+    const LevelDev& Ld = R.lv[item.level];
+    const int X = item.tx * kDownTW + ox, Y0 = item.ty * kDownTH + oy;
     for (int k = threadIdx.x; k < kDownTH * kDInW; k += kThreads) {
         const int r = k / kDInW, c = k - r * kDInW;
-        uint32_t lo = 0, hi = 0;
-#pragma unroll
-        for (int t = 0; t < 5; t++) {
-            const uint2 p = unpackBytes(sm.in[2 * r + t][c]);
-            lo += c_k5[t] * p.x;
-            hi += c_k5[t] * p.y;
-        }
-        sm.v[r][c] = make_uint2(lo, hi);
+        const uint2 p0 = sm.in[2 * r][c], p1 = sm.in[2 * r + 1][c], p2 = sm.in[2 * r + 2][c];
+        const uint2 p3 = sm.in[2 * r + 3][c], p4 = sm.in[2 * r + 4][c];
+        sm.v[r][c] = make_uint2(p0.x + 4 * (p1.x + p3.x) + 6 * p2.x + p4.x, p0.y + 4 * (p1.y + p3.y) + 6 * p2.y + p4.y);
     }
     __syncthreads();
 #pragma unroll
     for (int half = 0; half < 2; half++) {
-        const int r = oy + 8 * half;
+        const int r = oy + 8 * half, Y = Y0 + 8 * half;
         uint32_t lo = 0, hi = 0;
 #pragma unroll
         for (int t = 0; t < 5; t++) {
@@ -338,20 +442,67 @@ __device__ __forceinline__ void pyrDownTile(const RigDev& R, const DownItem item
             lo += c_k5[t] * q.x;
             hi += c_k5[t] * q.y;
         }
-        const int m = half ? m1 : m0;
+        const int m = half ? g.m1 : g.m0;
         uint32_t outv = 0;
         if (m) {
-            const unsigned long long mg = sm.magic[m];
-            const uint32_t b = (uint32_t)(((lo & 0xFFFFu) * mg) >> 24);
-            const uint32_t rr = (uint32_t)(((lo >> 16) * mg) >> 24);
-            const uint32_t g = (uint32_t)(((hi & 0xFFFFu) * mg) >> 24);
-            outv = b | (g << 8) | (rr << 16);
+            // floor(S / m) = floor(S * ceil(2^24 / m) / 2^24) = umulhi(S << 8, ceil(2^24 / m))
+            const uint32_t mg = sm.magic[m];
+            const uint32_t b = __umulhi((lo & 0xFFFFu) << 8, mg);
+            const uint32_t rr = __umulhi((lo >> 16) << 8, mg);
+            const uint32_t gg = __umulhi((hi & 0xFFFFu) << 8, mg);
+            outv = b | (gg << 8) | (rr << 16);
         }
-        if (half ? ok1 : ok0) reinterpret_cast<uint32_t*>(Ld.G)[half ? o1 : o0] = outv;
+        if (X < Ld.w && Y < Ld.h)
+            reinterpret_cast<uint32_t*>(Ld.G)[(size_t)item.cam * Ld.camStride + (size_t)Y * Ld.pitch + X] = outv;
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict__ segs, int nsegs, int total)
+__device__ __forceinline__ void downStage(const DownRegs& g, bool interior, DownSmem& sm)
+{
+    if (interior) {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+        for (int i = 0; i < kDRows; i++) {
+            const int r = w + 8 * i;
+            if (r < kDInH) {
+                const uint2 a = unpackBytes(g.v[3 * i]), b = unpackBytes(g.v[3 * i + 1]);
+                *reinterpret_cast<uint4*>(&sm.in[r][2 * lane]) = make_uint4(a.x, a.y, b.x, b.y);
+                if (lane < kDInW - 64) sm.in[r][64 + lane] = unpackBytes(g.v[3 * i + 2]);
+            }
+        }
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < kDLoads; q++) {
+        const int k = threadIdx.x + q * kThreads;
+        if (k < kDInH * kDInW) {
+            const int r = k / kDInW, c = k - r * kDInW;
+            sm.in[r][c] = unpackBytes(g.v[q]);
+        }
+    }
+}
+
+// One 32x16 output tile of one camera (all kThreads threads of the CTA),
+// without overlap (the tail kernel's few tiles).
+template <bool kFresh>
+__device__ __forceinline__ void pyrDownTile(const RigDev& R, const DownItem item, DownSmem& sm)
+{
+    const bool interior = downInterior(R, item);
+    if (!interior) {
+        downTables(R, item, sm.rowIdx[0], sm.colIdx[0]);
+        __syncthreads();
+    }
+    DownRegs g;
+    downLoad<kFresh>(R, item, interior, sm.rowIdx[0], sm.colIdx[0], g);
+    __syncthreads();  // the previous tile's readers are done with shared memory
+    downStage(g, interior, sm);
+    __syncthreads();
+    downCompute(R, item, g, sm);
+}
+
+// One CTA walks a contiguous run of tiles; the next tile's loads are issued
+// before the current tile is filtered, so their latency overlaps the work.
+__global__ void __launch_bounds__(kThreads, 4) k_pyrdown(const Segment* __restrict__ segs, int nsegs, int total)
 {
     __shared__ DownSmem sm;
     initMagic(sm.magic);
@@ -359,10 +510,37 @@ __global__ void __launch_bounds__(kThreads) k_pyrdown(const Segment* __restrict_
     itemRange(total, begin, end);
     waitPrevGrid();
     allowNextGrid();
+    if (begin >= end) return;
+    s = findSegment(segs, nsegs, begin, s);
+    const RigDev* R = segs[s].rig;
+    DownItem item = static_cast<const DownItem*>(segs[s].items)[begin - segs[s].prefix];
+    bool interior = downInterior(*R, item);
+    if (!interior) downTables(*R, item, sm.rowIdx[0], sm.colIdx[0]);
+    __syncthreads();
+    DownRegs g;
+    downLoad<false>(*R, item, interior, sm.rowIdx[0], sm.colIdx[0], g);
     for (int it = begin; it < end; it++) {
-        s = findSegment(segs, nsegs, it, s);
-        const Segment sg = segs[s];
-        pyrDownTile<false>(*sg.rig, static_cast<const DownItem*>(sg.items)[it - sg.prefix], sm);
+        const int buf = (it - begin + 1) & 1;  // tables of the next tile
+        const bool more = it + 1 < end;
+        int sn = s;
+        DownItem next = item;
+        bool nextInterior = true;
+        if (more) {
+            sn = findSegment(segs, nsegs, it + 1, s);
+            next = static_cast<const DownItem*>(segs[sn].items)[it + 1 - segs[sn].prefix];
+            nextInterior = downInterior(*segs[sn].rig, next);
+        }
+        __syncthreads();  // the previous tile's readers are done with shared memory
+        downStage(g, interior, sm);
+        if (more && !nextInterior) downTables(*segs[sn].rig, next, sm.rowIdx[buf], sm.colIdx[buf]);
+        __syncthreads();
+        const DownRegs cur = g;
+        if (more) downLoad<false>(*segs[sn].rig, next, nextInterior, sm.rowIdx[buf], sm.colIdx[buf], g);
+        downCompute(*R, item, cur, sm);
+        s = sn;
+        R = segs[s].rig;
+        item = next;
+        interior = nextInterior;
     }
 }
 
@@ -404,12 +582,18 @@ constexpr int kConsumers = kThreads;          // 8 warps
 constexpr int kBlendThreads = kConsumers + 32;  // + the producer warp
 constexpr int kConsumersYuv = kConsumers / 2;   // one chroma hand-over slot per odd-row thread
 
-struct alignas(16) BlendStage {
-    uint32_t gj[kCamsPerUnit][kBlendTH][kBlendTW];  // G_j, uchar4
-    uint16_t w[kCamsPerUnit][kBlendTH][kBlendTW];   // weights
-    uint32_t fp[kCamsPerUnit][kFH][kFpW];           // G_{j+1} footprint
-    uint2 cf[kFH][kCfW];                            // C_{j+1} footprint (short4 bits)
+// One unit's shared-memory stage: NC cameras of one tile (k_blend stages
+// two cameras per unit in a ring; the tail kernel stages up to eight at once).
+template <int NC>
+struct alignas(16) BlendStageT {
+    static constexpr int kCams = NC;
+    uint32_t gj[NC][kBlendTH][kBlendTW];  // G_j, uchar4
+    uint16_t w[NC][kBlendTH][kBlendTW];   // weights
+    uint32_t fp[NC][kFH][kFpW];           // G_{j+1} footprint
+    uint2 cf[kFH][kCfW];                  // C_{j+1} footprint (short4 bits)
 };
+using BlendStage = BlendStageT<kCamsPerUnit>;
+constexpr int kTailCamsPerUnit = 8;
 
 // What the consumers need of a unit besides its stage: the level geometry
 // and the frame's output, resolved once per unit (in k_blend by the
@@ -527,10 +711,11 @@ __device__ __forceinline__ int tileCam(const uint4& raw, const uint8_t* camLists
     return (int)((w >> (8 * (q & 3))) & 0xFF);
 }
 
+template <int NC = kCamsPerUnit>
 __device__ __forceinline__ int unitChunks(const uint4& raw)
 {
     const int cnt = (raw.x >> 16) & 0xFF;
-    return cnt <= kCamsPerUnit ? 1 : (cnt + kCamsPerUnit - 1) / kCamsPerUnit;
+    return cnt <= NC ? 1 : (cnt + NC - 1) / NC;
 }
 
 struct BlendAcc {
@@ -543,8 +728,8 @@ struct BlendAcc {
 // tail kernel).  Threads 0..kConsumers-1; the caller synchronises.
 // fRow / fCol: footprint index tables (kFH / kFW ints) filled here; sync is
 // the barrier over the calling threads.
-template <bool kFresh, class Sync>
-__device__ __forceinline__ void stageUnitDirect(BlendStage& S, const RigDev& R, const uint4& raw, int chunk, int* fRow,
+template <bool kFresh, class Stage, class Sync>
+__device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const uint4& raw, int chunk, int* fRow,
                                                 int* fCol, Sync sync)
 {
     const int lx = (threadIdx.x & 31) * 2, ly = threadIdx.x >> 5;
@@ -554,9 +739,10 @@ __device__ __forceinline__ void stageUnitDirect(BlendStage& S, const RigDev& R, 
     const bool hasUp = j < R.L;
     const LevelDev& Lu = R.lv[hasUp ? j + 1 : j];
     const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
-    const int c0 = chunk * kCamsPerUnit;
-    const int nc = max(0, min(kCamsPerUnit, camCnt - c0));
-    const bool last = chunk == unitChunks(raw) - 1;
+    constexpr int NC = Stage::kCams;
+    const int c0 = chunk * NC;
+    const int nc = max(0, min(NC, camCnt - c0));
+    const bool last = chunk == unitChunks<NC>(raw) - 1;
     const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
     for (int q = 0; q < nc; q++) {
         const int cam = tileCam(raw, R.camLists, c0 + q);
@@ -592,8 +778,8 @@ __device__ __forceinline__ void stageUnitDirect(BlendStage& S, const RigDev& R, 
 // collapse and store.  Threads 0..kConsumers-1, all of them (a YUV store
 // synchronises them with sync()).  staged: the unit came from the bulk
 // copies (weights absent for uniform tiles).
-template <class Sync>
-__device__ __forceinline__ void computeUnit(const BlendStage& S, const UnitGeo& G, const uint4& raw, int chunk,
+template <class Stage, class Sync>
+__device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, const uint4& raw, int chunk,
                                             bool staged, BlendAcc& acc, int2* xch, Sync sync)
 {
     const int lx = (threadIdx.x & 31) * 2, ly = threadIdx.x >> 5;
@@ -611,9 +797,10 @@ __device__ __forceinline__ void computeUnit(const BlendStage& S, const UnitGeo& 
     const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
     const bool rowOk = y < G.h;
     const bool active = !(j == 0 && cls == 0);
-    const int c0 = chunk * kCamsPerUnit;
-    const int nc = max(0, min(kCamsPerUnit, camCnt - c0));
-    const bool first = chunk == 0, last = chunk == unitChunks(raw) - 1;
+    constexpr int NC = Stage::kCams;
+    const int c0 = chunk * NC;
+    const int nc = max(0, min(NC, camCnt - c0));
+    const bool first = chunk == 0, last = chunk == unitChunks<NC>(raw) - 1;
     const bool fast = uni && staged;  // weights were not staged
     if (first) {
         acc.r0[0] = acc.r0[1] = acc.r0[2] = acc.r1[0] = acc.r1[1] = acc.r1[2] = 0;
@@ -937,7 +1124,7 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
 {
     __shared__ union {
         DownSmem down;
-        BlendStage blend;
+        BlendStageT<kTailCamsPerUnit> blend;
     } sm;
     __shared__ int fRow[kFH], fCol[kFW];
     __shared__ int2 xch[2 * kConsumersYuv];
@@ -961,7 +1148,7 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
         for (int k = rank; k < R.blendCnt[j]; k += cluster) {
             const uint4 raw = *reinterpret_cast<const uint4*>(items + k);
             const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
-            for (int chunk = 0; chunk < unitChunks(raw); chunk++) {
+            for (int chunk = 0; chunk < unitChunks<kTailCamsPerUnit>(raw); chunk++) {
                 __syncthreads();  // readers of the previous unit are done
                 if (active) stageUnitDirect<true>(sm.blend, R, raw, chunk, fRow, fCol, [] { __syncthreads(); });
                 __syncthreads();
@@ -1029,6 +1216,23 @@ static int gridFor(int total, int perSm)
     return total < cap ? total : cap;
 }
 
+// CTAs of `kernel` that fit on one SM (registers, shared memory, threads),
+// so a grid of residentPerSm * SMs runs in a single wave; cached per kernel.
+template <auto Kernel>
+static int residentPerSm(int threads, size_t dynSmem = 0)
+{
+    static int cached = 0;  // one per kernel
+    if (!cached) {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, Kernel, threads, dynSmem) != cudaSuccess || n < 1) {
+            cudaGetLastError();
+            n = 1;
+        }
+        cached = n;
+    }
+    return cached;
+}
+
 // Every per-frame kernel is launched with programmatic stream serialisation,
 // so its prologue overlaps the previous kernel's tail (see waitPrevGrid).
 template <class... Args>
@@ -1050,20 +1254,20 @@ static cudaError_t launchPdl(void (*kernel)(Args...), int grid, int block, cudaS
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_remap, gridFor(total, 8), kThreads, st, segs, nsegs, total);
+    return launchPdl(k_remap, gridFor(total, residentPerSm<k_remap>(kThreads)), kThreads, st, segs, nsegs, total);
 }
 
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_pyrdown, gridFor(total, 6), kThreads, st, segs, nsegs, total);
+    return launchPdl(k_pyrdown, gridFor(total, residentPerSm<k_pyrdown>(kThreads)), kThreads, st, segs, nsegs, total);
 }
 
 cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(gridFor(total, 8));
+    cfg.gridDim = dim3(gridFor(total, residentPerSm<k_linear>(kThreads, (size_t)PS_MAX_CAMS * 768)));
     cfg.blockDim = dim3(kThreads);
     cfg.dynamicSmemBytes = (size_t)maxCams * 768;
     cfg.stream = st;
@@ -1078,7 +1282,8 @@ cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams,
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_blend, gridFor(total, 4), kBlendThreads, st, segs, nsegs, total);
+    return launchPdl(k_blend, gridFor(total, residentPerSm<k_blend>(kBlendThreads)), kBlendThreads, st, segs, nsegs,
+                     total);
 }
 
 static int tailClusterSize()
