@@ -28,7 +28,7 @@ namespace ps {
 // ---- tiles ------------------------------------------------------------------
 constexpr int kRemapTW = 32, kRemapTH = 16;    // level-0 remap tile (two pixels per thread)
 constexpr int kDownTW = 32, kDownTH = 16;      // pyrDown output tile (two pixels per thread)
-constexpr int kBlendTW = 64, kBlendTH = 8;     // blend tile (two adjacent pixels per thread)
+constexpr int kBlendTW = 64, kBlendTH = 16;    // blend tile (a 2x2 pixel block per thread)
 constexpr int kThreads = 256;
 
 struct LevelDev {

@@ -558,9 +558,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_pyrdown(const Segment* __restri
 // A tile whose only camera has weight 256 on every pixel has N = L exactly
 // (R = 256 L, W = 256; (256 L + 128) >> 8 = L), so it skips the weights.
 //
-// A tile is 64x8 canvas pixels; consumer thread t (of 256) owns pixels
-// (2*(t%32), t/32) and the one to its right.  Work flows through a 3-stage
-// shared-memory ring of "units" (a tile and up to two of its cameras).  A
+// A tile is 64x16 canvas pixels; consumer thread t (of 256) owns the 2x2
+// block at (2*(t%32), 2*(t/32)), so the zero-inserted upsample's three
+// footprint rows serve both of its rows and the YUV chroma of the block is
+// its own.  Work flows through a 2-stage shared-memory ring of "units" (a
+// tile and up to two of its cameras).  A
 // dedicated producer warp stages each unit with bulk asynchronous copies of
 // whole rows -- the cameras' G_j and weight rows, their G_{j+1} footprint
 // rows and, with a tile's last unit, the C_{j+1} footprint rows -- completing
@@ -571,16 +573,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_pyrdown(const Segment* __restri
 // mapping.
 // ============================================================================
 constexpr int kFW = kBlendTW / 2 + 2;  // 34: footprint columns fx0 .. fx0+33
-constexpr int kFH = kBlendTH / 2 + 2;  // 6:  footprint rows    fy0 .. fy0+5
-constexpr int kFElems = kFW * kFH;     // 204
-constexpr int kBStages = 3;
+constexpr int kFH = kBlendTH / 2 + 2;  // 10: footprint rows    fy0 .. fy0+9
+constexpr int kFElems = kFW * kFH;     // 340
+constexpr int kBStages = 2;
 constexpr int kCamsPerUnit = 2;
 constexpr int kFpW = 40;   // staged footprint row: columns fx0-3 .. fx0+36 (16-byte aligned start)
 constexpr int kCfW = 36;   // staged collapse footprint row: columns fx0-1 .. fx0+34
 constexpr int kMaxSmemSegs = 64;
 constexpr int kConsumers = kThreads;          // 8 warps
 constexpr int kBlendThreads = kConsumers + 32;  // + the producer warp
-constexpr int kConsumersYuv = kConsumers / 2;   // one chroma hand-over slot per odd-row thread
 
 // One unit's shared-memory stage: NC cameras of one tile (k_blend stages
 // two cameras per unit in a ring; the tail kernel stages up to eight at once).
@@ -660,32 +661,23 @@ __device__ __forceinline__ int2 yuvChromaSums(uint32_t bgr)
     return make_int2(kUR * r + kUG * g + kUB * b + kCOff, kVR * r + kVG * g + kVB * b + kCOff);
 }
 
-// Level-0 store of a consumer thread's pixel pair as Y and, for even rows,
-// the block's U and V.  The block's lower-left pixel belongs to the next
-// consumer warp, so odd rows hand their chroma sums over through xch (two
-// alternating halves of 128 int2, so one barrier per tile suffices).
-// Every consumer thread must call this for the unit (it contains a barrier).
-template <class Sync>
-__device__ __forceinline__ void storeYuv(const UnitGeo& G, int x, int y, bool inside, uint32_t o0, uint32_t o1,
-                                         int2* xch, int& parity, Sync sync)
+// Level-0 store of a consumer thread's 2x2 block as four Y samples and the
+// block's U and V (from its left column, as cvtBGRToYUV2x2Block computes
+// them).  o[0] o[1] are the top pixels, o[2] o[3] the bottom ones.
+__device__ __forceinline__ void storeYuv(const UnitGeo& G, int x, int y, const uint32_t* o)
 {
-    const int lane = threadIdx.x & 31, ly = threadIdx.x >> 5;
-    int2* buf = xch + parity * (kConsumersYuv);
-    parity ^= 1;
-    const int2 c = yuvChromaSums(o0);
-    if (ly & 1) buf[(ly >> 1) * 32 + lane] = c;
-    sync();
-    if (!inside) return;
-    uint8_t* yrow = G.out + (size_t)y * G.outPitch + x;
-    const uint32_t y0 = yuvLuma(o0), y1 = yuvLuma(o1);
-    if ((reinterpret_cast<uintptr_t>(yrow) & 1) == 0) {
-        *reinterpret_cast<uint16_t*>(yrow) = (uint16_t)(y0 | (y1 << 8));
-    } else {
-        yrow[0] = (uint8_t)y0;
-        yrow[1] = (uint8_t)y1;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        uint8_t* yrow = G.out + (size_t)(y + r) * G.outPitch + x;
+        const uint32_t y0 = yuvLuma(o[2 * r]), y1 = yuvLuma(o[2 * r + 1]);
+        if ((reinterpret_cast<uintptr_t>(yrow) & 1) == 0) {
+            *reinterpret_cast<uint16_t*>(yrow) = (uint16_t)(y0 | (y1 << 8));
+        } else {
+            yrow[0] = (uint8_t)y0;
+            yrow[1] = (uint8_t)y1;
+        }
     }
-    if (ly & 1) return;
-    const int2 d = buf[(ly >> 1) * 32 + lane];
+    const int2 c = yuvChromaSums(o[0]), d = yuvChromaSums(o[2]);
     const uint8_t u = (uint8_t)clamp255((c.x + d.x) >> (kYuvShift + 1));
     const uint8_t v = (uint8_t)clamp255((c.y + d.y) >> (kYuvShift + 1));
     const size_t cy = (size_t)(y >> 1);
@@ -718,21 +710,25 @@ __device__ __forceinline__ int unitChunks(const uint4& raw)
     return cnt <= NC ? 1 : (cnt + NC - 1) / NC;
 }
 
+// Accumulators of a thread's 2x2 block: pixel p = 2 * row + column.
 struct BlendAcc {
-    int r0[3], r1[3];
-    int wsum0, wsum1;
-    int parity = 0;  // half of the chroma hand-over buffer in use
+    int r[4][3];
+    int wsum[4];
 };
 
 // Stage one unit with index-mapped loads (border tiles; every tile of the
 // tail kernel).  Threads 0..kConsumers-1; the caller synchronises.
 // fRow / fCol: footprint index tables (kFH / kFW ints) filled here; sync is
 // the barrier over the calling threads.
+// half >= 0 stages only what computeUnitRows reads for that 64x8 half:
+// its eight rows and footprint rows 4*half .. 4*half+5.
 template <bool kFresh, class Stage, class Sync>
 __device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const uint4& raw, int chunk, int* fRow,
-                                                int* fCol, Sync sync)
+                                                int* fCol, Sync sync, int half = -1)
 {
-    const int lx = (threadIdx.x & 31) * 2, ly = threadIdx.x >> 5;
+    const int lx = (threadIdx.x & 31) * 2;
+    const int ly = half < 0 ? (threadIdx.x >> 5) * 2 : 8 * half + (threadIdx.x >> 5);
+    const int rowsPerThread = half < 0 ? 2 : 1;
     const int j = raw.x & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
     const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
     const LevelDev& Lj = R.lv[j];
@@ -746,56 +742,81 @@ __device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const
     const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
     for (int q = 0; q < nc; q++) {
         const int cam = tileCam(raw, R.camLists, c0 + q);
-        uint2 g = make_uint2(0, 0);
-        uint32_t w = 0;
-        if (y < Lj.h) {
-            const size_t o = (size_t)cam * Lj.camStride + (size_t)y * Lj.pitch + x;
-            g = ldLevel<kFresh>(reinterpret_cast<const uint2*>(Lj.G + o));
-            w = __ldg(reinterpret_cast<const uint32_t*>(Lj.Wt + o));
+        for (int r = 0; r < rowsPerThread; r++) {
+            uint2 g = make_uint2(0, 0);
+            uint32_t w = 0;
+            if (y + r < Lj.h) {  // columns up to the pitch are allocated (and zero beyond the width)
+                const size_t o = (size_t)cam * Lj.camStride + (size_t)(y + r) * Lj.pitch + x;
+                g = ldLevel<kFresh>(reinterpret_cast<const uint2*>(Lj.G + o));
+                w = __ldg(reinterpret_cast<const uint32_t*>(Lj.Wt + o));
+            }
+            *reinterpret_cast<uint2*>(&S.gj[q][ly + r][lx]) = g;
+            *reinterpret_cast<uint32_t*>(&S.w[q][ly + r][lx]) = w;
         }
-        *reinterpret_cast<uint2*>(&S.gj[q][ly][lx]) = g;
-        *reinterpret_cast<uint32_t*>(&S.w[q][ly][lx]) = w;
     }
     if (hasUp) {
         if (threadIdx.x < kFH) fRow[threadIdx.x] = rowMap(fy0 + (int)threadIdx.x, Lu.h);
         else if (threadIdx.x < kFH + kFW) fCol[threadIdx.x - kFH] = colMap(fx0 + (int)threadIdx.x - kFH, Lu.w);
         sync();
-        for (int k = threadIdx.x; k < nc * kFElems; k += kConsumers) {
-            const int q = k / kFElems, e = k - q * kFElems;
-            const int r = e / kFW, c = e - r * kFW;
+        const int rb = half < 0 ? 0 : 4 * half, nr = half < 0 ? kFH : 6;
+        const int elems = nr * kFW;
+        for (int k = threadIdx.x; k < nc * elems; k += kConsumers) {
+            const int q = k / elems, e = k - q * elems;
+            const int r = rb + e / kFW, c = e % kFW;
             const int cam = tileCam(raw, R.camLists, c0 + q);
             S.fp[q][r][c + 3] = ldLevel<kFresh>(reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
-                                      (size_t)fRow[r] * Lu.pitch + fCol[c]);
+                                                (size_t)fRow[r] * Lu.pitch + fCol[c]);
         }
-        if (last && threadIdx.x < kFElems) {
-            const int r = threadIdx.x / kFW, c = threadIdx.x - r * kFW;
-            S.cf[r][c + 1] = ldLevel<kFresh>(reinterpret_cast<const uint2*>(Lu.C + (size_t)fRow[r] * Lu.pitch + fCol[c]));
-        }
+        if (last)
+            for (int k = threadIdx.x; k < elems; k += kConsumers) {
+                const int r = rb + k / kFW, c = k % kFW;
+                S.cf[r][c + 1] =
+                    ldLevel<kFresh>(reinterpret_cast<const uint2*>(Lu.C + (size_t)fRow[r] * Lu.pitch + fCol[c]));
+            }
     }
 }
 
 // Accumulate one unit from its stage; at a tile's last unit normalise,
-// collapse and store.  Threads 0..kConsumers-1, all of them (a YUV store
-// synchronises them with sync()).  staged: the unit came from the bulk
-// copies (weights absent for uniform tiles).
-template <class Stage, class Sync>
-__device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, const uint4& raw, int chunk,
-                                            bool staged, BlendAcc& acc, int2* xch, Sync sync)
+// collapse and store.  Threads 0..kConsumers-1.  staged: the unit came from
+// the bulk copies (weights absent for uniform tiles).
+//
+// Thread (lane, warp) owns rows ly = 2*warp, ly + 1 and columns lx = 2*lane,
+// lx + 1 of the tile.  The zero-inserted upsample (weights 1 6 1 for an even
+// output row / column, 4 4 for an odd one) reads footprint rows warp ..
+// warp+2 (even row: all three; odd row: the last two) and columns lane ..
+// lane+2 the same way.
+__device__ __forceinline__ void upsample2x2(const uint32_t* g, int pitchW, uint32_t* ulo, uint32_t* uhi)
 {
-    const int lx = (threadIdx.x & 31) * 2, ly = threadIdx.x >> 5;
-    // vertical taps of the zero-inserted upsample for this row's parity:
-    // even rows take footprint rows ly/2 .. ly/2+2 with weights 1 6 1,
-    // odd rows (ly+1)/2 .. (ly+1)/2+1 with weights 4 4
-    const bool evenRow = (ly & 1) == 0;
-    const int vr0 = evenRow ? ly / 2 : (ly - 1) / 2 + 1;
-    // footprint columns: even pixel fc .. fc+2 (1 6 1), odd pixel fc+1 .. fc+2 (4 4)
-    const int fc = lx / 2;
+    uint32_t elo[3], ehi[3], olo[3], ohi[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint2 a = unpackBytes(g[k]), b = unpackBytes(g[pitchW + k]), c = unpackBytes(g[2 * pitchW + k]);
+        elo[k] = a.x + 6 * b.x + c.x;
+        ehi[k] = a.y + 6 * b.y + c.y;
+        olo[k] = 4 * (b.x + c.x);
+        ohi[k] = 4 * (b.y + c.y);
+    }
+    ulo[0] = elo[0] + 6 * elo[1] + elo[2];
+    uhi[0] = ehi[0] + 6 * ehi[1] + ehi[2];
+    ulo[1] = 4 * (elo[1] + elo[2]);
+    uhi[1] = 4 * (ehi[1] + ehi[2]);
+    ulo[2] = olo[0] + 6 * olo[1] + olo[2];
+    uhi[2] = ohi[0] + 6 * ohi[1] + ohi[2];
+    ulo[3] = 4 * (olo[1] + olo[2]);
+    uhi[3] = 4 * (ohi[1] + ohi[2]);
+}
+
+template <class Stage>
+__device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, const uint4& raw, int chunk,
+                                            bool staged, BlendAcc& acc)
+{
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int lx = 2 * lane, ly = 2 * wp;
     const int j = raw.x & 0xFF, cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
     const bool uni = ((raw.x >> 24) & kTileUniform) != 0;
     const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
     const bool hasUp = G.hasUp != 0;
     const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
-    const bool rowOk = y < G.h;
     const bool active = !(j == 0 && cls == 0);
     constexpr int NC = Stage::kCams;
     const int c0 = chunk * NC;
@@ -803,60 +824,219 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
     const bool first = chunk == 0, last = chunk == unitChunks<NC>(raw) - 1;
     const bool fast = uni && staged;  // weights were not staged
     if (first) {
-        acc.r0[0] = acc.r0[1] = acc.r0[2] = acc.r1[0] = acc.r1[1] = acc.r1[2] = 0;
-        acc.wsum0 = acc.wsum1 = 0;
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            acc.r[p][0] = acc.r[p][1] = acc.r[p][2] = 0;
+            acc.wsum[p] = 0;
+        }
     }
     if (active) {
         for (int q = 0; q < nc; q++) {
-            uint32_t u0lo = 0, u0hi = 0, u1lo = 0, u1hi = 0;
-            if (hasUp) {
-                const uint32_t* g = &S.fp[q][0][0] + 3;
-                uint32_t vlo[3], vhi[3];
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    const uint2 a = unpackBytes(g[vr0 * kFpW + fc + k]);
-                    const uint2 b = unpackBytes(g[(vr0 + 1) * kFpW + fc + k]);
-                    if (evenRow) {
-                        const uint2 c = unpackBytes(g[(vr0 + 2) * kFpW + fc + k]);
-                        vlo[k] = a.x + 6 * b.x + c.x;
-                        vhi[k] = a.y + 6 * b.y + c.y;
-                    } else {
-                        vlo[k] = 4 * (a.x + b.x);
-                        vhi[k] = 4 * (a.y + b.y);
-                    }
-                }
-                u0lo = vlo[0] + 6 * vlo[1] + vlo[2];
-                u0hi = vhi[0] + 6 * vhi[1] + vhi[2];
-                u1lo = 4 * (vlo[1] + vlo[2]);
-                u1hi = 4 * (vhi[1] + vhi[2]);
+            uint32_t ulo[4] = {0, 0, 0, 0}, uhi[4] = {0, 0, 0, 0};
+            if (hasUp) upsample2x2(&S.fp[q][wp][3 + lane], kFpW, ulo, uhi);
+            const uint2 gt = *reinterpret_cast<const uint2*>(&S.gj[q][ly][lx]);
+            const uint2 gb = *reinterpret_cast<const uint2*>(&S.gj[q][ly + 1][lx]);
+            const uint32_t gp[4] = {gt.x, gt.y, gb.x, gb.y};
+            uint32_t wq[2] = {0, 0};
+            if (!fast) {
+                wq[0] = *reinterpret_cast<const uint32_t*>(&S.w[q][ly][lx]);
+                wq[1] = *reinterpret_cast<const uint32_t*>(&S.w[q][ly + 1][lx]);
             }
-            const uint2 gq = *reinterpret_cast<const uint2*>(&S.gj[q][ly][lx]);
-            // L = G - ((U + 32) >> 6), per channel
-            const int l0b = (int)(gq.x & 0xFF) - (int)(((u0lo & 0xFFFFu) + 32) >> 6);
-            const int l0g = (int)((gq.x >> 8) & 0xFF) - (int)(((u0hi & 0xFFFFu) + 32) >> 6);
-            const int l0r = (int)((gq.x >> 16) & 0xFF) - (int)(((u0lo >> 16) + 32) >> 6);
-            const int l1b = (int)(gq.y & 0xFF) - (int)(((u1lo & 0xFFFFu) + 32) >> 6);
-            const int l1g = (int)((gq.y >> 8) & 0xFF) - (int)(((u1hi & 0xFFFFu) + 32) >> 6);
-            const int l1r = (int)((gq.y >> 16) & 0xFF) - (int)(((u1lo >> 16) + 32) >> 6);
-            if (fast) {
-                acc.r0[0] = l0b; acc.r0[1] = l0g; acc.r0[2] = l0r;
-                acc.r1[0] = l1b; acc.r1[1] = l1g; acc.r1[2] = l1r;
-            } else {
-                const uint32_t wq = *reinterpret_cast<const uint32_t*>(&S.w[q][ly][lx]);
-                const int w0 = (int)(wq & 0xFFFFu), w1 = (int)(wq >> 16);
-                acc.r0[0] += w0 * l0b; acc.r0[1] += w0 * l0g; acc.r0[2] += w0 * l0r;
-                acc.r1[0] += w1 * l1b; acc.r1[1] += w1 * l1g; acc.r1[2] += w1 * l1r;
-                acc.wsum0 += w0;
-                acc.wsum1 += w1;
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                // L = G - ((U + 32) >> 6), per channel
+                const int lb = (int)(gp[p] & 0xFF) - (int)(((ulo[p] & 0xFFFFu) + 32) >> 6);
+                const int lg = (int)((gp[p] >> 8) & 0xFF) - (int)(((uhi[p] & 0xFFFFu) + 32) >> 6);
+                const int lr = (int)((gp[p] >> 16) & 0xFF) - (int)(((ulo[p] >> 16) + 32) >> 6);
+                if (fast) {
+                    acc.r[p][0] = lb;
+                    acc.r[p][1] = lg;
+                    acc.r[p][2] = lr;
+                } else {
+                    const int w = (int)((wq[p >> 1] >> (16 * (p & 1))) & 0xFFFFu);
+                    acc.r[p][0] += w * lb;
+                    acc.r[p][1] += w * lg;
+                    acc.r[p][2] += w * lr;
+                    acc.wsum[p] += w;
+                }
             }
         }
     }
     if (!last) return;
-    int n0[3], n1[3];
+    int n[4][3];
     if (fast) {
 #pragma unroll
-        for (int c = 0; c < 3; c++) { n0[c] = acc.r0[c]; n1[c] = acc.r1[c]; }
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) n[p][c] = acc.r[p][c];
     } else if (G.full) {
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) n[p][c] = (acc.r[p][c] + 128) >> 8;
+    } else {
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int d = acc.wsum[p] ? acc.wsum[p] : 1;
+            const float inv = __frcp_rn((float)d);
+#pragma unroll
+            for (int c = 0; c < 3; c++) n[p][c] = divTrunc(acc.r[p][c], d, inv);
+        }
+    }
+    // collapse: + pyrUp32(C_{j+1})
+    if (hasUp && active) {
+        const uint2* cf = &S.cf[wp][1 + lane];
+        int e[3][3], o[3][3];  // vertical sums per footprint column, even / odd row
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint2 a = cf[k], b = cf[kCfW + k], c = cf[2 * kCfW + k];
+            const int av[3] = {(short)(a.x & 0xFFFF), (short)(a.x >> 16), (short)(a.y & 0xFFFF)};
+            const int bv[3] = {(short)(b.x & 0xFFFF), (short)(b.x >> 16), (short)(b.y & 0xFFFF)};
+            const int cv[3] = {(short)(c.x & 0xFFFF), (short)(c.x >> 16), (short)(c.y & 0xFFFF)};
+#pragma unroll
+            for (int ch = 0; ch < 3; ch++) {
+                e[k][ch] = av[ch] + 6 * bv[ch] + cv[ch];
+                o[k][ch] = 4 * (bv[ch] + cv[ch]);
+            }
+        }
+#pragma unroll
+        for (int ch = 0; ch < 3; ch++) {
+            n[0][ch] += (e[0][ch] + 6 * e[1][ch] + e[2][ch] + 32) >> 6;
+            n[1][ch] += (4 * (e[1][ch] + e[2][ch]) + 32) >> 6;
+            n[2][ch] += (o[0][ch] + 6 * o[1][ch] + o[2][ch] + 32) >> 6;
+            n[3][ch] += (4 * (o[1][ch] + o[2][ch]) + 32) >> 6;
+        }
+    }
+    if (j > 0) {
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            if (y + r >= G.h) break;
+            short4* Cj = G.C + (size_t)(y + r) * G.pitch + x;
+            const int* a = n[2 * r];
+            const int* b = n[2 * r + 1];
+            if (x + 1 < G.w) {
+                *reinterpret_cast<int4*>(Cj) =
+                    make_int4((int)((uint32_t)(uint16_t)a[0] | ((uint32_t)(uint16_t)a[1] << 16)),
+                              (int)(uint32_t)(uint16_t)a[2],
+                              (int)((uint32_t)(uint16_t)b[0] | ((uint32_t)(uint16_t)b[1] << 16)),
+                              (int)(uint32_t)(uint16_t)b[2]);
+            } else if (x < G.w) {
+                Cj[0] = make_short4((short)a[0], (short)a[1], (short)a[2], 0);
+            }
+        }
+        return;
+    }
+    // level 0 (the render's canvas is even in both directions, the blender's need not be)
+    if (y >= G.h || x >= G.w) return;
+    const int rows = y + 1 < G.h ? 2 : 1, cols = x + 1 < G.w ? 2 : 1;
+    uint32_t o[4] = {0, 0, 0, 0};
+    if (cls != 0) {
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+            o[p] = (uint32_t)min(max(n[p][0], 0), 255) | ((uint32_t)min(max(n[p][1], 0), 255) << 8) |
+                   ((uint32_t)min(max(n[p][2], 0), 255) << 16);
+        if (cls == 2) {
+            for (int r = 0; r < rows; r++) {
+                const uint8_t* um = G.um + (size_t)(y + r) * G.pitch + x;
+                if (!um[0]) o[2 * r] = 0;
+                if (cols == 2 && !um[1]) o[2 * r + 1] = 0;
+            }
+        }
+    }
+    if (G.outFmt == PS_FMT_YUV420P || G.outFmt == PS_FMT_NV12) {  // even sizes only (checked at the API)
+        storeYuv(G, x, y, o);
+        return;
+    }
+    for (int r = 0; r < rows; r++) {
+        uint8_t* orow = G.out + (size_t)(y + r) * G.outPitch;
+        if (G.outFmt == PS_FMT_BGR32) {
+            if (cols == 2 && (reinterpret_cast<uintptr_t>(orow) & 7) == 0) {
+                reinterpret_cast<uint2*>(orow)[x / 2] = make_uint2(o[2 * r], o[2 * r + 1]);
+            } else {
+                reinterpret_cast<uint32_t*>(orow)[x] = o[2 * r];
+                if (cols == 2) reinterpret_cast<uint32_t*>(orow)[x + 1] = o[2 * r + 1];
+            }
+        } else {
+            for (int i = 0; i < cols; i++) {
+                const uint32_t v = o[2 * r + i];
+                orow[3 * (x + i)] = v & 0xFF;
+                orow[3 * (x + i) + 1] = (v >> 8) & 0xFF;
+                orow[3 * (x + i) + 2] = (v >> 16) & 0xFF;
+            }
+        }
+    }
+}
+
+// The tail kernel's variant for levels above 0: one 64x8 half of a tile
+// (rows 8*half ..), consumer thread t owning pixels (2*(t%32), t/32) and the
+// one to its right, so all eight warps share the few tiles of these levels.
+// Same arithmetic as computeUnit; output is the collapsed level C_j.
+struct PairAcc {
+    int r0[3], r1[3];
+    int wsum0, wsum1;
+};
+
+template <class Stage>
+__device__ __forceinline__ void computeUnitRows(const Stage& S, const UnitGeo& G, const uint4& raw, int chunk,
+                                                PairAcc& acc, int half)
+{
+    const int lx = (threadIdx.x & 31) * 2, lr = threadIdx.x >> 5;  // row in the half tile
+    const int ly = 8 * half + lr;                                    // row in the tile
+    // vertical taps: even rows footprint rows ly/2 .. ly/2+2 (1 6 1), odd rows
+    // (ly+1)/2 .. (ly+1)/2+1 (4 4); footprint columns lx/2 .. lx/2+2 as in computeUnit
+    const bool evenRow = (ly & 1) == 0;
+    const int vr0 = evenRow ? ly / 2 : (ly + 1) / 2;
+    const int fc = lx / 2;
+    const int j = raw.x & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
+    const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
+    const bool hasUp = G.hasUp != 0;
+    const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
+    constexpr int NC = Stage::kCams;
+    const int c0 = chunk * NC;
+    const int nc = max(0, min(NC, camCnt - c0));
+    const bool first = chunk == 0, last = chunk == unitChunks<NC>(raw) - 1;
+    if (first) {
+        acc.r0[0] = acc.r0[1] = acc.r0[2] = acc.r1[0] = acc.r1[1] = acc.r1[2] = 0;
+        acc.wsum0 = acc.wsum1 = 0;
+    }
+    for (int q = 0; q < nc; q++) {
+        uint32_t u0lo = 0, u0hi = 0, u1lo = 0, u1hi = 0;
+        if (hasUp) {
+            const uint32_t* g = &S.fp[q][0][0] + 3;
+            uint32_t vlo[3], vhi[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const uint2 a = unpackBytes(g[vr0 * kFpW + fc + k]);
+                const uint2 b = unpackBytes(g[(vr0 + 1) * kFpW + fc + k]);
+                if (evenRow) {
+                    const uint2 c = unpackBytes(g[(vr0 + 2) * kFpW + fc + k]);
+                    vlo[k] = a.x + 6 * b.x + c.x;
+                    vhi[k] = a.y + 6 * b.y + c.y;
+                } else {
+                    vlo[k] = 4 * (a.x + b.x);
+                    vhi[k] = 4 * (a.y + b.y);
+                }
+            }
+            u0lo = vlo[0] + 6 * vlo[1] + vlo[2];
+            u0hi = vhi[0] + 6 * vhi[1] + vhi[2];
+            u1lo = 4 * (vlo[1] + vlo[2]);
+            u1hi = 4 * (vhi[1] + vhi[2]);
+        }
+        const uint2 gq = *reinterpret_cast<const uint2*>(&S.gj[q][ly][lx]);
+        const uint32_t wq = *reinterpret_cast<const uint32_t*>(&S.w[q][ly][lx]);
+        const int w0 = (int)(wq & 0xFFFFu), w1 = (int)(wq >> 16);
+        acc.r0[0] += w0 * ((int)(gq.x & 0xFF) - (int)(((u0lo & 0xFFFFu) + 32) >> 6));
+        acc.r0[1] += w0 * ((int)((gq.x >> 8) & 0xFF) - (int)(((u0hi & 0xFFFFu) + 32) >> 6));
+        acc.r0[2] += w0 * ((int)((gq.x >> 16) & 0xFF) - (int)(((u0lo >> 16) + 32) >> 6));
+        acc.r1[0] += w1 * ((int)(gq.y & 0xFF) - (int)(((u1lo & 0xFFFFu) + 32) >> 6));
+        acc.r1[1] += w1 * ((int)((gq.y >> 8) & 0xFF) - (int)(((u1hi & 0xFFFFu) + 32) >> 6));
+        acc.r1[2] += w1 * ((int)((gq.y >> 16) & 0xFF) - (int)(((u1lo >> 16) + 32) >> 6));
+        acc.wsum0 += w0;
+        acc.wsum1 += w1;
+    }
+    if (!last) return;
+    int n0[3], n1[3];
+    if (G.full) {
 #pragma unroll
         for (int c = 0; c < 3; c++) { n0[c] = (acc.r0[c] + 128) >> 8; n1[c] = (acc.r1[c] + 128) >> 8; }
     } else {
@@ -865,8 +1045,7 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
 #pragma unroll
         for (int c = 0; c < 3; c++) { n0[c] = divTrunc(acc.r0[c], d0, i0); n1[c] = divTrunc(acc.r1[c], d1, i1); }
     }
-    // collapse: + pyrUp32(C_{j+1})
-    if (hasUp && active) {
+    if (hasUp) {
         const uint2* cf = &S.cf[0][0] + 1;
         int v[3][3];
 #pragma unroll
@@ -891,58 +1070,15 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
             n1[c] += (4 * (v[1][c] + v[2][c]) + 32) >> 6;
         }
     }
-    if (j > 0) {
-        if (!rowOk) return;
-        short4* Cj = G.C + (size_t)y * G.pitch + x;
-        if (x + 1 < G.w) {
-            *reinterpret_cast<int4*>(Cj) =
-                make_int4((int)((uint32_t)(uint16_t)n0[0] | ((uint32_t)(uint16_t)n0[1] << 16)),
-                          (int)(uint32_t)(uint16_t)n0[2],
-                          (int)((uint32_t)(uint16_t)n1[0] | ((uint32_t)(uint16_t)n1[1] << 16)),
-                          (int)(uint32_t)(uint16_t)n1[2]);
-        } else if (x < G.w) {
-            Cj[0] = make_short4((short)n0[0], (short)n0[1], (short)n0[2], 0);
-        }
-        return;
-    }
-    uint32_t o0 = 0, o1 = 0;
-    if (cls != 0 && rowOk) {
-        o0 = (uint32_t)min(max(n0[0], 0), 255) | ((uint32_t)min(max(n0[1], 0), 255) << 8) |
-             ((uint32_t)min(max(n0[2], 0), 255) << 16);
-        o1 = (uint32_t)min(max(n1[0], 0), 255) | ((uint32_t)min(max(n1[1], 0), 255) << 8) |
-             ((uint32_t)min(max(n1[2], 0), 255) << 16);
-        if (cls == 2) {
-            const uint8_t* um = G.um + (size_t)y * G.pitch + x;
-            if (!um[0]) o0 = 0;
-            if (x + 1 < G.w && !um[1]) o1 = 0;
-        }
-    }
-    if (G.outFmt == PS_FMT_YUV420P || G.outFmt == PS_FMT_NV12) {
-        // widths and heights are even, so a pixel pair and a 2x2 block are
-        // inside or outside the canvas together
-        storeYuv(G, x, y, rowOk && x < G.w, o0, o1, xch, acc.parity, sync);
-        return;
-    }
-    if (!rowOk) return;
-    uint8_t* orow = G.out + (size_t)y * G.outPitch;
-    if (G.outFmt == PS_FMT_BGR32) {
-        if (x + 1 < G.w && ((reinterpret_cast<uintptr_t>(orow) & 7) == 0)) {
-            reinterpret_cast<uint2*>(orow)[x / 2] = make_uint2(o0, o1);
-        } else {
-            if (x < G.w) reinterpret_cast<uint32_t*>(orow)[x] = o0;
-            if (x + 1 < G.w) reinterpret_cast<uint32_t*>(orow)[x + 1] = o1;
-        }
-    } else {
-        if (x < G.w) {
-            orow[3 * x] = o0 & 0xFF;
-            orow[3 * x + 1] = (o0 >> 8) & 0xFF;
-            orow[3 * x + 2] = (o0 >> 16) & 0xFF;
-        }
-        if (x + 1 < G.w) {
-            orow[3 * x + 3] = o1 & 0xFF;
-            orow[3 * x + 4] = (o1 >> 8) & 0xFF;
-            orow[3 * x + 5] = (o1 >> 16) & 0xFF;
-        }
+    if (y >= G.h || j == 0) return;  // level 0 goes through computeUnit
+    short4* Cj = G.C + (size_t)y * G.pitch + x;
+    if (x + 1 < G.w) {
+        *reinterpret_cast<int4*>(Cj) = make_int4((int)((uint32_t)(uint16_t)n0[0] | ((uint32_t)(uint16_t)n0[1] << 16)),
+                                                 (int)(uint32_t)(uint16_t)n0[2],
+                                                 (int)((uint32_t)(uint16_t)n1[0] | ((uint32_t)(uint16_t)n1[1] << 16)),
+                                                 (int)(uint32_t)(uint16_t)n1[2]);
+    } else if (x < G.w) {
+        Cj[0] = make_short4((short)n0[0], (short)n0[1], (short)n0[2], 0);
     }
 }
 
@@ -954,7 +1090,6 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
     __shared__ Segment s_segs[kMaxSmemSegs];
     __shared__ int s_timeout;
     __shared__ int fRow[kFH], fCol[kFW];
-    __shared__ int2 xch[2 * kConsumersYuv];
     const Segment* segs = gsegs;
     if (nsegs <= kMaxSmemSegs) {
         for (int k = threadIdx.x; k < nsegs; k += kBlendThreads) s_segs[k] = gsegs[k];
@@ -1012,7 +1147,7 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                 const bool active = !(j == 0 && cls == 0);
                 if (active && rowsIn && fpIn && (nc > 0 || (hasUp && last))) {
                     ui.staged = 1;
-                    cb = 8 + (uni ? 0 : 8) + (hasUp ? kFH : 0);
+                    cb = kBlendTH + (uni ? 0 : kBlendTH) + (hasUp ? kFH : 0);
                     nCopies = nc * cb + (hasUp && last ? kFH : 0);
                 }
             }
@@ -1034,23 +1169,23 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                         const int q = k / cb;
                         int r = k - q * cb;
                         const int cam = tileCam(raw, R->camLists, chunk * kCamsPerUnit + q);
-                        if (r < 8) {
+                        if (r < kBlendTH) {
                             bulkCopy(&st[stg].gj[q][r][0],
                                      Lj.G + (size_t)cam * Lj.camStride + (size_t)(ty * kBlendTH + r) * Lj.pitch +
                                          tx * kBlendTW,
                                      kBlendTW * 4, &full[stg]);
                             continue;
                         }
-                        r -= 8;
+                        r -= kBlendTH;
                         if (!uni) {
-                            if (r < 8) {
+                            if (r < kBlendTH) {
                                 bulkCopy(&st[stg].w[q][r][0],
                                          Lj.Wt + (size_t)cam * Lj.camStride + (size_t)(ty * kBlendTH + r) * Lj.pitch +
                                              tx * kBlendTW,
                                          kBlendTW * 2, &full[stg]);
                                 continue;
                             }
-                            r -= 8;
+                            r -= kBlendTH;
                         }
                         bulkCopy(&st[stg].fp[q][r][0],
                                  Lu.G + (size_t)cam * Lu.camStride + (size_t)(fy0 + r) * Lu.pitch + (fx0 - 3), kFpW * 4,
@@ -1096,7 +1231,7 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                                    [] { namedBarrier(1, kConsumers); });
             namedBarrier(1, kConsumers);
         }
-        computeUnit(st[stg], ui.geo, raw, chunk, staged, acc, xch, [] { namedBarrier(2, kConsumers); });
+        computeUnit(st[stg], ui.geo, raw, chunk, staged, acc);
         if (active && !staged) fenceProxyAsync();  // our stage writes precede later bulk copies into it
         __syncwarp();
         if (lane == 0) mbarArrive(&empty[stg]);  // this warp is done with the stage
@@ -1120,14 +1255,16 @@ __device__ __forceinline__ void clusterSync()
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+union TailSmem {
+    DownSmem down;
+    BlendStageT<kTailCamsPerUnit> blend;
+};
+
 __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ segs, int nsegs, int cluster)
 {
-    __shared__ union {
-        DownSmem down;
-        BlendStageT<kTailCamsPerUnit> blend;
-    } sm;
+    extern __shared__ __align__(16) uint8_t tailSmem[];  // a TailSmem (dynamic: above the 48 KB static limit)
+    TailSmem& sm = *reinterpret_cast<TailSmem*>(tailSmem);
     __shared__ int fRow[kFH], fCol[kFW];
-    __shared__ int2 xch[2 * kConsumersYuv];
     const int rig = blockIdx.x / cluster, rank = blockIdx.x % cluster;
     initMagic(sm.down.magic);
     waitPrevGrid();
@@ -1141,18 +1278,26 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
         clusterSync();
     }
     BlendAcc acc;
+    PairAcc pacc;
     for (int j = R.L; j >= R.tailBlend; j--) {
         const BlendItem* items = R.blendItems + R.blendOff[j];
         UnitGeo geo;
         fillGeo(geo, R, *sg.frame, j);
-        for (int k = rank; k < R.blendCnt[j]; k += cluster) {
-            const uint4 raw = *reinterpret_cast<const uint4*>(items + k);
+        // levels above 0: half tiles with two pixels per thread, so the few
+        // tiles of these levels keep twice the CTAs and all warps busy;
+        // level 0 (tiny canvases only): whole tiles, 2x2 blocks
+        const int parts = j > 0 ? 2 : 1;
+        for (int k = rank; k < parts * R.blendCnt[j]; k += cluster) {
+            const uint4 raw = *reinterpret_cast<const uint4*>(items + k / parts);
             const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
             for (int chunk = 0; chunk < unitChunks<kTailCamsPerUnit>(raw); chunk++) {
                 __syncthreads();  // readers of the previous unit are done
-                if (active) stageUnitDirect<true>(sm.blend, R, raw, chunk, fRow, fCol, [] { __syncthreads(); });
+                if (active)
+                    stageUnitDirect<true>(sm.blend, R, raw, chunk, fRow, fCol, [] { __syncthreads(); },
+                                          j > 0 ? (k & 1) : -1);
                 __syncthreads();
-                computeUnit(sm.blend, geo, raw, chunk, false, acc, xch, [] { __syncthreads(); });
+                if (j > 0) computeUnitRows(sm.blend, geo, raw, chunk, pacc, k & 1);
+                else computeUnit(sm.blend, geo, raw, chunk, false, acc);
             }
         }
         clusterSync();
@@ -1291,10 +1436,12 @@ static int tailClusterSize()
     static int size = 0;
     if (size) return size;
     size = kTailCluster;
+    cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TailSmem));
     if (cudaFuncSetAttribute(k_tail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(kTailClusterWide);
         cfg.blockDim = dim3(kThreads);
+        cfg.dynamicSmemBytes = sizeof(TailSmem);
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = kTailClusterWide;
@@ -1317,7 +1464,7 @@ cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st)
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nsegs * cluster);
     cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = sizeof(TailSmem);
     cfg.stream = st;
     cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;

@@ -476,7 +476,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     hBlend_ = blend;
     hCams_ = cams;
     // levels with few tiles (from the top down) go to the tail kernel
-    const int kTailMaxItems = 32;
+    const int kTailMaxItems = 16;
     tailDown_ = L + 1;
     while (tailDown_ > 1 && downCnt_[tailDown_ - 1] <= kTailMaxItems) tailDown_--;
     tailBlend_ = L + 1;
