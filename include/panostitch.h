@@ -108,6 +108,17 @@ void ps_render_destroy(ps_render* r);
    axis).  Synchronises the stream. */
 int ps_render_prepare(ps_render* r, const ps_photo_param* params, int num_params, int high_quality_blend,
                       int blend_param, int src_w, int src_h, int dst_w, int dst_h, void* stream);
+/* CudaPanoramaRender2::prepare(path, ...) itself: the camera parameters
+   are read from a PTGui .pts file as loadPhotoParams does
+   (source/Warp/PhotoParam.cpp:681-771).  The reference's XML camera files
+   need ticpp and are PS_EINVAL here, as is a file without cameras ("load
+   photo params failed", RicohUtil.cpp:1111-1116). */
+int ps_render_prepare_file(ps_render* r, const char* path, int high_quality_blend, int blend_param, int src_w,
+                           int src_h, int dst_w, int dst_h, void* stream);
+/* loadPhotoParams alone: writes up to capacity parameters and the number
+   found to *num (0 when the file holds no usable cameras). */
+int ps_load_photo_params(const char* path, ps_photo_param* params, int capacity, int* num);
+
 /* Same, with explicit seam (unique) masks: num_params host arrays of
    dst_h*dst_w uint8 (non-zero = owned), each a subset of that camera's
    coverage; they replace getNonIntersectingMasks

@@ -37,6 +37,14 @@ public:
                                     srcSize.width, srcSize.height, dstSize.width, dstSize.height, stream));
     }
 
+    // CudaPanoramaRender2::prepare(path, ...) with a PTGui .pts camera file
+    bool prepare(const std::string& path, int highQualityBlend, int blendParam, const Size& srcSize,
+                 const Size& dstSize, void* stream = nullptr)
+    {
+        return ok(ps_render_prepare_file(r_, path.c_str(), highQualityBlend, blendParam, srcSize.width, srcSize.height,
+                                         dstSize.width, dstSize.height, stream));
+    }
+
     // CudaPanoramaRender2::render (source/Task/RicohUtil.cpp:1207-1339).  Like
     // the reference, LUTs that are not numImages x 3 x 256 are skipped with a
     // warning (:1239-1265) instead of failing the frame.

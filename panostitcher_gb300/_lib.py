@@ -79,6 +79,9 @@ _SIGS = [
                                    C.POINTER(Image), C.c_void_p]),
     ("ps_render_render_yuv", C.c_int, [C.c_void_p, C.POINTER(Image), C.c_int, C.c_void_p, C.c_int,
                                        C.POINTER(PlanarImage), C.c_void_p]),
+    ("ps_render_prepare_file", C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_int, C.c_void_p]),
+    ("ps_load_photo_params", C.c_int, [C.c_char_p, C.POINTER(PhotoParam), C.c_int, C.POINTER(C.c_int)]),
     ("ps_render_set_seam_rule", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_set_graph", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_clear", None, [C.c_void_p]),

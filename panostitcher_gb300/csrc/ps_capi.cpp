@@ -159,6 +159,33 @@ static int prepareRender(ps_render* r, const ps_photo_param* params, int num, in
     });
 }
 
+int ps_load_photo_params(const char* path, ps_photo_param* params, int capacity, int* num)
+{
+    return guarded([&] {
+        if (!path || !num || capacity < 0 || (capacity > 0 && !params)) fail(PS_EINVAL, "NULL argument");
+        const std::vector<ps_photo_param> p = ps::loadPhotoParams(path);
+        *num = (int)p.size();
+        for (int i = 0; i < capacity && i < (int)p.size(); i++) params[i] = p[i];
+    });
+}
+
+int ps_render_prepare_file(ps_render* r, const char* path, int high_quality_blend, int blend_param, int src_w,
+                           int src_h, int dst_w, int dst_h, void* stream)
+{
+    std::vector<ps_photo_param> p;
+    const int st = guarded([&] {
+        if (!r || !path) fail(PS_EINVAL, "NULL argument");
+        p = ps::loadPhotoParams(path);
+        if (p.empty()) fail(PS_EINVAL, "load photo params failed");  // RicohUtil.cpp:1111-1116
+    });
+    if (st != PS_OK) {
+        if (r) ps_render_clear(r);
+        return st;
+    }
+    return ps_render_prepare(r, p.data(), (int)p.size(), high_quality_blend, blend_param, src_w, src_h, dst_w, dst_h,
+                             stream);
+}
+
 int ps_render_prepare(ps_render* r, const ps_photo_param* params, int num_params, int high_quality_blend,
                       int blend_param, int src_w, int src_h, int dst_w, int dst_h, void* stream)
 {

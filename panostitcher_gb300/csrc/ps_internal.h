@@ -150,6 +150,11 @@ cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st);
 // linear-blend mode: LinearItems of every segment; maxCams sizes the LUT stage
 cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams, cudaStream_t st);
 
+// ---- camera parameter files (ps_params.cpp) ----------------------------------------
+// loadPhotoParams for PTGui .pts files; empty when the file holds no usable
+// cameras; throws PS_EINVAL for other file types or an unreadable file.
+std::vector<ps_photo_param> loadPhotoParams(const std::string& path);
+
 // ---- standalone primitives -------------------------------------------------------
 cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,
                                  const float* xmap, const float* ymap, long long mapPitch, int dstW, int dstH,

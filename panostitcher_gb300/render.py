@@ -131,6 +131,13 @@ class CudaPanoramaRender2:
                                                     _stream_handle(stream))
         return self._status(st, check)
 
+    def prepare_file(self, path: str, high_quality_blend: int, blend_param: int, src_size, dst_size, stream=None,
+                     check: bool = False) -> bool:
+        """prepare(path, highQualityBlend, blendParam, srcSize, dstSize) with a PTGui .pts camera file."""
+        st = lib().ps_render_prepare_file(self._h, path.encode(), high_quality_blend, blend_param, src_size[0],
+                                          src_size[1], dst_size[0], dst_size[1], _stream_handle(stream))
+        return self._status(st, check)
+
     def set_seam_rule(self, rule: int) -> None:
         """PS_SEAMS_NEAREST_AXIS (default) or PS_SEAMS_DISTANCE (getNonIntersectingMasks); next prepare."""
         check(lib().ps_render_set_seam_rule(self._h, rule))
@@ -338,6 +345,15 @@ def cvt_bgr32_to_yuv(src, planes: Sequence, fmt: int = L.PS_FMT_YUV420P, stream=
     s = as_image(src)
     d = as_planar(planes, fmt)
     check(lib().ps_cvt_bgr32_to_yuv(C.byref(s), C.byref(d), _stream_handle(stream)))
+
+
+def load_photo_params(path: str) -> list:
+    """loadPhotoParams for a PTGui .pts file: a list of parameter dicts."""
+    n = C.c_int(0)
+    check(lib().ps_load_photo_params(path.encode(), None, 0, C.byref(n)))
+    arr = (PhotoParam * max(1, n.value))()
+    check(lib().ps_load_photo_params(path.encode(), arr, n.value, C.byref(n)))
+    return [{k: getattr(arr[i], k) for k, _ in PhotoParam._fields_} for i in range(n.value)]
 
 
 def get_lut(k: float) -> np.ndarray:
