@@ -133,8 +133,14 @@ int ps_render_prepare_with_seams(ps_render* r, const ps_photo_param* params, int
    3*256 bytes (B, G, R), host memory; a malformed count is PS_EINVAL (the
    reference logs a warning and skips the correction).  dst: a dst_w x dst_h
    BGR32 or BGR24 image, host or device.  Host src / dst are copied inside
-   the call on the stream (pinned memory keeps the copies asynchronous);
-   device src / dst are read / written in place.  Does not synchronise. */
+   the call (pinned memory keeps the copies asynchronous); device src / dst
+   are read / written in place.  The work runs on the render's own copy-in,
+   compute and copy-out streams, and the caller's stream waits for its
+   completion; when every src and dst is host memory the run does not wait
+   for the caller's earlier work, so consecutive renders overlap their
+   uploads, stitching and downloads (double-buffered staging).  Host src
+   and dst must stay untouched until the caller's stream reaches the call.
+   Does not synchronise. */
 int ps_render_render(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,
                      ps_image* dst, void* stream);
 
@@ -174,7 +180,8 @@ int ps_render_is_full_mask(const ps_render* r);
 long long ps_render_resident_bytes(const ps_render* r);
 /* Device-resident frame buffers owned by the render (BGR32, pitch in
    bytes), one per camera: writing frames there and passing them as device
-   src avoids any copy. */
+   src avoids any copy.  They also stage host sources of every other render
+   call, so do not mix the two on one render. */
 int ps_render_get_input_buffer(ps_render* r, int cam, void** data, long long* pitch);
 /* Copies of the prepared state to host memory, for parity checks:
    what: 0 x map (float, dst_h*dst_w, -1 where invalid), 1 y map (float),

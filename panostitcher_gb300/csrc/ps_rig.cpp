@@ -235,9 +235,9 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
         }
         hasMaps_ = true;
         inPitch_ = roundUp(srcW * 4, 256);
-        inputs_.alloc((size_t)inPitch_ * srcH * n);
+        inputs_.alloc((size_t)inPitch_ * srcH * n * kIoSlots);
         inputs_.zero(st);
-        output_.alloc(npx * 4);
+        output_.alloc(npx * 4 * kIoSlots);
         if (highQuality) preparePyramids(cov.as<uint8_t>(), seam.as<uint8_t>(), xmap.as<float>(), ymap.as<float>(), st);
         else prepareLinear(cov.as<uint8_t>(), seam.as<uint8_t>(), xmap.as<float>(), ymap.as<float>(), blendParam, st);
         PS_CUDA(cudaStreamSynchronize(st));
@@ -269,7 +269,7 @@ void Rig::prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* se
         }
         // CudaMultibandBlend.cpp:570-571
         if (!seams) distanceSeams(covDev_.as<uint8_t>(), n, W, H, seam.as<uint8_t>(), st);
-        output_.alloc(npx * 4);
+        output_.alloc(npx * 4 * kIoSlots);
         imgArgs_.alloc((sizeof(void*) + sizeof(long long)) * n);
         preparePyramids(covDev_.as<uint8_t>(), seam.as<uint8_t>(), nullptr, nullptr, st);
         PS_CUDA(cudaStreamSynchronize(st));
@@ -862,8 +862,32 @@ void Profiler::read(int kind, int level, long long* launches, double* ms, double
 // ---- Plan ---------------------------------------------------------------------------
 void Plan::dropGraph()
 {
-    if (graph_) cudaGraphExecDestroy(graph_);
-    graph_ = nullptr;
+    for (IoSlot& sl : io_) {
+        if (sl.graph) cudaGraphExecDestroy(sl.graph);
+        sl.graph = nullptr;
+    }
+}
+
+void Plan::ensureStreams()
+{
+    if (sComp_) return;
+    PS_CUDA(cudaStreamCreateWithFlags(&sIn_, cudaStreamNonBlocking));
+    PS_CUDA(cudaStreamCreateWithFlags(&sComp_, cudaStreamNonBlocking));
+    PS_CUDA(cudaStreamCreateWithFlags(&sOut_, cudaStreamNonBlocking));
+    PS_CUDA(cudaStreamCreateWithFlags(&capStream_, cudaStreamNonBlocking));
+    PS_CUDA(cudaEventCreateWithFlags(&callerEv_, cudaEventDisableTiming));
+    for (IoSlot& sl : io_) {
+        PS_CUDA(cudaEventCreateWithFlags(&sl.argsCopied, cudaEventDisableTiming));
+        PS_CUDA(cudaEventCreateWithFlags(&sl.computed, cudaEventDisableTiming));
+        PS_CUDA(cudaEventCreateWithFlags(&sl.downloaded, cudaEventDisableTiming));
+    }
+}
+
+// Wait until no run of this plan is in flight (before its buffers change).
+void Plan::quiesce()
+{
+    for (cudaStream_t st : {sIn_, sComp_, sOut_})
+        if (st) PS_CUDA(cudaStreamSynchronize(st));
 }
 
 void Plan::bind(const std::vector<Rig*>& rigs)
@@ -874,6 +898,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         if (!r || !r->ready()) fail(PS_ESTATE, "render not prepared");
         maxL = std::max(maxL, r->numLevels());
     }
+    quiesce();
     dropGraph();
     rigs_ = rigs;
     gens_.clear();
@@ -947,24 +972,26 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         addStep(2, parts, s);
     }
     const size_t need = segOff_ + std::max<size_t>(1, segs_.size()) * sizeof(Segment);
-    if (need > dArgs_.bytes()) {
-        if (stageUsed_) PS_CUDA(cudaEventSynchronize(stageDone_));
-        const size_t cap = need + need / 2;
-        dArgs_.alloc(cap);
-        stage_.alloc(cap);
-        stageUsed_ = false;
-    }
+    for (IoSlot& sl : io_)
+        if (need > sl.dArgs.bytes()) {
+            const size_t cap = need + need / 2;
+            sl.dArgs.alloc(cap);
+            sl.stage.alloc(cap);
+        }
     stageBytes_ = segOff_ + segs_.size() * sizeof(Segment);
-    const uintptr_t base = reinterpret_cast<uintptr_t>(dArgs_.get());
-    for (Segment& sg : segs_) sg.frame = reinterpret_cast<const FrameDev*>(base + reinterpret_cast<uintptr_t>(sg.frame));
-    if (!stageDone_) PS_CUDA(cudaEventCreateWithFlags(&stageDone_, cudaEventDisableTiming));
 }
 
 Plan::~Plan()
 {
+    for (cudaStream_t st : {sIn_, sComp_, sOut_})
+        if (st) cudaStreamSynchronize(st);
     dropGraph();
-    if (capStream_) cudaStreamDestroy(capStream_);
-    if (stageDone_) cudaEventDestroy(stageDone_);
+    for (cudaStream_t st : {sIn_, sComp_, sOut_, capStream_})
+        if (st) cudaStreamDestroy(st);
+    if (callerEv_) cudaEventDestroy(callerEv_);
+    for (IoSlot& sl : io_)
+        for (cudaEvent_t e : {sl.argsCopied, sl.computed, sl.downloaded})
+            if (e) cudaEventDestroy(e);
 }
 
 bool Plan::matches(const std::vector<Rig*>& rigs) const
@@ -975,9 +1002,9 @@ bool Plan::matches(const std::vector<Rig*>& rigs) const
     return true;
 }
 
-void Plan::launchAll(cudaStream_t st, Profiler* prof)
+void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
 {
-    const Segment* segs = reinterpret_cast<const Segment*>(static_cast<uint8_t*>(dArgs_.get()) + segOff_);
+    const Segment* segs = reinterpret_cast<const Segment*>(static_cast<const uint8_t*>(slot.dArgs.get()) + segOff_);
     for (const Step& s : steps_) {
         const Segment* p = segs + s.segOff;
         cudaEvent_t a = nullptr, b = nullptr;
@@ -1000,14 +1027,36 @@ void Plan::launchAll(cudaStream_t st, Profiler* prof)
 
 static int bytesPerPixel(int fmt) { return fmt == PS_FMT_BGR24 ? 3 : 4; }
 
+// One run, in three streams: copy-in (host frames, the staged arguments),
+// compute, copy-out (host canvases).  Runs alternate between two slots of
+// staging buffers; run k's copies wait only for run k - 2's use of the same
+// slot, so with host buffers on both sides consecutive runs overlap.  With
+// any device input or output the run also waits for the caller's stream.
+// The caller's stream waits for the run's completion.
 void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph, Profiler* prof)
 {
     if (prof && !prof->on()) prof = nullptr;
     if (prof) useGraph = false;
     if (in.size() != rigs_.size()) fail(PS_EINVAL, "plan input count mismatch");
-    if (stageUsed_) PS_CUDA(cudaEventSynchronize(stageDone_));  // the previous staging copy has been consumed
-    uint8_t* stage = stage_.as<uint8_t>();
-    uint8_t* dArgs = dArgs_.as<uint8_t>();
+    ensureStreams();
+    const int si = nextIo_;
+    IoSlot& S = io_[si];
+    bool hostOnly = true;
+    for (const FrameInput& f : in) {
+        if (!f.src) hostOnly = false;  // level 0 written on the caller's stream
+        else
+            for (int i = 0; i < (int)rigs_[&f - in.data()]->numImages(); i++)
+                if (f.src[i].location != PS_MEM_HOST) hostOnly = false;
+        if ((f.ydst ? f.ydst->location : f.dst->location) != PS_MEM_HOST) hostOnly = false;
+    }
+    if (S.used) PS_CUDA(cudaEventSynchronize(S.argsCopied));  // the slot's pinned stage is free again
+    PS_CUDA(cudaEventRecord(callerEv_, st));
+
+    // ---- copy-in
+    if (!hostOnly) PS_CUDA(cudaStreamWaitEvent(sIn_, callerEv_, 0));
+    if (S.used) PS_CUDA(cudaStreamWaitEvent(sIn_, S.computed, 0));  // run k - 2 is done with the slot's inputs
+    uint8_t* stage = S.stage.as<uint8_t>();
+    uint8_t* dArgs = S.dArgs.as<uint8_t>();
     for (size_t r = 0; r < rigs_.size(); r++) {
         Rig* rig = rigs_[r];
         const FrameInput& f = in[r];
@@ -1020,9 +1069,9 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
                 const ps_image& s = f.src[i];
                 if (s.location == PS_MEM_HOST) {
                     const size_t rowBytes = (size_t)s.width * bytesPerPixel(s.format);
-                    PS_CUDA(cudaMemcpy2DAsync(rig->inputBuffer(i), rig->inputPitch(), s.data, s.pitch, rowBytes,
-                                              s.height, cudaMemcpyHostToDevice, st));
-                    fd.src[i] = rig->inputBuffer(i);
+                    PS_CUDA(cudaMemcpy2DAsync(rig->inputBuffer(i, si), rig->inputPitch(), s.data, s.pitch, rowBytes,
+                                              s.height, cudaMemcpyHostToDevice, sIn_));
+                    fd.src[i] = rig->inputBuffer(i, si);
                     fd.srcPitch[i] = rig->inputPitch();
                 } else {
                     fd.src[i] = static_cast<const uint8_t*>(s.data);
@@ -1040,7 +1089,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
             const ps_planar_image& d = *f.ydst;
             if (d.location == PS_MEM_HOST) {  // planes staged tightly in the output buffer, then downloaded
                 const size_t luma = (size_t)d.width * d.height;
-                fd.out = rig->outputBuffer();
+                fd.out = rig->outputBuffer(si);
                 fd.outPitch = d.width;
                 fd.outU = fd.out + luma;
                 fd.outCPitch = d.format == PS_FMT_NV12 ? d.width : d.width / 2;
@@ -1058,7 +1107,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         } else {
             const ps_image& d = *f.dst;
             if (d.location == PS_MEM_HOST) {
-                fd.out = rig->outputBuffer();
+                fd.out = rig->outputBuffer(si);
                 fd.outPitch = (long long)d.width * bytesPerPixel(d.format);
             } else {
                 fd.out = static_cast<uint8_t*>(d.data);
@@ -1069,56 +1118,74 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         fd.status = rig->statusWord();
         std::memcpy(stage + sizeof(FrameDev) * r, &fd, sizeof fd);
     }
-    if (!segs_.empty()) std::memcpy(stage + segOff_, segs_.data(), segs_.size() * sizeof(Segment));
-    PS_CUDA(cudaMemcpyAsync(dArgs, stage, stageBytes_, cudaMemcpyHostToDevice, st));
-    PS_CUDA(cudaEventRecord(stageDone_, st));
-    stageUsed_ = true;
+    if (!segs_.empty()) {
+        Segment* sg = reinterpret_cast<Segment*>(stage + segOff_);
+        const uintptr_t base = reinterpret_cast<uintptr_t>(dArgs);
+        for (size_t k = 0; k < segs_.size(); k++) {
+            sg[k] = segs_[k];
+            sg[k].frame = reinterpret_cast<const FrameDev*>(base + reinterpret_cast<uintptr_t>(segs_[k].frame));
+        }
+    }
+    PS_CUDA(cudaMemcpyAsync(dArgs, stage, stageBytes_, cudaMemcpyHostToDevice, sIn_));
+    PS_CUDA(cudaEventRecord(S.argsCopied, sIn_));
+
+    // ---- compute
+    PS_CUDA(cudaStreamWaitEvent(sComp_, S.argsCopied, 0));
+    if (!hostOnly) PS_CUDA(cudaStreamWaitEvent(sComp_, callerEv_, 0));
+    if (S.used) PS_CUDA(cudaStreamWaitEvent(sComp_, S.downloaded, 0));  // run k - 2 has read the output staging
     if (useGraph) {
-        if (!graph_) {
-            if (!capStream_) PS_CUDA(cudaStreamCreateWithFlags(&capStream_, cudaStreamNonBlocking));
+        if (!S.graph) {
             cudaGraph_t g = nullptr;
             PS_CUDA(cudaStreamBeginCapture(capStream_, cudaStreamCaptureModeThreadLocal));
             try {
-                launchAll(capStream_);
+                launchAll(S, capStream_);
             } catch (...) {
                 cudaStreamEndCapture(capStream_, &g);
                 if (g) cudaGraphDestroy(g);
                 throw;
             }
             PS_CUDA(cudaStreamEndCapture(capStream_, &g));
-            const cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
+            const cudaError_t e = cudaGraphInstantiate(&S.graph, g, 0);
             cudaGraphDestroy(g);
             PS_CUDA(e);
         }
-        PS_CUDA(cudaGraphLaunch(graph_, st));
+        PS_CUDA(cudaGraphLaunch(S.graph, sComp_));
     } else {
-        launchAll(st, prof);
+        launchAll(S, sComp_, prof);
     }
+    PS_CUDA(cudaEventRecord(S.computed, sComp_));
+
+    // ---- copy-out
+    PS_CUDA(cudaStreamWaitEvent(sOut_, S.computed, 0));
     for (size_t r = 0; r < rigs_.size(); r++) {
         if (in[r].ydst) {
             const ps_planar_image& d = *in[r].ydst;
             if (d.location != PS_MEM_HOST) continue;
-            const uint8_t* out = rigs_[r]->outputBuffer();
+            const uint8_t* out = rigs_[r]->outputBuffer(si);
             const size_t w = d.width, h = d.height, luma = w * h;
-            PS_CUDA(cudaMemcpy2DAsync(d.planes[0], d.pitches[0], out, w, w, h, cudaMemcpyDeviceToHost, st));
+            PS_CUDA(cudaMemcpy2DAsync(d.planes[0], d.pitches[0], out, w, w, h, cudaMemcpyDeviceToHost, sOut_));
             if (d.format == PS_FMT_NV12) {
                 PS_CUDA(cudaMemcpy2DAsync(d.planes[1], d.pitches[1], out + luma, w, w, h / 2, cudaMemcpyDeviceToHost,
-                                          st));
+                                          sOut_));
             } else {
                 PS_CUDA(cudaMemcpy2DAsync(d.planes[1], d.pitches[1], out + luma, w / 2, w / 2, h / 2,
-                                          cudaMemcpyDeviceToHost, st));
+                                          cudaMemcpyDeviceToHost, sOut_));
                 PS_CUDA(cudaMemcpy2DAsync(d.planes[2], d.pitches[2], out + luma + luma / 4, w / 2, w / 2, h / 2,
-                                          cudaMemcpyDeviceToHost, st));
+                                          cudaMemcpyDeviceToHost, sOut_));
             }
             continue;
         }
         const ps_image& d = *in[r].dst;
         if (d.location == PS_MEM_HOST) {
             const size_t rowBytes = (size_t)d.width * bytesPerPixel(d.format);
-            PS_CUDA(cudaMemcpy2DAsync(d.data, d.pitch, rigs_[r]->outputBuffer(), rowBytes, rowBytes, d.height,
-                                      cudaMemcpyDeviceToHost, st));
+            PS_CUDA(cudaMemcpy2DAsync(d.data, d.pitch, rigs_[r]->outputBuffer(si), rowBytes, rowBytes, d.height,
+                                      cudaMemcpyDeviceToHost, sOut_));
         }
     }
+    PS_CUDA(cudaEventRecord(S.downloaded, sOut_));
+    PS_CUDA(cudaStreamWaitEvent(st, S.downloaded, 0));
+    S.used = true;
+    nextIo_ = (si + 1) % Rig::kIoSlots;
 }
 
 }  // namespace ps

@@ -49,9 +49,16 @@ public:
     static long long estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH,
                                    int dstW, int dstH);
 
-    uint8_t* inputBuffer(int cam) const { return inputs_.as<uint8_t>() + (size_t)cam * inPitch_ * srcH_; }
+    // Device staging of host frames and of a host canvas: kIoSlots sets, so
+    // consecutive renders with host buffers overlap their copies (slot 0's
+    // frame buffers are also the ones ps_render_get_input_buffer exposes).
+    static constexpr int kIoSlots = 2;
+    uint8_t* inputBuffer(int cam, int slot = 0) const
+    {
+        return inputs_.as<uint8_t>() + ((size_t)slot * n_ + cam) * inPitch_ * srcH_;
+    }
     long long inputPitch() const { return inPitch_; }
-    uint8_t* outputBuffer() const { return output_.as<uint8_t>(); }
+    uint8_t* outputBuffer(int slot = 0) const { return output_.as<uint8_t>() + (size_t)slot * W_ * H_ * 4; }
     int* statusWord() const { return status_.as<int>(); }
 
     void exportState(int what, int cam, int level, void* host, long long bytes) const;
@@ -167,22 +174,32 @@ private:
         int level;      // level of the first rig in the step
         double bytes;   // algorithmic bytes of the step (all rigs)
     };
-    void launchAll(cudaStream_t st, Profiler* prof = nullptr);
+    // Per-run state, double-buffered: run k uses slot k % 2, so while run k
+    // computes, run k + 1 uploads and run k - 1 downloads.
+    struct IoSlot {
+        DevBuf dArgs;   // [FrameDev x nr][LUTs][Segment x nseg]
+        HostBuf stage;  // pinned staging copy of dArgs
+        cudaGraphExec_t graph = nullptr;
+        cudaEvent_t argsCopied = nullptr, computed = nullptr, downloaded = nullptr;
+        bool used = false;
+    };
+    void launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof = nullptr);
     void dropGraph();
+    void ensureStreams();
+    void quiesce();
 
     std::vector<Rig*> rigs_;
     std::vector<uint64_t> gens_;
     std::vector<Step> steps_;
-    std::vector<Segment> segs_;      // frame pointers already absolute
+    std::vector<Segment> segs_;      // frame pointers hold offsets into the args block
     std::vector<size_t> lutOff_;
     size_t segOff_ = 0, stageBytes_ = 0;
     int maxCams_ = 0;
-    DevBuf dArgs_;          // [FrameDev x nr][LUTs][Segment x nseg]
-    HostBuf stage_;         // pinned staging copy of dArgs_
-    cudaGraphExec_t graph_ = nullptr;
-    cudaStream_t capStream_ = nullptr;
-    cudaEvent_t stageDone_ = nullptr;
-    bool stageUsed_ = false;
+    IoSlot io_[Rig::kIoSlots];
+    int nextIo_ = 0;
+    // copy-in, compute and copy-out streams (non-blocking), the capture stream
+    cudaStream_t sIn_ = nullptr, sComp_ = nullptr, sOut_ = nullptr, capStream_ = nullptr;
+    cudaEvent_t callerEv_ = nullptr;
 };
 
 }  // namespace ps
