@@ -465,7 +465,9 @@ int ps_blender_blend(ps_blender* b, const void* const* images, const long long* 
                 fail(PS_EINVAL, "image %d: bad pitch or alignment", i);
         }
         checkImage(dst, b->rig.width(), b->rig.height(), "dst", 0);
-        b->rig.imagesToLevel0(images, pitches, image_format, toStream(stream));
+        const int slot = b->rig.peekSlot();  // the state slot the next run takes
+        PS_CUDA(cudaStreamWaitEvent(toStream(stream), b->rig.slotComputed(slot), 0));
+        b->rig.imagesToLevel0(images, pitches, image_format, slot, toStream(stream));
         if (!b->plan || !b->plan->matches({&b->rig})) b->plan.reset(new ps::Plan({&b->rig}));
         b->plan->run({ps::FrameInput{nullptr, nullptr, dst}}, toStream(stream), false);
     });

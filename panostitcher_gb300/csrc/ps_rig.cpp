@@ -111,7 +111,15 @@ static inline int roundUp(int a, int b) { return divUp(a, b) * b; }
 // ---- Rig ---------------------------------------------------------------------------
 void Rig::clear()
 {
-    for (auto& l : lv_) { l.G.reset(); l.Wt.reset(); l.Am.reset(); l.C.reset(); }
+    for (auto& l : lv_) {
+        for (int k = 0; k < kIoSlots; k++) {
+            l.G[k].reset();
+            l.C[k].reset();
+        }
+        l.Wt.reset();
+        l.Am.reset();
+    }
+    nextSlot_ = lastSlot_ = 0;
     maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset();
     imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
     hRemap_.clear();
@@ -133,6 +141,19 @@ void Rig::clear()
     gen_ = 0;
 }
 
+Rig::~Rig()
+{
+    for (cudaEvent_t* es : {slotComputed_, slotDownloaded_})
+        for (int k = 0; k < kIoSlots; k++)
+            if (es[k]) cudaEventDestroy(es[k]);
+}
+
+cudaEvent_t Rig::slotEvent(cudaEvent_t& e)
+{
+    if (!e) PS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return e;
+}
+
 void Rig::setGeometry(int n, int W, int H, int L)
 {
     n_ = n;
@@ -151,7 +172,10 @@ void Rig::setGeometry(int n, int W, int H, int L)
 long long Rig::residentBytes() const
 {
     long long b = 0;
-    for (const auto& l : lv_) b += l.G.bytes() + l.Wt.bytes() + l.Am.bytes() + l.C.bytes();
+    for (const auto& l : lv_) {
+        for (int k = 0; k < kIoSlots; k++) b += l.G[k].bytes() + l.C[k].bytes();
+        b += l.Wt.bytes() + l.Am.bytes();
+    }
     b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
     b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
     b += dLinear_.bytes() + linW_.bytes();
@@ -181,12 +205,14 @@ long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam
     int w = dstW, h = dstH;
     for (int j = 0; j <= L; j++) {
         const long long px = (long long)roundUp(w, 64) * h;
-        b += px * n * (4 + 2 + (j ? 2 : 0)) + (j ? px * 8 : 0);
+        b += px * n * (4 * kIoSlots + 2 + (j ? 2 : 0)) + (j ? px * 8 * kIoSlots : 0);
         w = (w + 1) / 2;
         h = (h + 1) / 2;
     }
     // maps bounded by the full canvas per camera, inputs, output, union mask
-    b += (long long)dstW * dstH * 8 * n + (long long)roundUp(srcW * 4, 256) * srcH * n + (long long)dstW * dstH * 5;
+    b += (long long)dstW * dstH * 8 * n +
+         ((long long)roundUp(srcW * 4, 256) * srcH * n + (long long)dstW * dstH * 4) * kIoSlots +
+         (long long)dstW * dstH;
     return b;
 }
 
@@ -295,15 +321,19 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     for (int j = 0; j <= L; j++) {
         const LevelGeom& g = geom_[j];
         const size_t plane = (size_t)g.pitch * g.h;
-        lv_[j].G.alloc(plane * n * 4);
-        lv_[j].G.zero(st);
+        for (int k = 0; k < kIoSlots; k++) {
+            lv_[j].G[k].alloc(plane * n * 4);
+            lv_[j].G[k].zero(st);
+        }
         lv_[j].Wt.alloc(plane * n * 2);
         lv_[j].Wt.zero(st);
         if (j > 0) {
             lv_[j].Am.alloc(plane * n * 2);
             lv_[j].Am.zero(st);
-            lv_[j].C.alloc(plane * 8);
-            lv_[j].C.zero(st);
+            for (int k = 0; k < kIoSlots; k++) {
+                lv_[j].C[k].alloc(plane * 8);
+                lv_[j].C[k].zero(st);
+            }
         }
     }
     union_.alloc((size_t)geom_[0].pitch * H);
@@ -529,13 +559,20 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         d.lv[j].h = g.h;
         d.lv[j].pitch = g.pitch;
         d.lv[j].camStride = (long long)g.pitch * g.h;
-        d.lv[j].G = lv_[j].G.as<uchar4>();
         d.lv[j].Wt = lv_[j].Wt.as<uint16_t>();
         d.lv[j].Am = lv_[j].Am.as<uint16_t>();
-        d.lv[j].C = lv_[j].C.as<short4>();
     }
-    dDesc_.alloc(sizeof(RigDev));
-    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), &d, sizeof d, cudaMemcpyHostToDevice, st));
+    // one descriptor per state slot, differing in the pyramid pointers
+    RigDev ds[kIoSlots];
+    for (int k = 0; k < kIoSlots; k++) {
+        ds[k] = d;
+        for (int j = 0; j <= L; j++) {
+            ds[k].lv[j].G = lv_[j].G[k].as<uchar4>();
+            ds[k].lv[j].C = lv_[j].C[k].as<short4>();
+        }
+    }
+    dDesc_.alloc(sizeof ds);
+    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), ds, sizeof ds, cudaMemcpyHostToDevice, st));
     PS_CUDA(cudaStreamSynchronize(st));
     gen_ = g_generation++;
 }
@@ -621,14 +658,16 @@ void Rig::prepareLinear(const uint8_t* cov, const uint8_t* seam, const float* xm
     d.lv[0].w = W;
     d.lv[0].h = H;
     d.lv[0].pitch = geom_[0].pitch;
-    dDesc_.alloc(sizeof(RigDev));
-    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), &d, sizeof d, cudaMemcpyHostToDevice, st));
+    RigDev ds[kIoSlots];
+    for (int k = 0; k < kIoSlots; k++) ds[k] = d;
+    dDesc_.alloc(sizeof ds);
+    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), ds, sizeof ds, cudaMemcpyHostToDevice, st));
     PS_CUDA(cudaStreamSynchronize(st));
     tailDown_ = tailBlend_ = 1;  // no pyramid
     gen_ = g_generation++;
 }
 
-void Rig::imagesToLevel0(const void* const* images, const long long* pitches, int fmt, cudaStream_t st)
+void Rig::imagesToLevel0(const void* const* images, const long long* pitches, int fmt, int slot, cudaStream_t st)
 {
     const size_t n = n_;
     std::vector<uint8_t> args((sizeof(void*) + sizeof(long long)) * n);
@@ -639,7 +678,7 @@ void Rig::imagesToLevel0(const void* const* images, const long long* pitches, in
     const LevelGeom& g = geom_[0];
     PS_CUDA(launchImagesToLevel0(imgArgs_.as<const void* const>(),
                                  reinterpret_cast<const long long*>(imgArgs_.as<uint8_t>() + sizeof(void*) * n), fmt,
-                                 n_, W_, H_, covDev_.as<uint8_t>(), (long long)W_ * H_, lv_[0].G.as<uchar4>(), g.pitch,
+                                 n_, W_, H_, covDev_.as<uint8_t>(), (long long)W_ * H_, lv_[0].G[slot].as<uchar4>(), g.pitch,
                                  (long long)g.pitch * g.h, status_.as<int>(), st));
     int status = 0;
     PS_CUDA(cudaMemcpyAsync(&status, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -723,7 +762,7 @@ void Rig::exportCollapsed(int level, int16_t* host, long long bytes, cudaStream_
     if (level < 1 || level > L_) fail(PS_EINVAL, "level %d out of range 1..%d", level, L_);
     const LevelGeom& g = geom_[level];
     if ((size_t)bytes < (size_t)g.w * g.h * 8) fail(PS_EINVAL, "buffer too small");
-    PS_CUDA(cudaMemcpy2DAsync(host, (size_t)g.w * 8, lv_[level].C.get(), (size_t)g.pitch * 8, (size_t)g.w * 8, g.h,
+    PS_CUDA(cudaMemcpy2DAsync(host, (size_t)g.w * 8, lv_[level].C[lastSlot_].get(), (size_t)g.pitch * 8, (size_t)g.w * 8, g.h,
                               cudaMemcpyDeviceToHost, st));
     PS_CUDA(cudaStreamSynchronize(st));
 }
@@ -870,9 +909,9 @@ void Plan::dropGraph()
 
 void Plan::ensureStreams()
 {
-    if (sComp_) return;
+    if (sIn_) return;
     PS_CUDA(cudaStreamCreateWithFlags(&sIn_, cudaStreamNonBlocking));
-    PS_CUDA(cudaStreamCreateWithFlags(&sComp_, cudaStreamNonBlocking));
+    for (cudaStream_t& c : sComp_) PS_CUDA(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
     PS_CUDA(cudaStreamCreateWithFlags(&sOut_, cudaStreamNonBlocking));
     PS_CUDA(cudaStreamCreateWithFlags(&capStream_, cudaStreamNonBlocking));
     PS_CUDA(cudaEventCreateWithFlags(&callerEv_, cudaEventDisableTiming));
@@ -886,7 +925,7 @@ void Plan::ensureStreams()
 // Wait until no run of this plan is in flight (before its buffers change).
 void Plan::quiesce()
 {
-    for (cudaStream_t st : {sIn_, sComp_, sOut_})
+    for (cudaStream_t st : {sIn_, sComp_[0], sComp_[1], sOut_})
         if (st) PS_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -913,6 +952,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
 
     steps_.clear();
     segs_.clear();
+    segRig_.clear();
     maxCams_ = 0;
     for (Rig* r : rigs) maxCams_ = std::max(maxCams_, r->numImages());
     auto addStep = [&](int kind, const std::vector<std::pair<int, std::pair<const void*, int>>>& parts, int step) {
@@ -920,6 +960,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         for (const auto& p : parts) {
             if (p.second.second <= 0) continue;
             // frame pointer holds the FrameDev offset until the buffer is known
+            segRig_.push_back(p.first);
             segs_.push_back({p.second.first, rigs[p.first]->deviceDesc(),
                              reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * p.first), p.second.second, s.total});
             s.total += p.second.second;
@@ -950,6 +991,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         Step s{3, (int)segs_.size(), 0, 0, -1, 0.0};
         for (int r = 0; r < nr; r++) {
             if (rigs[r]->linear() || !rigs[r]->hasTail()) continue;
+            segRig_.push_back(r);
             segs_.push_back({nullptr, rigs[r]->deviceDesc(), reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * r), 1,
                              s.total});
             s.total += 1;
@@ -983,10 +1025,10 @@ void Plan::bind(const std::vector<Rig*>& rigs)
 
 Plan::~Plan()
 {
-    for (cudaStream_t st : {sIn_, sComp_, sOut_})
+    for (cudaStream_t st : {sIn_, sComp_[0], sComp_[1], sOut_})
         if (st) cudaStreamSynchronize(st);
     dropGraph();
-    for (cudaStream_t st : {sIn_, sComp_, sOut_, capStream_})
+    for (cudaStream_t st : {sIn_, sComp_[0], sComp_[1], sOut_, capStream_})
         if (st) cudaStreamDestroy(st);
     if (callerEv_) cudaEventDestroy(callerEv_);
     for (IoSlot& sl : io_)
@@ -1051,10 +1093,16 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
     }
     if (S.used) PS_CUDA(cudaEventSynchronize(S.argsCopied));  // the slot's pinned stage is free again
     PS_CUDA(cudaEventRecord(callerEv_, st));
+    // each rig's state slot (pyramids, I/O staging); without sources it is
+    // the slot imagesToLevel0 just filled (peekSlot)
+    std::vector<int> rs(rigs_.size());
+    for (size_t r = 0; r < rigs_.size(); r++) rs[r] = rigs_[r]->acquireSlot();
+    cudaStream_t comp = sComp_[si];
 
-    // ---- copy-in
+    // ---- copy-in: after the previous kernels on the rigs' slots (inputs, pyramids) and on this args slot
     if (!hostOnly) PS_CUDA(cudaStreamWaitEvent(sIn_, callerEv_, 0));
-    if (S.used) PS_CUDA(cudaStreamWaitEvent(sIn_, S.computed, 0));  // run k - 2 is done with the slot's inputs
+    if (S.used) PS_CUDA(cudaStreamWaitEvent(sIn_, S.computed, 0));
+    for (size_t r = 0; r < rigs_.size(); r++) PS_CUDA(cudaStreamWaitEvent(sIn_, rigs_[r]->slotComputed(rs[r]), 0));
     uint8_t* stage = S.stage.as<uint8_t>();
     uint8_t* dArgs = S.dArgs.as<uint8_t>();
     for (size_t r = 0; r < rigs_.size(); r++) {
@@ -1069,9 +1117,9 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
                 const ps_image& s = f.src[i];
                 if (s.location == PS_MEM_HOST) {
                     const size_t rowBytes = (size_t)s.width * bytesPerPixel(s.format);
-                    PS_CUDA(cudaMemcpy2DAsync(rig->inputBuffer(i, si), rig->inputPitch(), s.data, s.pitch, rowBytes,
+                    PS_CUDA(cudaMemcpy2DAsync(rig->inputBuffer(i, rs[r]), rig->inputPitch(), s.data, s.pitch, rowBytes,
                                               s.height, cudaMemcpyHostToDevice, sIn_));
-                    fd.src[i] = rig->inputBuffer(i, si);
+                    fd.src[i] = rig->inputBuffer(i, rs[r]);
                     fd.srcPitch[i] = rig->inputPitch();
                 } else {
                     fd.src[i] = static_cast<const uint8_t*>(s.data);
@@ -1089,7 +1137,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
             const ps_planar_image& d = *f.ydst;
             if (d.location == PS_MEM_HOST) {  // planes staged tightly in the output buffer, then downloaded
                 const size_t luma = (size_t)d.width * d.height;
-                fd.out = rig->outputBuffer(si);
+                fd.out = rig->outputBuffer(rs[r]);
                 fd.outPitch = d.width;
                 fd.outU = fd.out + luma;
                 fd.outCPitch = d.format == PS_FMT_NV12 ? d.width : d.width / 2;
@@ -1107,7 +1155,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         } else {
             const ps_image& d = *f.dst;
             if (d.location == PS_MEM_HOST) {
-                fd.out = rig->outputBuffer(si);
+                fd.out = rig->outputBuffer(rs[r]);
                 fd.outPitch = (long long)d.width * bytesPerPixel(d.format);
             } else {
                 fd.out = static_cast<uint8_t*>(d.data);
@@ -1124,15 +1172,17 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         for (size_t k = 0; k < segs_.size(); k++) {
             sg[k] = segs_[k];
             sg[k].frame = reinterpret_cast<const FrameDev*>(base + reinterpret_cast<uintptr_t>(segs_[k].frame));
+            sg[k].rig = rigs_[segRig_[k]]->deviceDesc(rs[segRig_[k]]);
         }
     }
     PS_CUDA(cudaMemcpyAsync(dArgs, stage, stageBytes_, cudaMemcpyHostToDevice, sIn_));
     PS_CUDA(cudaEventRecord(S.argsCopied, sIn_));
 
-    // ---- compute
-    PS_CUDA(cudaStreamWaitEvent(sComp_, S.argsCopied, 0));
-    if (!hostOnly) PS_CUDA(cudaStreamWaitEvent(sComp_, callerEv_, 0));
-    if (S.used) PS_CUDA(cudaStreamWaitEvent(sComp_, S.downloaded, 0));  // run k - 2 has read the output staging
+    // ---- compute: one stream per args slot, so two runs' kernels can overlap
+    PS_CUDA(cudaStreamWaitEvent(comp, S.argsCopied, 0));
+    if (!hostOnly) PS_CUDA(cudaStreamWaitEvent(comp, callerEv_, 0));
+    for (size_t r = 0; r < rigs_.size(); r++)  // the output staging has been read out
+        PS_CUDA(cudaStreamWaitEvent(comp, rigs_[r]->slotDownloaded(rs[r]), 0));
     if (useGraph) {
         if (!S.graph) {
             cudaGraph_t g = nullptr;
@@ -1149,11 +1199,12 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
             cudaGraphDestroy(g);
             PS_CUDA(e);
         }
-        PS_CUDA(cudaGraphLaunch(S.graph, sComp_));
+        PS_CUDA(cudaGraphLaunch(S.graph, comp));
     } else {
-        launchAll(S, sComp_, prof);
+        launchAll(S, comp, prof);
     }
-    PS_CUDA(cudaEventRecord(S.computed, sComp_));
+    PS_CUDA(cudaEventRecord(S.computed, comp));
+    for (size_t r = 0; r < rigs_.size(); r++) PS_CUDA(cudaEventRecord(rigs_[r]->slotComputed(rs[r]), comp));
 
     // ---- copy-out
     PS_CUDA(cudaStreamWaitEvent(sOut_, S.computed, 0));
@@ -1161,7 +1212,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         if (in[r].ydst) {
             const ps_planar_image& d = *in[r].ydst;
             if (d.location != PS_MEM_HOST) continue;
-            const uint8_t* out = rigs_[r]->outputBuffer(si);
+            const uint8_t* out = rigs_[r]->outputBuffer(rs[r]);
             const size_t w = d.width, h = d.height, luma = w * h;
             PS_CUDA(cudaMemcpy2DAsync(d.planes[0], d.pitches[0], out, w, w, h, cudaMemcpyDeviceToHost, sOut_));
             if (d.format == PS_FMT_NV12) {
@@ -1178,11 +1229,12 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         const ps_image& d = *in[r].dst;
         if (d.location == PS_MEM_HOST) {
             const size_t rowBytes = (size_t)d.width * bytesPerPixel(d.format);
-            PS_CUDA(cudaMemcpy2DAsync(d.data, d.pitch, rigs_[r]->outputBuffer(si), rowBytes, rowBytes, d.height,
+            PS_CUDA(cudaMemcpy2DAsync(d.data, d.pitch, rigs_[r]->outputBuffer(rs[r]), rowBytes, rowBytes, d.height,
                                       cudaMemcpyDeviceToHost, sOut_));
         }
     }
     PS_CUDA(cudaEventRecord(S.downloaded, sOut_));
+    for (size_t r = 0; r < rigs_.size(); r++) PS_CUDA(cudaEventRecord(rigs_[r]->slotDownloaded(rs[r]), sOut_));
     PS_CUDA(cudaStreamWaitEvent(st, S.downloaded, 0));
     S.used = true;
     nextIo_ = (si + 1) % Rig::kIoSlots;

@@ -16,7 +16,9 @@ struct LevelGeom {
 class Rig {
 public:
     Rig() = default;
-    ~Rig() = default;
+    ~Rig();
+    Rig(const Rig&) = delete;
+    Rig& operator=(const Rig&) = delete;
 
     // CudaPanoramaRender2::prepare: maps + coverage from the camera
     // parameters; seams given, or derived by seamRule (PS_SEAMS_*).
@@ -64,8 +66,25 @@ public:
     void exportState(int what, int cam, int level, void* host, long long bytes) const;
     void exportCollapsed(int level, int16_t* host, long long bytes, cudaStream_t st) const;
 
+    // Per-frame state slots: the Gaussian and collapsed pyramids, the I/O
+    // staging and the device descriptor that points at them come in
+    // kIoSlots copies, so two frames of one rig can be in flight.  Runs take
+    // slots in turn.  slotComputed(s) follows the last kernels that used
+    // slot s (its pyramids and input staging are free again);
+    // slotDownloaded(s) follows the copy out of its output staging.
+    int acquireSlot()
+    {
+        const int s = nextSlot_;
+        nextSlot_ = (s + 1) % kIoSlots;
+        lastSlot_ = s;
+        return s;
+    }
+    int peekSlot() const { return nextSlot_; }
+    cudaEvent_t slotComputed(int slot) { return slotEvent(slotComputed_[slot]); }
+    cudaEvent_t slotDownloaded(int slot) { return slotEvent(slotDownloaded_[slot]); }
+
     // building blocks of launch plans
-    const RigDev* deviceDesc() const { return dDesc_.as<RigDev>(); }
+    const RigDev* deviceDesc(int slot = 0) const { return dDesc_.as<RigDev>() + slot; }
     const RemapItem* remapItems() const { return dRemap_.as<RemapItem>(); }
     int numRemapItems() const { return (int)hRemap_.size(); }
     const DownItem* downItems(int level) const { return dDown_.as<DownItem>() + downOff_[level]; }
@@ -77,8 +96,8 @@ public:
     int tailBlend() const { return tailBlend_; }
     bool hasTail() const { return tailDown_ <= L_ || tailBlend_ <= L_; }
 
-    // blender input: int16x4 / uint8x4 device images -> level 0 (checks)
-    void imagesToLevel0(const void* const* images, const long long* pitches, int fmt, cudaStream_t st);
+    // blender input: int16x4 / uint8x4 device images -> level 0 of a slot (checks)
+    void imagesToLevel0(const void* const* images, const long long* pitches, int fmt, int slot, cudaStream_t st);
 
     // Bytes a step must move at minimum (each input / output element once,
     // no halo re-reads): kind 0 remap, 1 pyrDown to `level`, 2 blend of
@@ -91,8 +110,9 @@ public:
 
 private:
     struct LevelBufs {
-        DevBuf G, Wt, Am, C;
+        DevBuf G[kIoSlots], Wt, Am, C[kIoSlots];
     };
+    static cudaEvent_t slotEvent(cudaEvent_t& e);
     void setGeometry(int n, int W, int H, int L);
     void preparePyramids(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
                          cudaStream_t st);
@@ -101,6 +121,8 @@ private:
 
     int n_ = 0, W_ = 0, H_ = 0, L_ = 0, full_ = 0, srcW_ = 0, srcH_ = 0;
     bool hasMaps_ = false, linear_ = false;
+    int nextSlot_ = 0, lastSlot_ = 0;
+    cudaEvent_t slotComputed_[kIoSlots] = {}, slotDownloaded_[kIoSlots] = {};
     int numLinear_ = 0;
     DevBuf dLinear_, linW_;
     uint64_t gen_ = 0;
@@ -192,13 +214,14 @@ private:
     std::vector<uint64_t> gens_;
     std::vector<Step> steps_;
     std::vector<Segment> segs_;      // frame pointers hold offsets into the args block
+    std::vector<int> segRig_;        // rig of each segment (its descriptor depends on the rig's slot)
     std::vector<size_t> lutOff_;
     size_t segOff_ = 0, stageBytes_ = 0;
     int maxCams_ = 0;
     IoSlot io_[Rig::kIoSlots];
     int nextIo_ = 0;
     // copy-in, compute and copy-out streams (non-blocking), the capture stream
-    cudaStream_t sIn_ = nullptr, sComp_ = nullptr, sOut_ = nullptr, capStream_ = nullptr;
+    cudaStream_t sIn_ = nullptr, sComp_[Rig::kIoSlots] = {}, sOut_ = nullptr, capStream_ = nullptr;
     cudaEvent_t callerEv_ = nullptr;
 };
 
