@@ -570,7 +570,7 @@ def main(argv=None):
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
     ap.add_argument("--inflight", type=int, default=2, help="caller streams of the device-resident loop")
     ap.add_argument("--e2e-steps", type=int, default=0)
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0)
     ap.add_argument("--no-batched", action="store_true")

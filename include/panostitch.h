@@ -10,10 +10,11 @@
  *
  * Every entry point returns an int status (PS_OK or a PS_E* code) and never
  * throws; ps_last_error() returns the thread-local message of the last
- * failure.  All work is enqueued on the caller's CUDA stream (NULL = the
- * legacy default stream); no entry point synchronises the stream unless it
- * says so.  A ps_render is not thread-safe; distinct renders may be used
- * from different threads.
+ * failure.  Work is ordered on the caller's CUDA stream (NULL = the legacy
+ * default stream): the renders run on their own streams, and the caller's
+ * stream waits for each call's completion; no entry point synchronises the
+ * stream unless it says so.  A ps_render is not thread-safe; distinct
+ * renders may be used from different threads.
  *
  * Each declaration names the reference interface it replaces
  * (xpngzhng/PanoStitcher, path:line).
