@@ -1,0 +1,72 @@
+"""Renders in flight together (GPU).
+
+A render keeps two sets of per-frame state, so consecutive calls with host
+buffers, and calls issued on two streams, overlap on the GPU.  Every frame
+must still come out exactly as the oracle stitches it alone.
+"""
+import numpy as np
+import pytest
+
+import panostitcher_gb300 as P
+from panostitcher_gb300 import synth as S
+
+from _util import Prepared, diff_histogram
+
+pytestmark = pytest.mark.gpu
+
+FRAMES = 6
+
+
+@pytest.fixture(scope="module")
+def prepared(cuda, oracle_lib):
+    p = Prepared(S.scaled_rig(S.rig("c2"), 8))
+    frames = [p.frames.frame(k) for k in range(FRAMES)]
+    refs = [p.oracle_render(f, p.luts)[..., :3] for f in frames]
+    return p, frames, refs
+
+
+def test_host_buffers_back_to_back(prepared):
+    import torch
+    p, frames, refs = prepared
+    W, H = p.cfg.dst_size
+    outs = [np.zeros((H, W, 4), np.uint8) for _ in frames]
+    for f, o in zip(frames, outs):  # no synchronisation between the calls
+        assert p.r.render(f, o, p.luts, check=True)
+    torch.cuda.synchronize()
+    for k, (o, ref) in enumerate(zip(outs, refs)):
+        assert np.array_equal(o[..., :3], ref), (k, diff_histogram(o[..., :3], ref))
+
+
+def test_device_buffers_on_two_streams(prepared):
+    import torch
+    p, frames, refs = prepared
+    W, H = p.cfg.dst_size
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    dev_frames = [[torch.from_numpy(np.ascontiguousarray(c)).cuda() for c in f] for f in frames]
+    outs = [torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda") for _ in frames]
+    torch.cuda.synchronize()
+    for k in range(FRAMES):
+        assert p.r.render(dev_frames[k], outs[k], p.luts, stream=streams[k % 2], check=True)
+    torch.cuda.synchronize()
+    for k, (o, ref) in enumerate(zip(outs, refs)):
+        got = o.cpu().numpy()[..., :3]
+        assert np.array_equal(got, ref), (k, diff_histogram(got, ref))
+
+
+def test_yuv_and_bgr_interleaved(prepared):
+    import oracle as O
+    import torch
+    p, frames, refs = prepared
+    W, H = p.cfg.dst_size
+    bgr = [np.zeros((H, W, 4), np.uint8) for _ in range(3)]
+    nv12 = [[np.zeros((H, W), np.uint8), np.zeros((H // 2, W), np.uint8)] for _ in range(3)]
+    for k in range(3):
+        assert p.r.render(frames[2 * k], bgr[k], p.luts, check=True)
+        assert p.r.render_yuv(frames[2 * k + 1], nv12[k], p.luts, P.PS_FMT_NV12, check=True)
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert np.array_equal(bgr[k][..., :3], refs[2 * k])
+        full = np.zeros((H, W, 4), np.uint8)
+        full[..., :3] = refs[2 * k + 1]
+        for got, want in zip(nv12[k], O.bgr32_to_yuv(full, O.FMT_NV12)):
+            assert np.array_equal(got, want)
