@@ -137,11 +137,11 @@ int ps_render_prepare_with_seams(ps_render* r, const ps_photo_param* params, int
    the call (pinned memory keeps the copies asynchronous); device src / dst
    are read / written in place.  The work runs on the render's own copy-in,
    compute and copy-out streams, and the caller's stream waits for its
-   completion.  A render keeps two sets of per-frame state, so two calls can
-   be in flight: with host src and dst a call does not wait for the
+   completion.  A render keeps three sets of per-frame state, so three calls
+   can be in flight: with host src and dst a call does not wait for the
    caller's earlier work (consecutive calls overlap their uploads, kernels
    and downloads); with device src or dst it waits for the caller's stream,
-   so calls on two different streams overlap.  Host src and dst must stay
+   so calls on different streams overlap.  Host src and dst must stay
    untouched until the caller's stream reaches the call.  Does not
    synchronise. */
 int ps_render_render(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,

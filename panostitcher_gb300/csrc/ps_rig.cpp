@@ -156,6 +156,8 @@ cudaEvent_t Rig::slotEvent(cudaEvent_t& e)
 
 void Rig::setGeometry(int n, int W, int H, int L)
 {
+    slots_ = slotsWanted_;
+    nextSlot_ = lastSlot_ = 0;
     n_ = n;
     W_ = W;
     H_ = H;
@@ -197,7 +199,7 @@ static void validateParams(const ps_photo_param* params, int n, int srcW, int sr
 }
 
 long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
-                             int dstH)
+                             int dstH, int slots)
 {
     validateParams(params, n, srcW, srcH, dstW, dstH);
     const int L = std::max(0, trueNumLevels(dstW, dstH, blendParam, 2));
@@ -205,13 +207,13 @@ long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam
     int w = dstW, h = dstH;
     for (int j = 0; j <= L; j++) {
         const long long px = (long long)roundUp(w, 64) * h;
-        b += px * n * (4 * kIoSlots + 2 + (j ? 2 : 0)) + (j ? px * 8 * kIoSlots : 0);
+        b += px * n * (4 * slots + 2 + (j ? 2 : 0)) + (j ? px * 8 * slots : 0);
         w = (w + 1) / 2;
         h = (h + 1) / 2;
     }
     // maps bounded by the full canvas per camera, inputs, output, union mask
     b += (long long)dstW * dstH * 8 * n +
-         ((long long)roundUp(srcW * 4, 256) * srcH * n + (long long)dstW * dstH * 4) * kIoSlots +
+         ((long long)roundUp(srcW * 4, 256) * srcH * n + (long long)dstW * dstH * 4) * slots +
          (long long)dstW * dstH;
     return b;
 }
@@ -261,9 +263,9 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
         }
         hasMaps_ = true;
         inPitch_ = roundUp(srcW * 4, 256);
-        inputs_.alloc((size_t)inPitch_ * srcH * n * kIoSlots);
+        inputs_.alloc((size_t)inPitch_ * srcH * n * slots_);
         inputs_.zero(st);
-        output_.alloc(npx * 4 * kIoSlots);
+        output_.alloc(npx * 4 * slots_);
         if (highQuality) preparePyramids(cov.as<uint8_t>(), seam.as<uint8_t>(), xmap.as<float>(), ymap.as<float>(), st);
         else prepareLinear(cov.as<uint8_t>(), seam.as<uint8_t>(), xmap.as<float>(), ymap.as<float>(), blendParam, st);
         PS_CUDA(cudaStreamSynchronize(st));
@@ -295,7 +297,7 @@ void Rig::prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* se
         }
         // CudaMultibandBlend.cpp:570-571
         if (!seams) distanceSeams(covDev_.as<uint8_t>(), n, W, H, seam.as<uint8_t>(), st);
-        output_.alloc(npx * 4 * kIoSlots);
+        output_.alloc(npx * 4 * slots_);
         imgArgs_.alloc((sizeof(void*) + sizeof(long long)) * n);
         preparePyramids(covDev_.as<uint8_t>(), seam.as<uint8_t>(), nullptr, nullptr, st);
         PS_CUDA(cudaStreamSynchronize(st));
@@ -321,7 +323,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     for (int j = 0; j <= L; j++) {
         const LevelGeom& g = geom_[j];
         const size_t plane = (size_t)g.pitch * g.h;
-        for (int k = 0; k < kIoSlots; k++) {
+        for (int k = 0; k < slots_; k++) {
             lv_[j].G[k].alloc(plane * n * 4);
             lv_[j].G[k].zero(st);
         }
@@ -330,7 +332,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         if (j > 0) {
             lv_[j].Am.alloc(plane * n * 2);
             lv_[j].Am.zero(st);
-            for (int k = 0; k < kIoSlots; k++) {
+            for (int k = 0; k < slots_; k++) {
                 lv_[j].C[k].alloc(plane * 8);
                 lv_[j].C[k].zero(st);
             }
@@ -564,15 +566,15 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     }
     // one descriptor per state slot, differing in the pyramid pointers
     RigDev ds[kIoSlots];
-    for (int k = 0; k < kIoSlots; k++) {
+    for (int k = 0; k < slots_; k++) {
         ds[k] = d;
         for (int j = 0; j <= L; j++) {
             ds[k].lv[j].G = lv_[j].G[k].as<uchar4>();
             ds[k].lv[j].C = lv_[j].C[k].as<short4>();
         }
     }
-    dDesc_.alloc(sizeof ds);
-    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), ds, sizeof ds, cudaMemcpyHostToDevice, st));
+    dDesc_.alloc(sizeof(RigDev) * slots_);
+    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), ds, sizeof(RigDev) * slots_, cudaMemcpyHostToDevice, st));
     PS_CUDA(cudaStreamSynchronize(st));
     gen_ = g_generation++;
 }
@@ -659,9 +661,9 @@ void Rig::prepareLinear(const uint8_t* cov, const uint8_t* seam, const float* xm
     d.lv[0].h = H;
     d.lv[0].pitch = geom_[0].pitch;
     RigDev ds[kIoSlots];
-    for (int k = 0; k < kIoSlots; k++) ds[k] = d;
-    dDesc_.alloc(sizeof ds);
-    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), ds, sizeof ds, cudaMemcpyHostToDevice, st));
+    for (int k = 0; k < slots_; k++) ds[k] = d;
+    dDesc_.alloc(sizeof(RigDev) * slots_);
+    PS_CUDA(cudaMemcpyAsync(dDesc_.get(), ds, sizeof(RigDev) * slots_, cudaMemcpyHostToDevice, st));
     PS_CUDA(cudaStreamSynchronize(st));
     tailDown_ = tailBlend_ = 1;  // no pyramid
     gen_ = g_generation++;
@@ -925,7 +927,9 @@ void Plan::ensureStreams()
 // Wait until no run of this plan is in flight (before its buffers change).
 void Plan::quiesce()
 {
-    for (cudaStream_t st : {sIn_, sComp_[0], sComp_[1], sOut_})
+    for (cudaStream_t st : {sIn_, sOut_})
+        if (st) PS_CUDA(cudaStreamSynchronize(st));
+    for (cudaStream_t st : sComp_)
         if (st) PS_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -1025,10 +1029,14 @@ void Plan::bind(const std::vector<Rig*>& rigs)
 
 Plan::~Plan()
 {
-    for (cudaStream_t st : {sIn_, sComp_[0], sComp_[1], sOut_})
+    for (cudaStream_t st : {sIn_, sOut_})
+        if (st) cudaStreamSynchronize(st);
+    for (cudaStream_t st : sComp_)
         if (st) cudaStreamSynchronize(st);
     dropGraph();
-    for (cudaStream_t st : {sIn_, sComp_[0], sComp_[1], sOut_, capStream_})
+    for (cudaStream_t st : {sIn_, sOut_, capStream_})
+        if (st) cudaStreamDestroy(st);
+    for (cudaStream_t st : sComp_)
         if (st) cudaStreamDestroy(st);
     if (callerEv_) cudaEventDestroy(callerEv_);
     for (IoSlot& sl : io_)
@@ -1069,12 +1077,12 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
 
 static int bytesPerPixel(int fmt) { return fmt == PS_FMT_BGR24 ? 3 : 4; }
 
-// One run, in three streams: copy-in (host frames, the staged arguments),
-// compute, copy-out (host canvases).  Runs alternate between two slots of
-// staging buffers; run k's copies wait only for run k - 2's use of the same
-// slot, so with host buffers on both sides consecutive runs overlap.  With
-// any device input or output the run also waits for the caller's stream.
-// The caller's stream waits for the run's completion.
+// One run: copy-in (host frames, the staged arguments), compute (one stream
+// per slot), copy-out (host canvases).  Runs take the kIoSlots slots of
+// arguments and rig state in turn and wait only for the previous run on the
+// same slot, so with host buffers on both sides consecutive runs overlap.
+// With any device input or output the run also waits for the caller's
+// stream.  The caller's stream waits for the run's completion.
 void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph, Profiler* prof)
 {
     if (prof && !prof->on()) prof = nullptr;

@@ -49,12 +49,15 @@ public:
     long long residentBytes() const;
     // resident bytes a rig of this shape would hold (no allocation)
     static long long estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH,
-                                   int dstW, int dstH);
+                                   int dstW, int dstH, int slots = kIoSlots);
 
-    // Device staging of host frames and of a host canvas: kIoSlots sets, so
-    // consecutive renders with host buffers overlap their copies (slot 0's
+    // Device staging of host frames and of a host canvas: one set per state
+    // slot, so consecutive renders with host buffers overlap their copies (slot 0's
     // frame buffers are also the ones ps_render_get_input_buffer exposes).
-    static constexpr int kIoSlots = 2;
+    static constexpr int kIoSlots = 3;  // most state slots a rig keeps
+    // state slots of the next prepare (1..kIoSlots; default kIoSlots)
+    void setSlots(int n) { slotsWanted_ = n < 1 ? 1 : (n > kIoSlots ? kIoSlots : n); }
+    int slots() const { return slots_; }
     uint8_t* inputBuffer(int cam, int slot = 0) const
     {
         return inputs_.as<uint8_t>() + ((size_t)slot * n_ + cam) * inPitch_ * srcH_;
@@ -68,14 +71,14 @@ public:
 
     // Per-frame state slots: the Gaussian and collapsed pyramids, the I/O
     // staging and the device descriptor that points at them come in
-    // kIoSlots copies, so two frames of one rig can be in flight.  Runs take
+    // slots() copies, so that many frames of one rig can be in flight.  Runs take
     // slots in turn.  slotComputed(s) follows the last kernels that used
     // slot s (its pyramids and input staging are free again);
     // slotDownloaded(s) follows the copy out of its output staging.
     int acquireSlot()
     {
         const int s = nextSlot_;
-        nextSlot_ = (s + 1) % kIoSlots;
+        nextSlot_ = (s + 1) % slots_;
         lastSlot_ = s;
         return s;
     }
@@ -121,7 +124,7 @@ private:
 
     int n_ = 0, W_ = 0, H_ = 0, L_ = 0, full_ = 0, srcW_ = 0, srcH_ = 0;
     bool hasMaps_ = false, linear_ = false;
-    int nextSlot_ = 0, lastSlot_ = 0;
+    int nextSlot_ = 0, lastSlot_ = 0, slots_ = kIoSlots, slotsWanted_ = kIoSlots;
     cudaEvent_t slotComputed_[kIoSlots] = {}, slotDownloaded_[kIoSlots] = {};
     int numLinear_ = 0;
     DevBuf dLinear_, linW_;
@@ -196,8 +199,8 @@ private:
         int level;      // level of the first rig in the step
         double bytes;   // algorithmic bytes of the step (all rigs)
     };
-    // Per-run state, double-buffered: run k uses slot k % 2, so while run k
-    // computes, run k + 1 uploads and run k - 1 downloads.
+    // Per-run state in kIoSlots copies: run k uses slot k % kIoSlots, so while
+    // run k computes, run k + 1 uploads and run k - 1 downloads.
     struct IoSlot {
         DevBuf dArgs;   // [FrameDev x nr][LUTs][Segment x nseg]
         HostBuf stage;  // pinned staging copy of dArgs

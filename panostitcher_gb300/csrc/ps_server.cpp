@@ -27,6 +27,8 @@ struct ps_server {
     std::map<int, std::unique_ptr<ps::Rig>> streams;
     int nextId = 0;
     static constexpr int kSlots = 2;
+    // a stream has at most one frame in flight, so its rig keeps one state slot
+    static constexpr int kRigSlots = 1;
     cudaStream_t cs[kSlots] = {};
     cudaEvent_t end[kSlots] = {};
     ps::Plan plans[kSlots];
@@ -104,12 +106,14 @@ int ps_server_admit(ps_server* s, const ps_photo_param* params, int num_params, 
 {
     return forward(sguard([&] {
         if (!s || !stream_id) fail(PS_EINVAL, "NULL argument");
-        const long long est = ps::Rig::estimateBytes(params, num_params, blend_param, src_w, src_h, dst_w, dst_h);
+        const long long est = ps::Rig::estimateBytes(params, num_params, blend_param, src_w, src_h, dst_w, dst_h,
+                                                     ps_server::kRigSlots);
         const long long used = s->resident();
         if (used + est > s->budget)
             fail(PS_ENOMEM, "stream needs about %lld bytes; %lld of the %lld-byte budget are in use", est, used,
                  s->budget);
         std::unique_ptr<ps::Rig> rig(new ps::Rig());
+        rig->setSlots(ps_server::kRigSlots);
         rig->prepareFromParams(params, num_params, blend_param, src_w, src_h, dst_w, dst_h, nullptr,
                                s->cs[0]);
         if (used + rig->residentBytes() > s->budget)

@@ -1,7 +1,7 @@
 """Renders in flight together (GPU).
 
-A render keeps two sets of per-frame state, so consecutive calls with host
-buffers, and calls issued on two streams, overlap on the GPU.  Every frame
+A render keeps three sets of per-frame state, so consecutive calls with host
+buffers, and calls issued on several streams, overlap on the GPU.  Every frame
 must still come out exactly as the oracle stitches it alone.
 """
 import numpy as np
