@@ -12,6 +12,8 @@ The same line carries:
   roofline    the dominant kernel's algorithmic GB/s against the measured
               HBM copy bandwidth (CUDA events around every launch of a
               profiled pass over the same workload);
+  launch_shape  the launch shape the autotuner chose after prepare (untimed)
+              and its ms per frame against the default shape's;
   linear_blend  the linear-blend render mode (highQualityBlend 0) on the same rig;
   batched     four rigs of uneven size per launch sequence (CUDA graph);
   serve       16 live streams over those rigs, Poisson 30 fps arrivals,
@@ -191,6 +193,13 @@ def run_ours(args, world, rank, local, dist):
     t = time.perf_counter()
     r.prepare(cfg.cams, 1, cfg.levels, cfg.src_size, cfg.dst_size, check=True)
     prepare_s = time.perf_counter() - t
+    # launch-shape autotuning (untimed, like prepare): frames issued the way
+    # the timed loop issues them
+    tune = None
+    if not args.no_tune:
+        t = time.perf_counter()
+        tune = r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 3))
+        tune["seconds"] = round(time.perf_counter() - t, 2)
     fs = S.FrameSource(cfg)
     pool_host = [fs.frame(k) for k in range(args.pool)]
     pool_dev = [[torch.from_numpy(f).to(dev) for f in fr] for fr in pool_host]
@@ -247,6 +256,7 @@ def run_ours(args, world, rank, local, dist):
                      "l2": f"inputs larger than L2: {args.pool} distinct {frame_mb:.1f} MB frames cycled, "
                            f"rig state {resident / 1e6:.0f} MB resident", "parallelism": f"replicas x{world}",
                      "prepare_s": round(prepare_s, 3)}
+    out["launch_shape"] = tune if tune is not None else {"shape": r.launch_shape(), "tuned": False}
 
     # ---- e2e: pinned host frames in, host canvas out, through the C ABI
     pinned = []
@@ -576,6 +586,7 @@ def main(argv=None):
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-linear", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)

@@ -217,9 +217,49 @@ int ps_render_launches_per_frame(const ps_render* r);
    Returns < 0 if the render is not prepared. */
 double ps_render_algorithmic_bytes(const ps_render* r, int bytes_in_per_px, int bytes_out_per_px);
 
+/* ==== launch shapes and the autotuner (no reference counterpart: CudaAccel
+   fixes its launch shapes at compile time, e.g. the 16x16 blocks of
+   source/CudaAccel/CudaPyramid2.cu:989-1016) ==== */
+/* The launch choices that can change after prepare.  Tile sizes stay fixed
+   (32x16 remap and pyrDown tiles, 64x16 blend tiles); every shape gives the
+   same output bytes. */
+typedef struct ps_launch_shape {
+    int tail_max_items;   /* pyramid levels (from the top) with at most this many
+                             tiles run in the one-cluster tail kernel; 0 = no tail
+                             (default 16) */
+    int tail_cluster;     /* CTAs per rig in the tail kernel: 8, 16, or 0 = the
+                             widest the GPU co-schedules (default 0) */
+    int tail_half_tiles;  /* 1: the tail blends levels above 0 in 64x8 half tiles,
+                             two pixels per thread; 0: whole tiles (default 1) */
+    int ctas_per_sm[3];   /* CTAs per SM of the remap, pyrDown and blend kernels'
+                             one-wave grids; 0 = as many as fit (default 0) */
+} ps_launch_shape;
+typedef struct ps_tune_report {
+    double ms_per_frame_default;  /* device ms per frame of the default shape */
+    double ms_per_frame_chosen;   /* device ms per frame of the chosen shape */
+    int trials;                   /* timed runs (0 when the result was cached) */
+    int cached;                   /* 1: an earlier tuning of the same geometry */
+} ps_tune_report;
+/* Set before prepare, the shape applies at prepare; set after, the call waits
+   for the device to go idle and the next render re-records its launches.
+   Out-of-range fields: PS_EINVAL. */
+int ps_render_set_launch_shape(ps_render* r, const ps_launch_shape* shape);
+int ps_render_get_launch_shape(const ps_render* r, ps_launch_shape* shape);
+/* Times launch shapes on the prepared render (frames_per_trial frames per
+   timed run, 0 = 20; issued round-robin on in_flight streams, 0 = the
+   render's three frames in flight) by coordinate descent from the default
+   shape, and keeps the fastest.  The render's slot-0 input buffers are
+   overwritten with a test pattern.  A geometry tuned before in this
+   process is not timed again unless force is non-zero.  Blocks (about a
+   second at 4096x2048).  chosen and report may be NULL. */
+int ps_render_autotune(ps_render* r, int frames_per_trial, int in_flight, int force, ps_launch_shape* chosen,
+                       ps_tune_report* report);
+
 /* ==== batched render: several rigs, one frame each, in one launch sequence ==== */
 /* All rigs' work goes into shared persistent launches (one per pyramid step)
-   captured once per batch composition as a CUDA graph.  srcs[k] holds
+   captured once per batch composition as a CUDA graph.  Each rig keeps its
+   own tail split; a launch's grid and cluster widths are the widest any of
+   its rigs' launch shapes asks for.  srcs[k] holds
    ps_render_get_num_images(renders[k]) frames.  No reference counterpart
    (the reference renders one rig per call, source/Task/RicohUtil.cpp:1207). */
 int ps_render_batch(ps_render* const* renders, int num_renders, const ps_image* const* srcs,

@@ -61,6 +61,18 @@ class PlanarImage(C.Structure):
                 ("height", C.c_int), ("format", C.c_int), ("location", C.c_int)]
 
 
+class LaunchShape(C.Structure):
+    """ps_launch_shape: the launch choices that can change after prepare."""
+
+    _fields_ = [("tail_max_items", C.c_int), ("tail_cluster", C.c_int), ("tail_half_tiles", C.c_int),
+                ("ctas_per_sm", C.c_int * 3)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("ms_per_frame_default", C.c_double), ("ms_per_frame_chosen", C.c_double), ("trials", C.c_int),
+                ("cached", C.c_int)]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -98,6 +110,10 @@ _SIGS = [
                                          C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("ps_render_launches_per_frame", C.c_int, [C.c_void_p]),
     ("ps_render_algorithmic_bytes", C.c_double, [C.c_void_p, C.c_int, C.c_int]),
+    ("ps_render_set_launch_shape", C.c_int, [C.c_void_p, C.POINTER(LaunchShape)]),
+    ("ps_render_get_launch_shape", C.c_int, [C.c_void_p, C.POINTER(LaunchShape)]),
+    ("ps_render_autotune", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(LaunchShape),
+                                     C.POINTER(TuneReport)]),
     ("ps_render_batch", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.POINTER(Image)),
                                   C.POINTER(C.c_void_p), C.POINTER(Image), C.c_void_p]),
     ("ps_generate_reproject_map_and_mask", C.c_int, [C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,

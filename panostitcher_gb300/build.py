@@ -23,6 +23,7 @@ SOURCES = {
     "csrc/ps_capi.cpp": [],
     "csrc/ps_server.cpp": [],
     "csrc/ps_params.cpp": [],
+    "csrc/ps_tune.cpp": [],
 }
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include")]
 

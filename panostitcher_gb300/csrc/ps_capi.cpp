@@ -244,6 +244,65 @@ double ps_render_algorithmic_bytes(const ps_render* r, int bytes_in_per_px, int 
     return r->rig.algorithmicBytes(bytes_in_per_px, bytes_out_per_px);
 }
 
+// ---- launch shapes ------------------------------------------------------------
+namespace {
+
+ps::LaunchShape fromAbi(const ps_launch_shape& s)
+{
+    ps::LaunchShape o;
+    o.tailMaxItems = s.tail_max_items;
+    o.tailCluster = s.tail_cluster;
+    o.tailHalf = s.tail_half_tiles;
+    for (int k = 0; k < 3; k++) o.ctasPerSm[k] = s.ctas_per_sm[k];
+    return o;
+}
+
+void toAbi(const ps::LaunchShape& s, ps_launch_shape* o)
+{
+    o->tail_max_items = s.tailMaxItems;
+    o->tail_cluster = s.tailCluster;
+    o->tail_half_tiles = s.tailHalf;
+    for (int k = 0; k < 3; k++) o->ctas_per_sm[k] = s.ctasPerSm[k];
+}
+
+}  // namespace
+
+int ps_render_set_launch_shape(ps_render* r, const ps_launch_shape* shape)
+{
+    return guarded([&] {
+        if (!r || !shape) fail(PS_EINVAL, "NULL argument");
+        r->rig.setShape(fromAbi(*shape));
+    });
+}
+
+int ps_render_get_launch_shape(const ps_render* r, ps_launch_shape* shape)
+{
+    return guarded([&] {
+        if (!r || !shape) fail(PS_EINVAL, "NULL argument");
+        toAbi(r->rig.shape(), shape);
+    });
+}
+
+int ps_render_autotune(ps_render* r, int frames_per_trial, int in_flight, int force, ps_launch_shape* chosen,
+                       ps_tune_report* report)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (!r->rig.ready()) fail(PS_ESTATE, "render not prepared");
+        if (!r->plan || !r->plan->matches({&r->rig})) r->plan.reset(new ps::Plan({&r->rig}));
+        ps::TuneReport rep;
+        const ps::LaunchShape s =
+            ps::autotune(r->rig, *r->plan, frames_per_trial, in_flight, r->useGraph, force != 0, &rep);
+        if (chosen) toAbi(s, chosen);
+        if (report) {
+            report->ms_per_frame_default = rep.msDefault;
+            report->ms_per_frame_chosen = rep.msChosen;
+            report->trials = rep.trials;
+            report->cached = rep.cached ? 1 : 0;
+        }
+    });
+}
+
 int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const uint8_t* luts, int num_luts,
                          const ps_planar_image* dst, void* stream)
 {

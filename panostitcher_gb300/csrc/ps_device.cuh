@@ -71,8 +71,9 @@ struct RigDev {
     int downOff[PS_MAX_LEVELS + 1], downCnt[PS_MAX_LEVELS + 1];
     int blendOff[PS_MAX_LEVELS + 1], blendCnt[PS_MAX_LEVELS + 1];
     // the small top of the pyramid runs in one launch: pyrDown levels
-    // tailDown..L, then blend levels L..tailBlend (L + 1 = none)
-    int tailDown, tailBlend;
+    // tailDown..L, then blend levels L..tailBlend (L + 1 = none); with
+    // tailHalf the blend levels above 0 go in 64x8 half tiles
+    int tailDown, tailBlend, tailHalf;
     // linear-blend mode: the remap items (tile-major) and their weights,
     // 512 floats per item in the layout of the maps
     const RemapItem* remapItems;

@@ -141,12 +141,38 @@ cudaError_t launchImagesToLevel0(const void* const* images, const long long* pit
                                  int H, const uint8_t* cov, long long maskStride, uchar4* g0, int pitch,
                                  long long camStride, int* status, cudaStream_t st);
 
+// ---- launch shapes ----------------------------------------------------------------
+// The launch choices that can change after prepare.  Tile sizes are fixed
+// at compile time (the tile-compact maps and the 2x2 blend layout depend on
+// them); what varies is which levels the tail kernel runs, its cluster
+// width and tile split, and the CTAs per SM of the persistent kernels.
+// Set by hand or chosen by the autotuner (ps_tune.cpp).
+struct LaunchShape {
+    int tailMaxItems = 16;         // levels with at most this many tiles run in the tail kernel (0: none)
+    int tailCluster = 0;           // CTAs per rig in the tail kernel: 8, 16, or 0 = the widest co-schedulable
+    int tailHalf = 1;              // the tail blends levels above 0 in 64x8 half tiles
+    int ctasPerSm[3] = {0, 0, 0};  // k_remap, k_pyrdown, k_blend; 0 = as many as fit
+    bool operator==(const LaunchShape& o) const
+    {
+        return tailMaxItems == o.tailMaxItems && tailCluster == o.tailCluster && tailHalf == o.tailHalf &&
+               ctasPerSm[0] == o.ctasPerSm[0] && ctasPerSm[1] == o.ctasPerSm[1] && ctasPerSm[2] == o.ctasPerSm[2];
+    }
+    bool operator!=(const LaunchShape& o) const { return !(*this == o); }
+};
+
 // ---- per-frame kernels ------------------------------------------------------------
-cudaError_t launchRemap(const Segment* segs, int nsegs, int total, cudaStream_t st);
-cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_t st);
-cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st);
-// one cluster per segment: the rig's pyrDown levels tailDown..L and blend levels L..tailBlend
-cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st);
+// perSm > 0 caps the CTAs per SM of the one-wave persistent grid
+cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
+cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
+cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
+// one cluster per segment: the rig's pyrDown levels tailDown..L and blend
+// levels L..tailBlend; cluster 8 or 16 CTAs (0 or more than the GPU
+// co-schedules: the widest it does)
+cudaError_t launchTail(const Segment* segs, int nsegs, int cluster, cudaStream_t st);
+// CTAs of k_remap (kind 0), k_pyrdown (1), k_blend (2) resident per SM;
+// the widest tail cluster the GPU co-schedules (8 or 16)
+int residentCtasPerSm(int kind);
+int tailClusterMax();
 // linear-blend mode: LinearItems of every segment; maxCams sizes the LUT stage
 cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams, cudaStream_t st);
 

@@ -1283,10 +1283,10 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
         const BlendItem* items = R.blendItems + R.blendOff[j];
         UnitGeo geo;
         fillGeo(geo, R, *sg.frame, j);
-        // levels above 0: half tiles with two pixels per thread, so the few
-        // tiles of these levels keep twice the CTAs and all warps busy;
-        // level 0 (tiny canvases only): whole tiles, 2x2 blocks
-        const int parts = j > 0 ? 2 : 1;
+        // levels above 0 (with tailHalf): half tiles with two pixels per
+        // thread, so the few tiles of these levels keep twice the CTAs and
+        // all warps busy; otherwise whole tiles, 2x2 blocks
+        const int parts = j > 0 && R.tailHalf ? 2 : 1;
         for (int k = rank; k < parts * R.blendCnt[j]; k += cluster) {
             const uint4 raw = *reinterpret_cast<const uint4*>(items + k / parts);
             const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
@@ -1294,9 +1294,9 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
                 __syncthreads();  // readers of the previous unit are done
                 if (active)
                     stageUnitDirect<true>(sm.blend, R, raw, chunk, fRow, fCol, [] { __syncthreads(); },
-                                          j > 0 ? (k & 1) : -1);
+                                          parts == 2 ? (k & 1) : -1);
                 __syncthreads();
-                if (j > 0) computeUnitRows(sm.blend, geo, raw, chunk, pacc, k & 1);
+                if (parts == 2) computeUnitRows(sm.blend, geo, raw, chunk, pacc, k & 1);
                 else computeUnit(sm.blend, geo, raw, chunk, false, acc);
             }
         }
@@ -1355,8 +1355,10 @@ static int smCount()
     return sms;
 }
 
-static int gridFor(int total, int perSm)
+// One wave of `perSm` CTAs per SM, capped by `want` (> 0) and by the work.
+static int gridFor(int total, int perSm, int want = 0)
 {
+    if (want > 0 && want < perSm) perSm = want;
     const int cap = smCount() * perSm;
     return total < cap ? total : cap;
 }
@@ -1396,16 +1398,28 @@ static cudaError_t launchPdl(void (*kernel)(Args...), int grid, int block, cudaS
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
-cudaError_t launchRemap(const Segment* segs, int nsegs, int total, cudaStream_t st)
+int residentCtasPerSm(int kind)
 {
-    if (total <= 0) return cudaSuccess;
-    return launchPdl(k_remap, gridFor(total, residentPerSm<k_remap>(kThreads)), kThreads, st, segs, nsegs, total);
+    switch (kind) {
+    case 0: return residentPerSm<k_remap>(kThreads);
+    case 1: return residentPerSm<k_pyrdown>(kThreads);
+    case 2: return residentPerSm<k_blend>(kBlendThreads);
+    default: return 1;
+    }
 }
 
-cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, cudaStream_t st)
+cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_pyrdown, gridFor(total, residentPerSm<k_pyrdown>(kThreads)), kThreads, st, segs, nsegs, total);
+    return launchPdl(k_remap, gridFor(total, residentPerSm<k_remap>(kThreads), perSm), kThreads, st, segs, nsegs,
+                     total);
+}
+
+cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st)
+{
+    if (total <= 0) return cudaSuccess;
+    return launchPdl(k_pyrdown, gridFor(total, residentPerSm<k_pyrdown>(kThreads), perSm), kThreads, st, segs, nsegs,
+                     total);
 }
 
 cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams, cudaStream_t st)
@@ -1424,14 +1438,14 @@ cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams,
     return cudaLaunchKernelEx(&cfg, k_linear, segs, nsegs, total);
 }
 
-cudaError_t launchBlend(const Segment* segs, int nsegs, int total, cudaStream_t st)
+cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_blend, gridFor(total, residentPerSm<k_blend>(kBlendThreads)), kBlendThreads, st, segs, nsegs,
-                     total);
+    return launchPdl(k_blend, gridFor(total, residentPerSm<k_blend>(kBlendThreads), perSm), kBlendThreads, st, segs,
+                     nsegs, total);
 }
 
-static int tailClusterSize()
+int tailClusterMax()
 {
     static int size = 0;
     if (size) return size;
@@ -1457,10 +1471,12 @@ static int tailClusterSize()
     return size;
 }
 
-cudaError_t launchTail(const Segment* segs, int nsegs, cudaStream_t st)
+cudaError_t launchTail(const Segment* segs, int nsegs, int cluster, cudaStream_t st)
 {
     if (nsegs <= 0) return cudaSuccess;
-    const int cluster = tailClusterSize();
+    const int widest = tailClusterMax();
+    if (cluster <= 0 || cluster > widest) cluster = widest;
+    else cluster = cluster >= kTailClusterWide ? kTailClusterWide : kTailCluster;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nsegs * cluster);
     cfg.blockDim = dim3(kThreads);

@@ -508,11 +508,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     hBlend_ = blend;
     hCams_ = cams;
     // levels with few tiles (from the top down) go to the tail kernel
-    const int kTailMaxItems = 16;
-    tailDown_ = L + 1;
-    while (tailDown_ > 1 && downCnt_[tailDown_ - 1] <= kTailMaxItems) tailDown_--;
-    tailBlend_ = L + 1;
-    while (tailBlend_ > 0 && blendCnt_[tailBlend_ - 1] <= kTailMaxItems) tailBlend_--;
+    tailSplit(shape_.tailMaxItems, &tailDown_, &tailBlend_);
     dRemap_.alloc(std::max<size_t>(1, hRemap_.size()) * sizeof(RemapItem));
     dDown_.alloc(std::max<size_t>(1, down.size()) * sizeof(DownItem));
     dBlend_.alloc(std::max<size_t>(1, blend.size()) * sizeof(BlendItem));
@@ -555,6 +551,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     }
     d.tailDown = tailDown_;
     d.tailBlend = tailBlend_;
+    d.tailHalf = shape_.tailHalf;
     for (int j = 0; j <= L; j++) {
         const LevelGeom& g = geom_[j];
         d.lv[j].w = g.w;
@@ -564,18 +561,56 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         d.lv[j].Wt = lv_[j].Wt.as<uint16_t>();
         d.lv[j].Am = lv_[j].Am.as<uint16_t>();
     }
-    // one descriptor per state slot, differing in the pyramid pointers
+    hDesc_ = d;
+    dDesc_.alloc(sizeof(RigDev) * slots_);
+    writeDescriptors(st);
+    gen_ = g_generation++;
+}
+
+// One descriptor per state slot, differing in the pyramid pointers.
+void Rig::writeDescriptors(cudaStream_t st)
+{
     RigDev ds[kIoSlots];
     for (int k = 0; k < slots_; k++) {
-        ds[k] = d;
-        for (int j = 0; j <= L; j++) {
+        ds[k] = hDesc_;
+        for (int j = 0; j <= L_; j++) {
             ds[k].lv[j].G = lv_[j].G[k].as<uchar4>();
             ds[k].lv[j].C = lv_[j].C[k].as<short4>();
         }
     }
-    dDesc_.alloc(sizeof(RigDev) * slots_);
     PS_CUDA(cudaMemcpyAsync(dDesc_.get(), ds, sizeof(RigDev) * slots_, cudaMemcpyHostToDevice, st));
     PS_CUDA(cudaStreamSynchronize(st));
+}
+
+void Rig::tailSplit(int maxItems, int* down, int* blend) const
+{
+    int d = L_ + 1, b = L_ + 1;
+    while (d > 1 && downCnt_[d - 1] <= maxItems) d--;
+    while (b > 0 && blendCnt_[b - 1] <= maxItems) b--;
+    *down = d;
+    *blend = b;
+}
+
+void Rig::setShape(const LaunchShape& s)
+{
+    if (s.tailMaxItems < 0 || s.tailMaxItems > (1 << 24)) fail(PS_EINVAL, "tail_max_items %d out of range", s.tailMaxItems);
+    if (s.tailCluster != 0 && s.tailCluster != 8 && s.tailCluster != 16)
+        fail(PS_EINVAL, "tail_cluster must be 0, 8 or 16 (got %d)", s.tailCluster);
+    if (s.tailHalf != 0 && s.tailHalf != 1) fail(PS_EINVAL, "tail_half_tiles must be 0 or 1 (got %d)", s.tailHalf);
+    for (int k = 0; k < 3; k++)
+        if (s.ctasPerSm[k] < 0 || s.ctasPerSm[k] > 64)
+            fail(PS_EINVAL, "ctas_per_sm[%d] = %d out of range 0..64", k, s.ctasPerSm[k]);
+    if (s == shape_) return;
+    shape_ = s;
+    if (!ready() || linear_) return;
+    // the descriptors change under no run: launch lists follow the new
+    // generation (plans rebind), and no kernel may read the old split
+    PS_CUDA(cudaDeviceSynchronize());
+    tailSplit(shape_.tailMaxItems, &tailDown_, &tailBlend_);
+    hDesc_.tailDown = tailDown_;
+    hDesc_.tailBlend = tailBlend_;
+    hDesc_.tailHalf = shape_.tailHalf;
+    writeDescriptors(nullptr);
     gen_ = g_generation++;
 }
 
@@ -959,6 +994,19 @@ void Plan::bind(const std::vector<Rig*>& rigs)
     segRig_.clear();
     maxCams_ = 0;
     for (Rig* r : rigs) maxCams_ = std::max(maxCams_, r->numImages());
+    // launch widths shared by the rigs of a launch: the widest any rig asks
+    // for, 0 (as many as fit) counting as widest
+    auto widest = [&](auto field) {
+        int v = -1;
+        for (Rig* r : rigs) {
+            const int x = field(r->shape());
+            if (x == 0) return 0;
+            v = std::max(v, x);
+        }
+        return v < 0 ? 0 : v;
+    };
+    tailCluster_ = widest([](const LaunchShape& s) { return s.tailCluster; });
+    for (int k = 0; k < 3; k++) perSm_[k] = widest([k](const LaunchShape& s) { return s.ctasPerSm[k]; });
     auto addStep = [&](int kind, const std::vector<std::pair<int, std::pair<const void*, int>>>& parts, int step) {
         Step s{kind, (int)segs_.size(), 0, 0, -1, 0.0};
         for (const auto& p : parts) {
@@ -1063,10 +1111,10 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
             b = prof->event();
             PS_CUDA(cudaEventRecord(a, st));
         }
-        if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, st));
-        else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, st));
-        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, st));
-        else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, st));
+        if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, perSm_[0], st));
+        else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, perSm_[1], st));
+        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], st));
+        else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, tailCluster_, st));
         else PS_CUDA(launchLinear(p, s.nsegs, s.total, maxCams_, st));
         if (prof) {
             PS_CUDA(cudaEventRecord(b, st));

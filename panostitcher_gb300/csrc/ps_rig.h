@@ -94,6 +94,13 @@ public:
     int numDownItems(int level) const { return downCnt_[level]; }
     const BlendItem* blendItems(int level) const { return dBlend_.as<BlendItem>() + blendOff_[level]; }
     int numBlendItems(int level) const { return blendCnt_[level]; }
+    // Launch shape (tail split, tail cluster and tile split, CTAs per SM).
+    // Set before prepare, it applies at prepare; set after, it waits for the
+    // device to go idle, rewrites the descriptors and starts a new generation.
+    void setShape(const LaunchShape& s);
+    const LaunchShape& shape() const { return shape_; }
+    // the tail levels a tail_max_items value gives: pyrDown down..L, blend L..blend
+    void tailSplit(int maxItems, int* down, int* blend) const;
     // pyrDown levels tailDown()..L and blend levels L..tailBlend() run in the tail kernel
     int tailDown() const { return tailDown_; }
     int tailBlend() const { return tailBlend_; }
@@ -121,6 +128,7 @@ private:
                          cudaStream_t st);
     void prepareLinear(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
                        int radius, cudaStream_t st);
+    void writeDescriptors(cudaStream_t st);
 
     int n_ = 0, W_ = 0, H_ = 0, L_ = 0, full_ = 0, srcW_ = 0, srcH_ = 0;
     bool hasMaps_ = false, linear_ = false;
@@ -138,6 +146,8 @@ private:
     int downOff_[PS_MAX_LEVELS + 1] = {}, downCnt_[PS_MAX_LEVELS + 1] = {};
     int blendOff_[PS_MAX_LEVELS + 1] = {}, blendCnt_[PS_MAX_LEVELS + 1] = {};
     int tailDown_ = 1, tailBlend_ = 1;
+    LaunchShape shape_;
+    RigDev hDesc_ = {};  // slot-independent part of the descriptors
     std::vector<uint8_t> covBits_, seamBits_;  // host copies for exports (1 bit / pixel)
     std::vector<DownItem> hDown_;
     std::vector<BlendItem> hBlend_;
@@ -221,11 +231,27 @@ private:
     std::vector<size_t> lutOff_;
     size_t segOff_ = 0, stageBytes_ = 0;
     int maxCams_ = 0;
+    int tailCluster_ = 0, perSm_[3] = {0, 0, 0};  // launch widths (from the rigs' shapes)
     IoSlot io_[Rig::kIoSlots];
     int nextIo_ = 0;
     // copy-in, compute and copy-out streams (non-blocking), the capture stream
     cudaStream_t sIn_ = nullptr, sComp_[Rig::kIoSlots] = {}, sOut_ = nullptr, capStream_ = nullptr;
     cudaEvent_t callerEv_ = nullptr;
 };
+
+// The autotuner (ps_tune.cpp): times launch shapes on a prepared rig by
+// coordinate descent from the default shape (tail split, tail tile split,
+// tail cluster width, CTAs per SM of k_blend, k_pyrdown, k_remap), frames
+// issued round-robin on `inflight` streams, and leaves the fastest set on
+// the rig and bound to the plan.  Results are kept per rig geometry, GPU and
+// concurrency, so a later call for the same geometry times nothing unless
+// forced.  Blocks until done.
+struct TuneReport {
+    double msDefault = 0, msChosen = 0;  // ms per frame of the default and the chosen shape
+    int trials = 0;                      // timed runs
+    bool cached = false;
+};
+LaunchShape autotune(Rig& rig, Plan& plan, int framesPerTrial, int inflight, bool useGraph, bool force,
+                     TuneReport* rep);
 
 }  // namespace ps

@@ -202,6 +202,38 @@ class CudaPanoramaRender2:
     def algorithmic_bytes(self, bytes_in_per_px: int = 4, bytes_out_per_px: int = 4) -> float:
         return lib().ps_render_algorithmic_bytes(self._h, bytes_in_per_px, bytes_out_per_px)
 
+    SHAPE_DEFAULT = {"tail_max_items": 16, "tail_cluster": 0, "tail_half_tiles": 1, "ctas_per_sm": (0, 0, 0)}
+
+    @staticmethod
+    def _shape_dict(s: "L.LaunchShape") -> dict:
+        return {"tail_max_items": s.tail_max_items, "tail_cluster": s.tail_cluster,
+                "tail_half_tiles": s.tail_half_tiles, "ctas_per_sm": tuple(s.ctas_per_sm)}
+
+    def launch_shape(self) -> dict:
+        """The render's launch shape (ps_launch_shape fields)."""
+        s = L.LaunchShape()
+        check(lib().ps_render_get_launch_shape(self._h, C.byref(s)))
+        return self._shape_dict(s)
+
+    def set_launch_shape(self, **fields) -> None:
+        """Change some fields of the launch shape (the others keep their value)."""
+        cur = self.launch_shape()
+        unknown = set(fields) - set(cur)
+        if unknown:
+            raise ValueError(f"unknown launch-shape fields {sorted(unknown)}")
+        cur.update(fields)
+        s = L.LaunchShape(cur["tail_max_items"], cur["tail_cluster"], cur["tail_half_tiles"],
+                          (C.c_int * 3)(*cur["ctas_per_sm"]))
+        check(lib().ps_render_set_launch_shape(self._h, C.byref(s)))
+
+    def autotune(self, frames_per_trial: int = 0, in_flight: int = 0, force: bool = False) -> dict:
+        """Time launch shapes on this rig and keep the fastest (ps_render_autotune)."""
+        s, rep = L.LaunchShape(), L.TuneReport()
+        check(lib().ps_render_autotune(self._h, frames_per_trial, in_flight, int(bool(force)), C.byref(s),
+                                       C.byref(rep)))
+        return {"shape": self._shape_dict(s), "ms_per_frame_default": rep.ms_per_frame_default,
+                "ms_per_frame_chosen": rep.ms_per_frame_chosen, "trials": rep.trials, "cached": bool(rep.cached)}
+
     def input_buffer(self, cam: int):
         p, pitch = C.c_void_p(), C.c_longlong()
         check(lib().ps_render_get_input_buffer(self._h, cam, C.byref(p), C.byref(pitch)))

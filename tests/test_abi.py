@@ -117,3 +117,25 @@ def test_yuv_entry_points_validate_before_the_gpu(built_lib):
     pl.format = P.PS_FMT_NV12
     pl.height = 5
     assert built_lib.ps_cvt_bgr32_to_yuv(C.byref(im), C.byref(pl), None) == L.PS_EINVAL  # size mismatch
+
+
+def test_launch_shape_validation_before_the_gpu(built_lib):
+    r = P.CudaPanoramaRender2()
+    assert r.launch_shape() == P.CudaPanoramaRender2.SHAPE_DEFAULT
+    for bad in ({"tail_cluster": 5}, {"tail_half_tiles": 2}, {"tail_max_items": -1}, {"ctas_per_sm": (0, -1, 0)},
+                {"ctas_per_sm": (0, 0, 65)}):
+        with pytest.raises(P.PsError) as e:
+            r.set_launch_shape(**bad)
+        assert e.value.code == L.PS_EINVAL
+    assert r.launch_shape() == P.CudaPanoramaRender2.SHAPE_DEFAULT  # rejected shapes leave it unchanged
+    # before prepare the shape is only stored (it applies at prepare)
+    r.set_launch_shape(tail_max_items=0, tail_cluster=8, tail_half_tiles=0, ctas_per_sm=(1, 2, 3))
+    assert r.launch_shape() == {"tail_max_items": 0, "tail_cluster": 8, "tail_half_tiles": 0,
+                                "ctas_per_sm": (1, 2, 3)}
+    with pytest.raises(ValueError):
+        r.set_launch_shape(tile=64)
+    with pytest.raises(P.PsError) as e:
+        r.autotune()
+    assert e.value.code == L.PS_ESTATE
+    assert built_lib.ps_render_set_launch_shape(None, None) == L.PS_EINVAL
+    assert built_lib.ps_render_autotune(None, 0, 0, 0, None, None) == L.PS_EINVAL
