@@ -4,11 +4,12 @@
 Headline: stitched output Mpix/s of the plain per-frame path on the
 6-camera rig (6 x 1920x1080 rectilinear, 100 deg -> 4096x2048 equirect,
 8-level multiband blend, per-camera LUT gains), frames resident in HBM,
-issued in turn on three streams so three frames are in flight (the
+issued in turn on four streams so four frames are in flight (the
 single-stream figure is reported beside it).
 The same line carries:
   e2e         the same metric through the C ABI with pinned host frames in
-              and the host canvas out (H2D + D2H inside the timed region);
+              and the host canvas out (H2D + D2H inside the timed region),
+              beside its host-link bound (a copy-only loop of the same bytes);
   roofline    the dominant kernel's algorithmic GB/s against the measured
               HBM copy bandwidth (CUDA events around every launch of a
               profiled pass over the same workload);
@@ -176,6 +177,42 @@ def pinned_copy(a: np.ndarray):
     return arr, t
 
 
+def link_bound(h2d_srcs, d2h_dsts, steps, dev):
+    """Seconds for `steps` copy-only steps over the host link: per step the
+    bytes an e2e render moves (every camera frame up, the outputs down), the
+    uploads and the downloads on two streams."""
+    import torch
+    up = [torch.empty(t.shape, dtype=t.dtype, device=dev) for t in h2d_srcs[0]]
+    down = [torch.empty(t.shape, dtype=t.dtype, device=dev) for t in d2h_dsts]
+    s_up, s_down = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+
+    def go(n):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for k in range(n):
+            with torch.cuda.stream(s_up):
+                for d, h in zip(up, h2d_srcs[k % len(h2d_srcs)]):
+                    d.copy_(h, non_blocking=True)
+            with torch.cuda.stream(s_down):
+                for h, d in zip(d2h_dsts, down):
+                    h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    go(3)
+    return go(steps)
+
+
+def link_fields(e2e, secs, steps, npx):
+    """The e2e line's host-link bound: the copy-only rate of the same bytes."""
+    bound = steps * npx / secs / 1e6
+    return {"value": round(bound, 3), "unit": "Mpix/s",
+            "h2d_gbs": round(steps * e2e["h2d_bytes_per_step"] / secs / 1e9, 1),
+            "d2h_gbs": round(steps * e2e["d2h_bytes_per_step"] / secs / 1e9, 1),
+            "frac": round(e2e["value"] / bound, 4),
+            "how": "copy-only loop of the same pinned buffers: frames up and outputs down on two streams"}
+
+
 # ----------------------------------------------------------------------------- our arm
 def run_ours(args, world, rank, local, dist):
     import torch
@@ -198,7 +235,7 @@ def run_ours(args, world, rank, local, dist):
     tune = None
     if not args.no_tune:
         t = time.perf_counter()
-        tune = r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 3))
+        tune = r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 4))
         tune["seconds"] = round(time.perf_counter() - t, 2)
     fs = S.FrameSource(cfg)
     pool_host = [fs.frame(k) for k in range(args.pool)]
@@ -208,7 +245,7 @@ def run_ours(args, world, rank, local, dist):
 
     # ---- device-resident throughput (CUDA graph per frame).  Frames go out
     # in turn on `inflight` streams, each with its own canvas, so up to that
-    # many frames are in flight (the render keeps three state slots).
+    # many frames are in flight (the render keeps four state slots).
     streams = [torch.cuda.Stream(device=dev) for _ in range(args.inflight)]
     dsts = [dst] + [torch.empty_like(dst) for _ in range(args.inflight - 1)]
 
@@ -259,15 +296,15 @@ def run_ours(args, world, rank, local, dist):
     out["launch_shape"] = tune if tune is not None else {"shape": r.launch_shape(), "tuned": False}
 
     # ---- e2e: pinned host frames in, host canvas out, through the C ABI
-    pinned = []
-    keep = []
+    pinned, pinned_t = [], []
     for fr in pool_host:
-        cams = []
+        cams, cams_t = [], []
         for f in fr:
             a, tt = pinned_copy(f)
             cams.append(a)
-            keep.append(tt)
+            cams_t.append(tt)
         pinned.append(cams)
+        pinned_t.append(cams_t)
     hdst, hdst_t = pinned_copy(np.zeros((H, W, 4), np.uint8))
     e2e_steps = args.e2e_steps or args.steps
     for k in range(2):
@@ -283,6 +320,8 @@ def run_ours(args, world, rank, local, dist):
                   "h2d_bytes_per_step": int(sum(f.nbytes for f in pinned[0])),
                   "d2h_bytes_per_step": int(hdst.nbytes), "steps": e2e_steps,
                   "path": "ps_render_render, pinned BGR32 host frames -> pinned BGR32 host canvas"}
+    out["e2e"]["link_bound"] = link_fields(out["e2e"], link_bound(pinned_t, [hdst_t], e2e_steps, dev), e2e_steps,
+                                           npx)
 
     # ---- e2e with the encoder handoff: NV12 planes downloaded (the Task layer's render + cvt + download)
     hy, hy_t = pinned_copy(np.zeros((H, W), np.uint8))
@@ -301,6 +340,8 @@ def run_ours(args, world, rank, local, dist):
                        "d2h_bytes_per_step": int(hy.nbytes + huv.nbytes), "steps": e2e_steps,
                        "path": "ps_render_render_yuv, pinned BGR32 host frames -> pinned NV12 host planes "
                                "(conversion fused into the level-0 blend)"}
+    out["e2e_nv12"]["link_bound"] = link_fields(out["e2e_nv12"], link_bound(pinned_t, [hy_t, huv_t], e2e_steps, dev),
+                                                e2e_steps, npx)
 
     # ---- roofline: profiled pass (a CUDA event pair around every launch)
     r.profile(True)
@@ -578,7 +619,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--pool", type=int, default=4)
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
-    ap.add_argument("--inflight", type=int, default=3, help="caller streams of the device-resident loop")
+    ap.add_argument("--inflight", type=int, default=4, help="caller streams of the device-resident loop")
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

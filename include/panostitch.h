@@ -137,7 +137,7 @@ int ps_render_prepare_with_seams(ps_render* r, const ps_photo_param* params, int
    the call (pinned memory keeps the copies asynchronous); device src / dst
    are read / written in place.  The work runs on the render's own copy-in,
    compute and copy-out streams, and the caller's stream waits for its
-   completion.  A render keeps three sets of per-frame state, so three calls
+   completion.  A render keeps four sets of per-frame state, so four calls
    can be in flight: with host src and dst a call does not wait for the
    caller's earlier work (consecutive calls overlap their uploads, kernels
    and downloads); with device src or dst it waits for the caller's stream,
@@ -247,7 +247,7 @@ int ps_render_set_launch_shape(ps_render* r, const ps_launch_shape* shape);
 int ps_render_get_launch_shape(const ps_render* r, ps_launch_shape* shape);
 /* Times launch shapes on the prepared render (frames_per_trial frames per
    timed run, 0 = 20; issued round-robin on in_flight streams, 0 = the
-   render's three frames in flight) by coordinate descent from the default
+   render's four frames in flight) by coordinate descent from the default
    shape, and keeps the fastest.  The render's slot-0 input buffers are
    overwritten with a test pattern.  A geometry tuned before in this
    process is not timed again unless force is non-zero.  Blocks (about a

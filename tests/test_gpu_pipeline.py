@@ -1,6 +1,6 @@
 """Renders in flight together (GPU).
 
-A render keeps three sets of per-frame state, so consecutive calls with host
+A render keeps four sets of per-frame state, so consecutive calls with host
 buffers, and calls issued on several streams, overlap on the GPU.  Every frame
 must still come out exactly as the oracle stitches it alone.
 """
