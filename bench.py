@@ -10,6 +10,8 @@ The same line carries:
   e2e         the same metric through the C ABI with pinned host frames in
               and the host canvas out (H2D + D2H inside the timed region),
               beside its host-link bound (a copy-only loop of the same bytes);
+  e2e_nv12 / e2e_planar  the same with NV12 host planes out, and with NV12
+              decoder frames in as well (1.5 bytes per source pixel);
   roofline    the dominant kernel's algorithmic GB/s against the measured
               HBM copy bandwidth (CUDA events around every launch of a
               profiled pass over the same workload);
@@ -342,6 +344,53 @@ def run_ours(args, world, rank, local, dist):
                                "(conversion fused into the level-0 blend)"}
     out["e2e_nv12"]["link_bound"] = link_fields(out["e2e_nv12"], link_bound(pinned_t, [hy_t, huv_t], e2e_steps, dev),
                                                 e2e_steps, npx)
+
+    # ---- e2e of the whole handoff: NV12 decoder frames in, NV12 encoder planes
+    # out.  The input planes are made from the BGR pool by the library's own
+    # device conversion, then staged in pinned host memory.
+    Ws, Hs = cfg.src_size
+    nv12_t, nv12_h, nv12_dev = [], [], []
+    for fr in pool_dev:
+        cams_t, cams_h, cams_d = [], [], []
+        for f in fr:
+            y = torch.empty((Hs, Ws), dtype=torch.uint8, device=dev)
+            uv = torch.empty((Hs // 2, Ws), dtype=torch.uint8, device=dev)
+            P.cvt_bgr32_to_yuv(f, [y, uv], P.PS_FMT_NV12)
+            ha, ht = pinned_copy(y.cpu().numpy())
+            ua, ut = pinned_copy(uv.cpu().numpy())
+            cams_t += [ht, ut]
+            cams_h.append([ha, ua])
+            cams_d.append([y, uv])
+        nv12_t.append(cams_t)
+        nv12_h.append(cams_h)
+        nv12_dev.append(cams_d)
+    for k in range(2):
+        r.render_planar(nv12_h[k % args.pool], luts=luts, ydst=[hy, huv], check=True)
+    torch.cuda.synchronize()
+    barrier(dist)
+    t = time.perf_counter()
+    for k in range(e2e_steps):
+        r.render_planar(nv12_h[k % args.pool], luts=luts, ydst=[hy, huv], check=True)
+    torch.cuda.synchronize()
+    pl_s = reduce_max(time.perf_counter() - t, dist, dev)
+    out["e2e_planar"] = {"value": round(world * e2e_steps * npx / pl_s / 1e6, 3), "unit": "Mpix/s",
+                         "h2d_bytes_per_step": int(sum(x.nbytes for x in nv12_t[0])),
+                         "d2h_bytes_per_step": int(hy.nbytes + huv.nbytes), "steps": e2e_steps,
+                         "path": "ps_render_render_planar, pinned NV12 host frames -> pinned NV12 host planes "
+                                 "(decoder frames converted on the device, encoder conversion fused into the "
+                                 "level-0 blend)"}
+    out["e2e_planar"]["link_bound"] = link_fields(out["e2e_planar"],
+                                                  link_bound([nv12_t[k] for k in range(args.pool)], [hy_t, huv_t],
+                                                             e2e_steps, dev), e2e_steps, npx)
+    # the conversion kernel alone (device planes, profiled pass)
+    r.profile(True)
+    for k in range(10):
+        r.render_planar(nv12_dev[k % args.pool], dst, luts, check=True)
+    torch.cuda.synchronize()
+    n5, ms5, b5 = r.profile_read(5)
+    r.profile(False)
+    out["e2e_planar"]["k_yuv_to_bgr32"] = {"us_per_frame": round(ms5 / max(n5, 1) * 1e3, 2),
+                                           "alg_GBps": round(b5 / max(ms5, 1e-9) / 1e6, 1)}
 
     # ---- roofline: profiled pass (a CUDA event pair around every launch)
     r.profile(True)

@@ -168,6 +168,18 @@ int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const u
 #define PS_SEAMS_NEAREST_AXIS 0
 #define PS_SEAMS_DISTANCE 1
 int ps_render_set_seam_rule(ps_render* r, int rule);
+/* CudaPanoramaRender2::render with decoder frames: src holds num_src YUV420P
+   or NV12 frames (BT.601 studio range, src_w x src_h, host or device, each
+   its own format), converted on the device to BGR32 as cvtYUV420PToBGR32 /
+   cvtNV12ToBGR32 do (source/CudaAccel/ImageProc.cu:165-259) and then
+   stitched as ps_render_render stitches BGR32 frames.  Host frames cross
+   the host link at 1.5 bytes per pixel instead of 4.  Exactly one of dst
+   (as ps_render_render) and ydst (as ps_render_render_yuv) is given.  The
+   first call allocates the render's planar staging (1.5 bytes per source
+   pixel per camera and frame in flight).  Streams and lifetimes as
+   ps_render_render. */
+int ps_render_render_planar(ps_render* r, const ps_planar_image* src, int num_src, const uint8_t* luts,
+                            int num_luts, const ps_image* dst, const ps_planar_image* ydst, void* stream);
 
 /* Launch the per-frame kernels as one captured CUDA graph (default 1) or as
    individual launches (0).  No reference counterpart. */
@@ -202,9 +214,10 @@ int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out,
    (no graph); ps_render_profile_read aggregates the finished launches of
    one kernel kind (0 remap, 1 pyrDown, 2 blend, 3 the tail kernel that runs
    the few-tile top levels, reported at its lowest blend level, 4 the
-   linear-blend render) at one level (-1 = all levels): launch count, summed
-   device milliseconds and summed algorithmic bytes (each input and output
-   element counted once).
+   linear-blend render, 5 the conversion of decoder frames, at level 0) at
+   one level (-1 = all levels): launch count, summed device milliseconds
+   and summed algorithmic bytes (each input and output element counted
+   once).
    Enabling resets the aggregates. */
 int ps_render_profile(ps_render* r, int enable);
 int ps_render_profile_read(ps_render* r, int kind, int level, long long* launches, double* total_ms,
@@ -298,6 +311,12 @@ int ps_distance_transform_l1(const uint8_t* mask, int width, int height, int32_t
    pixel; U and V per 2x2 block from its left column, as the reference
    computes them. */
 int ps_cvt_bgr32_to_yuv(const ps_image* src, const ps_planar_image* dst, void* stream);
+/* cvtYUV420PToBGR32 / cvtNV12ToBGR32 (source/CudaAccel/CudaInterface.h:
+   167-171, kernels source/CudaAccel/ImageProc.cu:165-222): device planes of
+   an even-sized frame to a device BGR32 image of the same size, BT.601
+   studio range in 20-bit fixed point; the fourth byte is written 0 (the
+   reference leaves it unwritten). */
+int ps_cvt_yuv_to_bgr32(const ps_planar_image* src, const ps_image* dst, void* stream);
 
 /* No counterpart in the reference.  The nearest-optical-axis seam masks of a
    rig (the masks ps_render_prepare derives internally), computed without

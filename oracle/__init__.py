@@ -101,6 +101,8 @@ def lib():
             L.orc_non_intersecting_masks.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
             L.orc_bgr32_to_yuv.argtypes = [vp, C.c_longlong, C.c_int, C.c_int, C.c_int, vp, C.c_longlong, vp,
                                            C.c_longlong, vp, C.c_longlong]
+            L.orc_yuv_to_bgr32.argtypes = [vp, C.c_longlong, vp, C.c_longlong, vp, C.c_longlong, C.c_int, C.c_int,
+                                           C.c_int, vp, C.c_longlong]
             _lib = L
     return _lib
 
@@ -214,6 +216,24 @@ def bgr32_to_yuv(bgr: np.ndarray, fmt: int = FMT_YUV420P):
     v = np.empty((H // 2, W // 2), np.uint8)
     lib().orc_bgr32_to_yuv(_ptr(bgr), W * 4, W, H, FMT_YUV420P, _ptr(y), W, _ptr(u), W // 2, _ptr(v), W // 2)
     return y, u, v
+
+
+def yuv_to_bgr32(planes, fmt: int = FMT_YUV420P) -> np.ndarray:
+    """(Y, U, V) planes (YUV420P) or (Y, UV) planes (NV12) -> BGR32 HxWx4 (fourth byte 0)."""
+    planes = [np.ascontiguousarray(p, np.uint8) for p in planes]
+    H, W = planes[0].shape
+    if H % 2 or W % 2:
+        raise ValueError("even width and height expected")
+    out = np.empty((H, W, 4), np.uint8)
+    if fmt == FMT_NV12:
+        y, uv = planes
+        assert uv.shape == (H // 2, W)
+        lib().orc_yuv_to_bgr32(_ptr(y), W, _ptr(uv), W, None, 0, W, H, fmt, _ptr(out), W * 4)
+    else:
+        y, u, v = planes
+        assert u.shape == (H // 2, W // 2) and v.shape == (H // 2, W // 2)
+        lib().orc_yuv_to_bgr32(_ptr(y), W, _ptr(u), W // 2, _ptr(v), W // 2, W, H, FMT_YUV420P, _ptr(out), W * 4)
+    return out
 
 
 # ------------------------------------------------------------------- remap

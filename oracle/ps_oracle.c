@@ -938,6 +938,52 @@ void orc_bgr32_to_yuv(const uint8_t* bgr, long long bgrStep, int w, int h, int f
     }
 }
 
+/* ---- decoder frames: YUV420P / NV12 -> BGR32 ------------------------------
+ * source/CudaAccel/ImageProc.cu:165-222 (cvtYUV2x2BlockToBGR over 2x2
+ * blocks): u = U - 128, v = V - 128, y' = max(Y - 16, 0) * 1220542; each
+ * channel is (y' + 2^19 + chroma term) >> 20 clamped to 0..255, with the
+ * chroma terms 1673527 v (R), -852492 v - 409993 u (G), 2116026 u (B).  The
+ * device's >> of a negative int is a floor; floor_shift20 states it without
+ * relying on C's implementation-defined shift of negative values.  The
+ * fourth byte is written 0.
+ */
+static int floor_shift20(int v) { return v >= 0 ? v >> 20 : -((-v + (1 << 20) - 1) >> 20); }
+
+static void yuv_to_bgr_px(int yv, int ruv, int guv, int buv, uint8_t* o)
+{
+    const int yy = (yv > 16 ? yv - 16 : 0) * 1220542;
+    o[0] = (uint8_t)yuv_clamp(floor_shift20(yy + buv));
+    o[1] = (uint8_t)yuv_clamp(floor_shift20(yy + guv));
+    o[2] = (uint8_t)yuv_clamp(floor_shift20(yy + ruv));
+    o[3] = 0;
+}
+
+void orc_yuv_to_bgr32(const uint8_t* y, long long yStep, const uint8_t* u, long long uStep, const uint8_t* v,
+                      long long vStep, int w, int h, int fmt, uint8_t* bgr, long long bgrStep)
+{
+    for (int by = 0; by < h / 2; by++)
+        for (int bx = 0; bx < w / 2; bx++) {
+            const int x = 2 * bx, yr = 2 * by;
+            int cu, cv;
+            if (fmt == 12) {
+                cu = u[(size_t)by * uStep + x];
+                cv = u[(size_t)by * uStep + x + 1];
+            } else {
+                cu = u[(size_t)by * uStep + bx];
+                cv = v[(size_t)by * vStep + bx];
+            }
+            cu -= 128;
+            cv -= 128;
+            const int ruv = (1 << 19) + 1673527 * cv;
+            const int guv = (1 << 19) - 852492 * cv - 409993 * cu;
+            const int buv = (1 << 19) + 2116026 * cu;
+            for (int r = 0; r < 2; r++)
+                for (int c = 0; c < 2; c++)
+                    yuv_to_bgr_px(y[(size_t)(yr + r) * yStep + x + c], ruv, guv, buv,
+                                  bgr + (size_t)(yr + r) * bgrStep + 4 * (size_t)(x + c));
+        }
+}
+
 /* ---- getNonIntersectingMasks (source/Blend/Mask.cpp:376-398) ---------------
  * Distance transform: OpenCV 3.0's cv::distanceTransform with CV_DIST_L1 and
  * a 3x3 mask is a two-pass chamfer (forward: up-left, up, up-right, left;

@@ -131,6 +131,11 @@ void orc_linear_render(const uint8_t* const* srcs, int srcW, int srcH, int chann
    fmt 12 (NV12): planes y, uv (v unused).  w, h even. */
 void orc_bgr32_to_yuv(const uint8_t* bgr, long long bgrStep, int w, int h, int fmt, uint8_t* y, long long yStep,
                       uint8_t* u, long long uStep, uint8_t* v, long long vStep);
+/* cvtYUV420PToBGR32 / cvtNV12ToBGR32 (source/CudaAccel/ImageProc.cu:165-222):
+   planes y, u, v (fmt 420) or y, uv (fmt 12) of an even-sized frame to
+   BGR32 (fourth byte 0). */
+void orc_yuv_to_bgr32(const uint8_t* y, long long yStep, const uint8_t* u, long long uStep, const uint8_t* v,
+                      long long vStep, int w, int h, int fmt, uint8_t* bgr, long long bgrStep);
 
 #ifdef __cplusplus
 }

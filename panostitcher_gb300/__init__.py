@@ -9,11 +9,11 @@ from ._lib import (PsError, PhotoParam, Image, PlanarImage, lib, PS_FMT_YUV420P,
                    PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE)
 from .render import (CudaPanoramaRender2, CudaTilingMultibandBlendFast, render_batch,  # noqa: F401
                      generate_reproject_map_and_mask, reproject_to_16s, get_lut, as_image, as_planar,
-                     cvt_bgr32_to_yuv, non_intersecting_masks, distance_transform_l1, load_photo_params)
+                     cvt_bgr32_to_yuv, cvt_yuv_to_bgr32, non_intersecting_masks, distance_transform_l1,
+                     load_photo_params)
 
 __all__ = ["CudaPanoramaRender2", "CudaTilingMultibandBlendFast", "render_batch",
            "generate_reproject_map_and_mask", "reproject_to_16s", "get_lut", "as_image", "as_planar",
-           "cvt_bgr32_to_yuv", "non_intersecting_masks", "distance_transform_l1", "load_photo_params", "PsError",
-           "PhotoParam",
-           "Image", "PlanarImage", "lib", "PS_FMT_YUV420P", "PS_FMT_NV12", "PS_SEAMS_NEAREST_AXIS",
-           "PS_SEAMS_DISTANCE"]
+           "cvt_bgr32_to_yuv", "cvt_yuv_to_bgr32", "non_intersecting_masks", "distance_transform_l1",
+           "load_photo_params", "PsError", "PhotoParam", "Image", "PlanarImage", "lib", "PS_FMT_YUV420P",
+           "PS_FMT_NV12", "PS_SEAMS_NEAREST_AXIS", "PS_SEAMS_DISTANCE"]

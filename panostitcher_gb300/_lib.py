@@ -95,6 +95,8 @@ _SIGS = [
                                          C.c_int, C.c_void_p]),
     ("ps_load_photo_params", C.c_int, [C.c_char_p, C.POINTER(PhotoParam), C.c_int, C.POINTER(C.c_int)]),
     ("ps_render_set_seam_rule", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_render_render_planar", C.c_int, [C.c_void_p, C.POINTER(PlanarImage), C.c_int, C.c_void_p, C.c_int,
+                                          C.POINTER(Image), C.POINTER(PlanarImage), C.c_void_p]),
     ("ps_render_set_graph", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_clear", None, [C.c_void_p]),
     ("ps_render_get_num_images", C.c_int, [C.c_void_p]),
@@ -124,6 +126,7 @@ _SIGS = [
     ("ps_non_intersecting_masks", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     ("ps_distance_transform_l1", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     ("ps_cvt_bgr32_to_yuv", C.c_int, [C.POINTER(Image), C.POINTER(PlanarImage), C.c_void_p]),
+    ("ps_cvt_yuv_to_bgr32", C.c_int, [C.POINTER(PlanarImage), C.POINTER(Image), C.c_void_p]),
     ("ps_nearest_axis_seams_no_alloc", C.c_int, [C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,
                                                  C.c_int, C.c_void_p, C.c_void_p]),
     ("ps_blender_create", C.c_int, [C.POINTER(C.c_void_p)]),

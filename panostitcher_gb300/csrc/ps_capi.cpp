@@ -228,7 +228,7 @@ int ps_render_profile_read(ps_render* r, int kind, int level, long long* launche
 {
     return guarded([&] {
         if (!r) fail(PS_EINVAL, "render is NULL");
-        if (kind < 0 || kind > 4) fail(PS_EINVAL, "kind %d not in 0..4", kind);
+        if (kind < 0 || kind > 5) fail(PS_EINVAL, "kind %d not in 0..5", kind);
         r->prof.read(kind, level, launches, total_ms, bytes);
     });
 }
@@ -316,6 +316,34 @@ int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const u
         checkFrame(r->rig, src, num_src, luts, num_luts, &probe);
         if (!r->plan || !r->plan->matches({&r->rig})) r->plan.reset(new ps::Plan({&r->rig}));
         r->plan->run({ps::FrameInput{src, luts, nullptr, dst}}, toStream(stream), r->useGraph, &r->prof);
+    });
+}
+
+int ps_render_render_planar(ps_render* r, const ps_planar_image* src, int num_src, const uint8_t* luts,
+                            int num_luts, const ps_image* dst, const ps_planar_image* ydst, void* stream)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        const ps::Rig& rig = r->rig;
+        if (!rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        if (!rig.hasMaps()) fail(PS_ESTATE, "prepared without camera parameters");
+        if (!src || num_src != rig.numImages())
+            fail(PS_EINVAL, "%d source frames given, %d cameras prepared", num_src, rig.numImages());
+        for (int i = 0; i < num_src; i++) checkPlanar(&src[i], rig.srcW(), rig.srcH(), "src");
+        if (luts && num_luts != rig.numImages())
+            fail(PS_EINVAL, "%d look-up tables given, %d cameras prepared (each 3 x 256 bytes)", num_luts,
+                 rig.numImages());
+        if ((dst == nullptr) == (ydst == nullptr)) fail(PS_EINVAL, "give exactly one of dst and ydst");
+        if (dst) {
+            checkImage(dst, rig.width(), rig.height(), "dst", 0);
+        } else {
+            if (rig.linear()) fail(PS_EINVAL, "the linear-blend mode writes BGR only; use ps_cvt_bgr32_to_yuv");
+            checkPlanar(ydst, rig.width(), rig.height(), "ydst");
+        }
+        if (!r->plan || !r->plan->matches({&r->rig})) r->plan.reset(new ps::Plan({&r->rig}));
+        ps::FrameInput in{nullptr, luts, dst, ydst};
+        in.psrc = src;
+        r->plan->run({in}, toStream(stream), r->useGraph, &r->prof);
     });
 }
 
@@ -471,6 +499,36 @@ int ps_cvt_bgr32_to_yuv(const ps_image* src, const ps_planar_image* dst, void* s
                                  dst->format, static_cast<uint8_t*>(dst->planes[0]), dst->pitches[0],
                                  static_cast<uint8_t*>(dst->planes[1]), dst->pitches[1],
                                  static_cast<uint8_t*>(dst->planes[2]), dst->pitches[2], toStream(stream)));
+    });
+}
+
+int ps_cvt_yuv_to_bgr32(const ps_planar_image* src, const ps_image* dst, void* stream)
+{
+    return guarded([&] {
+        if (!src || !dst) fail(PS_EINVAL, "NULL argument");
+        checkPlanar(src, src->width, src->height, "src");
+        if (src->location != PS_MEM_DEVICE) fail(PS_EINVAL, "src must be device memory");
+        checkImage(dst, src->width, src->height, "dst", 0);
+        if (dst->format != PS_FMT_BGR32) fail(PS_EINVAL, "dst must be BGR32");  // CV_8UC4, ImageProc.cu:231
+        if (dst->location != PS_MEM_DEVICE) fail(PS_EINVAL, "dst must be device memory");
+        ps::YuvFrames f;
+        std::memset(&f, 0, sizeof f);
+        f.n = 1;
+        f.w = src->width;
+        f.h = src->height;
+        ps::YuvFrame& F = f.frame[0];
+        F.fmt = src->format;
+        F.y = static_cast<const uint8_t*>(src->planes[0]);
+        F.yPitch = src->pitches[0];
+        F.u = static_cast<const uint8_t*>(src->planes[1]);
+        F.uPitch = src->pitches[1];
+        if (src->format == PS_FMT_YUV420P) {
+            F.v = static_cast<const uint8_t*>(src->planes[2]);
+            F.vPitch = src->pitches[2];
+        }
+        F.dst = static_cast<uint8_t*>(dst->data);
+        F.dstPitch = dst->pitch;
+        PS_CUDA(ps::launchYuvToBgr32(f, toStream(stream)));
     });
 }
 

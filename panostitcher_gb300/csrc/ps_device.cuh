@@ -97,6 +97,21 @@ struct FrameDev {
     int* status;              // device error word (0 = ok)
 };
 
+// Decoder frames to convert to BGR32 (k_yuv_to_bgr32): YUV420P (u, v
+// planes) or NV12 (u = the interleaved UV plane), all w x h (even).
+struct YuvFrame {
+    const uint8_t *y, *u, *v;
+    long long yPitch, uPitch, vPitch;
+    uint8_t* dst;
+    long long dstPitch;
+    int fmt;
+    int vec;  // w % 8 == 0 and every plane aligned for 8-pixel-wide vector access
+};
+struct YuvFrames {
+    YuvFrame frame[PS_MAX_CAMS];
+    int n, w, h;
+};
+
 // A launch runs the concatenation of segments: `count` items of one rig,
 // numbered from `prefix` in the launch.  Several rigs (a batch, or the
 // frames of a serving tick) share one launch this way.

@@ -185,6 +185,8 @@ std::vector<ps_photo_param> loadPhotoParams(const std::string& path);
 cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int srcW, int srcH, int srcFmt,
                                  const float* xmap, const float* ymap, long long mapPitch, int dstW, int dstH,
                                  const uint8_t* lut, int16_t* dst, long long dstPitch, cudaStream_t st);
+// YUV420P / NV12 frames -> BGR32 (one launch for all f.n frames)
+cudaError_t launchYuvToBgr32(const YuvFrames& f, cudaStream_t st);
 // BGR32 -> YUV420P (u, v planes) or NV12 (u = the UV plane, v unused); w, h even
 cudaError_t launchCvtYuv(const uint8_t* src, long long srcPitch, int w, int h, int fmt, uint8_t* y, long long yPitch,
                          uint8_t* u, long long uPitch, uint8_t* v, long long vPitch, cudaStream_t st);

@@ -1342,6 +1342,133 @@ __global__ void __launch_bounds__(kThreads) k_cvt_yuv(const uint8_t* __restrict_
     }
 }
 
+// ============================================================================
+// k_yuv_to_bgr32: decoder frames YUV420P / NV12 -> BGR32 (cvtYUV420PToBGR32
+// / cvtNV12ToBGR32, ImageProc.cu:165-259): per 2x2 block, with u = U - 128,
+// v = V - 128 and y' = max(Y - 16, 0) * CY,
+//   R = clamp((y' + 2^19 + CVR v) >> 20), G = clamp((y' + 2^19 + CVG v + CUG u) >> 20),
+//   B = clamp((y' + 2^19 + CUB u) >> 20)
+// (the standard BT.601 studio-range coefficients scaled by 2^20; the shift
+// of a negative sum rounds toward minus infinity).  The fourth byte is
+// written 0.  One thread per 2x2 block; blockIdx.y is the frame.
+// ============================================================================
+constexpr int kInvCY = 1220542, kInvCUB = 2116026, kInvCUG = -409993, kInvCVG = -852492, kInvCVR = 1673527;
+
+__device__ __forceinline__ uint32_t yuvPixel(int yv, int ruv, int guv, int buv)
+{
+    const int yy = max(yv - 16, 0) * kInvCY;
+    return (uint32_t)clamp255((yy + buv) >> kYuvShift) | ((uint32_t)clamp255((yy + guv) >> kYuvShift) << 8) |
+           ((uint32_t)clamp255((yy + ruv) >> kYuvShift) << 16);
+}
+
+// Eight pixels of a row pair (four 2x2 blocks) per thread: 8-byte luma
+// loads, the blocks' chroma in one load, 16-byte stores.
+struct YuvChunk {
+    uint2 yt, yb;     // luma of the top and bottom rows
+    uint32_t us, vs;  // the four blocks' U and V, one byte each
+};
+
+__device__ __forceinline__ YuvChunk yuvLoad(const YuvFrame& F, int cx, int by)
+{
+    const int x = 8 * cx, y = 2 * by;
+    YuvChunk c;
+    c.yt = *reinterpret_cast<const uint2*>(F.y + (size_t)y * F.yPitch + x);
+    c.yb = *reinterpret_cast<const uint2*>(F.y + (size_t)(y + 1) * F.yPitch + x);
+    if (F.fmt == PS_FMT_NV12) {
+        const uint2 uv = *reinterpret_cast<const uint2*>(F.u + (size_t)by * F.uPitch + x);
+        c.us = __byte_perm(uv.x, uv.y, 0x6420);
+        c.vs = __byte_perm(uv.x, uv.y, 0x7531);
+    } else {
+        c.us = *reinterpret_cast<const uint32_t*>(F.u + (size_t)by * F.uPitch + (x >> 1));
+        c.vs = *reinterpret_cast<const uint32_t*>(F.v + (size_t)by * F.vPitch + (x >> 1));
+    }
+    return c;
+}
+
+__device__ __forceinline__ void yuvStore(const YuvFrame& F, int cx, int by, const YuvChunk& c)
+{
+    const int half = 1 << (kYuvShift - 1);
+    uint32_t ot[8], ob[8];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int u = (int)((c.us >> (8 * k)) & 0xFF) - 128, v = (int)((c.vs >> (8 * k)) & 0xFF) - 128;
+        const int ruv = half + kInvCVR * v, guv = half + kInvCVG * v + kInvCUG * u, buv = half + kInvCUB * u;
+        const uint32_t wt = k < 2 ? c.yt.x : c.yt.y, wb = k < 2 ? c.yb.x : c.yb.y;
+        const int s = 16 * (k & 1);
+        ot[2 * k] = yuvPixel((wt >> s) & 0xFF, ruv, guv, buv);
+        ot[2 * k + 1] = yuvPixel((wt >> (s + 8)) & 0xFF, ruv, guv, buv);
+        ob[2 * k] = yuvPixel((wb >> s) & 0xFF, ruv, guv, buv);
+        ob[2 * k + 1] = yuvPixel((wb >> (s + 8)) & 0xFF, ruv, guv, buv);
+    }
+    const int y = 2 * by;
+    uint4* t = reinterpret_cast<uint4*>(F.dst + (size_t)y * F.dstPitch) + 2 * cx;
+    uint4* b = reinterpret_cast<uint4*>(F.dst + (size_t)(y + 1) * F.dstPitch) + 2 * cx;
+    t[0] = make_uint4(ot[0], ot[1], ot[2], ot[3]);
+    t[1] = make_uint4(ot[4], ot[5], ot[6], ot[7]);
+    b[0] = make_uint4(ob[0], ob[1], ob[2], ob[3]);
+    b[1] = make_uint4(ob[4], ob[5], ob[6], ob[7]);
+}
+
+__global__ void __launch_bounds__(kThreads) k_yuv_to_bgr32(YuvFrames f)
+{
+    const int cam = blockIdx.y;
+    const int bw = f.w >> 1, bh = f.h >> 1;
+    const YuvFrame& F = f.frame[cam];
+    if (F.vec) {
+        // two chunks per step, both loaded before either is converted
+        const int cw = f.w >> 3;
+        const long long chunks = (long long)cw * bh, stride = (long long)gridDim.x * blockDim.x;
+        for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < chunks; c += 2 * stride) {
+            const int by0 = (int)(c / cw), cx0 = (int)(c - (long long)by0 * cw);
+            const YuvChunk a = yuvLoad(F, cx0, by0);
+            const long long c1 = c + stride;
+            if (c1 < chunks) {
+                const int by1 = (int)(c1 / cw), cx1 = (int)(c1 - (long long)by1 * cw);
+                const YuvChunk b = yuvLoad(F, cx1, by1);
+                yuvStore(F, cx0, by0, a);
+                yuvStore(F, cx1, by1, b);
+            } else {
+                yuvStore(F, cx0, by0, a);
+            }
+        }
+        return;
+    }
+    const long long total = (long long)bw * bh;
+    for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < total;
+         b += (long long)gridDim.x * blockDim.x) {
+        const int by = (int)(b / bw), bx = (int)(b - (long long)by * bw);
+        const int x = 2 * bx, y = 2 * by;
+        const uint8_t* y0 = F.y + (size_t)y * F.yPitch + x;
+        const uint8_t* y1 = y0 + F.yPitch;
+        int u, v;
+        if (F.fmt == PS_FMT_NV12) {
+            const uint8_t* c = F.u + (size_t)by * F.uPitch + x;
+            u = c[0];
+            v = c[1];
+        } else {
+            u = F.u[(size_t)by * F.uPitch + bx];
+            v = F.v[(size_t)by * F.vPitch + bx];
+        }
+        u -= 128;
+        v -= 128;
+        const int half = 1 << (kYuvShift - 1);
+        const int ruv = half + kInvCVR * v, guv = half + kInvCVG * v + kInvCUG * u, buv = half + kInvCUB * u;
+        uint32_t* o0 = reinterpret_cast<uint32_t*>(F.dst + (size_t)y * F.dstPitch) + x;
+        uint32_t* o1 = reinterpret_cast<uint32_t*>(F.dst + (size_t)(y + 1) * F.dstPitch) + x;
+        const uint32_t p00 = yuvPixel(y0[0], ruv, guv, buv), p01 = yuvPixel(y0[1], ruv, guv, buv);
+        const uint32_t p10 = yuvPixel(y1[0], ruv, guv, buv), p11 = yuvPixel(y1[1], ruv, guv, buv);
+        if ((F.dstPitch & 7) == 0) {  // x is even, so 8-byte aligned
+            *reinterpret_cast<uint2*>(o0) = make_uint2(p00, p01);
+            *reinterpret_cast<uint2*>(o1) = make_uint2(p10, p11);
+        } else {
+            o0[0] = p00;
+            o0[1] = p01;
+            o1[0] = p10;
+            o1[1] = p11;
+        }
+    }
+}
+
 // ---- launch helpers ---------------------------------------------------------
 static int smCount()
 {
@@ -1501,6 +1628,35 @@ cudaError_t launchCvtYuv(const uint8_t* src, long long srcPitch, int w, int h, i
     if (blocks <= 0) return cudaSuccess;
     const int grid = (int)std::min<long long>((blocks + kThreads - 1) / kThreads, (long long)smCount() * 8);
     k_cvt_yuv<<<grid, kThreads, 0, st>>>(src, srcPitch, w, h, fmt, y, yPitch, u, uPitch, v, vPitch);
+    return cudaGetLastError();
+}
+
+// Frames whose width and planes allow the 8-pixel path.
+static bool yuvVector(const YuvFrame& F, int w)
+{
+    auto al = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; };
+    if (w % 8 || !al(F.y, 8) || F.yPitch % 8) return false;
+    if (F.fmt == PS_FMT_NV12) {
+        if (!al(F.u, 8) || F.uPitch % 8) return false;
+    } else if (!al(F.u, 4) || F.uPitch % 4 || !al(F.v, 4) || F.vPitch % 4) {
+        return false;
+    }
+    return al(F.dst, 16) && F.dstPitch % 16 == 0;
+}
+
+cudaError_t launchYuvToBgr32(const YuvFrames& frames, cudaStream_t st)
+{
+    if (frames.n <= 0 || frames.w <= 0 || frames.h <= 0) return cudaSuccess;
+    YuvFrames f = frames;
+    for (int i = 0; i < f.n; i++) f.frame[i].vec = yuvVector(f.frame[i], f.w) ? 1 : 0;
+    // work items per frame: 2x2 blocks, or 8x2 chunks (two per thread) on the vector path
+    bool vec = true;
+    for (int i = 0; i < f.n; i++) vec = vec && f.frame[i].vec;
+    const long long items = vec ? ((long long)(f.w / 8) * (f.h / 2) + 1) / 2 : (long long)(f.w / 2) * (f.h / 2);
+    // one wave of 8 CTAs per SM across all frames, or fewer CTAs if the work is smaller
+    const long long want = std::max<long long>(1, (long long)smCount() * 8 / f.n);
+    const int gx = (int)std::min<long long>((items + kThreads - 1) / kThreads, want);
+    k_yuv_to_bgr32<<<dim3(gx, f.n), kThreads, 0, st>>>(f);
     return cudaGetLastError();
 }
 

@@ -120,7 +120,7 @@ void Rig::clear()
         l.Am.reset();
     }
     nextSlot_ = lastSlot_ = 0;
-    maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset();
+    maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset(); planar_.reset();
     imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
     hRemap_.clear();
     hDown_.clear();
@@ -180,7 +180,7 @@ long long Rig::residentBytes() const
     }
     b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
     b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
-    b += dLinear_.bytes() + linW_.bytes();
+    b += dLinear_.bytes() + linW_.bytes() + planar_.bytes();
     return b;
 }
 
@@ -1141,10 +1141,17 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
     IoSlot& S = io_[si];
     bool hostOnly = true;
     for (const FrameInput& f : in) {
-        if (!f.src) hostOnly = false;  // level 0 written on the caller's stream
-        else
-            for (int i = 0; i < (int)rigs_[&f - in.data()]->numImages(); i++)
+        Rig* rig = rigs_[&f - in.data()];
+        if (f.psrc) {
+            rig->ensurePlanar();  // before any work of this run is queued
+            for (int i = 0; i < rig->numImages(); i++)
+                if (f.psrc[i].location != PS_MEM_HOST) hostOnly = false;
+        } else if (!f.src) {
+            hostOnly = false;  // level 0 written on the caller's stream
+        } else {
+            for (int i = 0; i < rig->numImages(); i++)
                 if (f.src[i].location != PS_MEM_HOST) hostOnly = false;
+        }
         if ((f.ydst ? f.ydst->location : f.dst->location) != PS_MEM_HOST) hostOnly = false;
     }
     if (S.used) PS_CUDA(cudaEventSynchronize(S.argsCopied));  // the slot's pinned stage is free again
@@ -1161,13 +1168,63 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
     for (size_t r = 0; r < rigs_.size(); r++) PS_CUDA(cudaStreamWaitEvent(sIn_, rigs_[r]->slotComputed(rs[r]), 0));
     uint8_t* stage = S.stage.as<uint8_t>();
     uint8_t* dArgs = S.dArgs.as<uint8_t>();
+    std::vector<YuvFrames> cvt;  // decoder frames converted into the slots' BGR32 staging
+    double cvtBytes = 0;
     for (size_t r = 0; r < rigs_.size(); r++) {
         Rig* rig = rigs_[r];
         const FrameInput& f = in[r];
         FrameDev fd;
         std::memset(&fd, 0, sizeof fd);
         const int n = rig->numImages();
-        if (f.src) {
+        if (f.psrc) {
+            YuvFrames y;
+            std::memset(&y, 0, sizeof y);
+            y.n = n;
+            y.w = rig->srcW();
+            y.h = rig->srcH();
+            const size_t w = y.w, h = y.h;
+            fd.srcFmt = PS_FMT_BGR32;
+            for (int i = 0; i < n; i++) {
+                const ps_planar_image& s = f.psrc[i];
+                YuvFrame& F = y.frame[i];
+                F.fmt = s.format;
+                const bool nv12 = s.format == PS_FMT_NV12;
+                if (s.location == PS_MEM_HOST) {  // packed planes in the slot's staging
+                    uint8_t* base = rig->planarBuffer(i, rs[r]);
+                    PS_CUDA(cudaMemcpy2DAsync(base, w, s.planes[0], s.pitches[0], w, h, cudaMemcpyHostToDevice, sIn_));
+                    F.y = base;
+                    F.yPitch = (long long)w;
+                    F.u = base + w * h;
+                    if (nv12) {
+                        F.uPitch = (long long)w;
+                        PS_CUDA(cudaMemcpy2DAsync(base + w * h, w, s.planes[1], s.pitches[1], w, h / 2,
+                                                  cudaMemcpyHostToDevice, sIn_));
+                    } else {
+                        F.uPitch = F.vPitch = (long long)(w / 2);
+                        F.v = F.u + w * h / 4;
+                        PS_CUDA(cudaMemcpy2DAsync(base + w * h, w / 2, s.planes[1], s.pitches[1], w / 2, h / 2,
+                                                  cudaMemcpyHostToDevice, sIn_));
+                        PS_CUDA(cudaMemcpy2DAsync(base + w * h + w * h / 4, w / 2, s.planes[2], s.pitches[2], w / 2,
+                                                  h / 2, cudaMemcpyHostToDevice, sIn_));
+                    }
+                } else {
+                    F.y = static_cast<const uint8_t*>(s.planes[0]);
+                    F.yPitch = s.pitches[0];
+                    F.u = static_cast<const uint8_t*>(s.planes[1]);
+                    F.uPitch = s.pitches[1];
+                    if (!nv12) {
+                        F.v = static_cast<const uint8_t*>(s.planes[2]);
+                        F.vPitch = s.pitches[2];
+                    }
+                }
+                F.dst = rig->inputBuffer(i, rs[r]);
+                F.dstPitch = rig->inputPitch();
+                fd.src[i] = F.dst;
+                fd.srcPitch[i] = rig->inputPitch();
+            }
+            cvt.push_back(y);
+            cvtBytes += (double)n * w * h * (1.5 + 4);
+        } else if (f.src) {
             fd.srcFmt = f.src[0].format;
             for (int i = 0; i < n; i++) {
                 const ps_image& s = f.src[i];
@@ -1239,6 +1296,19 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
     if (!hostOnly) PS_CUDA(cudaStreamWaitEvent(comp, callerEv_, 0));
     for (size_t r = 0; r < rigs_.size(); r++)  // the output staging has been read out
         PS_CUDA(cudaStreamWaitEvent(comp, rigs_[r]->slotDownloaded(rs[r]), 0));
+    for (const YuvFrames& y : cvt) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (prof) {
+            a = prof->event();
+            b = prof->event();
+            PS_CUDA(cudaEventRecord(a, comp));
+        }
+        PS_CUDA(launchYuvToBgr32(y, comp));
+        if (prof) {
+            PS_CUDA(cudaEventRecord(b, comp));
+            prof->record(5, 0, cvtBytes / cvt.size(), a, b);
+        }
+    }
     if (useGraph) {
         if (!S.graph) {
             cudaGraph_t g = nullptr;

@@ -63,6 +63,18 @@ public:
         return inputs_.as<uint8_t>() + ((size_t)slot * n_ + cam) * inPitch_ * srcH_;
     }
     long long inputPitch() const { return inPitch_; }
+    // Staging of decoder frames (YUV420P / NV12 host planes, 1.5 bytes per
+    // pixel, packed: Y, then U and V or UV), one set per state slot;
+    // allocated by the first render with planar sources.
+    void ensurePlanar()
+    {
+        if (!planar_.get()) planar_.alloc((size_t)slots_ * n_ * planarBytes());
+    }
+    size_t planarBytes() const { return (size_t)srcW_ * srcH_ * 3 / 2; }
+    uint8_t* planarBuffer(int cam, int slot) const
+    {
+        return planar_.as<uint8_t>() + ((size_t)slot * n_ + cam) * planarBytes();
+    }
     uint8_t* outputBuffer(int slot = 0) const { return output_.as<uint8_t>() + (size_t)slot * W_ * H_ * 4; }
     int* statusWord() const { return status_.as<int>(); }
 
@@ -139,7 +151,7 @@ private:
     uint64_t gen_ = 0;
     std::vector<LevelGeom> geom_;
     LevelBufs lv_[PS_MAX_LEVELS + 1];
-    DevBuf maps_, union_, inputs_, output_, covDev_, status_, imgArgs_;
+    DevBuf maps_, union_, inputs_, output_, covDev_, status_, imgArgs_, planar_;
     long long inPitch_ = 0;
     DevBuf dDesc_, dRemap_, dDown_, dBlend_, dCams_;
     std::vector<RemapItem> hRemap_;
@@ -182,6 +194,7 @@ struct FrameInput {
     const uint8_t* luts;      // n*768 host bytes or nullptr (identity)
     const ps_image* dst;      // BGR canvas, or nullptr when ydst is given
     const ps_planar_image* ydst = nullptr;  // YUV420P / NV12 planes instead of dst
+    const ps_planar_image* psrc = nullptr;  // numImages decoder frames (YUV420P / NV12) instead of src
 };
 
 // The launch sequence for a set of rigs: one remap launch, one pyrDown

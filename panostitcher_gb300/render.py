@@ -162,6 +162,25 @@ class CudaPanoramaRender2:
         del keep
         return self._status(st, check)
 
+    def render_planar(self, src: Sequence, dst=None, luts=None, src_fmt: int = L.PS_FMT_NV12, ydst=None,
+                      ydst_fmt: int = L.PS_FMT_NV12, stream=None, check: bool = False) -> bool:
+        """render from decoder frames: src holds one (Y, U, V) or (Y, UV) plane list
+        per camera (src_fmt, or a (planes, fmt) pair per camera), host arrays or
+        CUDA tensors; out to the BGR canvas dst or to the planes ydst."""
+        frames = []
+        for s in src:
+            if isinstance(s, tuple) and len(s) == 2 and isinstance(s[1], int):
+                frames.append(as_planar(s[0], s[1]))
+            else:
+                frames.append(as_planar(s, src_fmt))
+        arr = (PlanarImage * len(frames))(*frames)
+        keep, nl, lp = _luts_arg(luts, len(src))
+        d = C.byref(as_image(dst)) if dst is not None else None
+        y = C.byref(as_planar(ydst, ydst_fmt)) if ydst is not None else None
+        st = lib().ps_render_render_planar(self._h, arr, len(frames), lp, nl, d, y, _stream_handle(stream))
+        del keep
+        return self._status(st, check)
+
     def clear(self) -> None:
         lib().ps_render_clear(self._h)
 
@@ -187,7 +206,7 @@ class CudaPanoramaRender2:
     def profile(self, enabled: bool) -> None:
         check(lib().ps_render_profile(self._h, int(bool(enabled))))
 
-    KERNELS = {0: "k_remap", 1: "k_pyrdown", 2: "k_blend", 3: "k_tail", 4: "k_linear"}
+    KERNELS = {0: "k_remap", 1: "k_pyrdown", 2: "k_blend", 3: "k_tail", 4: "k_linear", 5: "k_yuv_to_bgr32"}
 
     def profile_read(self, kind: int, level: int = -1):
         """(launches, total_ms, algorithmic_bytes) of finished profiled launches."""
@@ -377,6 +396,14 @@ def cvt_bgr32_to_yuv(src, planes: Sequence, fmt: int = L.PS_FMT_YUV420P, stream=
     s = as_image(src)
     d = as_planar(planes, fmt)
     check(lib().ps_cvt_bgr32_to_yuv(C.byref(s), C.byref(d), _stream_handle(stream)))
+
+
+def cvt_yuv_to_bgr32(planes: Sequence, dst, fmt: int = L.PS_FMT_YUV420P, stream=None) -> None:
+    """cvtYUV420PToBGR32 / cvtNV12ToBGR32 (ImageProc.cu:165-259): (Y, U, V) or (Y, UV)
+    CUDA tensor planes to a BGR32 CUDA tensor (fourth byte 0)."""
+    s = as_planar(planes, fmt)
+    d = as_image(dst)
+    check(lib().ps_cvt_yuv_to_bgr32(C.byref(s), C.byref(d), _stream_handle(stream)))
 
 
 def load_photo_params(path: str) -> list:

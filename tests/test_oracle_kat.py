@@ -285,3 +285,58 @@ def test_linear_render_identity_kat(oracle_lib):
     ym = [np.where(cov[i] > 0, yy, -1).astype(np.float32) for i in range(2)]
     out = O.linear_render([src, src], None, xm, ym, w)
     assert np.array_equal(out[..., :3], src[..., :3]) and (out[..., 3] == 0).all()
+
+
+# ---- decoder frames: YUV420P / NV12 -> BGR32 (ImageProc.cu:165-222) ----------
+def _yuv_to_bgr_numpy(y, u, v):
+    """The reference arithmetic again, in numpy int64 (its >> is a floor)."""
+    yy = np.maximum(y.astype(np.int64) - 16, 0) * 1220542
+    cu = (u.astype(np.int64) - 128).repeat(2, 0).repeat(2, 1)
+    cv = (v.astype(np.int64) - 128).repeat(2, 0).repeat(2, 1)
+    half = 1 << 19
+    out = np.zeros(y.shape + (4,), np.uint8)
+    out[..., 0] = np.clip((yy + half + 2116026 * cu) >> 20, 0, 255)
+    out[..., 1] = np.clip((yy + half - 852492 * cv - 409993 * cu) >> 20, 0, 255)
+    out[..., 2] = np.clip((yy + half + 1673527 * cv) >> 20, 0, 255)
+    return out
+
+
+@pytest.mark.parametrize("yuv,bgr", [
+    ((16, 128, 128), (0, 0, 0)),
+    ((235, 128, 128), (255, 255, 255)),
+    ((126, 128, 128), (128, 128, 128)),
+    ((0, 128, 128), (0, 0, 0)),          # below the studio floor: max(Y - 16, 0)
+    ((16, 0, 0), (0, 154, 0)),           # B and R sums negative: floor shift, then clamp
+])
+def test_yuv_to_bgr_known_answers(oracle_lib, yuv, bgr):
+    y = np.full((2, 2), yuv[0], np.uint8)
+    u = np.full((1, 1), yuv[1], np.uint8)
+    v = np.full((1, 1), yuv[2], np.uint8)
+    out = O.yuv_to_bgr32([y, u, v])
+    assert (out[..., :3] == bgr).all(), out[0, 0]
+    assert (out[..., 3] == 0).all()
+
+
+def test_yuv_to_bgr_matches_restatement_and_nv12(oracle_lib):
+    rng = np.random.default_rng(11)
+    H, W = 34, 50
+    y = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    u = rng.integers(0, 256, (H // 2, W // 2), dtype=np.uint8)
+    v = rng.integers(0, 256, (H // 2, W // 2), dtype=np.uint8)
+    u[0, :4] = [0, 255, 0, 255]  # extremes of both chroma planes
+    v[0, :4] = [0, 0, 255, 255]
+    out = O.yuv_to_bgr32([y, u, v])
+    assert np.array_equal(out, _yuv_to_bgr_numpy(y, u, v))
+    uv = np.empty((H // 2, W), np.uint8)
+    uv[:, 0::2], uv[:, 1::2] = u, v
+    assert np.array_equal(O.yuv_to_bgr32([y, uv], O.FMT_NV12), out)
+
+
+def test_yuv_round_trip_of_block_constant_colours(oracle_lib):
+    rng = np.random.default_rng(12)
+    blk = rng.integers(0, 256, (16, 24, 3), dtype=np.uint8)
+    img = np.zeros((32, 48, 4), np.uint8)
+    img[..., :3] = blk.repeat(2, 0).repeat(2, 1)
+    for fmt in (O.FMT_YUV420P, O.FMT_NV12):
+        back = O.yuv_to_bgr32(O.bgr32_to_yuv(img, fmt), fmt)
+        assert np.abs(back[..., :3].astype(int) - img[..., :3]).max() <= 2
