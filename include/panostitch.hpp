@@ -68,6 +68,19 @@ public:
                                        correct ? getNumImages() : 0, &dst, stream));
     }
 
+    // render from decoder frames (YUV420P / NV12, host or device): the
+    // device converts them as cvtYUV420PToBGR32 / cvtNV12ToBGR32 do
+    // (source/CudaAccel/ImageProc.cu:165-259); out to a BGR canvas, or with
+    // the encoder handoff to planes (ydst)
+    bool renderPlanar(const std::vector<ps_planar_image>& src, ps_image* dst, const ps_planar_image* ydst,
+                      const std::vector<std::vector<std::vector<unsigned char>>>& luts = {}, void* stream = nullptr)
+    {
+        std::vector<unsigned char> flat;
+        const bool correct = flattenLuts(luts, flat);
+        return ok(ps_render_render_planar(r_, src.data(), (int)src.size(), correct ? flat.data() : nullptr,
+                                          correct ? getNumImages() : 0, dst, ydst, stream));
+    }
+
     void clear() { ps_render_clear(r_); }
     int getNumImages() const { return ps_render_get_num_images(r_); }
     const std::string& lastError() const { return err_; }

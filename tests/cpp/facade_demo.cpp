@@ -34,6 +34,11 @@ int main(int argc, char** argv)
                                  {frame.data(), 160 * 4, 160, 120, PS_FMT_BGR32, PS_MEM_HOST}};
     ps_image dst = {out.data(), 256 * 4, 256, 128, PS_FMT_BGR32, PS_MEM_HOST};
     if (r.render(src, dst)) return 4;  // not prepared
+    // decoder frames: NV12 gray (Y 126, U = V = 128 convert to BGR 128)
+    std::vector<unsigned char> yp(160 * 120, 126), uvp(160 * 60, 128);
+    const ps_planar_image nv12 = {{yp.data(), uvp.data(), nullptr}, {160, 160, 0}, 160, 120, PS_FMT_NV12, PS_MEM_HOST};
+    std::vector<ps_planar_image> psrc(2, nv12);
+    if (r.renderPlanar(psrc, &dst, nullptr)) return 10;  // not prepared
     if (!render) {
         std::printf("facade check ok\n");
         return 0;
@@ -60,6 +65,19 @@ int main(int argc, char** argv)
     }
     if (covered == 0) return 8;
     if (exact < covered * 9 / 10) return 9;
-    std::printf("facade render ok: %ld covered pixels, %ld exactly 77\n", covered, exact);
+    if (!r.renderPlanar(psrc, &dst, nullptr)) {
+        std::fprintf(stderr, "%s\n", r.lastError().c_str());
+        return 11;
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) return 12;
+    long covered2 = 0, exact2 = 0;
+    for (size_t i = 0; i < out.size(); i += 4) {
+        if (out[i] == 0 && out[i + 1] == 0 && out[i + 2] == 0) continue;
+        covered2++;
+        exact2 += out[i] == 128 && out[i + 1] == 128 && out[i + 2] == 128;
+    }
+    if (covered2 != covered || exact2 < covered2 * 9 / 10) return 13;
+    std::printf("facade render ok: %ld covered pixels, %ld exactly 77; from NV12 %ld exactly 128\n", covered, exact,
+                exact2);
     return 0;
 }
