@@ -648,6 +648,17 @@ constexpr int kCOff = (128 << kYuvShift) + kYuvHalf;
 
 __device__ __forceinline__ int clamp255(int v) { return min(max(v, 0), 255); }
 
+// B | G << 8 | R << 16 with each channel saturated to 0..255: two
+// cvt.pack.sat.u8.s32.b32 (PTX: d = sat(b) | sat(a) << 8 | c[15:0] << 16)
+// instead of six min / max and the shifts.
+__device__ __forceinline__ uint32_t packSatBgr(int b, int g, int r)
+{
+    uint32_t hi, out;
+    asm("cvt.pack.sat.u8.s32.b32 %0, %1, %2, %3;" : "=r"(hi) : "r"(0), "r"(r), "r"(0));
+    asm("cvt.pack.sat.u8.s32.b32 %0, %1, %2, %3;" : "=r"(out) : "r"(g), "r"(b), "r"(hi));
+    return out;
+}
+
 __device__ __forceinline__ uint32_t yuvLuma(uint32_t bgr)
 {
     const int b = bgr & 0xFF, g = (bgr >> 8) & 0xFF, r = (bgr >> 16) & 0xFF;
@@ -933,8 +944,7 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
     if (cls != 0) {
 #pragma unroll
         for (int p = 0; p < 4; p++)
-            o[p] = (uint32_t)min(max(n[p][0], 0), 255) | ((uint32_t)min(max(n[p][1], 0), 255) << 8) |
-                   ((uint32_t)min(max(n[p][2], 0), 255) << 16);
+            o[p] = packSatBgr(n[p][0], n[p][1], n[p][2]);
         if (cls == 2) {
             for (int r = 0; r < rows; r++) {
                 const uint8_t* um = G.um + (size_t)(y + r) * G.pitch + x;
@@ -1357,12 +1367,13 @@ constexpr int kInvCY = 1220542, kInvCUB = 2116026, kInvCUG = -409993, kInvCVG = 
 __device__ __forceinline__ uint32_t yuvPixel(int yv, int ruv, int guv, int buv)
 {
     const int yy = max(yv - 16, 0) * kInvCY;
-    return (uint32_t)clamp255((yy + buv) >> kYuvShift) | ((uint32_t)clamp255((yy + guv) >> kYuvShift) << 8) |
-           ((uint32_t)clamp255((yy + ruv) >> kYuvShift) << 16);
+    return packSatBgr((yy + buv) >> kYuvShift, (yy + guv) >> kYuvShift, (yy + ruv) >> kYuvShift);
 }
 
 // Eight pixels of a row pair (four 2x2 blocks) per thread: 8-byte luma
 // loads, the blocks' chroma in one load, 16-byte stores.
+constexpr int kYuvChunks = 2;  // chunks a thread has in flight (4 measured slower)
+
 struct YuvChunk {
     uint2 yt, yb;     // luma of the top and bottom rows
     uint32_t us, vs;  // the four blocks' U and V, one byte each
@@ -1414,29 +1425,29 @@ __global__ void __launch_bounds__(kThreads) k_yuv_to_bgr32(YuvFrames f)
     const int cam = blockIdx.y;
     const int bw = f.w >> 1, bh = f.h >> 1;
     const YuvFrame& F = f.frame[cam];
+    // the launcher takes frames below 2^32 pixels, so 32-bit indices cover the work
     if (F.vec) {
-        // two chunks per step, both loaded before either is converted
-        const int cw = f.w >> 3;
-        const long long chunks = (long long)cw * bh, stride = (long long)gridDim.x * blockDim.x;
-        for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < chunks; c += 2 * stride) {
-            const int by0 = (int)(c / cw), cx0 = (int)(c - (long long)by0 * cw);
-            const YuvChunk a = yuvLoad(F, cx0, by0);
-            const long long c1 = c + stride;
-            if (c1 < chunks) {
-                const int by1 = (int)(c1 / cw), cx1 = (int)(c1 - (long long)by1 * cw);
-                const YuvChunk b = yuvLoad(F, cx1, by1);
-                yuvStore(F, cx0, by0, a);
-                yuvStore(F, cx1, by1, b);
-            } else {
-                yuvStore(F, cx0, by0, a);
+        // kYuvChunks chunks per step, all loaded before any is converted
+        const unsigned cw = (unsigned)f.w >> 3;
+        const unsigned chunks = cw * (unsigned)bh, stride = gridDim.x * blockDim.x;
+        for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < chunks; c += kYuvChunks * stride) {
+            YuvChunk v[kYuvChunks];
+#pragma unroll
+            for (int k = 0; k < kYuvChunks; k++) {
+                const unsigned ck = c + k * stride, by = ck / cw;
+                if (ck < chunks) v[k] = yuvLoad(F, (int)(ck - by * cw), (int)by);
+            }
+#pragma unroll
+            for (int k = 0; k < kYuvChunks; k++) {
+                const unsigned ck = c + k * stride, by = ck / cw;
+                if (ck < chunks) yuvStore(F, (int)(ck - by * cw), (int)by, v[k]);
             }
         }
         return;
     }
-    const long long total = (long long)bw * bh;
-    for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < total;
-         b += (long long)gridDim.x * blockDim.x) {
-        const int by = (int)(b / bw), bx = (int)(b - (long long)by * bw);
+    const unsigned total = (unsigned)bw * (unsigned)bh;
+    for (unsigned b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
+        const int by = (int)(b / (unsigned)bw), bx = (int)(b - (unsigned)by * (unsigned)bw);
         const int x = 2 * bx, y = 2 * by;
         const uint8_t* y0 = F.y + (size_t)y * F.yPitch + x;
         const uint8_t* y1 = y0 + F.yPitch;
@@ -1647,12 +1658,14 @@ static bool yuvVector(const YuvFrame& F, int w)
 cudaError_t launchYuvToBgr32(const YuvFrames& frames, cudaStream_t st)
 {
     if (frames.n <= 0 || frames.w <= 0 || frames.h <= 0) return cudaSuccess;
+    if ((long long)frames.w * frames.h >= (1LL << 32)) return cudaErrorInvalidValue;
     YuvFrames f = frames;
     for (int i = 0; i < f.n; i++) f.frame[i].vec = yuvVector(f.frame[i], f.w) ? 1 : 0;
-    // work items per frame: 2x2 blocks, or 8x2 chunks (two per thread) on the vector path
+    // work items per frame: 2x2 blocks, or 8x2 chunks (kYuvChunks per thread) on the vector path
     bool vec = true;
     for (int i = 0; i < f.n; i++) vec = vec && f.frame[i].vec;
-    const long long items = vec ? ((long long)(f.w / 8) * (f.h / 2) + 1) / 2 : (long long)(f.w / 2) * (f.h / 2);
+    const long long items = vec ? ((long long)(f.w / 8) * (f.h / 2) + kYuvChunks - 1) / kYuvChunks
+                                : (long long)(f.w / 2) * (f.h / 2);
     // one wave of 8 CTAs per SM across all frames, or fewer CTAs if the work is smaller
     const long long want = std::max<long long>(1, (long long)smCount() * 8 / f.n);
     const int gx = (int)std::min<long long>((items + kThreads - 1) / kThreads, want);
