@@ -659,10 +659,21 @@ __device__ __forceinline__ uint32_t packSatBgr(int b, int g, int r)
     return out;
 }
 
-__device__ __forceinline__ uint32_t yuvLuma(uint32_t bgr)
+// Luma before saturation; yuvLuma saturates it.
+__device__ __forceinline__ int yuvLumaRaw(uint32_t bgr)
 {
     const int b = bgr & 0xFF, g = (bgr >> 8) & 0xFF, r = (bgr >> 16) & 0xFF;
-    return (uint32_t)clamp255((kYR * r + kYG * g + kYB * b + kYOff) >> kYuvShift);
+    return (kYR * r + kYG * g + kYB * b + kYOff) >> kYuvShift;
+}
+
+__device__ __forceinline__ uint32_t yuvLuma(uint32_t bgr) { return (uint32_t)clamp255(yuvLumaRaw(bgr)); }
+
+// sat(lo) | sat(hi) << 8, each saturated to 0..255 (one cvt.pack.sat)
+__device__ __forceinline__ uint32_t packSat2(int lo, int hi)
+{
+    uint32_t out;
+    asm("cvt.pack.sat.u8.s32.b32 %0, %1, %2, %3;" : "=r"(out) : "r"(hi), "r"(lo), "r"(0));
+    return out;
 }
 
 // Unshifted chroma sums of one pixel (both are non-negative).
@@ -680,22 +691,22 @@ __device__ __forceinline__ void storeYuv(const UnitGeo& G, int x, int y, const u
 #pragma unroll
     for (int r = 0; r < 2; r++) {
         uint8_t* yrow = G.out + (size_t)(y + r) * G.outPitch + x;
-        const uint32_t y0 = yuvLuma(o[2 * r]), y1 = yuvLuma(o[2 * r + 1]);
+        const uint32_t yy = packSat2(yuvLumaRaw(o[2 * r]), yuvLumaRaw(o[2 * r + 1]));
         if ((reinterpret_cast<uintptr_t>(yrow) & 1) == 0) {
-            *reinterpret_cast<uint16_t*>(yrow) = (uint16_t)(y0 | (y1 << 8));
+            *reinterpret_cast<uint16_t*>(yrow) = (uint16_t)yy;
         } else {
-            yrow[0] = (uint8_t)y0;
-            yrow[1] = (uint8_t)y1;
+            yrow[0] = (uint8_t)yy;
+            yrow[1] = (uint8_t)(yy >> 8);
         }
     }
     const int2 c = yuvChromaSums(o[0]), d = yuvChromaSums(o[2]);
-    const uint8_t u = (uint8_t)clamp255((c.x + d.x) >> (kYuvShift + 1));
-    const uint8_t v = (uint8_t)clamp255((c.y + d.y) >> (kYuvShift + 1));
+    const uint32_t uv = packSat2((c.x + d.x) >> (kYuvShift + 1), (c.y + d.y) >> (kYuvShift + 1));
+    const uint8_t u = (uint8_t)uv, v = (uint8_t)(uv >> 8);
     const size_t cy = (size_t)(y >> 1);
     if (G.outFmt == PS_FMT_NV12) {
         uint8_t* p = G.outU + cy * G.outCPitch + x;
         if ((reinterpret_cast<uintptr_t>(p) & 1) == 0) {
-            *reinterpret_cast<uint16_t*>(p) = (uint16_t)(u | (v << 8));
+            *reinterpret_cast<uint16_t*>(p) = (uint16_t)uv;
         } else {
             p[0] = u;
             p[1] = v;
