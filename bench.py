@@ -4,7 +4,7 @@
 Headline: stitched output Mpix/s of the plain per-frame path on the
 6-camera rig (6 x 1920x1080 rectilinear, 100 deg -> 4096x2048 equirect,
 8-level multiband blend, per-camera LUT gains), frames resident in HBM,
-issued in turn on four streams so four frames are in flight (the
+issued in turn on eight streams so eight frames are in flight (the
 single-stream figure is reported beside it).
 The same line carries:
   e2e         the same metric through the C ABI with pinned host frames in
@@ -237,7 +237,7 @@ def run_ours(args, world, rank, local, dist):
     tune = None
     if not args.no_tune:
         t = time.perf_counter()
-        tune = r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 4))
+        tune = r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 8))
         tune["seconds"] = round(time.perf_counter() - t, 2)
     fs = S.FrameSource(cfg)
     pool_host = [fs.frame(k) for k in range(args.pool)]
@@ -247,7 +247,7 @@ def run_ours(args, world, rank, local, dist):
 
     # ---- device-resident throughput (CUDA graph per frame).  Frames go out
     # in turn on `inflight` streams, each with its own canvas, so up to that
-    # many frames are in flight (the render keeps four state slots).
+    # many frames are in flight (the render keeps eight state slots).
     streams = [torch.cuda.Stream(device=dev) for _ in range(args.inflight)]
     dsts = [dst] + [torch.empty_like(dst) for _ in range(args.inflight - 1)]
 
@@ -275,8 +275,16 @@ def run_ours(args, world, rank, local, dist):
     sampler.start()
     ms = timed(args.steps, args.inflight)
     clocks = sampler.stop()
+    # one frame at a time, with the launch shape tuned for that (cached after
+    # the first call), then the in-flight shape again for the legs below
     single_steps = max(10, args.steps // 2)
+    single_shape = r.launch_shape()
+    if not args.no_tune:
+        single_shape = r.autotune(frames_per_trial=20, in_flight=1)["shape"]
+    timed(args.warmup, 1)
     single_ms = timed(single_steps, 1) / single_steps
+    if not args.no_tune:
+        r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 8))
     ms_max = reduce_max(ms, dist, dev)
     barrier(dist)
     value = aggregate_mpix(world, args.steps, npx, ms_max)
@@ -286,7 +294,8 @@ def run_ours(args, world, rank, local, dist):
            "data": f"synthetic: seeded smooth field + per-frame noise, pool of {args.pool} frames in HBM",
            "gpu_launches": args.steps * r.launches_per_frame,
            "frames_in_flight": args.inflight,
-           "single_stream": {"value": round(npx / single_ms / 1e3, 3), "ms_per_step": round(single_ms, 5)},
+           "single_stream": {"value": round(npx / single_ms / 1e3, 3), "ms_per_step": round(single_ms, 5),
+                             "launch_shape": single_shape},
            "clocks": clocks}
     resident = r.resident_bytes
     frame_mb = sum(f.nbytes for f in pool_host[0]) / 1e6
@@ -392,7 +401,11 @@ def run_ours(args, world, rank, local, dist):
     out["e2e_planar"]["k_yuv_to_bgr32"] = {"us_per_frame": round(ms5 / max(n5, 1) * 1e3, 2),
                                            "alg_GBps": round(b5 / max(ms5, 1e-9) / 1e6, 1)}
 
-    # ---- roofline: profiled pass (a CUDA event pair around every launch)
+    # ---- roofline: profiled pass (a CUDA event pair around every launch).
+    # Launches are timed one at a time, so the pass uses the shape tuned for
+    # one frame in flight.
+    if not args.no_tune:
+        r.set_launch_shape(**single_shape)
     r.profile(True)
     prof_steps = min(args.steps, 30)
     for k in range(prof_steps):
@@ -668,7 +681,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--pool", type=int, default=4)
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
-    ap.add_argument("--inflight", type=int, default=4, help="caller streams of the device-resident loop")
+    ap.add_argument("--inflight", type=int, default=8, help="caller streams of the device-resident loop")
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -39,6 +39,7 @@ extern "C" {
 
 #define PS_MAX_LEVELS 16   /* getTrueNumLevels cap, source/Blend/MultiBandBlend.cpp:325 */
 #define PS_MAX_CAMS 64     /* cameras per rig */
+#define PS_MAX_IN_FLIGHT 8 /* frames of one render in flight (state slots) */
 
 /* PhotoParam, source/Warp/ZReproject.h:17-50 (same fields, same order,
    same meaning: image_type 0 rectilinear, 1 full-frame fisheye,
@@ -137,7 +138,8 @@ int ps_render_prepare_with_seams(ps_render* r, const ps_photo_param* params, int
    the call (pinned memory keeps the copies asynchronous); device src / dst
    are read / written in place.  The work runs on the render's own copy-in,
    compute and copy-out streams, and the caller's stream waits for its
-   completion.  A render keeps four sets of per-frame state, so four calls
+   completion.  A render keeps a set of per-frame state per frame in flight
+   (ps_render_set_frames_in_flight; eight by default), so that many calls
    can be in flight: with host src and dst a call does not wait for the
    caller's earlier work (consecutive calls overlap their uploads, kernels
    and downloads); with device src or dst it waits for the caller's stream,
@@ -168,6 +170,13 @@ int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const u
 #define PS_SEAMS_NEAREST_AXIS 0
 #define PS_SEAMS_DISTANCE 1
 int ps_render_set_seam_rule(ps_render* r, int rule);
+/* Frames in flight, 1..PS_MAX_IN_FLIGHT (default PS_MAX_IN_FLIGHT): the sets
+   of per-frame state (pyramids, staging) the next prepare allocates.  Fewer
+   save device memory; more let consecutive renders overlap on the GPU.
+   No reference counterpart (the reference renders one frame at a time). */
+int ps_render_set_frames_in_flight(ps_render* r, int n);
+/* The prepared render's frames in flight (0 before prepare). */
+int ps_render_get_frames_in_flight(const ps_render* r);
 /* CudaPanoramaRender2::render with decoder frames: src holds num_src YUV420P
    or NV12 frames (BT.601 studio range, src_w x src_h, host or device, each
    its own format), converted on the device to BGR32 as cvtYUV420PToBGR32 /
@@ -260,7 +269,7 @@ int ps_render_set_launch_shape(ps_render* r, const ps_launch_shape* shape);
 int ps_render_get_launch_shape(const ps_render* r, ps_launch_shape* shape);
 /* Times launch shapes on the prepared render (frames_per_trial frames per
    timed run, 0 = 20; issued round-robin on in_flight streams, 0 = the
-   render's four frames in flight) by coordinate descent from the default
+   render's frames in flight) by coordinate descent from the default
    shape, and keeps the fastest.  The render's slot-0 input buffers are
    overwritten with a test pattern.  A geometry tuned before in this
    process is not timed again unless force is non-zero.  Blocks (about a

@@ -6,7 +6,7 @@ to 8-bit BGR.  The kernels live in libpanostitch.so (built in-tree by
 ``panostitcher_gb300.build``); this package only binds and drives them.
 """
 from ._lib import (PsError, PhotoParam, Image, PlanarImage, lib, PS_FMT_YUV420P, PS_FMT_NV12,  # noqa: F401
-                   PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE)
+                   PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE, PS_MAX_IN_FLIGHT)
 from .render import (CudaPanoramaRender2, CudaTilingMultibandBlendFast, render_batch,  # noqa: F401
                      generate_reproject_map_and_mask, reproject_to_16s, get_lut, as_image, as_planar,
                      cvt_bgr32_to_yuv, cvt_yuv_to_bgr32, non_intersecting_masks, distance_transform_l1,
@@ -16,4 +16,4 @@ __all__ = ["CudaPanoramaRender2", "CudaTilingMultibandBlendFast", "render_batch"
            "generate_reproject_map_and_mask", "reproject_to_16s", "get_lut", "as_image", "as_planar",
            "cvt_bgr32_to_yuv", "cvt_yuv_to_bgr32", "non_intersecting_masks", "distance_transform_l1",
            "load_photo_params", "PsError", "PhotoParam", "Image", "PlanarImage", "lib", "PS_FMT_YUV420P",
-           "PS_FMT_NV12", "PS_SEAMS_NEAREST_AXIS", "PS_SEAMS_DISTANCE"]
+           "PS_FMT_NV12", "PS_SEAMS_NEAREST_AXIS", "PS_SEAMS_DISTANCE", "PS_MAX_IN_FLIGHT"]

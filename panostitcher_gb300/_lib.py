@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpanostitch.so")
 
 PS_OK, PS_EINVAL, PS_ENOMEM, PS_ECUDA, PS_ETIMEOUT, PS_ESTATE = 0, 1, 2, 3, 4, 5
-PS_MAX_LEVELS, PS_MAX_CAMS = 16, 64
+PS_MAX_LEVELS, PS_MAX_CAMS, PS_MAX_IN_FLIGHT = 16, 64, 8
 PS_FMT_BGR24, PS_FMT_BGR32 = 24, 32
 PS_FMT_YUV420P, PS_FMT_NV12 = 420, 12
 PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE = 0, 1
@@ -95,6 +95,8 @@ _SIGS = [
                                          C.c_int, C.c_void_p]),
     ("ps_load_photo_params", C.c_int, [C.c_char_p, C.POINTER(PhotoParam), C.c_int, C.POINTER(C.c_int)]),
     ("ps_render_set_seam_rule", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_render_set_frames_in_flight", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_render_get_frames_in_flight", C.c_int, [C.c_void_p]),
     ("ps_render_render_planar", C.c_int, [C.c_void_p, C.POINTER(PlanarImage), C.c_int, C.c_void_p, C.c_int,
                                           C.POINTER(Image), C.POINTER(PlanarImage), C.c_void_p]),
     ("ps_render_set_graph", C.c_int, [C.c_void_p, C.c_int]),

@@ -319,6 +319,17 @@ int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const u
     });
 }
 
+int ps_render_set_frames_in_flight(ps_render* r, int n)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (n < 1 || n > PS_MAX_IN_FLIGHT) fail(PS_EINVAL, "frames in flight %d not in 1..%d", n, PS_MAX_IN_FLIGHT);
+        r->rig.setSlots(n);
+    });
+}
+
+int ps_render_get_frames_in_flight(const ps_render* r) { return r && r->rig.ready() ? r->rig.slots() : 0; }
+
 int ps_render_render_planar(ps_render* r, const ps_planar_image* src, int num_src, const uint8_t* luts,
                             int num_luts, const ps_image* dst, const ps_planar_image* ydst, void* stream)
 {

@@ -54,7 +54,7 @@ public:
     // Device staging of host frames and of a host canvas: one set per state
     // slot, so consecutive renders with host buffers overlap their copies (slot 0's
     // frame buffers are also the ones ps_render_get_input_buffer exposes).
-    static constexpr int kIoSlots = 4;  // most state slots a rig keeps
+    static constexpr int kIoSlots = PS_MAX_IN_FLIGHT;  // most state slots a rig keeps
     // state slots of the next prepare (1..kIoSlots; default kIoSlots)
     void setSlots(int n) { slotsWanted_ = n < 1 ? 1 : (n > kIoSlots ? kIoSlots : n); }
     int slots() const { return slots_; }

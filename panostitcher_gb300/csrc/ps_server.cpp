@@ -27,6 +27,7 @@ struct ps_server {
     std::map<int, std::unique_ptr<ps::Rig>> streams;
     int nextId = 0;
     static constexpr int kSlots = 2;
+    static constexpr long long kTickBytes = 256LL << 20;  // host-frame bytes a tick uploads at most
     // a stream has at most one frame in flight, so its rig keeps one state slot
     static constexpr int kRigSlots = 1;
     cudaStream_t cs[kSlots] = {};
@@ -219,6 +220,18 @@ int ps_server_run_trace(ps_server* s, int num_frames, const int* stream_ids, con
                     if (heads.empty()) break;
                     std::sort(heads.begin(), heads.end());
                     if ((int)heads.size() > s->maxBatch) heads.resize(s->maxBatch);
+                    // every frame of a tick completes with the tick, so a tick
+                    // takes frames (oldest first) only up to kTickBytes of
+                    // uploads: a small frame is not held behind many large ones
+                    long long bytes = 0;
+                    size_t take = 0;
+                    for (; take < heads.size(); take++) {
+                        const ps::Rig& rg = *s->streams[heads[take].second];
+                        const long long b = (long long)rg.numImages() * rg.srcW() * rg.srcH() * 4;
+                        if (take > 0 && bytes + b > ps_server::kTickBytes) break;
+                        bytes += b;
+                    }
+                    heads.resize(take);
                     std::vector<ps::Rig*> rigs;
                     std::vector<ps::FrameInput> in;
                     for (auto& h : heads) {
@@ -240,7 +253,9 @@ int ps_server_run_trace(ps_server* s, int num_frames, const int* stream_ids, con
                 } else {
                     if (nowNs() - lastProgress > stallLimit) fail(PS_ETIMEOUT, "no progress for 120 s");
                     long long wait = 20000;  // poll every 20 us while ticks run
-                    if (next < num_frames && !active[0] && !active[1])
+                    bool anyActive = false;
+                    for (int sl = 0; sl < ps_server::kSlots; sl++) anyActive = anyActive || active[sl];
+                    if (next < num_frames && !anyActive)
                         wait = std::max(0LL, std::min(arrival_ns[next] - nowNs(), 1000000LL));
                     if (wait > 0) std::this_thread::sleep_for(std::chrono::nanoseconds(wait));
                 }

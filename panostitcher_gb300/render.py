@@ -138,6 +138,14 @@ class CudaPanoramaRender2:
                                           src_size[1], dst_size[0], dst_size[1], _stream_handle(stream))
         return self._status(st, check)
 
+    def set_frames_in_flight(self, n: int) -> None:
+        """Sets of per-frame state the next prepare allocates (1..PS_MAX_IN_FLIGHT)."""
+        check(lib().ps_render_set_frames_in_flight(self._h, n))
+
+    @property
+    def frames_in_flight(self) -> int:
+        return lib().ps_render_get_frames_in_flight(self._h)
+
     def set_seam_rule(self, rule: int) -> None:
         """PS_SEAMS_NEAREST_AXIS (default) or PS_SEAMS_DISTANCE (getNonIntersectingMasks); next prepare."""
         check(lib().ps_render_set_seam_rule(self._h, rule))

@@ -139,3 +139,16 @@ def test_launch_shape_validation_before_the_gpu(built_lib):
     assert e.value.code == L.PS_ESTATE
     assert built_lib.ps_render_set_launch_shape(None, None) == L.PS_EINVAL
     assert built_lib.ps_render_autotune(None, 0, 0, 0, None, None) == L.PS_EINVAL
+
+
+def test_frames_in_flight_validation_before_the_gpu(built_lib):
+    r = P.CudaPanoramaRender2()
+    assert r.frames_in_flight == 0  # not prepared
+    for bad in (0, -1, L.PS_MAX_IN_FLIGHT + 1):
+        with pytest.raises(P.PsError) as e:
+            r.set_frames_in_flight(bad)
+        assert e.value.code == L.PS_EINVAL
+    r.set_frames_in_flight(1)
+    r.set_frames_in_flight(L.PS_MAX_IN_FLIGHT)
+    assert built_lib.ps_render_set_frames_in_flight(None, 2) == L.PS_EINVAL
+    assert built_lib.ps_render_get_frames_in_flight(None) == 0

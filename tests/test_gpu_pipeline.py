@@ -1,6 +1,6 @@
 """Renders in flight together (GPU).
 
-A render keeps four sets of per-frame state, so consecutive calls with host
+A render keeps eight sets of per-frame state, so consecutive calls with host
 buffers, and calls issued on several streams, overlap on the GPU.  Every frame
 must still come out exactly as the oracle stitches it alone.
 """
@@ -70,3 +70,24 @@ def test_yuv_and_bgr_interleaved(prepared):
         full[..., :3] = refs[2 * k + 1]
         for got, want in zip(nv12[k], O.bgr32_to_yuv(full, O.FMT_NV12)):
             assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("slots", [1, 3])
+def test_fewer_frames_in_flight(cuda, oracle_lib, slots):
+    torch = cuda
+    cfg = S.scaled_rig(S.rig("c2"), 8)
+    full = Prepared(cfg)
+    r = P.CudaPanoramaRender2()
+    r.set_frames_in_flight(slots)
+    r.prepare(cfg.cams, 1, cfg.levels, cfg.src_size, cfg.dst_size, check=True)
+    assert r.frames_in_flight == slots and full.r.frames_in_flight == P.PS_MAX_IN_FLIGHT
+    assert r.resident_bytes < full.r.resident_bytes  # fewer sets of per-frame state
+    W, H = cfg.dst_size
+    frames = [full.frames.frame(k) for k in range(5)]
+    outs = [np.zeros((H, W, 4), np.uint8) for _ in frames]
+    for f, o in zip(frames, outs):  # more calls than slots, no synchronisation
+        assert r.render(f, o, full.luts, check=True)
+    torch.cuda.synchronize()
+    for f, o in zip(frames, outs):
+        ref = full.oracle_render(f, full.luts)[..., :3]
+        assert np.array_equal(o[..., :3], ref), diff_histogram(o[..., :3], ref)

@@ -78,7 +78,7 @@ def test_autotune_one_stream_and_bad_arguments(cuda):
     rep = r.autotune(frames_per_trial=3, in_flight=1)
     assert rep["trials"] >= 2
     with pytest.raises(P.PsError):
-        r.autotune(in_flight=5)  # more than the render's four frames in flight
+        r.autotune(in_flight=9)  # more than the render's eight frames in flight
     with pytest.raises(P.PsError):
         r.autotune(frames_per_trial=-1)
 
