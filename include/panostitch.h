@@ -223,7 +223,8 @@ int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out,
    (no graph); ps_render_profile_read aggregates the finished launches of
    one kernel kind (0 remap, 1 pyrDown, 2 blend, 3 the tail kernel that runs
    the few-tile top levels, reported at its lowest blend level, 4 the
-   linear-blend render, 5 the conversion of decoder frames, at level 0) at
+   linear-blend render, 5 the conversion of decoder frames, at level 0, 6
+   the blend of few-tile levels in half tiles) at
    one level (-1 = all levels): launch count, summed device milliseconds
    and summed algorithmic bytes (each input and output element counted
    once).
@@ -255,6 +256,9 @@ typedef struct ps_launch_shape {
                              two pixels per thread; 0: whole tiles (default 1) */
     int ctas_per_sm[3];   /* CTAs per SM of the remap, pyrDown and blend kernels'
                              one-wave grids; 0 = as many as fit (default 0) */
+    int small_blend_max_items; /* blend levels above 0 (below the tail) with at
+                             most this many tiles run as 64x8 half tiles, up to
+                             eight cameras staged at once; 0 = none (default 0) */
 } ps_launch_shape;
 typedef struct ps_tune_report {
     double ms_per_frame_default;  /* device ms per frame of the default shape */

@@ -152,10 +152,12 @@ struct LaunchShape {
     int tailCluster = 0;           // CTAs per rig in the tail kernel: 8, 16, or 0 = the widest co-schedulable
     int tailHalf = 1;              // the tail blends levels above 0 in 64x8 half tiles
     int ctasPerSm[3] = {0, 0, 0};  // k_remap, k_pyrdown, k_blend; 0 = as many as fit
+    int smallBlendMaxItems = 0;    // blend levels above 0 with at most this many tiles run in k_blend_small
     bool operator==(const LaunchShape& o) const
     {
         return tailMaxItems == o.tailMaxItems && tailCluster == o.tailCluster && tailHalf == o.tailHalf &&
-               ctasPerSm[0] == o.ctasPerSm[0] && ctasPerSm[1] == o.ctasPerSm[1] && ctasPerSm[2] == o.ctasPerSm[2];
+               ctasPerSm[0] == o.ctasPerSm[0] && ctasPerSm[1] == o.ctasPerSm[1] && ctasPerSm[2] == o.ctasPerSm[2] &&
+               smallBlendMaxItems == o.smallBlendMaxItems;
     }
     bool operator!=(const LaunchShape& o) const { return !(*this == o); }
 };
@@ -165,6 +167,8 @@ struct LaunchShape {
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
+// blend of few-tile levels above 0: two work items (the 64x8 halves) per tile
+cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st);
 // one cluster per segment: the rig's pyrDown levels tailDown..L and blend
 // levels L..tailBlend; cluster 8 or 16 CTAs (0 or more than the GPU
 // co-schedules: the widest it does)

@@ -1326,6 +1326,42 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
 }
 
 // ============================================================================
+// k_blend_small: blend levels above 0 with few tiles, below the tail.  The
+// tail kernel's per-unit code on a plain grid: one 64x8 half tile per work
+// item (items 2t and 2t + 1 are the halves of tile t), up to eight cameras
+// staged per unit.  In k_blend a CTA walks a tile's cameras two at a time,
+// a chain of load-and-compute rounds that these levels cannot hide behind
+// other tiles; here each CTA has one short chain and all its warps busy.
+// ============================================================================
+using SmallStage = BlendStageT<kTailCamsPerUnit>;
+
+__global__ void __launch_bounds__(kThreads) k_blend_small(const Segment* __restrict__ segs, int nsegs, int total)
+{
+    extern __shared__ __align__(16) uint8_t smallSmem[];  // a SmallStage (dynamic: above the 48 KB static limit)
+    SmallStage& st = *reinterpret_cast<SmallStage*>(smallSmem);
+    __shared__ int fRow[kFH], fCol[kFW];
+    waitPrevGrid();
+    allowNextGrid();
+    int s = 0;
+    PairAcc acc;
+    for (int it = blockIdx.x; it < total; it += gridDim.x) {
+        s = findSegment(segs, nsegs, it, s);
+        const Segment& sg = segs[s];
+        const RigDev& R = *sg.rig;
+        const int local = it - sg.prefix, half = local & 1;
+        const uint4 raw = __ldg(static_cast<const uint4*>(sg.items) + (local >> 1));
+        UnitGeo geo;
+        fillGeo(geo, R, *sg.frame, raw.x & 0xFF);
+        for (int chunk = 0; chunk < unitChunks<kTailCamsPerUnit>(raw); chunk++) {
+            __syncthreads();  // readers of the previous unit are done
+            stageUnitDirect<false>(st, R, raw, chunk, fRow, fCol, [] { __syncthreads(); }, half);
+            __syncthreads();
+            computeUnitRows(st, geo, raw, chunk, acc, half);
+        }
+    }
+}
+
+// ============================================================================
 // k_cvt_yuv: standalone BGR32 -> YUV420P / NV12 of a device image
 // (cvtBGR32ToYUV420P / cvtBGR32ToNV12, ImageProc.cu:97-160).  One thread per
 // 2x2 block, consecutive threads on consecutive blocks of a block row.
@@ -1592,6 +1628,27 @@ cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, cu
     if (total <= 0) return cudaSuccess;
     return launchPdl(k_blend, gridFor(total, residentPerSm<k_blend>(kBlendThreads), perSm), kBlendThreads, st, segs,
                      nsegs, total);
+}
+
+cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st)
+{
+    if (total <= 0) return cudaSuccess;
+    static int perSm = 0;
+    if (!perSm) {
+        cudaFuncSetAttribute(k_blend_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmallStage));
+        perSm = residentPerSm<k_blend_small>(kThreads, sizeof(SmallStage));
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(gridFor(total, perSm));
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = sizeof(SmallStage);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_blend_small, segs, nsegs, total);
 }
 
 int tailClusterMax()

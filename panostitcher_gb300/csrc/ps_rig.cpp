@@ -597,6 +597,8 @@ void Rig::setShape(const LaunchShape& s)
     if (s.tailCluster != 0 && s.tailCluster != 8 && s.tailCluster != 16)
         fail(PS_EINVAL, "tail_cluster must be 0, 8 or 16 (got %d)", s.tailCluster);
     if (s.tailHalf != 0 && s.tailHalf != 1) fail(PS_EINVAL, "tail_half_tiles must be 0 or 1 (got %d)", s.tailHalf);
+    if (s.smallBlendMaxItems < 0 || s.smallBlendMaxItems > (1 << 24))
+        fail(PS_EINVAL, "small_blend_max_items %d out of range", s.smallBlendMaxItems);
     for (int k = 0; k < 3; k++)
         if (s.ctasPerSm[k] < 0 || s.ctasPerSm[k] > 64)
             fail(PS_EINVAL, "ctas_per_sm[%d] = %d out of range 0..64", k, s.ctasPerSm[k]);
@@ -1019,7 +1021,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
             const Rig* rg = rigs[p.first];
             const int lvl = kind == 0 || kind == 4 ? 0 : (kind == 1 ? step : rg->tailBlend() - 1 - step);
             if (s.level < 0) s.level = lvl;
-            s.bytes += rg->stepBytes(kind, lvl);
+            s.bytes += rg->stepBytes(kind == 6 ? 2 : kind, lvl);
         }
         s.nsegs = (int)segs_.size() - s.segOff;
         if (s.total > 0) steps_.push_back(s);
@@ -1057,12 +1059,18 @@ void Plan::bind(const std::vector<Rig*>& rigs)
     for (Rig* r : rigs)
         if (!r->linear()) maxB = std::max(maxB, r->tailBlend());
     for (int s = 0; s < maxB; s++) {
+        // levels above 0 with few tiles go to k_blend_small (two halves per tile)
+        std::vector<std::pair<int, std::pair<const void*, int>>> small;
         parts.clear();
         for (int r = 0; r < nr; r++) {
             if (rigs[r]->linear()) continue;
             const int j = rigs[r]->tailBlend() - 1 - s;
-            if (j >= 0) parts.push_back({r, {rigs[r]->blendItems(j), rigs[r]->numBlendItems(j)}});
+            if (j < 0) continue;
+            const int cnt = rigs[r]->numBlendItems(j);
+            if (j > 0 && cnt <= rigs[r]->shape().smallBlendMaxItems) small.push_back({r, {rigs[r]->blendItems(j), 2 * cnt}});
+            else parts.push_back({r, {rigs[r]->blendItems(j), cnt}});
         }
+        addStep(6, small, s);
         addStep(2, parts, s);
     }
     const size_t need = segOff_ + std::max<size_t>(1, segs_.size()) * sizeof(Segment);
@@ -1115,6 +1123,7 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, perSm_[1], st));
         else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], st));
         else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, tailCluster_, st));
+        else if (s.kind == 6) PS_CUDA(launchBlendSmall(p, s.nsegs, s.total, st));
         else PS_CUDA(launchLinear(p, s.nsegs, s.total, maxCams_, st));
         if (prof) {
             PS_CUDA(cudaEventRecord(b, st));

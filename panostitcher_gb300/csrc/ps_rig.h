@@ -217,7 +217,7 @@ public:
 
 private:
     struct Step {
-        int kind;  // 0 remap, 1 pyrDown, 2 blend, 3 tail, 4 linear-blend render
+        int kind;  // 0 remap, 1 pyrDown, 2 blend, 3 tail, 4 linear-blend render, 6 few-tile blend
         int segOff, nsegs, total;
         int level;      // level of the first rig in the step
         double bytes;   // algorithmic bytes of the step (all rigs)
@@ -253,8 +253,9 @@ private:
 };
 
 // The autotuner (ps_tune.cpp): times launch shapes on a prepared rig by
-// coordinate descent from the default shape (tail split, tail tile split,
-// tail cluster width, CTAs per SM of k_blend, k_pyrdown, k_remap), frames
+// coordinate descent from the default shape (tail split, the levels run as
+// half tiles by k_blend_small, tail tile split, tail cluster width, CTAs per
+// SM of k_blend, k_pyrdown, k_remap), frames
 // issued round-robin on `inflight` streams, and leaves the fastest set on
 // the rig and bound to the plan.  Results are kept per rig geometry, GPU and
 // concurrency, so a later call for the same geometry times nothing unless

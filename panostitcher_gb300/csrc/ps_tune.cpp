@@ -175,6 +175,23 @@ std::vector<LaunchShape> neighbours(const Rig& rig, const LaunchShape& cur, int 
             out.push_back(s);
         }
         break;
+    case 6: {  // the blend levels run as half tiles by k_blend_small: one value per distinct set
+        auto smallLevels = [&](int v) {
+            int c = 0;
+            for (int j = 1; j < curBlend; j++) c += rig.numBlendItems(j) <= v;
+            return c;
+        };
+        std::vector<int> seen{smallLevels(cur.smallBlendMaxItems)};
+        for (int v : {0, 32, 64, 128, 256, 512, 1024, 2048, 4096}) {
+            const int c = smallLevels(v);
+            if (std::find(seen.begin(), seen.end(), c) != seen.end()) continue;
+            seen.push_back(c);
+            LaunchShape s = cur;
+            s.smallBlendMaxItems = v;
+            out.push_back(s);
+        }
+        break;
+    }
     default: {  // CTAs per SM of k_blend (3), k_pyrdown (4), k_remap (5)
         const int k = 5 - knob;
         const int resident = residentCtasPerSm(k);
@@ -235,7 +252,7 @@ LaunchShape autotune(Rig& rig, Plan& plan, int framesPerTrial, int inflight, boo
         // coordinate descent, two passes; a move must gain 1%
         for (int pass = 0; pass < 2; pass++) {
             bool moved = false;
-            for (int knob = 0; knob < 6; knob++)
+            for (int knob : {0, 6, 1, 2, 3, 4, 5})
                 for (const LaunchShape& s : neighbours(rig, best, knob)) {
                     const double t = trials.time(s);
                     report.trials++;
