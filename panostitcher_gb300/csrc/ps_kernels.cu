@@ -828,6 +828,24 @@ __device__ __forceinline__ void upsample2x2(const uint32_t* g, int pitchW, uint3
     uhi[3] = 4 * (ohi[1] + ohi[2]);
 }
 
+// The Laplacian L = G - ((U + 32) >> 6) of one pixel, B and R in the two
+// 16-bit lanes of one word, each biased by 256: lanes hold 256 + L in
+// 1..511, so neither the lane sums nor the subtraction carry or borrow
+// across lanes (U is at most 64 * 255).  G is returned unbiased.
+struct Lap {
+    uint32_t br;  // (256 + L_B) | (256 + L_R) << 16
+    int g;        // L_G
+};
+
+__device__ __forceinline__ Lap laplacian(uint32_t gpx, uint32_t ulo, uint32_t uhi)
+{
+    const uint32_t ubr = ((ulo + 0x00200020u) >> 6) & 0x03FF03FFu;  // round(U) of B and R, per lane
+    Lap l;
+    l.br = __byte_perm(gpx, 0, 0x4240) + 0x01000100u - ubr;         // G's B and R bytes into the lanes
+    l.g = (int)__byte_perm(gpx, 0, 0x4441) - (int)(((uhi & 0xFFFFu) + 32u) >> 6);
+    return l;
+}
+
 template <class Stage>
 __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, const uint4& raw, int chunk,
                                             bool staged, BlendAcc& acc)
@@ -866,25 +884,30 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
             }
 #pragma unroll
             for (int p = 0; p < 4; p++) {
-                // L = G - ((U + 32) >> 6), per channel
-                const int lb = (int)(gp[p] & 0xFF) - (int)(((ulo[p] & 0xFFFFu) + 32) >> 6);
-                const int lg = (int)((gp[p] >> 8) & 0xFF) - (int)(((uhi[p] & 0xFFFFu) + 32) >> 6);
-                const int lr = (int)((gp[p] >> 16) & 0xFF) - (int)(((ulo[p] >> 16) + 32) >> 6);
+                const Lap l = laplacian(gp[p], ulo[p], uhi[p]);
                 if (fast) {
-                    acc.r[p][0] = lb;
-                    acc.r[p][1] = lg;
-                    acc.r[p][2] = lr;
+                    acc.r[p][0] = (int)(l.br & 0xFFFFu) - 256;
+                    acc.r[p][1] = l.g;
+                    acc.r[p][2] = (int)(l.br >> 16) - 256;
                 } else {
+                    // B and R accumulate w * (256 + L); the 256 * sum(w) comes off at normalisation
                     const int w = (int)((wq[p >> 1] >> (16 * (p & 1))) & 0xFFFFu);
-                    acc.r[p][0] += w * lb;
-                    acc.r[p][1] += w * lg;
-                    acc.r[p][2] += w * lr;
+                    acc.r[p][0] += w * (int)(l.br & 0xFFFFu);
+                    acc.r[p][1] += w * l.g;
+                    acc.r[p][2] += w * (int)(l.br >> 16);
                     acc.wsum[p] += w;
                 }
             }
         }
     }
     if (!last) return;
+    if (!fast) {
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            acc.r[p][0] -= acc.wsum[p] << 8;
+            acc.r[p][2] -= acc.wsum[p] << 8;
+        }
+    }
     int n[4][3];
     if (fast) {
 #pragma unroll
@@ -1046,16 +1069,22 @@ __device__ __forceinline__ void computeUnitRows(const Stage& S, const UnitGeo& G
         const uint2 gq = *reinterpret_cast<const uint2*>(&S.gj[q][ly][lx]);
         const uint32_t wq = *reinterpret_cast<const uint32_t*>(&S.w[q][ly][lx]);
         const int w0 = (int)(wq & 0xFFFFu), w1 = (int)(wq >> 16);
-        acc.r0[0] += w0 * ((int)(gq.x & 0xFF) - (int)(((u0lo & 0xFFFFu) + 32) >> 6));
-        acc.r0[1] += w0 * ((int)((gq.x >> 8) & 0xFF) - (int)(((u0hi & 0xFFFFu) + 32) >> 6));
-        acc.r0[2] += w0 * ((int)((gq.x >> 16) & 0xFF) - (int)(((u0lo >> 16) + 32) >> 6));
-        acc.r1[0] += w1 * ((int)(gq.y & 0xFF) - (int)(((u1lo & 0xFFFFu) + 32) >> 6));
-        acc.r1[1] += w1 * ((int)((gq.y >> 8) & 0xFF) - (int)(((u1hi & 0xFFFFu) + 32) >> 6));
-        acc.r1[2] += w1 * ((int)((gq.y >> 16) & 0xFF) - (int)(((u1lo >> 16) + 32) >> 6));
+        // B and R accumulate w * (256 + L); the 256 * sum(w) comes off below
+        const Lap l0 = laplacian(gq.x, u0lo, u0hi), l1 = laplacian(gq.y, u1lo, u1hi);
+        acc.r0[0] += w0 * (int)(l0.br & 0xFFFFu);
+        acc.r0[1] += w0 * l0.g;
+        acc.r0[2] += w0 * (int)(l0.br >> 16);
+        acc.r1[0] += w1 * (int)(l1.br & 0xFFFFu);
+        acc.r1[1] += w1 * l1.g;
+        acc.r1[2] += w1 * (int)(l1.br >> 16);
         acc.wsum0 += w0;
         acc.wsum1 += w1;
     }
     if (!last) return;
+    acc.r0[0] -= acc.wsum0 << 8;
+    acc.r0[2] -= acc.wsum0 << 8;
+    acc.r1[0] -= acc.wsum1 << 8;
+    acc.r1[2] -= acc.wsum1 << 8;
     int n0[3], n1[3];
     if (G.full) {
 #pragma unroll
