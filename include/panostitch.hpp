@@ -118,6 +118,63 @@ private:
     std::string err_;
 };
 
+// CudaRicohPanoramaRender (source/Task/RicohUtil.cpp:1363-1406): a dual
+// fisheye camera that delivers both lenses in one frame.  The rig has two
+// cameras whose crops select the halves of that frame; render takes the one
+// frame and stitches it as both cameras' source (the library uploads a host
+// frame that appears twice only once).  getNumImages is 1.
+class CudaRicohPanoramaRender {
+public:
+    bool prepare(const std::vector<ps_photo_param>& params, int highQualityBlend, int blendParam,
+                 const Size& srcSize, const Size& dstSize, void* stream = nullptr)
+    {
+        return checked(r_.prepare(params, highQualityBlend, blendParam, srcSize, dstSize, stream));
+    }
+    bool prepare(const std::string& path, int highQualityBlend, int blendParam, const Size& srcSize,
+                 const Size& dstSize, void* stream = nullptr)
+    {
+        return checked(r_.prepare(path, highQualityBlend, blendParam, srcSize, dstSize, stream));
+    }
+    bool render(const std::vector<ps_image>& src, ps_image& dst,
+                const std::vector<std::vector<std::vector<unsigned char>>>& luts = {}, void* stream = nullptr)
+    {
+        if (r_.getNumImages() != 2) {
+            err_ = "have not prepared or prepare failed before";
+            return false;
+        }
+        if (src.size() != 1) {
+            err_ = "src size = " + std::to_string(src.size()) + ", requires 1";
+            return false;
+        }
+        const std::vector<ps_image> both(2, src[0]);
+        if (r_.render(both, dst, luts, stream)) return true;
+        err_ = r_.lastError();
+        return false;
+    }
+    void clear() { r_.clear(); }
+    int getNumImages() const { return r_.getNumImages() == 2 ? 1 : 0; }
+    const std::string& lastError() const { return err_; }
+    ps_render* handle() const { return r_.handle(); }
+
+private:
+    // RicohUtil.cpp:1368-1373: the prepared rig must have two cameras
+    bool checked(bool prepared)
+    {
+        if (!prepared) {
+            err_ = r_.lastError();
+            return false;
+        }
+        if (r_.getNumImages() != 2) {
+            err_ = "num images = " + std::to_string(r_.getNumImages()) + ", requires 2";
+            r_.clear();
+            return false;
+        }
+        return true;
+    }
+    CudaPanoramaRender2 r_;
+    std::string err_;
+};
+
 // CudaTilingMultibandBlendFast (source/CudaAccel/CudaInterface.h:45-82)
 class CudaTilingMultibandBlendFast {
 public:

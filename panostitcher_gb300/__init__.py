@@ -7,12 +7,13 @@ to 8-bit BGR.  The kernels live in libpanostitch.so (built in-tree by
 """
 from ._lib import (PsError, PhotoParam, Image, PlanarImage, lib, PS_FMT_YUV420P, PS_FMT_NV12,  # noqa: F401
                    PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE, PS_MAX_IN_FLIGHT)
-from .render import (CudaPanoramaRender2, CudaTilingMultibandBlendFast, render_batch,  # noqa: F401
+from .render import (CudaPanoramaRender2, CudaRicohPanoramaRender, CudaTilingMultibandBlendFast,  # noqa: F401
+                     render_batch,
                      generate_reproject_map_and_mask, reproject_to_16s, get_lut, as_image, as_planar,
                      cvt_bgr32_to_yuv, cvt_yuv_to_bgr32, non_intersecting_masks, distance_transform_l1,
                      load_photo_params)
 
-__all__ = ["CudaPanoramaRender2", "CudaTilingMultibandBlendFast", "render_batch",
+__all__ = ["CudaPanoramaRender2", "CudaRicohPanoramaRender", "CudaTilingMultibandBlendFast", "render_batch",
            "generate_reproject_map_and_mask", "reproject_to_16s", "get_lut", "as_image", "as_planar",
            "cvt_bgr32_to_yuv", "cvt_yuv_to_bgr32", "non_intersecting_masks", "distance_transform_l1",
            "load_photo_params", "PsError", "PhotoParam", "Image", "PlanarImage", "lib", "PS_FMT_YUV420P",

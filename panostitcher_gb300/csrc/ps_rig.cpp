@@ -1188,14 +1188,26 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         if (f.psrc) {
             YuvFrames y;
             std::memset(&y, 0, sizeof y);
-            y.n = n;
             y.w = rig->srcW();
             y.h = rig->srcH();
             const size_t w = y.w, h = y.h;
             fd.srcFmt = PS_FMT_BGR32;
             for (int i = 0; i < n; i++) {
                 const ps_planar_image& s = f.psrc[i];
-                YuvFrame& F = y.frame[i];
+                // a host frame given for several cameras goes up and is converted once
+                int same = -1;
+                for (int q = 0; q < i && same < 0 && s.location == PS_MEM_HOST; q++)
+                    if (f.psrc[q].location == PS_MEM_HOST && f.psrc[q].format == s.format &&
+                        f.psrc[q].planes[0] == s.planes[0] && f.psrc[q].planes[1] == s.planes[1] &&
+                        f.psrc[q].planes[2] == s.planes[2] && f.psrc[q].pitches[0] == s.pitches[0] &&
+                        f.psrc[q].pitches[1] == s.pitches[1] && f.psrc[q].pitches[2] == s.pitches[2])
+                        same = q;
+                if (same >= 0) {
+                    fd.src[i] = fd.src[same];
+                    fd.srcPitch[i] = fd.srcPitch[same];
+                    continue;
+                }
+                YuvFrame& F = y.frame[y.n++];
                 F.fmt = s.format;
                 const bool nv12 = s.format == PS_FMT_NV12;
                 if (s.location == PS_MEM_HOST) {  // packed planes in the slot's staging
@@ -1232,12 +1244,23 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
                 fd.srcPitch[i] = rig->inputPitch();
             }
             cvt.push_back(y);
-            cvtBytes += (double)n * w * h * (1.5 + 4);
+            cvtBytes += (double)y.n * w * h * (1.5 + 4);
         } else if (f.src) {
             fd.srcFmt = f.src[0].format;
             for (int i = 0; i < n; i++) {
                 const ps_image& s = f.src[i];
                 if (s.location == PS_MEM_HOST) {
+                    // a host frame given for several cameras (both lenses of a
+                    // dual-fisheye frame) goes up once
+                    int same = -1;
+                    for (int q = 0; q < i && same < 0; q++)
+                        if (f.src[q].location == PS_MEM_HOST && f.src[q].data == s.data && f.src[q].pitch == s.pitch)
+                            same = q;
+                    if (same >= 0) {
+                        fd.src[i] = fd.src[same];
+                        fd.srcPitch[i] = fd.srcPitch[same];
+                        continue;
+                    }
                     const size_t rowBytes = (size_t)s.width * bytesPerPixel(s.format);
                     PS_CUDA(cudaMemcpy2DAsync(rig->inputBuffer(i, rs[r]), rig->inputPitch(), s.data, s.pitch, rowBytes,
                                               s.height, cudaMemcpyHostToDevice, sIn_));

@@ -296,6 +296,64 @@ class CudaPanoramaRender2:
         return out
 
 
+class CudaRicohPanoramaRender:
+    """CudaRicohPanoramaRender (source/Task/RicohUtil.cpp:1363-1406): a dual
+    fisheye camera delivering both lenses in one frame.  The rig has two
+    cameras whose crops select the halves of the frame; render takes the one
+    frame and stitches it as both cameras' source."""
+
+    def __init__(self):
+        self._r = CudaPanoramaRender2()
+        self.last_error = ""
+
+    def _fail(self, code: int, msg: str, check_: bool) -> bool:
+        self.last_error = msg
+        if check_:
+            raise PsError(code, msg)
+        return False
+
+    def _checked(self, ok: bool, check_: bool) -> bool:
+        if not ok:
+            return self._fail(L.PS_EINVAL, self._r.last_error, check_)
+        n = self._r.getNumImages()
+        if n != 2:  # RicohUtil.cpp:1368-1373
+            self._r.clear()
+            return self._fail(L.PS_EINVAL, f"num images = {n}, requires 2", check_)
+        return True
+
+    def prepare(self, params: Sequence[dict], high_quality_blend: int, blend_param: int, src_size, dst_size,
+                stream=None, check: bool = False) -> bool:
+        return self._checked(self._r.prepare(params, high_quality_blend, blend_param, src_size, dst_size,
+                                             stream=stream), check)
+
+    def prepare_file(self, path: str, high_quality_blend: int, blend_param: int, src_size, dst_size, stream=None,
+                     check: bool = False) -> bool:
+        return self._checked(self._r.prepare_file(path, high_quality_blend, blend_param, src_size, dst_size,
+                                                  stream=stream), check)
+
+    def render(self, src: Sequence, dst, luts=None, stream=None, check: bool = False) -> bool:
+        """render(src, dst, luts) with src the one dual-fisheye frame."""
+        if self._r.getNumImages() != 2:
+            return self._fail(L.PS_ESTATE, "have not prepared or prepare failed before", check)
+        if len(src) != 1:
+            return self._fail(L.PS_EINVAL, f"src size = {len(src)}, requires 1", check)
+        ok = self._r.render([src[0], src[0]], dst, luts, stream=stream)
+        if not ok:
+            return self._fail(L.PS_EINVAL, self._r.last_error, check)
+        return True
+
+    def clear(self) -> None:
+        self._r.clear()
+
+    def getNumImages(self) -> int:
+        return 1 if self._r.getNumImages() == 2 else 0
+
+    @property
+    def render2(self) -> CudaPanoramaRender2:
+        """The two-camera render underneath (for exports and measurement hooks)."""
+        return self._r
+
+
 def render_batch(renders: Sequence[CudaPanoramaRender2], srcs: Sequence[Sequence], dsts: Sequence,
                  luts: Sequence | None = None, stream=None) -> None:
     """One launch sequence for several rigs (one frame each)."""

@@ -94,6 +94,9 @@ def rig(name: str, seed: int = 1234) -> RigConfig:
     c3d: 8 rectilinear 2704x2028, 120 deg, yaw every 45 deg -> 7680x3840
     c5:  8 rectilinear 3840x2160, 120 deg, yaw every 45 deg -> 7680x3840, 10 levels,
          gains U[0.7,1.3], noise +-20
+    ricoh: one 1920x960 dual-fisheye frame, two circular 200 deg fisheyes back to back,
+         each camera's crop one 960x960 half -> 2048x1024, 5 levels (the rig
+         CudaRicohPanoramaRender stitches from one frame)
     """
     if name == "c1":
         cams = [photo_param(1, 200.0, 0.0), photo_param(1, 200.0, 180.0)]
@@ -115,15 +118,26 @@ def rig(name: str, seed: int = 1234) -> RigConfig:
     if name == "c5":
         cams = [photo_param(0, 120.0, 45.0 * k) for k in range(8)]
         return RigConfig(name, cams, (3840, 2160), (7680, 3840), 10, (0.7, 1.3), 20, seed, 120)
+    if name == "ricoh":
+        cams = [photo_param(3, 200.0, 0.0, crop_x=0, crop_y=0, crop_width=960, crop_height=960),
+                photo_param(3, 200.0, 180.0, crop_x=960, crop_y=0, crop_width=960, crop_height=960)]
+        return RigConfig(name, cams, (1920, 960), (2048, 1024), 5, (0.9, 1.1), 10, seed)
     raise KeyError(name)
 
 
 def scaled_rig(base: RigConfig, factor: int, name: str | None = None) -> RigConfig:
-    """Same cameras, source and canvas sizes divided by factor (for tests)."""
+    """Same cameras, source and canvas sizes divided by factor (for tests);
+    crop rectangles and circles, in source pixels, are divided too."""
     sw, sh = base.src_size
     dw, dh = base.dst_size
     dw2 = max(4, (dw // factor) // 4 * 4)
-    return RigConfig(name or f"{base.name}/{factor}", [dict(c) for c in base.cams],
+    cams = []
+    for c in base.cams:
+        c = dict(c)
+        for k in ("crop_x", "crop_y", "crop_width", "crop_height", "circle_x", "circle_y", "circle_r"):
+            c[k] = int(c[k]) // factor
+        cams.append(c)
+    return RigConfig(name or f"{base.name}/{factor}", cams,
                      (max(2, sw // factor), max(2, sh // factor)), (dw2, dw2 // 2), base.levels,
                      base.gain_range, base.noise, base.seed, base.frames)
 

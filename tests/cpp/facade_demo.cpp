@@ -39,6 +39,11 @@ int main(int argc, char** argv)
     const ps_planar_image nv12 = {{yp.data(), uvp.data(), nullptr}, {160, 160, 0}, 160, 120, PS_FMT_NV12, PS_MEM_HOST};
     std::vector<ps_planar_image> psrc(2, nv12);
     if (r.renderPlanar(psrc, &dst, nullptr)) return 10;  // not prepared
+    // the dual-fisheye render: one frame, two cameras (not prepared yet)
+    panostitch::CudaRicohPanoramaRender ricoh;
+    if (ricoh.render({src[0]}, dst)) return 14;
+    if (ricoh.lastError().find("prepare") == std::string::npos) return 15;
+    if (ricoh.getNumImages() != 0) return 16;
     if (!render) {
         std::printf("facade check ok\n");
         return 0;
