@@ -267,7 +267,7 @@ typedef struct ps_tune_report {
     int cached;                   /* 1: an earlier tuning of the same geometry */
 } ps_tune_report;
 /* Set before prepare, the shape applies at prepare; set after, the call waits
-   for the device to go idle and the next render re-records its launches.
+   for the render's frames in flight and the next render re-records its launches.
    Out-of-range fields: PS_EINVAL. */
 int ps_render_set_launch_shape(ps_render* r, const ps_launch_shape* shape);
 int ps_render_get_launch_shape(const ps_render* r, ps_launch_shape* shape);

@@ -1557,15 +1557,17 @@ __global__ void __launch_bounds__(kThreads) k_yuv_to_bgr32(YuvFrames f)
 }
 
 // ---- launch helpers ---------------------------------------------------------
+// The lazily computed launch facts below are function-local statics, so
+// their first computation is thread-safe (renders may launch from several
+// threads).
 static int smCount()
 {
-    static int sms = 0;
-    if (!sms) {
+    static const int sms = [] {
         int dev = 0, v = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        sms = v > 0 ? v : 1;
-    }
+        return v > 0 ? v : 1;
+    }();
     return sms;
 }
 
@@ -1582,15 +1584,14 @@ static int gridFor(int total, int perSm, int want = 0)
 template <auto Kernel>
 static int residentPerSm(int threads, size_t dynSmem = 0)
 {
-    static int cached = 0;  // one per kernel
-    if (!cached) {
+    static const int cached = [threads, dynSmem] {  // one per kernel
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, Kernel, threads, dynSmem) != cudaSuccess || n < 1) {
             cudaGetLastError();
             n = 1;
         }
-        cached = n;
-    }
+        return n;
+    }();
     return cached;
 }
 
@@ -1662,11 +1663,10 @@ cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, cu
 cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    static int perSm = 0;
-    if (!perSm) {
+    static const int perSm = [] {  // the attribute is set before any launch can see perSm
         cudaFuncSetAttribute(k_blend_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmallStage));
-        perSm = residentPerSm<k_blend_small>(kThreads, sizeof(SmallStage));
-    }
+        return residentPerSm<k_blend_small>(kThreads, sizeof(SmallStage));
+    }();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(gridFor(total, perSm));
     cfg.blockDim = dim3(kThreads);
@@ -1682,28 +1682,29 @@ cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStre
 
 int tailClusterMax()
 {
-    static int size = 0;
-    if (size) return size;
-    size = kTailCluster;
-    cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TailSmem));
-    if (cudaFuncSetAttribute(k_tail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(kTailClusterWide);
-        cfg.blockDim = dim3(kThreads);
-        cfg.dynamicSmemBytes = sizeof(TailSmem);
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = kTailClusterWide;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        int clusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&clusters, k_tail, &cfg) == cudaSuccess && clusters >= 1)
-            size = kTailClusterWide;
-    }
-    cudaGetLastError();
-    return size;
+    static const int widest = [] {  // the attributes are set before any launch can see the width
+        int size = kTailCluster;
+        cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TailSmem));
+        if (cudaFuncSetAttribute(k_tail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(kTailClusterWide);
+            cfg.blockDim = dim3(kThreads);
+            cfg.dynamicSmemBytes = sizeof(TailSmem);
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = kTailClusterWide;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&clusters, k_tail, &cfg) == cudaSuccess && clusters >= 1)
+                size = kTailClusterWide;
+        }
+        cudaGetLastError();
+        return size;
+    }();
+    return widest;
 }
 
 cudaError_t launchTail(const Segment* segs, int nsegs, int cluster, cudaStream_t st)

@@ -582,6 +582,14 @@ void Rig::writeDescriptors(cudaStream_t st)
     PS_CUDA(cudaStreamSynchronize(st));
 }
 
+void Rig::waitIdle()
+{
+    for (int k = 0; k < kIoSlots; k++) {
+        if (slotComputed_[k]) PS_CUDA(cudaEventSynchronize(slotComputed_[k]));
+        if (slotDownloaded_[k]) PS_CUDA(cudaEventSynchronize(slotDownloaded_[k]));
+    }
+}
+
 void Rig::tailSplit(int maxItems, int* down, int* blend) const
 {
     int d = L_ + 1, b = L_ + 1;
@@ -607,7 +615,7 @@ void Rig::setShape(const LaunchShape& s)
     if (!ready() || linear_) return;
     // the descriptors change under no run: launch lists follow the new
     // generation (plans rebind), and no kernel may read the old split
-    PS_CUDA(cudaDeviceSynchronize());
+    waitIdle();
     tailSplit(shape_.tailMaxItems, &tailDown_, &tailBlend_);
     hDesc_.tailDown = tailDown_;
     hDesc_.tailBlend = tailBlend_;

@@ -97,6 +97,11 @@ public:
     int peekSlot() const { return nextSlot_; }
     cudaEvent_t slotComputed(int slot) { return slotEvent(slotComputed_[slot]); }
     cudaEvent_t slotDownloaded(int slot) { return slotEvent(slotDownloaded_[slot]); }
+    // Waits for every run that used this rig, whatever plan issued it (each
+    // records its slot's events after the kernels and after the download).
+    // Unlike a device-wide synchronise it leaves other work alone, such as a
+    // capture in progress on another thread.
+    void waitIdle();
 
     // building blocks of launch plans
     const RigDev* deviceDesc(int slot = 0) const { return dDesc_.as<RigDev>() + slot; }
@@ -108,7 +113,8 @@ public:
     int numBlendItems(int level) const { return blendCnt_[level]; }
     // Launch shape (tail split, tail cluster and tile split, CTAs per SM).
     // Set before prepare, it applies at prepare; set after, it waits for the
-    // device to go idle, rewrites the descriptors and starts a new generation.
+    // rig's runs to finish (waitIdle), rewrites the descriptors and starts a
+    // new generation.
     void setShape(const LaunchShape& s);
     const LaunchShape& shape() const { return shape_; }
     // the tail levels a tail_max_items value gives: pyrDown down..L, blend L..blend

@@ -237,7 +237,7 @@ LaunchShape autotune(Rig& rig, Plan& plan, int framesPerTrial, int inflight, boo
     const LaunchShape start = rig.shape();
     LaunchShape best;  // the default shape is the first point
     try {
-        PS_CUDA(cudaDeviceSynchronize());
+        rig.waitIdle();  // the render's earlier frames are done with the staging the trials overwrite
         Trials trials(rig, plan, framesPerTrial, inflight, useGraph);
         double tBest = trials.time(best);
         report.trials = 1;
