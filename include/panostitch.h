@@ -14,7 +14,12 @@
  * default stream): the renders run on their own streams, and the caller's
  * stream waits for each call's completion; no entry point synchronises the
  * stream unless it says so.  A ps_render is not thread-safe; distinct
- * renders may be used from different threads.
+ * renders may be used from different threads.  A render records its launch
+ * sequence as a CUDA graph with stream capture (on its first frames, after
+ * prepare or a launch-shape change, and throughout ps_render_autotune);
+ * CUDA forbids synchronising the whole device or context while any of its
+ * streams captures, so threads that share a device with renders wait on
+ * their own streams or events, not with cudaDeviceSynchronize.
  *
  * Each declaration names the reference interface it replaces
  * (xpngzhng/PanoStitcher, path:line).

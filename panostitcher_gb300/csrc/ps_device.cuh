@@ -132,14 +132,15 @@ __device__ __forceinline__ int findSegment(const Segment* segs, int nsegs, int i
     return s;
 }
 
-// Contiguous chunk of items for this CTA: neighbouring tiles of one camera
-// stay on one SM (source-texel and footprint reuse in L1 / L2).
+// Contiguous chunk of items for this CTA (k_pyrdown): neighbouring tiles of
+// one camera stay on one SM, and no item is handed out through an atomic.
 __device__ __forceinline__ void itemRange(int total, int& begin, int& end)
 {
     const int chunk = (total + gridDim.x - 1) / gridDim.x;
     begin = min(total, (int)blockIdx.x * chunk);
     end = min(total, begin + chunk);
 }
+
 
 // ---- borders: source/CudaAccel/CudaUtil.cuh:6-98 ------------------------------
 // Vertical reflect-101 (BrdColReflect101) and horizontal wrap (BrdRowWrap),

@@ -163,10 +163,13 @@ struct LaunchShape {
 };
 
 // ---- per-frame kernels ------------------------------------------------------------
-// perSm > 0 caps the CTAs per SM of the one-wave persistent grid
-cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
+// perSm > 0 caps the CTAs per SM of the one-wave persistent grid; counter
+// (remap and blend) is a zeroed int through which the launch hands out its
+// work items
+cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st);
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
-cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
+// counter: a zeroed int the launch hands its tiles out through
+cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st);
 // blend of few-tile levels above 0: two work items (the 64x8 halves) per tile
 cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st);
 // one cluster per segment: the rig's pyrDown levels tailDown..L and blend

@@ -146,18 +146,31 @@ __device__ __forceinline__ RemapSeg remapSeg(const Segment* segs, int nsegs, int
             sg.frame};
 }
 
-__global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict__ segs, int nsegs, int total)
+// Items are handed out in chunks of kRemapChunk through `counter` (zero at
+// launch); the next chunk is fetched one chunk ahead, so the next item and
+// its map are always known before the current item is gathered.
+constexpr int kRemapChunk = 8;
+
+__global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict__ segs, int nsegs, int total,
+                                                       int* __restrict__ counter)
 {
     __shared__ uint8_t lut[3 * 256];
-    int begin, end;
-    itemRange(total, begin, end);
+    __shared__ int s_grab;
+    auto grab = [&] {  // all threads together
+        __syncthreads();
+        if (threadIdx.x == 0) s_grab = atomicAdd(counter, kRemapChunk);
+        __syncthreads();
+        return s_grab;
+    };
     const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
     waitPrevGrid();
     allowNextGrid();
-    if (begin >= end) return;
-    int s = findSegment(segs, nsegs, begin, 0);
+    int it = grab();
+    if (it >= total) return;
+    int end = min(it + kRemapChunk, total), nextBegin = grab();
+    int s = findSegment(segs, nsegs, it, 0);
     RemapSeg cur = remapSeg(segs, nsegs, s, total);
-    RemapItem item = cur.items[begin - cur.prefix];
+    RemapItem item = cur.items[it - cur.prefix];
     const float2* mt = cur.R->maps + (size_t)item.mapTile * (kRemapTW * kRemapTH);
     float2 m0 = __ldg(mt + threadIdx.x), m1 = __ldg(mt + threadIdx.x + kThreads);
     // constants of the loaded camera
@@ -166,7 +179,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
     long long pitch = 0;
     int fmt = 0, sw = 0, sh = 0, W = 0, H = 0, gpitch = 0;
     uint32_t* G = nullptr;
-    for (int it = begin; it < end; it++) {
+    for (;;) {
         if (item.cam != cam || s != camSeg) {  // uniform across the block
             const FrameDev& F = *cur.F;
             const RigDev& R = *cur.R;
@@ -186,16 +199,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
             for (int k = threadIdx.x; k < 768; k += kThreads) lut[k] = __ldg(src + k);
             __syncthreads();
         }
-        // the next item and its map
+        // the next item (the rest of this chunk, else the next chunk's first) and its map
+        const int nit = it + 1 < end ? it + 1 : (nextBegin < total ? nextBegin : -1);
         RemapItem nitem = item;
         float2 n0 = m0, n1 = m1;
-        const int sCur = s;
-        if (it + 1 < end) {
-            if (it + 1 >= cur.end) {
-                s = findSegment(segs, nsegs, it + 1, s);
+        if (nit >= 0) {
+            if (nit >= cur.end) {
+                s = findSegment(segs, nsegs, nit, s);
                 cur = remapSeg(segs, nsegs, s, total);
             }
-            nitem = cur.items[it + 1 - cur.prefix];
+            nitem = cur.items[nit - cur.prefix];
             const float2* nt = cur.R->maps + (size_t)nitem.mapTile * (kRemapTW * kRemapTH);
             n0 = __ldg(nt + threadIdx.x);
             n1 = __ldg(nt + threadIdx.x + kThreads);
@@ -207,7 +220,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
             if (y0 < H) G[(size_t)y0 * gpitch + x] = v0;
             if (y1 < H) G[(size_t)y1 * gpitch + x] = v1;
         }
-        (void)sCur;
+        if (nit < 0) break;
+        if (it + 1 >= end) {  // into the next chunk; fetch the one after it
+            end = min(nextBegin + kRemapChunk, total);
+            nextBegin = grab();
+        }
+        it = nit;
         item = nitem;
         m0 = n0;
         m1 = n1;
@@ -1132,7 +1150,10 @@ __device__ __forceinline__ void computeUnitRows(const Stage& S, const UnitGeo& G
     }
 }
 
-__global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total)
+// Tiles are handed out one at a time through `counter` (zero at launch), so
+// a CTA that starts late, behind other frames' kernels, simply takes fewer.
+__global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total,
+                                                            int* __restrict__ counter)
 {
     __shared__ BlendStage st[kBStages];
     __shared__ UnitInfo info[kBStages];
@@ -1159,7 +1180,12 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
 
     if (threadIdx.x >= kConsumers) {
         // ---------------- producer warp ----------------
-        int it = blockIdx.x, chunk = 0, seg = 0;
+        auto nextItem = [&] {
+            int v = 0;
+            if (lane == 0) v = atomicAdd(counter, 1);
+            return __shfl_sync(0xffffffffu, v, 0);
+        };
+        int it = nextItem(), chunk = 0, seg = 0;
         uint4 raw = make_uint4(0, 0, 0, 0);
         bool valid = it < total;
         if (valid) {
@@ -1254,7 +1280,7 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                 chunk++;
             } else {
                 chunk = 0;
-                it += gridDim.x;
+                it = nextItem();
                 valid = it < total;
                 if (valid) {
                     seg = findSegment(segs, nsegs, it, seg);
@@ -1623,11 +1649,11 @@ int residentCtasPerSm(int kind)
     }
 }
 
-cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st)
+cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
     return launchPdl(k_remap, gridFor(total, residentPerSm<k_remap>(kThreads), perSm), kThreads, st, segs, nsegs,
-                     total);
+                     total, counter);
 }
 
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st)
@@ -1653,11 +1679,11 @@ cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams,
     return cudaLaunchKernelEx(&cfg, k_linear, segs, nsegs, total);
 }
 
-cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st)
+cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
     return launchPdl(k_blend, gridFor(total, residentPerSm<k_blend>(kBlendThreads), perSm), kBlendThreads, st, segs,
-                     nsegs, total);
+                     nsegs, total, counter);
 }
 
 cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st)

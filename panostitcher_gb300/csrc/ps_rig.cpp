@@ -1081,14 +1081,16 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         addStep(6, small, s);
         addStep(2, parts, s);
     }
-    const size_t need = segOff_ + std::max<size_t>(1, segs_.size()) * sizeof(Segment);
+    // one work counter per step after the segments, zeroed in every run's staged copy
+    counterOff_ = (segOff_ + segs_.size() * sizeof(Segment) + 15) / 16 * 16;
+    const size_t need = counterOff_ + std::max<size_t>(1, steps_.size()) * sizeof(int);
     for (IoSlot& sl : io_)
         if (need > sl.dArgs.bytes()) {
             const size_t cap = need + need / 2;
             sl.dArgs.alloc(cap);
             sl.stage.alloc(cap);
         }
-    stageBytes_ = segOff_ + segs_.size() * sizeof(Segment);
+    stageBytes_ = counterOff_ + steps_.size() * sizeof(int);
 }
 
 Plan::~Plan()
@@ -1119,7 +1121,9 @@ bool Plan::matches(const std::vector<Rig*>& rigs) const
 void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
 {
     const Segment* segs = reinterpret_cast<const Segment*>(static_cast<const uint8_t*>(slot.dArgs.get()) + segOff_);
-    for (const Step& s : steps_) {
+    int* counters = reinterpret_cast<int*>(static_cast<uint8_t*>(slot.dArgs.get()) + counterOff_);
+    for (size_t si = 0; si < steps_.size(); si++) {
+        const Step& s = steps_[si];
         const Segment* p = segs + s.segOff;
         cudaEvent_t a = nullptr, b = nullptr;
         if (prof) {
@@ -1127,9 +1131,9 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
             b = prof->event();
             PS_CUDA(cudaEventRecord(a, st));
         }
-        if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, perSm_[0], st));
+        if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, perSm_[0], counters + si, st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, perSm_[1], st));
-        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], st));
+        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, st));
         else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, tailCluster_, st));
         else if (s.kind == 6) PS_CUDA(launchBlendSmall(p, s.nsegs, s.total, st));
         else PS_CUDA(launchLinear(p, s.nsegs, s.total, maxCams_, st));
@@ -1328,6 +1332,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
             sg[k].rig = rigs_[segRig_[k]]->deviceDesc(rs[segRig_[k]]);
         }
     }
+    std::memset(stage + counterOff_, 0, steps_.size() * sizeof(int));
     PS_CUDA(cudaMemcpyAsync(dArgs, stage, stageBytes_, cudaMemcpyHostToDevice, sIn_));
     PS_CUDA(cudaEventRecord(S.argsCopied, sIn_));
 

@@ -248,7 +248,7 @@ private:
     std::vector<Segment> segs_;      // frame pointers hold offsets into the args block
     std::vector<int> segRig_;        // rig of each segment (its descriptor depends on the rig's slot)
     std::vector<size_t> lutOff_;
-    size_t segOff_ = 0, stageBytes_ = 0;
+    size_t segOff_ = 0, counterOff_ = 0, stageBytes_ = 0;
     int maxCams_ = 0;
     int tailCluster_ = 0, perSm_[3] = {0, 0, 0};  // launch widths (from the rigs' shapes)
     IoSlot io_[Rig::kIoSlots];

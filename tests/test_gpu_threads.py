@@ -1,7 +1,11 @@
 """Distinct renders used from different threads at once (GPU).  The C ABI
 allows it; ctypes releases the GIL during the calls, so the renders' host
 work, launches and the library's shared launch facts and caches are
-exercised concurrently.  Every frame must still equal the oracle's."""
+exercised concurrently.  Every frame must still equal the oracle's.
+
+A render records its launch graph with stream capture on its first frames
+and throughout autotuning; CUDA forbids synchronising the whole device while
+any stream captures, so each thread waits on its own stream only."""
 import threading
 
 import numpy as np
@@ -26,9 +30,10 @@ def test_distinct_renders_on_threads(cuda, oracle_lib):
     errors = []
     start = threading.Barrier(len(preps))
 
+    streams = [torch.cuda.Stream() for _ in preps]
+
     def work(t):
         try:
-            torch.cuda.set_device(0)
             p = preps[t]
             W, H = p.cfg.dst_size
             start.wait()
@@ -36,9 +41,9 @@ def test_distinct_renders_on_threads(cuda, oracle_lib):
                 p.r.autotune(frames_per_trial=3, in_flight=2, force=True)
             for k in range(4):
                 o = np.zeros((H, W, 4), np.uint8)
-                assert p.r.render(frames[t][k], o, p.luts, check=True)
+                assert p.r.render(frames[t][k], o, p.luts, stream=streams[t], check=True)
                 outs[t][k] = o
-            torch.cuda.synchronize()
+            streams[t].synchronize()  # this thread's stream only
         except Exception as e:  # reported on the main thread
             errors.append((t, repr(e)))
 
