@@ -402,10 +402,10 @@ def run_ours(args, world, rank, local, dist):
                                            "alg_GBps": round(b5 / max(ms5, 1e-9) / 1e6, 1)}
 
     # ---- roofline: profiled pass (a CUDA event pair around every launch).
-    # Launches are timed one at a time, so the pass uses the shape tuned for
-    # one frame in flight.
-    if not args.no_tune:
-        r.set_launch_shape(**single_shape)
+    # Launches are timed one at a time with the default launch shape (full
+    # one-wave grids, the tail kernel for the top levels), as the committed
+    # ncu summaries capture them.
+    r.set_launch_shape(**P.CudaPanoramaRender2.SHAPE_DEFAULT)
     r.profile(True)
     prof_steps = min(args.steps, 30)
     for k in range(prof_steps):
