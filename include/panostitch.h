@@ -97,7 +97,8 @@ typedef struct ps_render ps_render;
 
 /* Construct an empty render (CudaPanoramaRender2::CudaPanoramaRender2). */
 int ps_render_create(ps_render** out);
-/* Destroy; NULL is a no-op (~CudaPanoramaRender2). */
+/* Destroy; NULL is a no-op (~CudaPanoramaRender2).  Waits for the render's
+   frames in flight first (its own work only, not the whole device). */
 void ps_render_destroy(ps_render* r);
 
 /* CudaPanoramaRender2::prepare (source/Task/RicohUtil.cpp:1091-1205) with the
@@ -199,7 +200,9 @@ int ps_render_render_planar(ps_render* r, const ps_planar_image* src, int num_sr
    individual launches (0).  No reference counterpart. */
 int ps_render_set_graph(ps_render* r, int enabled);
 
-/* CudaPanoramaRender2::clear / getNumImages (source/Task/RicohUtil.cpp:1341-1361). */
+/* CudaPanoramaRender2::clear / getNumImages (source/Task/RicohUtil.cpp:1341-1361).
+   clear, like a new prepare, waits for the render's frames in flight before
+   it frees their state. */
 void ps_render_clear(ps_render* r);
 int ps_render_get_num_images(const ps_render* r);
 

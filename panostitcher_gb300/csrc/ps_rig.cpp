@@ -111,6 +111,7 @@ static inline int roundUp(int a, int b) { return divUp(a, b) * b; }
 // ---- Rig ---------------------------------------------------------------------------
 void Rig::clear()
 {
+    waitIdleQuiet();  // kernels and downloads of earlier frames may still use the buffers
     for (auto& l : lv_) {
         for (int k = 0; k < kIoSlots; k++) {
             l.G[k].reset();
@@ -143,6 +144,7 @@ void Rig::clear()
 
 Rig::~Rig()
 {
+    waitIdleQuiet();
     for (cudaEvent_t* es : {slotComputed_, slotDownloaded_})
         for (int k = 0; k < kIoSlots; k++)
             if (es[k]) cudaEventDestroy(es[k]);
@@ -588,6 +590,13 @@ void Rig::waitIdle()
         if (slotComputed_[k]) PS_CUDA(cudaEventSynchronize(slotComputed_[k]));
         if (slotDownloaded_[k]) PS_CUDA(cudaEventSynchronize(slotDownloaded_[k]));
     }
+}
+
+void Rig::waitIdleQuiet() noexcept
+{
+    for (cudaEvent_t* es : {slotComputed_, slotDownloaded_})
+        for (int k = 0; k < kIoSlots; k++)
+            if (es[k] && cudaEventSynchronize(es[k]) != cudaSuccess) cudaGetLastError();
 }
 
 void Rig::tailSplit(int maxItems, int* down, int* blend) const

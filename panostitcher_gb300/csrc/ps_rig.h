@@ -31,6 +31,7 @@ public:
     // given, or getNonIntersectingMasks of the coverage when seams is NULL.
     void prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* seams, int n, int W, int H,
                           int maxLevels, int minLength, cudaStream_t st);
+    // Frees the resident state after the rig's runs in flight have finished.
     void clear();
 
     bool ready() const { return n_ > 0; }
@@ -102,6 +103,8 @@ public:
     // Unlike a device-wide synchronise it leaves other work alone, such as a
     // capture in progress on another thread.
     void waitIdle();
+    // The same, for teardown: errors of the runs are dropped, not thrown.
+    void waitIdleQuiet() noexcept;
 
     // building blocks of launch plans
     const RigDev* deviceDesc(int slot = 0) const { return dDesc_.as<RigDev>() + slot; }

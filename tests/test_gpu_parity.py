@@ -252,11 +252,12 @@ def test_blender_rejects_bad_inputs(cuda):
         b.blend([outside], out)
 
 
-@pytest.mark.parametrize("name", ["c1", "c2", "ricoh", "c5"])
+@pytest.mark.parametrize("name", ["c1", "c2", "c3a", "c3c", "c3d", "ricoh", "c5"])
 def test_render_full_size_bit_exact(cuda, oracle_lib, name):
-    """The benchmark rigs at full size: every kernel path (bulk-copied interior
+    """Every benchmark rig at full size: every kernel path (bulk-copied interior
     tiles, border tiles, uniform tiles, the tail kernel) against the oracle,
-    up to the largest one (8 x 3840x2160 -> 7680x3840, 10 levels)."""
+    up to the largest ones (8 x 2704x2028 and 8 x 3840x2160 -> 7680x3840, 8 and
+    10 levels)."""
     import os
     cfg = S.rig(name)
     p = Prepared(cfg)

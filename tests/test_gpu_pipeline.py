@@ -91,3 +91,41 @@ def test_fewer_frames_in_flight(cuda, oracle_lib, slots):
     for f, o in zip(frames, outs):
         ref = full.oracle_render(f, full.luts)[..., :3]
         assert np.array_equal(o[..., :3], ref), diff_histogram(o[..., :3], ref)
+
+
+def test_prepare_again_with_frames_in_flight(cuda, oracle_lib):
+    """A new prepare (and clear) while frames are still in flight waits for
+    them before freeing their state: the frames finish with the old rig, the
+    next frames use the new one."""
+    torch = cuda
+    a = Prepared(S.scaled_rig(S.rig("c2"), 8))
+    b_cfg = S.scaled_rig(S.rig("c3c"), 8)
+    b = Prepared(b_cfg)
+    fa = [a.frames.frame(k) for k in range(3)]
+    refs_a = [a.oracle_render(f, a.luts)[..., :3] for f in fa]
+    fb = b.frames.frame(0)
+    ref_b = b.oracle_render(fb, b.luts)[..., :3]
+    r = P.CudaPanoramaRender2()
+    assert r.prepare(a.cfg.cams, 1, a.cfg.levels, a.cfg.src_size, a.cfg.dst_size, check=True)
+    Wa, Ha = a.cfg.dst_size
+    st = torch.cuda.Stream()
+    dev = [[torch.from_numpy(np.ascontiguousarray(c)).cuda() for c in f] for f in fa]
+    outs = [torch.zeros((Ha, Wa, 4), dtype=torch.uint8, device="cuda") for _ in fa]
+    host_out = np.zeros((Ha, Wa, 4), np.uint8)
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert r.render(dev[k], outs[k], a.luts, stream=st, check=True)
+    assert r.render(fa[0], host_out, a.luts, check=True)  # a host frame in flight too
+    # no synchronisation: prepare the other rig at once
+    assert r.prepare(b_cfg.cams, 1, b_cfg.levels, b_cfg.src_size, b_cfg.dst_size, check=True)
+    Wb, Hb = b_cfg.dst_size
+    ob = np.zeros((Hb, Wb, 4), np.uint8)
+    assert r.render(fb, ob, b.luts, check=True)
+    torch.cuda.synchronize()
+    for k in range(3):
+        got = outs[k].cpu().numpy()[..., :3]
+        assert np.array_equal(got, refs_a[k]), (k, diff_histogram(got, refs_a[k]))
+    assert np.array_equal(host_out[..., :3], refs_a[0])
+    assert np.array_equal(ob[..., :3], ref_b), diff_histogram(ob[..., :3], ref_b)
+    r.clear()
+    assert r.getNumImages() == 0
