@@ -163,16 +163,26 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
         return s_grab;
     };
     const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    // The hand-out counter, items, descriptors and maps are written before
+    // the launch sequence, not by a kernel: the first chunk and its map are
+    // fetched while the previous kernel finishes.
+    int it = grab(), end = 0, nextBegin = total, s = 0;
+    RemapSeg cur{};
+    RemapItem item{};
+    float2 m0{}, m1{};
+    if (it < total) {
+        end = min(it + kRemapChunk, total);
+        nextBegin = grab();
+        s = findSegment(segs, nsegs, it, 0);
+        cur = remapSeg(segs, nsegs, s, total);
+        item = cur.items[it - cur.prefix];
+        const float2* mt = cur.R->maps + (size_t)item.mapTile * (kRemapTW * kRemapTH);
+        m0 = __ldg(mt + threadIdx.x);
+        m1 = __ldg(mt + threadIdx.x + kThreads);
+    }
     waitPrevGrid();
     allowNextGrid();
-    int it = grab();
     if (it >= total) return;
-    int end = min(it + kRemapChunk, total), nextBegin = grab();
-    int s = findSegment(segs, nsegs, it, 0);
-    RemapSeg cur = remapSeg(segs, nsegs, s, total);
-    RemapItem item = cur.items[it - cur.prefix];
-    const float2* mt = cur.R->maps + (size_t)item.mapTile * (kRemapTW * kRemapTH);
-    float2 m0 = __ldg(mt + threadIdx.x), m1 = __ldg(mt + threadIdx.x + kThreads);
     // constants of the loaded camera
     int camSeg = -1, cam = -1;
     const uint8_t* base = nullptr;
@@ -526,14 +536,21 @@ __global__ void __launch_bounds__(kThreads, 4) k_pyrdown(const Segment* __restri
     initMagic(sm.magic);
     int s = 0, begin, end;
     itemRange(total, begin, end);
+    // Items and descriptors are written before the launch sequence, not by
+    // a kernel: the first tile's are read while the previous kernel finishes.
+    const RigDev* R = nullptr;
+    DownItem item{};
+    bool interior = true;
+    if (begin < end) {
+        s = findSegment(segs, nsegs, begin, s);
+        R = segs[s].rig;
+        item = static_cast<const DownItem*>(segs[s].items)[begin - segs[s].prefix];
+        interior = downInterior(*R, item);
+        if (!interior) downTables(*R, item, sm.rowIdx[0], sm.colIdx[0]);
+    }
     waitPrevGrid();
     allowNextGrid();
     if (begin >= end) return;
-    s = findSegment(segs, nsegs, begin, s);
-    const RigDev* R = segs[s].rig;
-    DownItem item = static_cast<const DownItem*>(segs[s].items)[begin - segs[s].prefix];
-    bool interior = downInterior(*R, item);
-    if (!interior) downTables(*R, item, sm.rowIdx[0], sm.colIdx[0]);
     __syncthreads();
     DownRegs g;
     downLoad<false>(*R, item, interior, sm.rowIdx[0], sm.colIdx[0], g);
@@ -1174,12 +1191,15 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
         s_timeout = 0;
     }
     __syncthreads();
-    waitPrevGrid();
-    allowNextGrid();
     const int lane = threadIdx.x & 31;
 
     if (threadIdx.x >= kConsumers) {
         // ---------------- producer warp ----------------
+        // The hand-out counter, items and descriptors are written before the
+        // launch sequence, not by a kernel: the first unit is worked out
+        // while the previous kernel finishes, and the wait comes before its
+        // first copy of level data.
+        bool waited = false;
         auto nextItem = [&] {
             int v = 0;
             if (lane == 0) v = atomicAdd(counter, 1);
@@ -1229,6 +1249,11 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
             }
             fenceProxyAsync();
             if (lane == 0) info[stg] = ui;
+            if (!waited) {
+                waitPrevGrid();
+                allowNextGrid();
+                waited = true;
+            }
             if (ui.staged) {
                 const LevelDev& Lj = R->lv[j];
                 const LevelDev& Lu = R->lv[hasUp ? j + 1 : j];
@@ -1292,6 +1317,8 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
     }
 
     // ---------------- consumer warps ----------------
+    waitPrevGrid();
+    allowNextGrid();
     BlendAcc acc;
     for (int u = 0;; u++) {
         const int stg = u % kBStages;
@@ -1395,18 +1422,29 @@ __global__ void __launch_bounds__(kThreads) k_blend_small(const Segment* __restr
     extern __shared__ __align__(16) uint8_t smallSmem[];  // a SmallStage (dynamic: above the 48 KB static limit)
     SmallStage& st = *reinterpret_cast<SmallStage*>(smallSmem);
     __shared__ int fRow[kFH], fCol[kFW];
+    // Items and descriptors are written before the launch sequence, not by
+    // a kernel: the first item's are read while the previous kernel finishes.
+    int s = 0;
+    uint4 raw = make_uint4(0, 0, 0, 0);
+    UnitGeo geo;
+    const int first = blockIdx.x;
+    if (first < total) {
+        s = findSegment(segs, nsegs, first, s);
+        raw = __ldg(static_cast<const uint4*>(segs[s].items) + ((first - segs[s].prefix) >> 1));
+        fillGeo(geo, *segs[s].rig, *segs[s].frame, raw.x & 0xFF);
+    }
     waitPrevGrid();
     allowNextGrid();
-    int s = 0;
     PairAcc acc;
-    for (int it = blockIdx.x; it < total; it += gridDim.x) {
-        s = findSegment(segs, nsegs, it, s);
+    for (int it = first; it < total; it += gridDim.x) {
+        if (it != first) {
+            s = findSegment(segs, nsegs, it, s);
+            raw = __ldg(static_cast<const uint4*>(segs[s].items) + ((it - segs[s].prefix) >> 1));
+            fillGeo(geo, *segs[s].rig, *segs[s].frame, raw.x & 0xFF);
+        }
         const Segment& sg = segs[s];
         const RigDev& R = *sg.rig;
-        const int local = it - sg.prefix, half = local & 1;
-        const uint4 raw = __ldg(static_cast<const uint4*>(sg.items) + (local >> 1));
-        UnitGeo geo;
-        fillGeo(geo, R, *sg.frame, raw.x & 0xFF);
+        const int half = (it - sg.prefix) & 1;
         for (int chunk = 0; chunk < unitChunks<kTailCamsPerUnit>(raw); chunk++) {
             __syncthreads();  // readers of the previous unit are done
             stageUnitDirect<false>(st, R, raw, chunk, fRow, fCol, [] { __syncthreads(); }, half);
