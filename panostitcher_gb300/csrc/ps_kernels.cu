@@ -344,24 +344,25 @@ __global__ void __launch_bounds__(kThreads) k_reproject16s(const uint8_t* __rest
 //   columns wrap;  G_{j+1} = alpha ? (S << 8) / alpha : 0.
 // With alpha = 256*m this is floor(S / m), evaluated exactly as
 // (S * ceil(2^24 / m)) >> 24 (exact for S < 65793; S <= 65280 here).
-// One CTA produces a 32x16 output tile from a 67x35 input tile staged in
-// shared memory; the separable passes add two channels per 32-bit word.
+// One CTA produces a 32x16 output tile of one camera from its 67x35 input
+// tile.  Warp w owns output rows 2w and 2w + 1, i.e. input rows 4w .. 4w+6:
+// lane l loads input columns 2l and 2l + 1 of those seven rows (lanes 0..2
+// also column 64 + l), forms the vertical sums of both output rows in
+// registers, two channels per 32-bit word, and hands them to the warp
+// through the warp's own rows of shared memory; lane l then filters output
+// columns 2(l % 16) and 2(l % 16) + 1 of output row 2w + l / 16.  No step
+// waits for another warp.
 // ============================================================================
-constexpr int kDInW = 2 * kDownTW + 3;   // 67
-constexpr int kDInH = 2 * kDownTH + 3;   // 35
-constexpr int kDInP = kDInW + 1;         // 68: row stride of the staged tile (16-byte aligned rows)
+constexpr int kDInW = 2 * kDownTW + 3;   // 67 input columns
+constexpr int kDVP = kDInW + 1;          // 68: row stride of the vertical sums (16-byte aligned rows)
+constexpr int kDWarps = kThreads / 32;   // 8
+constexpr int kDRows = 7;                // input rows of a warp's two output rows
+static_assert(kDownTH == 2 * kDWarps, "a warp owns two output rows");
+static_assert(kDownTW == 32 && kDInW - 64 <= 32, "lanes cover the input columns as 2 x 32 + 3");
 
-constexpr int kDLoads = (kDInH * kDInW + kThreads - 1) / kThreads;   // 10 tile elements per thread (border tiles)
-constexpr int kDRows = (kDInH + 7) / 8;                               // 5 tile rows per warp (interior tiles)
-
-// The input tile is staged unpacked: element (r, c) holds the B|R and G|0
-// 16-bit lane pairs of the uchar4, so the filter passes add two channels per
-// 32-bit operation without unpacking every tap.
-struct DownSmem {
-    uint2 in[kDInH][kDInP];
-    uint2 v[kDownTH][kDInP];
+struct alignas(16) DownSmem {
+    uint2 v[kDWarps][2][kDVP];  // vertical sums (B|R, G|X lanes) of each warp's two output rows
     uint32_t magic[257];
-    int rowIdx[2][kDInH], colIdx[2][kDInW];  // border index tables, double-buffered across tiles
 };
 
 __device__ __forceinline__ void initMagic(uint32_t* magic)
@@ -379,157 +380,150 @@ __device__ __forceinline__ T ldLevel(const T* p)
     else return __ldg(p);
 }
 
-// The input tile of a 32x16 output tile of one camera, read into registers
-// (thread t holds elements t, t + 256, ... of the 35x67 tile in row-major
-// order), and the output's two alpha divisors.
+// A lane's part of its warp's input rows, and the alpha divisors of the
+// lane's two outputs (low half: the left one).
 struct DownRegs {
-    uint32_t v[3 * kDRows];  // interior: per warp row, two elements + one of the last three; border: kDLoads elements
-    int m0, m1;
+    uint32_t a[kDRows], b[kDRows];  // input columns 2*lane, 2*lane + 1
+    uint32_t c[kDRows];             // input column 64 + lane (lanes 0..2)
+    uint32_t m;
 };
 
 __device__ __forceinline__ bool downInterior(const RigDev& R, const DownItem& item)
 {
     const LevelDev& Ls = R.lv[item.level - 1];
     const int ix0 = 2 * item.tx * kDownTW - 2, iy0 = 2 * item.ty * kDownTH - 2;
-    return ix0 >= 0 && iy0 >= 0 && ix0 + kDInW <= Ls.w && iy0 + kDInH <= Ls.h;
+    return ix0 >= 0 && iy0 >= 0 && ix0 + kDInW <= Ls.w && iy0 + 2 * kDownTH + 3 <= Ls.h;
 }
 
-// Border tiles: the row / column index tables (threads 0..101), read after
-// the caller's next barrier.
-__device__ __forceinline__ void downTables(const RigDev& R, const DownItem& item, int* rowIdx, int* colIdx)
-{
-    const LevelDev& Ls = R.lv[item.level - 1];
-    const int ix0 = 2 * item.tx * kDownTW - 2, iy0 = 2 * item.ty * kDownTH - 2;
-    if (threadIdx.x < kDInH) rowIdx[threadIdx.x] = rowMap(iy0 + (int)threadIdx.x, Ls.h);
-    else if (threadIdx.x < kDInH + kDInW) colIdx[threadIdx.x - kDInH] = colMap(ix0 + (int)threadIdx.x - kDInH, Ls.w);
-}
-
+// The lane's loads for a tile.  Interior tiles read whole rows (8-byte loads:
+// the first input column is even and rows are 256-byte aligned); tiles whose
+// input crosses the level's border map every row and column with the
+// reference's reflect-101 / wrap rules.
 template <bool kFresh>
-__device__ __forceinline__ void downLoad(const RigDev& R, const DownItem& item, bool interior, const int* rowIdx,
-                                         const int* colIdx, DownRegs& g)
+__device__ __forceinline__ void downLoad(const RigDev& R, const DownItem& item, DownRegs& g)
 {
-    const int ox = threadIdx.x & 31, oy = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const LevelDev& Ls = R.lv[item.level - 1];
     const LevelDev& Ld = R.lv[item.level];
     const int ox0 = item.tx * kDownTW, oy0 = item.ty * kDownTH;
-    const int ix0 = 2 * ox0 - 2, iy0 = 2 * oy0 - 2;
+    const int ix0 = 2 * ox0 - 2, iy0 = 2 * oy0 - 2 + 4 * w;  // the warp's first input row
     const uint32_t* G = reinterpret_cast<const uint32_t*>(Ls.G) + (size_t)item.cam * Ls.camStride;
-    const int X = ox0 + ox, Y0 = oy0 + oy, Y1 = Y0 + 8;
-    const size_t o0 = (size_t)item.cam * Ld.camStride + (size_t)Y0 * Ld.pitch + X;
-    const size_t o1 = o0 + (size_t)8 * Ld.pitch;
-    g.m0 = X < Ld.w && Y0 < Ld.h ? __ldg(Ld.Am + o0) : 0;
-    g.m1 = X < Ld.w && Y1 < Ld.h ? __ldg(Ld.Am + o1) : 0;
-    if (interior) {
-        // warp w loads tile rows w, w + 8, ...: columns 2*lane, 2*lane + 1 as one 8-byte load
-        // (ix0 is even and rows are 256-byte aligned), lanes 0..2 also column 64 + lane
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        const uint32_t* row0 = G + (size_t)(iy0 + w) * Ls.pitch + ix0;
+    // the lane's outputs (X, Y), (X + 1, Y): X is even, so both divisors are
+    // one aligned 4-byte load (X + 1 stays inside the row pitch)
+    const int X = ox0 + 2 * (lane & 15), Y = oy0 + 2 * w + (lane >> 4);
+    g.m = X < Ld.w && Y < Ld.h
+              ? __ldg(reinterpret_cast<const uint32_t*>(Ld.Am + (size_t)item.cam * Ld.camStride + (size_t)Y * Ld.pitch + X))
+              : 0u;
+    const bool extra = lane < kDInW - 64;
+    if (downInterior(R, item)) {
+        const uint32_t* row = G + (size_t)iy0 * Ls.pitch + ix0;
 #pragma unroll
-        for (int i = 0; i < kDRows; i++) {
-            if (w + 8 * i < kDInH) {
-                const uint32_t* row = row0 + (size_t)(8 * i) * Ls.pitch;
-                const uint2 a = ldLevel<kFresh>(reinterpret_cast<const uint2*>(row) + lane);
-                g.v[3 * i] = a.x;
-                g.v[3 * i + 1] = a.y;
-                g.v[3 * i + 2] = lane < kDInW - 64 ? ldLevel<kFresh>(row + 64 + lane) : 0u;
-            }
+        for (int r = 0; r < kDRows; r++, row += Ls.pitch) {
+            const uint2 v = ldLevel<kFresh>(reinterpret_cast<const uint2*>(row) + lane);
+            g.a[r] = v.x;
+            g.b[r] = v.y;
+            g.c[r] = extra ? ldLevel<kFresh>(row + 64 + lane) : 0u;
         }
         return;
     }
+    const int c0 = colMap(ix0 + 2 * lane, Ls.w), c1 = colMap(ix0 + 2 * lane + 1, Ls.w);
+    const int c2 = extra ? colMap(ix0 + 64 + lane, Ls.w) : 0;
 #pragma unroll
-    for (int q = 0; q < kDLoads; q++) {
-        const int k = threadIdx.x + q * kThreads;
-        if (k < kDInH * kDInW) {
-            const int r = k / kDInW, c = k - r * kDInW;
-            g.v[q] = ldLevel<kFresh>(G + (size_t)rowIdx[r] * Ls.pitch + colIdx[c]);
-        }
+    for (int r = 0; r < kDRows; r++) {
+        const uint32_t* row = G + (size_t)rowMap(iy0 + r, Ls.h) * Ls.pitch;
+        g.a[r] = ldLevel<kFresh>(row + c0);
+        g.b[r] = ldLevel<kFresh>(row + c1);
+        g.c[r] = extra ? ldLevel<kFresh>(row + c2) : 0u;
     }
 }
 
-// Filter the staged tile: the caller has written it to sm.in and
-// synchronised.  Ends with the outputs stored.
-__device__ __forceinline__ void downCompute(const RigDev& R, const DownItem& item, const DownRegs& g, DownSmem& sm)
+// [1 4 6 4 1] over five 16-bit-lane words (sums of up to 16 * 4080 stay in
+// the lanes).
+__device__ __forceinline__ uint32_t k5(uint32_t p0, uint32_t p1, uint32_t p2, uint32_t p3, uint32_t p4)
 {
-    const int ox = threadIdx.x & 31, oy = threadIdx.x >> 5;
+    return p0 + p4 + 4 * (p1 + p3) + 6 * p2;
+}
+
+// Vertical sums of one input column: the even output row from input rows
+// 0..4, the odd one from rows 2..6.
+__device__ __forceinline__ void downColumn(const uint32_t* p, uint2& e, uint2& o)
+{
+    uint2 u[kDRows];
+#pragma unroll
+    for (int r = 0; r < kDRows; r++) u[r] = unpackBytes(p[r]);
+    e = make_uint2(k5(u[0].x, u[1].x, u[2].x, u[3].x, u[4].x), k5(u[0].y, u[1].y, u[2].y, u[3].y, u[4].y));
+    o = make_uint2(k5(u[2].x, u[3].x, u[4].x, u[5].x, u[6].x), k5(u[2].y, u[3].y, u[4].y, u[5].y, u[6].y));
+}
+
+// The lane's vertical sums into the warp's rows.
+__device__ __forceinline__ void downVertical(const DownRegs& g, DownSmem& sm)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint2 ea, oa, eb, ob;
+    downColumn(g.a, ea, oa);
+    downColumn(g.b, eb, ob);
+    __syncwarp();  // the warp's reads of its previous tile are done
+    *reinterpret_cast<uint4*>(&sm.v[w][0][2 * lane]) = make_uint4(ea.x, ea.y, eb.x, eb.y);
+    *reinterpret_cast<uint4*>(&sm.v[w][1][2 * lane]) = make_uint4(oa.x, oa.y, ob.x, ob.y);
+    if (lane < kDInW - 64) {
+        uint2 ec, oc;
+        downColumn(g.c, ec, oc);
+        sm.v[w][0][64 + lane] = ec;
+        sm.v[w][1][64 + lane] = oc;
+    }
+    __syncwarp();
+}
+
+// floor(S / m) of the B, G, R sums (lo = B | R << 16, hi = G | X << 16):
+// floor(S / m) = floor(S * ceil(2^24 / m) / 2^24) = umulhi(S << 8, ceil(2^24 / m)).
+__device__ __forceinline__ uint32_t downDivide(uint32_t lo, uint32_t hi, uint32_t m, const uint32_t* magic)
+{
+    if (!m) return 0;
+    const uint32_t mg = magic[m];
+    const uint32_t b = __umulhi((lo & 0xFFFFu) << 8, mg);
+    const uint32_t r = __umulhi((lo >> 16) << 8, mg);
+    const uint32_t gg = __umulhi((hi & 0xFFFFu) << 8, mg);
+    return b | (gg << 8) | (r << 16);
+}
+
+// Horizontal pass of the lane's two outputs from the warp's rows, and the
+// stores.  m: the divisors loaded with the tile.
+__device__ __forceinline__ void downHorizontal(const RigDev& R, const DownItem& item, uint32_t m, const DownSmem& sm)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int k = lane & 15, rsel = lane >> 4;
+    // output columns 2k and 2k + 1 read vertical sums 4k .. 4k + 4 and 4k + 2 .. 4k + 6
+    const uint2* vr = &sm.v[w][rsel][4 * k];
+    const uint4 q01 = *reinterpret_cast<const uint4*>(vr);
+    const uint4 q23 = *reinterpret_cast<const uint4*>(vr + 2);
+    const uint4 q45 = *reinterpret_cast<const uint4*>(vr + 4);
+    const uint2 q6 = vr[6];
+    const uint32_t lo0 = k5(q01.x, q01.z, q23.x, q23.z, q45.x), hi0 = k5(q01.y, q01.w, q23.y, q23.w, q45.y);
+    const uint32_t lo1 = k5(q23.x, q23.z, q45.x, q45.z, q6.x), hi1 = k5(q23.y, q23.w, q45.y, q45.w, q6.y);
+    const uint32_t out0 = downDivide(lo0, hi0, m & 0xFFFFu, sm.magic);
+    const uint32_t out1 = downDivide(lo1, hi1, m >> 16, sm.magic);
     const LevelDev& Ld = R.lv[item.level];
-    const int X = item.tx * kDownTW + ox, Y0 = item.ty * kDownTH + oy;
-    for (int k = threadIdx.x; k < kDownTH * kDInW; k += kThreads) {
-        const int r = k / kDInW, c = k - r * kDInW;
-        const uint2 p0 = sm.in[2 * r][c], p1 = sm.in[2 * r + 1][c], p2 = sm.in[2 * r + 2][c];
-        const uint2 p3 = sm.in[2 * r + 3][c], p4 = sm.in[2 * r + 4][c];
-        sm.v[r][c] = make_uint2(p0.x + 4 * (p1.x + p3.x) + 6 * p2.x + p4.x, p0.y + 4 * (p1.y + p3.y) + 6 * p2.y + p4.y);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int half = 0; half < 2; half++) {
-        const int r = oy + 8 * half, Y = Y0 + 8 * half;
-        uint32_t lo = 0, hi = 0;
-#pragma unroll
-        for (int t = 0; t < 5; t++) {
-            const uint2 q = sm.v[r][2 * ox + t];
-            lo += c_k5[t] * q.x;
-            hi += c_k5[t] * q.y;
-        }
-        const int m = half ? g.m1 : g.m0;
-        uint32_t outv = 0;
-        if (m) {
-            // floor(S / m) = floor(S * ceil(2^24 / m) / 2^24) = umulhi(S << 8, ceil(2^24 / m))
-            const uint32_t mg = sm.magic[m];
-            const uint32_t b = __umulhi((lo & 0xFFFFu) << 8, mg);
-            const uint32_t rr = __umulhi((lo >> 16) << 8, mg);
-            const uint32_t gg = __umulhi((hi & 0xFFFFu) << 8, mg);
-            outv = b | (gg << 8) | (rr << 16);
-        }
-        if (X < Ld.w && Y < Ld.h)
-            reinterpret_cast<uint32_t*>(Ld.G)[(size_t)item.cam * Ld.camStride + (size_t)Y * Ld.pitch + X] = outv;
+    const int X = item.tx * kDownTW + 2 * k, Y = item.ty * kDownTH + 2 * w + rsel;
+    if (X < Ld.w && Y < Ld.h) {
+        uint32_t* dst = reinterpret_cast<uint32_t*>(Ld.G) + (size_t)item.cam * Ld.camStride + (size_t)Y * Ld.pitch + X;
+        if (X + 1 < Ld.w) *reinterpret_cast<uint2*>(dst) = make_uint2(out0, out1);
+        else dst[0] = out0;
     }
 }
 
-__device__ __forceinline__ void downStage(const DownRegs& g, bool interior, DownSmem& sm)
-{
-    if (interior) {
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-        for (int i = 0; i < kDRows; i++) {
-            const int r = w + 8 * i;
-            if (r < kDInH) {
-                const uint2 a = unpackBytes(g.v[3 * i]), b = unpackBytes(g.v[3 * i + 1]);
-                *reinterpret_cast<uint4*>(&sm.in[r][2 * lane]) = make_uint4(a.x, a.y, b.x, b.y);
-                if (lane < kDInW - 64) sm.in[r][64 + lane] = unpackBytes(g.v[3 * i + 2]);
-            }
-        }
-        return;
-    }
-#pragma unroll
-    for (int q = 0; q < kDLoads; q++) {
-        const int k = threadIdx.x + q * kThreads;
-        if (k < kDInH * kDInW) {
-            const int r = k / kDInW, c = k - r * kDInW;
-            sm.in[r][c] = unpackBytes(g.v[q]);
-        }
-    }
-}
-
-// One 32x16 output tile of one camera (all kThreads threads of the CTA),
-// without overlap (the tail kernel's few tiles).
+// One 32x16 output tile of one camera (all warps of the CTA; the magic table
+// is ready), without overlap (the tail kernel's few tiles).
 template <bool kFresh>
 __device__ __forceinline__ void pyrDownTile(const RigDev& R, const DownItem item, DownSmem& sm)
 {
-    const bool interior = downInterior(R, item);
-    if (!interior) {
-        downTables(R, item, sm.rowIdx[0], sm.colIdx[0]);
-        __syncthreads();
-    }
     DownRegs g;
-    downLoad<kFresh>(R, item, interior, sm.rowIdx[0], sm.colIdx[0], g);
-    __syncthreads();  // the previous tile's readers are done with shared memory
-    downStage(g, interior, sm);
-    __syncthreads();
-    downCompute(R, item, g, sm);
+    downLoad<kFresh>(R, item, g);
+    downVertical(g, sm);
+    downHorizontal(R, item, g.m, sm);
 }
 
 // One CTA walks a contiguous run of tiles; the next tile's loads are issued
-// before the current tile is filtered, so their latency overlaps the work.
+// before the current tile's horizontal pass, so their latency overlaps it.
 __global__ void __launch_bounds__(kThreads, 4) k_pyrdown(const Segment* __restrict__ segs, int nsegs, int total)
 {
     __shared__ DownSmem sm;
@@ -540,42 +534,32 @@ __global__ void __launch_bounds__(kThreads, 4) k_pyrdown(const Segment* __restri
     // a kernel: the first tile's are read while the previous kernel finishes.
     const RigDev* R = nullptr;
     DownItem item{};
-    bool interior = true;
     if (begin < end) {
         s = findSegment(segs, nsegs, begin, s);
         R = segs[s].rig;
         item = static_cast<const DownItem*>(segs[s].items)[begin - segs[s].prefix];
-        interior = downInterior(*R, item);
-        if (!interior) downTables(*R, item, sm.rowIdx[0], sm.colIdx[0]);
     }
     waitPrevGrid();
     allowNextGrid();
     if (begin >= end) return;
-    __syncthreads();
+    __syncthreads();  // the magic table
     DownRegs g;
-    downLoad<false>(*R, item, interior, sm.rowIdx[0], sm.colIdx[0], g);
+    downLoad<false>(*R, item, g);
     for (int it = begin; it < end; it++) {
-        const int buf = (it - begin + 1) & 1;  // tables of the next tile
         const bool more = it + 1 < end;
         int sn = s;
         DownItem next = item;
-        bool nextInterior = true;
         if (more) {
             sn = findSegment(segs, nsegs, it + 1, s);
             next = static_cast<const DownItem*>(segs[sn].items)[it + 1 - segs[sn].prefix];
-            nextInterior = downInterior(*segs[sn].rig, next);
         }
-        __syncthreads();  // the previous tile's readers are done with shared memory
-        downStage(g, interior, sm);
-        if (more && !nextInterior) downTables(*segs[sn].rig, next, sm.rowIdx[buf], sm.colIdx[buf]);
-        __syncthreads();
-        const DownRegs cur = g;
-        if (more) downLoad<false>(*segs[sn].rig, next, nextInterior, sm.rowIdx[buf], sm.colIdx[buf], g);
-        downCompute(*R, item, cur, sm);
+        downVertical(g, sm);
+        const uint32_t m = g.m;
+        if (more) downLoad<false>(*segs[sn].rig, next, g);
+        downHorizontal(*R, item, m, sm);
         s = sn;
         R = segs[s].rig;
         item = next;
-        interior = nextInterior;
     }
 }
 
@@ -1373,6 +1357,7 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
     waitPrevGrid();
     allowNextGrid();
     if (rig >= nsegs) return;  // never: the grid is nsegs clusters
+    __syncthreads();  // the magic table
     const Segment& sg = segs[rig];
     const RigDev& R = *sg.rig;
     for (int J = R.tailDown; J <= R.L; J++) {
