@@ -524,7 +524,7 @@ __device__ __forceinline__ void pyrDownTile(const RigDev& R, const DownItem item
 
 // One CTA walks a contiguous run of tiles; the next tile's loads are issued
 // before the current tile's horizontal pass, so their latency overlaps it.
-__global__ void __launch_bounds__(kThreads, 4) k_pyrdown(const Segment* __restrict__ segs, int nsegs, int total)
+__global__ void __launch_bounds__(kThreads, 5) k_pyrdown(const Segment* __restrict__ segs, int nsegs, int total)
 {
     __shared__ DownSmem sm;
     initMagic(sm.magic);
