@@ -66,3 +66,31 @@ def test_blender_more_than_max_cameras_rejected(cuda):
     b = P.CudaTilingMultibandBlendFast()
     assert not b.prepare(list(cov), None, 4)
     assert b.num_levels == 0
+
+
+@pytest.mark.parametrize("n,W,H,levels", [(3, 130, 67, 6), (12, 96, 48, 5)])
+def test_blender_overlapping_seams_bit_exact(cuda, oracle_lib, n, W, H, levels):
+    """Explicit seams that overlap (each camera's seam is its whole
+    coverage): weight sums reach 256 n, so the normalisation divides by sums
+    from 256 up to 768 (three cameras) and past the 1024 of its table (twelve
+    cameras), with partial coverage."""
+    import torch
+    rng = np.random.default_rng(n * 104729 + W)
+    cov, _ = _overlapping(rng, n, H, W)
+    cov[:, :2, :3] = 0  # an uncovered corner: the weighted normalisation, not the full-mask shift
+    ob = O.Blender(cov, cov, levels)
+    b = P.CudaTilingMultibandBlendFast()
+    assert b.prepare(list(cov), list(cov), levels), b.last_error
+    imgs = []
+    for i in range(n):
+        im = rng.integers(0, 256, (H, W, 4)).astype(np.int16)
+        im[..., 3] = 0
+        im[cov[i] == 0] = 0
+        imgs.append(im)
+    ref = ob.blend(imgs)
+    dev = [torch.from_numpy(im).cuda() for im in imgs]
+    out = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    b.blend(dev, out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()[..., :3]
+    assert np.array_equal(got, ref[..., :3]), diff_histogram(got, ref[..., :3])
