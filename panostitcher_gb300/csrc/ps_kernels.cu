@@ -593,7 +593,6 @@ __global__ void __launch_bounds__(kThreads, 5) k_pyrdown(const Segment* __restri
 // ============================================================================
 constexpr int kFW = kBlendTW / 2 + 2;  // 34: footprint columns fx0 .. fx0+33
 constexpr int kFH = kBlendTH / 2 + 2;  // 10: footprint rows    fy0 .. fy0+9
-constexpr int kFElems = kFW * kFH;     // 340
 constexpr int kBStages = 2;
 constexpr int kCamsPerUnit = 2;
 constexpr int kFpW = 40;   // staged footprint row: columns fx0-3 .. fx0+36 (16-byte aligned start)
