@@ -130,7 +130,8 @@ int ps_load_photo_params(const char* path, ps_photo_param* params, int capacity,
 /* Same, with explicit seam (unique) masks: num_params host arrays of
    dst_h*dst_w uint8 (non-zero = owned), each a subset of that camera's
    coverage; they replace getNonIntersectingMasks
-   (source/CudaAccel/CudaMultibandBlend.cpp:570-571). */
+   (source/CudaAccel/CudaMultibandBlend.cpp:570-571) and, like its masks,
+   must not intersect (PS_EINVAL naming the first shared pixel). */
 int ps_render_prepare_with_seams(ps_render* r, const ps_photo_param* params, int num_params,
                                  int high_quality_blend, int blend_param, int src_w, int src_h, int dst_w,
                                  int dst_h, const uint8_t* const* seam_masks, void* stream);
@@ -362,9 +363,9 @@ int ps_blender_create(ps_blender** out);
 void ps_blender_destroy(ps_blender* b);
 /* prepare(masks, maxLevels, minLength) (source/CudaAccel/CudaMultibandBlend.cpp:
    549-642): masks = num host uint8 coverage masks (width x height), seams =
-   num host uint8 unique masks (subsets of the masks), or NULL to derive them
-   from the masks with getNonIntersectingMasks as the reference does
-   (:570-571).  Synchronises. */
+   num host uint8 unique masks (subsets of the masks that do not intersect,
+   else PS_EINVAL), or NULL to derive them from the masks with
+   getNonIntersectingMasks as the reference does (:570-571).  Synchronises. */
 int ps_blender_prepare(ps_blender* b, const uint8_t* const* masks, const uint8_t* const* seams, int num,
                        int width, int height, int max_levels, int min_length, void* stream);
 /* blend(images, blendImage) (:785-823): num device images of int16 x4

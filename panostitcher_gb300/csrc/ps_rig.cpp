@@ -230,6 +230,26 @@ static void distanceSeams(const uint8_t* cov, int n, int W, int H, uint8_t* seam
     PS_CUDA(cudaStreamSynchronize(st));  // before the scratch is freed
 }
 
+// Explicit seam masks must not intersect, as getNonIntersectingMasks'
+// never do (source/Blend/Mask.cpp:376-398): the collapsed levels are int16,
+// which holds only while the seam weights at a pixel sum to at most 256 at
+// level 0 (and 256 + n*j/2 at level j, from the per-level rounding).
+static void checkSeamsDisjoint(const uint8_t* const* seams, int n, int W, int H)
+{
+    const size_t npx = (size_t)W * H;
+    std::vector<uint8_t> owner(npx, 0);  // 1 + the camera whose seam holds the pixel
+    for (int i = 0; i < n; i++) {
+        const uint8_t* s = seams[i];
+        for (size_t p = 0; p < npx; p++) {
+            if (!s[p]) continue;
+            if (owner[p])
+                fail(PS_EINVAL, "seam masks %d and %d intersect at (%d, %d)", owner[p] - 1, i, (int)(p % W),
+                     (int)(p / W));
+            owner[p] = (uint8_t)(i + 1);
+        }
+    }
+}
+
 void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
                             int dstH, const uint8_t* const* seams, cudaStream_t st, int seamRule, int highQuality)
 {
@@ -253,10 +273,11 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
             PS_CUDA(launchGenMap(dParams.as<RemapDev>() + i, dstW, dstH, xmap.as<float>() + i * npx,
                                  ymap.as<float>() + i * npx, cov.as<uint8_t>() + i * npx, st));
         if (seams) {
-            for (int i = 0; i < n; i++) {
+            for (int i = 0; i < n; i++)
                 if (!seams[i]) fail(PS_EINVAL, "seam mask %d is NULL", i);
+            checkSeamsDisjoint(seams, n, dstW, dstH);
+            for (int i = 0; i < n; i++)
                 PS_CUDA(cudaMemcpyAsync(seam.as<uint8_t>() + i * npx, seams[i], npx, cudaMemcpyHostToDevice, st));
-            }
         } else if (seamRule == PS_SEAMS_DISTANCE) {
             distanceSeams(cov.as<uint8_t>(), n, dstW, dstH, seam.as<uint8_t>(), st);
         } else {
@@ -287,6 +308,7 @@ void Rig::prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* se
     if (W <= 0 || H <= 0) fail(PS_EINVAL, "mask size (%d, %d) must be positive", W, H);
     for (int i = 0; i < n; i++)
         if (!masks[i] || (seams && !seams[i])) fail(PS_EINVAL, "mask %d is NULL", i);
+    if (seams) checkSeamsDisjoint(seams, n, W, H);
     try {
         setGeometry(n, W, H, std::max(0, trueNumLevels(W, H, maxLevels, minLength)));
         const size_t npx = (size_t)W * H;

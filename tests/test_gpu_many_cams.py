@@ -68,29 +68,30 @@ def test_blender_more_than_max_cameras_rejected(cuda):
     assert b.num_levels == 0
 
 
-@pytest.mark.parametrize("n,W,H,levels", [(3, 130, 67, 6), (12, 96, 48, 5)])
-def test_blender_overlapping_seams_bit_exact(cuda, oracle_lib, n, W, H, levels):
-    """Explicit seams that overlap (each camera's seam is its whole
-    coverage): weight sums reach 256 n, so the normalisation divides by sums
-    from 256 up to 768 (three cameras) and past the 1024 of its table (twelve
-    cameras), with partial coverage."""
-    import torch
-    rng = np.random.default_rng(n * 104729 + W)
-    cov, _ = _overlapping(rng, n, H, W)
-    cov[:, :2, :3] = 0  # an uncovered corner: the weighted normalisation, not the full-mask shift
-    ob = O.Blender(cov, cov, levels)
+def test_intersecting_seams_rejected(cuda):
+    """Explicit seams must not intersect, as getNonIntersectingMasks' never
+    do: the collapsed levels are int16, bounded only while the seam weights
+    at a pixel sum to at most 256.  Both prepares reject shared pixels and
+    name the first one."""
+    n, H, W = 3, 48, 96
+    cov = np.full((n, H, W), 255, np.uint8)
+    seams = np.zeros_like(cov)
+    seams[0][:, :40] = 255
+    seams[1][:, 40:] = 255
+    seams[2][5, 41] = 255  # also camera 1's
     b = P.CudaTilingMultibandBlendFast()
-    assert b.prepare(list(cov), list(cov), levels), b.last_error
-    imgs = []
-    for i in range(n):
-        im = rng.integers(0, 256, (H, W, 4)).astype(np.int16)
-        im[..., 3] = 0
-        im[cov[i] == 0] = 0
-        imgs.append(im)
-    ref = ob.blend(imgs)
-    dev = [torch.from_numpy(im).cuda() for im in imgs]
-    out = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
-    b.blend(dev, out)
-    torch.cuda.synchronize()
-    got = out.cpu().numpy()[..., :3]
-    assert np.array_equal(got, ref[..., :3]), diff_histogram(got, ref[..., :3])
+    assert not b.prepare(list(cov), list(seams), 4)
+    assert "intersect at (41, 5)" in b.last_error and b.num_levels == 0
+    seams[2][5, 41] = 0
+    assert b.prepare(list(cov), list(seams), 4), b.last_error
+    # the render's prepare with explicit seams
+    from panostitcher_gb300 import synth as S
+    cfg = S.scaled_rig(S.rig("c2"), 8)
+    W, H = cfg.dst_size
+    full = np.zeros((cfg.num_cams, H, W), np.uint8)
+    full[0][:, : W // 2] = 255
+    full[1][:, W // 2:] = 255
+    full[1][3, 7] = 255
+    r = P.CudaPanoramaRender2()
+    assert not r.prepare(cfg.cams, 1, cfg.levels, cfg.src_size, cfg.dst_size, seams=list(full))
+    assert "seam masks 0 and 1 intersect at (7, 3)" in r.last_error and r.getNumImages() == 0
