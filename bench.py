@@ -156,19 +156,34 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """Per-launch DRAM bytes of a kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
-    if not os.path.exists(path):
+NCU_TRAFFIC = {"c2": "ncu_traffic.txt", "c5": "ncu_traffic_c5.txt"}
+
+
+def ncu_traffic(kernel: str, workload: str, alg_bytes_per_launch: float):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary of the workload, if any.  A line
+    `kernel bytes` was captured on the workload itself; a line `kernel bytes alg_bytes` on a scaled-down
+    copy of it (the full one holds too much device memory for a capture), and is scaled to a full launch by
+    the algorithmic bytes, which the kernel's traffic follows."""
+    name = NCU_TRAFFIC.get(workload)
+    path = os.path.join(ROOT, "profiles", name) if name else None
+    if not path or not os.path.exists(path):
         return None
     for line in open(path):
         parts = line.split()
         if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
             try:
-                return float(parts[1])
-            except ValueError:
+                nbytes = float(parts[1])
+                return nbytes if len(parts) < 3 else round(nbytes * alg_bytes_per_launch / float(parts[2]))
+            except (ValueError, ZeroDivisionError):
                 return None
     return None
+
+
+def workload_rig(args):
+    """The workload's rig, divided by --scale for profiler captures."""
+    from panostitcher_gb300 import synth as S
+    cfg = S.rig(args.workload)
+    return S.scaled_rig(cfg, args.scale) if args.scale > 1 else cfg
 
 
 def pinned_copy(a: np.ndarray):
@@ -225,7 +240,7 @@ def run_ours(args, world, rank, local, dist):
     B.build()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    cfg = S.rig(args.workload)
+    cfg = workload_rig(args)
     W, H = cfg.dst_size
     npx = W * H
     r = P.CudaPanoramaRender2()
@@ -304,6 +319,8 @@ def run_ours(args, world, rank, local, dist):
                      "l2": f"inputs larger than L2: {args.pool} distinct {frame_mb:.1f} MB frames cycled, "
                            f"rig state {resident / 1e6:.0f} MB resident", "parallelism": f"replicas x{world}",
                      "prepare_s": round(prepare_s, 3)}
+    if args.scale > 1:
+        out["config"]["workload"] += f"; every size divided by {args.scale}"
     out["launch_shape"] = tune if tune is not None else {"shape": r.launch_shape(), "tuned": False}
 
     # ---- e2e: pinned host frames in, host canvas out, through the C ABI
@@ -436,7 +453,8 @@ def run_ours(args, world, rank, local, dist):
     dom = max(kernels, key=lambda k: kernels[k]["ms_per_frame"])
     peak, peak_src = measured_peak()
     achieved = kernels[dom]["gbs"]
-    traffic = ncu_traffic(dom) if args.workload == "c2" else None  # the ncu summary covers that workload
+    # the committed ncu summaries cover the full-size workloads
+    traffic = ncu_traffic(dom, args.workload, kernels[dom]["alg_bytes_per_launch"]) if args.scale == 1 else None
     out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                        "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
                        "traffic": traffic,
@@ -470,7 +488,7 @@ def run_linear(args, dev):
     import torch
     import panostitcher_gb300 as P
     from panostitcher_gb300 import synth as S
-    cfg = S.rig(args.workload)
+    cfg = workload_rig(args)
     W, H = cfg.dst_size
     radius = int(W * 0.05)
     r = P.CudaPanoramaRender2()
@@ -681,6 +699,8 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--pool", type=int, default=4)
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    ap.add_argument("--scale", type=int, default=1,
+                    help="divide the workload's source and canvas sizes by this (small profiler captures)")
     ap.add_argument("--inflight", type=int, default=8, help="caller streams of the device-resident loop")
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
