@@ -258,6 +258,11 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
     if (blendParam <= 0) fail(PS_EINVAL, "blendParam = %d, should be positive", blendParam);  // RicohUtil.cpp:1105
     if (!highQuality && blendParam > kMaxLinearRadius)
         fail(PS_EINVAL, "blendParam = %d, the linear-blend radius is at most %d", blendParam, kMaxLinearRadius);
+    if (seams) {
+        for (int i = 0; i < n; i++)
+            if (!seams[i]) fail(PS_EINVAL, "seam mask %d is NULL", i);
+        checkSeamsDisjoint(seams, n, dstW, dstH);
+    }
     try {
         // MIN_SIDE_LENGTH = 2, source/Task/RicohUtil.cpp:15
         setGeometry(n, dstW, dstH, highQuality ? std::max(0, trueNumLevels(dstW, dstH, blendParam, 2)) : 0);
@@ -273,9 +278,6 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
             PS_CUDA(launchGenMap(dParams.as<RemapDev>() + i, dstW, dstH, xmap.as<float>() + i * npx,
                                  ymap.as<float>() + i * npx, cov.as<uint8_t>() + i * npx, st));
         if (seams) {
-            for (int i = 0; i < n; i++)
-                if (!seams[i]) fail(PS_EINVAL, "seam mask %d is NULL", i);
-            checkSeamsDisjoint(seams, n, dstW, dstH);
             for (int i = 0; i < n; i++)
                 PS_CUDA(cudaMemcpyAsync(seam.as<uint8_t>() + i * npx, seams[i], npx, cudaMemcpyHostToDevice, st));
         } else if (seamRule == PS_SEAMS_DISTANCE) {

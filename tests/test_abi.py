@@ -153,3 +153,23 @@ def test_frames_in_flight_validation_before_the_gpu(built_lib):
     r.set_frames_in_flight(L.PS_MAX_IN_FLIGHT)
     assert built_lib.ps_render_set_frames_in_flight(None, 2) == L.PS_EINVAL
     assert built_lib.ps_render_get_frames_in_flight(None) == 0
+
+
+def test_intersecting_seams_rejected_before_the_gpu(built_lib):
+    """Explicit seams must not intersect (as getNonIntersectingMasks' never do); both prepares check it on
+    the host before any device work and name the first shared pixel."""
+    cfg = S.rig("c1")
+    W, H = cfg.dst_size
+    seams = np.zeros((cfg.num_cams, H, W), np.uint8)
+    seams[0][:, : W // 2] = 255
+    seams[1][:, W // 2 - 1:] = 255  # column W/2 - 1 is both cameras'
+    r = P.CudaPanoramaRender2()
+    assert not r.prepare(cfg.cams, 1, 5, cfg.src_size, cfg.dst_size, seams=list(seams))
+    assert f"seam masks 0 and 1 intersect at ({W // 2 - 1}, 0)" in r.last_error and r.getNumImages() == 0
+    b = P.CudaTilingMultibandBlendFast()
+    cov = np.full((2, 16, 32), 255, np.uint8)
+    small = np.zeros_like(cov)
+    small[0][:, :20] = 255
+    small[1][:, 19:] = 255
+    assert not b.prepare(list(cov), list(small), 3)
+    assert "intersect at (19, 0)" in b.last_error and b.num_levels == 0
