@@ -21,6 +21,12 @@ from . import _lib as L
 from ._lib import PhotoParam, Image, PlanarImage, PsError, check, lib
 
 
+def _require(ok: bool, what: str) -> None:
+    """Argument checks that stay on under python -O (ValueError, like the other shape errors here)."""
+    if not ok:
+        raise ValueError(what)
+
+
 def _is_device(a) -> bool:
     return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
 
@@ -28,11 +34,13 @@ def _is_device(a) -> bool:
 def as_image(a) -> Image:
     """ps_image view of a numpy array (host) or a CUDA tensor (device)."""
     if _is_device(a):
-        assert a.dim() == 3 and a.shape[2] in (3, 4) and a.stride(2) == 1 and a.stride(1) == a.shape[2]
+        _require(a.dim() == 3 and a.shape[2] in (3, 4) and a.stride(2) == 1 and a.stride(1) == a.shape[2]
+                 and a.element_size() == 1, "a device image is a uint8 (H, W, 3 or 4) tensor with dense rows")
         return Image(a.data_ptr(), a.stride(0) * a.element_size(), a.shape[1], a.shape[0],
                      L.PS_FMT_BGR32 if a.shape[2] == 4 else L.PS_FMT_BGR24, L.PS_MEM_DEVICE)
-    assert isinstance(a, np.ndarray) and a.dtype == np.uint8 and a.ndim == 3 and a.shape[2] in (3, 4)
-    assert a.strides[2] == 1 and a.strides[1] == a.shape[2]
+    _require(isinstance(a, np.ndarray) and a.dtype == np.uint8 and a.ndim == 3 and a.shape[2] in (3, 4)
+             and a.strides[2] == 1 and a.strides[1] == a.shape[2],
+             "a host image is a uint8 (H, W, 3 or 4) numpy array with dense rows")
     return Image(a.ctypes.data, a.strides[0], a.shape[1], a.shape[0],
                  L.PS_FMT_BGR32 if a.shape[2] == 4 else L.PS_FMT_BGR24, L.PS_MEM_HOST)
 
@@ -49,11 +57,13 @@ def as_planar(planes: Sequence, fmt: int) -> PlanarImage:
         if _is_device(p) != dev:
             raise ValueError("planes must all be host arrays or all CUDA tensors")
         if dev:
-            assert p.dim() == 2 and p.stride(1) == 1 and p.element_size() == 1
+            _require(p.dim() == 2 and p.stride(1) == 1 and p.element_size() == 1,
+                     "a device plane is a 2-D uint8 tensor with dense rows")
             ptrs.append(p.data_ptr())
             pitches.append(p.stride(0))
         else:
-            assert isinstance(p, np.ndarray) and p.dtype == np.uint8 and p.ndim == 2 and p.strides[1] == 1
+            _require(isinstance(p, np.ndarray) and p.dtype == np.uint8 and p.ndim == 2 and p.strides[1] == 1,
+                     "a host plane is a 2-D uint8 numpy array with dense rows")
             ptrs.append(p.ctypes.data)
             pitches.append(p.strides[0])
     while len(ptrs) < 3:
@@ -448,14 +458,16 @@ def reproject_to_16s(src, xmap, ymap, dst, lut=None, stream=None) -> None:
 def non_intersecting_masks(masks, out, stream=None) -> None:
     """getNonIntersectingMasks: (n, H, W) uint8 CUDA tensor -> (n, H, W) 0/255 CUDA tensor."""
     n, H, W = masks.shape
-    assert masks.is_contiguous() and out.is_contiguous() and tuple(out.shape) == (n, H, W)
+    _require(masks.is_contiguous() and out.is_contiguous() and tuple(out.shape) == (n, H, W),
+             "masks and out are contiguous (n, H, W) tensors")
     check(lib().ps_non_intersecting_masks(masks.data_ptr(), n, W, H, out.data_ptr(), _stream_handle(stream)))
 
 
 def distance_transform_l1(mask, dist, stream=None) -> None:
     """cv::distanceTransform(mask, dist, CV_DIST_L1, 3): uint8 (H, W) -> int32 (H, W) CUDA tensors."""
     H, W = mask.shape
-    assert mask.is_contiguous() and dist.is_contiguous()
+    _require(mask.is_contiguous() and dist.is_contiguous() and tuple(dist.shape) == (H, W),
+             "mask and dist are contiguous (H, W) tensors")
     check(lib().ps_distance_transform_l1(mask.data_ptr(), W, H, dist.data_ptr(), _stream_handle(stream)))
 
 
