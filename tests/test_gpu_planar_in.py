@@ -165,3 +165,29 @@ def test_render_planar_rejects_bad_inputs(cuda, rig):
     frames = [[np.zeros((h, w), np.uint8), np.zeros((h // 2, w), np.uint8)] for _ in range(odd.num_cams)]
     assert not r.render_planar(frames, np.zeros((odd.dst_size[1], odd.dst_size[0], 4), np.uint8))
     assert "even" in r.last_error
+
+
+def test_full_size_decoder_and_encoder_handoffs(cuda, oracle_lib):
+    """The bench's planar leg at full size: 6 x 1920x1080 NV12 host frames in,
+    4096x2048 NV12 host planes out, against the oracle's conversion, render
+    and conversion of the same frames; and the same frames as BGR24 host
+    images against the oracle's render of them."""
+    import os
+    torch = cuda
+    p = Prepared(S.rig("c2"))
+    W, H = p.cfg.dst_size
+    n = p.cfg.num_cams
+    planes, conv = _decoder_frames(p, 5, [P.PS_FMT_NV12] * n)
+    ref = np.zeros((H, W, 4), np.uint8)
+    ref[..., :3] = p.oracle_render(conv, p.luts, nthreads=os.cpu_count() or 4)[..., :3]
+    want = O.bgr32_to_yuv(ref, O.FMT_NV12)
+    got = [np.zeros_like(w) for w in want]
+    assert p.r.render_planar(planes, luts=p.luts, ydst=got, ydst_fmt=P.PS_FMT_NV12, check=True)
+    torch.cuda.synchronize()
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w), diff_histogram(g, w)
+    bgr24 = [np.ascontiguousarray(f[..., :3]) for f in p.frames.frame(6)]
+    ref24 = p.oracle_render([np.concatenate([f, np.zeros_like(f[..., :1])], axis=2) for f in bgr24], p.luts,
+                            nthreads=os.cpu_count() or 4)[..., :3]
+    out = p.product_render(bgr24, p.luts)[..., :3]
+    assert np.array_equal(out, ref24), diff_histogram(out, ref24)
