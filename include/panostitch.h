@@ -177,6 +177,20 @@ int ps_render_render_yuv(ps_render* r, const ps_image* src, int num_src, const u
 #define PS_SEAMS_NEAREST_AXIS 0
 #define PS_SEAMS_DISTANCE 1
 int ps_render_set_seam_rule(ps_render* r, int rule);
+/* Custom masks (CudaTilingMultibandBlendFast::blend(images, masks, blendImage),
+   source/CudaAccel/CudaMultibandBlend.cpp:825-893, as the Tasks call it per
+   frame with each camera's custom mask of the frame's interval or else its
+   unique mask, source/Task/PanoramaPreviewTask.cpp:382-400): the frames
+   rendered after this call weight the cameras by num_masks host uint8
+   masks (dst_w x dst_h, non-zero = weight 256) instead of the unique masks,
+   normalise by the weight sums whatever the coverage, and are zero outside
+   the masks' union.  The masks may overlap.  The reference rebuilds the
+   weight pyramids on every such frame; here they are rebuilt once per mask
+   set, since the masks change only between intervals.  masks = NULL (and
+   num_masks 0) returns to the unique masks.  Waits for the render's frames
+   in flight; synchronises.  Multiband blend only: a linear-blend render is
+   PS_EINVAL (the reference warns and ignores them, RicohUtil.cpp:929-930). */
+int ps_render_set_custom_masks(ps_render* r, const uint8_t* const* masks, int num_masks, void* stream);
 /* Frames in flight, 1..PS_MAX_IN_FLIGHT (default PS_MAX_IN_FLIGHT): the sets
    of per-frame state (pyramids, staging) the next prepare allocates.  Fewer
    save device memory; more let consecutive renders overlap on the GPU.
@@ -376,6 +390,10 @@ int ps_blender_prepare(ps_blender* b, const uint8_t* const* masks, const uint8_t
 int ps_blender_blend(ps_blender* b, const void* const* images, const long long* pitches, int image_format,
                      ps_image* dst, void* stream);
 int ps_blender_get_num_levels(const ps_blender* b);
+/* blend(images, masks, blendImage) (:825-893): later blends use num host
+   uint8 custom masks (width x height) as ps_render_set_custom_masks
+   describes; masks = NULL returns to the unique masks.  Synchronises. */
+int ps_blender_set_custom_masks(ps_blender* b, const uint8_t* const* masks, int num_masks, void* stream);
 
 /* ==== serving loop: live streams with continuous batching ==== */
 typedef struct ps_server ps_server;

@@ -81,6 +81,16 @@ public:
                                           correct ? getNumImages() : 0, dst, ydst, stream));
     }
 
+    // The custom masks of the frame's interval (one host uint8 dstSize mask per
+    // camera: its custom mask, or its unique mask where it has none), as the
+    // Tasks pass them to CudaTilingMultibandBlendFast::blend(images, masks,
+    // blendImage) (source/Task/PanoramaPreviewTask.cpp:382-400); an empty
+    // vector returns to the unique masks.  Call when the interval changes.
+    bool setCustomMasks(const std::vector<const uint8_t*>& masks, void* stream = nullptr)
+    {
+        return ok(ps_render_set_custom_masks(r_, masks.empty() ? nullptr : masks.data(), (int)masks.size(), stream));
+    }
+
     void clear() { ps_render_clear(r_); }
     int getNumImages() const { return ps_render_get_num_images(r_); }
     const std::string& lastError() const { return err_; }

@@ -85,6 +85,8 @@ def lib():
             L.orc_mb_prepare.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
             L.orc_mb_prepare.restype = vp
             L.orc_mb_free.argtypes = [vp]
+            L.orc_mb_set_custom_masks.argtypes = [vp, vp]
+            L.orc_mb_set_custom_masks.restype = C.c_int
             L.orc_mb_num_levels.argtypes = [vp]
             L.orc_mb_num_levels.restype = C.c_int
             L.orc_mb_full_mask.argtypes = [vp]
@@ -329,6 +331,19 @@ class Blender:
         if h:
             lib().orc_mb_free(h)
             self._h = None
+
+    def set_custom_masks(self, masks) -> None:
+        """blend(images, masks, blendImage) (CudaMultibandBlend.cpp:825-893): later blends weight the
+        cameras by these (n, H, W) masks, normalise by the weight sums and zero the pixels outside the
+        masks' union; None restores the prepared unique masks."""
+        if masks is None:
+            lib().orc_mb_set_custom_masks(self._h, None)
+        else:
+            m = np.ascontiguousarray(masks, np.uint8)
+            if m.shape != (self.n, self.H, self.W):
+                raise ValueError(f"custom masks of shape {(self.n, self.H, self.W)} expected")
+            lib().orc_mb_set_custom_masks(self._h, _ptr(m))
+        self.full_mask = bool(lib().orc_mb_full_mask(self._h))
 
     def alpha(self, cam: int, level: int) -> np.ndarray:
         w, h = self.sizes[level]

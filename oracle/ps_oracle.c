@@ -587,12 +587,55 @@ struct orc_blender {
     int ws[17], hs[17];
     size_t off[18];        /* pixel offset of each level in a packed pyramid */
     int32_t* alpha;        /* n * total : alphaPyrs (level 0 unused) */
-    int16_t* weight;       /* n * total : weightPyrs */
+    int16_t* weight;       /* n * total : weightPyrs (or the custom masks' weights) */
     int32_t* wsum;         /* total : resultWeightPyr (only if !full) */
     uint8_t* masknot;      /* W*H (only if !full) */
+    uint8_t* cov;          /* n*W*H : the prepared coverage masks */
+    uint8_t* seams;        /* n*W*H : the prepared unique masks */
 };
 
 static size_t level_total(const orc_blender* b) { return b->off[b->L + 1]; }
+
+/* Weight pyramids, weight sums and maskNot from the n weight masks `w`, with
+   `uni_src` deciding maskNot (and fullMask): the prepared unique masks over
+   the coverage (prepare, CudaMultibandBlend.cpp:586-642), or a set of custom
+   masks (blend(images, masks, blendImage), :825-893: weights from the masks,
+   the weighted normalisation whatever the coverage, maskNot from the masks'
+   union). */
+static void build_weights(orc_blender* b, const uint8_t* w, const uint8_t* uni_src, int custom)
+{
+    const int n = b->n;
+    const size_t tot = level_total(b), npx = (size_t)b->W * b->H;
+    for (int i = 0; i < n; i++) {
+        int16_t* wt = b->weight + (size_t)i * tot;
+        for (size_t p = 0; p < npx; p++) wt[p] = w[(size_t)i * npx + p] ? 256 : 0;
+        for (int j = 0; j < b->L; j++)
+            orc_pyr_down_16sc1_to_16sc1(wt + b->off[j], b->ws[j], b->hs[j], wt + b->off[j + 1], b->ws[j + 1],
+                                        b->hs[j + 1]);
+    }
+    uint8_t* uni = (uint8_t*)calloc(npx, 1);
+    size_t covered = 0;
+    for (size_t p = 0; p < npx; p++) {
+        for (int i = 0; i < n; i++)
+            if (uni_src[(size_t)i * npx + p]) { uni[p] = 1; break; }
+        covered += uni[p];
+    }
+    b->full = !custom && covered == npx;
+    free(b->wsum);
+    free(b->masknot);
+    b->wsum = NULL;
+    b->masknot = NULL;
+    if (!b->full) {
+        b->wsum = (int32_t*)calloc(tot, sizeof(int32_t));
+        for (int i = 0; i < n; i++) {
+            const int16_t* wt = b->weight + (size_t)i * tot;
+            for (size_t p = 0; p < tot; p++) b->wsum[p] += wt[p];
+        }
+        b->masknot = (uint8_t*)malloc(npx);
+        for (size_t p = 0; p < npx; p++) b->masknot[p] = uni[p] ? 0 : 255;
+    }
+    free(uni);
+}
 
 orc_blender* orc_mb_prepare(const uint8_t* masks, const uint8_t* seams, int n, int W, int H, int maxLevels,
                             int minLength)
@@ -610,44 +653,31 @@ orc_blender* orc_mb_prepare(const uint8_t* masks, const uint8_t* seams, int n, i
     size_t tot = level_total(b), npx = (size_t)W * H;
     b->alpha = (int32_t*)calloc((size_t)n * tot, sizeof(int32_t));
     b->weight = (int16_t*)calloc((size_t)n * tot, sizeof(int16_t));
+    b->cov = (uint8_t*)malloc((size_t)n * npx);
+    b->seams = (uint8_t*)malloc((size_t)n * npx);
+    memcpy(b->cov, masks, (size_t)n * npx);
+    memcpy(b->seams, seams, (size_t)n * npx);
     int16_t* tmpAlpha = (int16_t*)malloc(sizeof(int16_t) * tot);
     for (int i = 0; i < n; i++) {
         int32_t* al = b->alpha + (size_t)i * tot;
-        int16_t* wt = b->weight + (size_t)i * tot;
-        for (size_t p = 0; p < npx; p++) {
-            tmpAlpha[p] = masks[(size_t)i * npx + p] ? 256 : 0;
-            wt[p] = seams[(size_t)i * npx + p] ? 256 : 0;
-        }
+        for (size_t p = 0; p < npx; p++) tmpAlpha[p] = masks[(size_t)i * npx + p] ? 256 : 0;
         for (int j = 0; j < b->L; j++) {
             orc_pyr_down_16sc1_to_32sc1(tmpAlpha + b->off[j], b->ws[j], b->hs[j], al + b->off[j + 1],
                                         b->ws[j + 1], b->hs[j + 1]);
             /* scaledSet16SC1Mask32SC1(temp, 256, alpha) */
             for (size_t p = b->off[j + 1]; p < b->off[j + 2]; p++) tmpAlpha[p] = al[p] ? 256 : 0;
-            orc_pyr_down_16sc1_to_16sc1(wt + b->off[j], b->ws[j], b->hs[j], wt + b->off[j + 1], b->ws[j + 1],
-                                        b->hs[j + 1]);
         }
     }
     free(tmpAlpha);
-
-    uint8_t* uni = (uint8_t*)calloc(npx, 1);
-    size_t covered = 0;
-    for (size_t p = 0; p < npx; p++) {
-        for (int i = 0; i < n; i++)
-            if (masks[(size_t)i * npx + p]) { uni[p] = 1; break; }
-        covered += uni[p];
-    }
-    b->full = covered == npx;
-    if (!b->full) {
-        b->wsum = (int32_t*)calloc(tot, sizeof(int32_t));
-        for (int i = 0; i < n; i++) {
-            const int16_t* wt = b->weight + (size_t)i * tot;
-            for (size_t p = 0; p < tot; p++) b->wsum[p] += wt[p];
-        }
-        b->masknot = (uint8_t*)malloc(npx);
-        for (size_t p = 0; p < npx; p++) b->masknot[p] = uni[p] ? 0 : 255;
-    }
-    free(uni);
+    build_weights(b, seams, masks, 0);
     return b;
+}
+
+int orc_mb_set_custom_masks(orc_blender* b, const uint8_t* masks)
+{
+    if (masks) build_weights(b, masks, masks, 1);
+    else build_weights(b, b->seams, b->cov, 0);
+    return 0;
 }
 
 void orc_mb_free(orc_blender* b)
@@ -657,6 +687,8 @@ void orc_mb_free(orc_blender* b)
     free(b->weight);
     free(b->wsum);
     free(b->masknot);
+    free(b->cov);
+    free(b->seams);
     free(b);
 }
 

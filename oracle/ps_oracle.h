@@ -78,6 +78,11 @@ typedef struct orc_blender orc_blender;
 orc_blender* orc_mb_prepare(const uint8_t* masks /* n*W*H coverage */, const uint8_t* seams /* n*W*H */,
                             int n, int W, int H, int maxLevels, int minLength);
 void orc_mb_free(orc_blender* b);
+/* blend(images, masks, blendImage) (CudaMultibandBlend.cpp:825-893): later
+   blends take their weights from the n*W*H custom masks, normalise by the
+   weight sums whatever the coverage and zero the pixels outside the masks'
+   union; masks = NULL restores the prepared unique masks. */
+int orc_mb_set_custom_masks(orc_blender* b, const uint8_t* masks);
 int orc_mb_num_levels(const orc_blender* b);
 int orc_mb_full_mask(const orc_blender* b);
 /* copies of prepared pyramids for bit-exact checks */

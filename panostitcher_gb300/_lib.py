@@ -95,6 +95,8 @@ _SIGS = [
                                          C.c_int, C.c_void_p]),
     ("ps_load_photo_params", C.c_int, [C.c_char_p, C.POINTER(PhotoParam), C.c_int, C.POINTER(C.c_int)]),
     ("ps_render_set_seam_rule", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_render_set_custom_masks", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int, C.c_void_p]),
+    ("ps_blender_set_custom_masks", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int, C.c_void_p]),
     ("ps_render_set_frames_in_flight", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_get_frames_in_flight", C.c_int, [C.c_void_p]),
     ("ps_render_render_planar", C.c_int, [C.c_void_p, C.POINTER(PlanarImage), C.c_int, C.c_void_p, C.c_int,

@@ -369,6 +369,23 @@ int ps_render_set_seam_rule(ps_render* r, int rule)
     });
 }
 
+static void setCustomMasks(ps::Rig& rig, const uint8_t* const* masks, int num, void* stream)
+{
+    if (!rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+    if (masks && num != rig.numImages())
+        fail(PS_EINVAL, "%d custom masks given, %d cameras prepared", num, rig.numImages());
+    if (!masks && num != 0) fail(PS_EINVAL, "masks is NULL but num_masks = %d", num);
+    rig.setCustomMasks(masks, toStream(stream));
+}
+
+int ps_render_set_custom_masks(ps_render* r, const uint8_t* const* masks, int num_masks, void* stream)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        setCustomMasks(r->rig, masks, num_masks, stream);
+    });
+}
+
 int ps_render_set_graph(ps_render* r, int enabled)
 {
     return guarded([&] {
@@ -576,6 +593,14 @@ int ps_blender_prepare(ps_blender* b, const uint8_t* const* masks, const uint8_t
         b->plan.reset();
         b->rig.prepareFromMasks(masks, seams, num, width, height, max_levels, min_length, toStream(stream));
         b->plan.reset(new ps::Plan({&b->rig}));
+    });
+}
+
+int ps_blender_set_custom_masks(ps_blender* b, const uint8_t* const* masks, int num_masks, void* stream)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        setCustomMasks(b->rig, masks, num_masks, stream);
     });
 }
 

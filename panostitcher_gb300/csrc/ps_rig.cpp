@@ -134,7 +134,7 @@ void Rig::clear()
     seamBits_.clear();
     geom_.clear();
     n_ = W_ = H_ = L_ = full_ = srcW_ = srcH_ = 0;
-    hasMaps_ = linear_ = false;
+    hasMaps_ = linear_ = custom_ = false;
     numLinear_ = 0;
     dLinear_.reset();
     linW_.reset();
@@ -392,79 +392,41 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         PS_CUDA(cudaStreamSynchronize(st));
     }
 
-    // union coverage, per level-0 blend tile counts
-    const int bX0 = divUp(W, kBlendTW), bY0 = divUp(H, kBlendTH);
-    DevBuf tileCounts((size_t)bX0 * bY0 * sizeof(int)), total(sizeof(unsigned long long));
-    total.zero(st);
-    PS_CUDA(launchUnion(cov, n, W, H, (long long)npx, union_.as<uint8_t>(), geom_[0].pitch, kBlendTW, kBlendTH, bX0,
-                        tileCounts.as<int>(), total.as<unsigned long long>(), st));
-
-    // tile activity flags
+    // tile activity flags of the remap and the pyrDown levels
     const int rX = divUp(W, kRemapTW), rY = divUp(H, kRemapTH);
     DevBuf rflags((size_t)n * rX * rY);
     if (xmap) {
         rflags.zero(st);
         PS_CUDA(launchTileFlags8(cov, W, H, W, (long long)npx, n, kRemapTW, kRemapTH, rX, rY, rflags.as<uint8_t>(), st));
     }
-    std::vector<DevBuf> dflags(L + 1), bflags(L + 1), uflags(L + 1);
-    for (int j = 0; j <= L; j++) {
-        const LevelGeom& g = geom_[j];
-        const long long stride = (long long)g.pitch * g.h;
-        if (j > 0) {
-            const int dX = divUp(g.w, kDownTW), dY = divUp(g.h, kDownTH);
-            dflags[j].alloc((size_t)n * dX * dY);
-            dflags[j].zero(st);
-            PS_CUDA(launchTileFlags16(lv_[j].Am.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kDownTW, kDownTH, dX, dY,
-                                      dflags[j].as<uint8_t>(), st));
-        }
-        const int bX = divUp(g.w, kBlendTW), bY = divUp(g.h, kBlendTH);
-        bflags[j].alloc((size_t)n * bX * bY);
-        bflags[j].zero(st);
-        uflags[j].alloc((size_t)n * bX * bY);
-        uflags[j].zero(st);
-        PS_CUDA(launchTileNot256(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kBlendTW, kBlendTH, bX, bY,
-                                 uflags[j].as<uint8_t>(), st));
-        PS_CUDA(launchTileFlags16(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kBlendTW, kBlendTH, bX, bY,
-                                  bflags[j].as<uint8_t>(), st));
-    }
-    DevBuf counts(2 * sizeof(unsigned long long));
+    std::vector<DevBuf> dflags(L + 1);
+    DevBuf counts(sizeof(unsigned long long));
     counts.zero(st);
-    for (int j = 0; j <= L; j++) {
+    for (int j = 1; j <= L; j++) {
         const LevelGeom& g = geom_[j];
         const long long stride = (long long)g.pitch * g.h;
-        PS_CUDA(launchCountNonzero16(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n,
+        const int dX = divUp(g.w, kDownTW), dY = divUp(g.h, kDownTH);
+        dflags[j].alloc((size_t)n * dX * dY);
+        dflags[j].zero(st);
+        PS_CUDA(launchTileFlags16(lv_[j].Am.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kDownTW, kDownTH, dX, dY,
+                                  dflags[j].as<uint8_t>(), st));
+        PS_CUDA(launchCountNonzero16(lv_[j].Am.as<uint16_t>(), g.w, g.h, g.pitch, stride, n,
                                      counts.as<unsigned long long>(), st));
-        if (j > 0)
-            PS_CUDA(launchCountNonzero16(lv_[j].Am.as<uint16_t>(), g.w, g.h, g.pitch, stride, n,
-                                         counts.as<unsigned long long>() + 1, st));
     }
-    unsigned long long hc[2] = {0, 0};
-    // host copies
-    std::vector<int> hCounts((size_t)bX0 * bY0);
-    unsigned long long hTotal = 0;
+    unsigned long long hAlpha = 0;
     std::vector<uint8_t> hR(xmap ? rflags.bytes() : 0);
-    std::vector<std::vector<uint8_t>> hD(L + 1), hB(L + 1), hU(L + 1);
-    PS_CUDA(cudaMemcpyAsync(hCounts.data(), tileCounts.get(), tileCounts.bytes(), cudaMemcpyDeviceToHost, st));
-    PS_CUDA(cudaMemcpyAsync(&hTotal, total.get(), sizeof hTotal, cudaMemcpyDeviceToHost, st));
-    PS_CUDA(cudaMemcpyAsync(hc, counts.get(), sizeof hc, cudaMemcpyDeviceToHost, st));
+    std::vector<std::vector<uint8_t>> hD(L + 1);
+    PS_CUDA(cudaMemcpyAsync(&hAlpha, counts.get(), sizeof hAlpha, cudaMemcpyDeviceToHost, st));
     if (xmap) PS_CUDA(cudaMemcpyAsync(hR.data(), rflags.get(), hR.size(), cudaMemcpyDeviceToHost, st));
-    for (int j = 0; j <= L; j++) {
-        if (j > 0) {
-            hD[j].resize(dflags[j].bytes());
-            PS_CUDA(cudaMemcpyAsync(hD[j].data(), dflags[j].get(), hD[j].size(), cudaMemcpyDeviceToHost, st));
-        }
-        hB[j].resize(bflags[j].bytes());
-        PS_CUDA(cudaMemcpyAsync(hB[j].data(), bflags[j].get(), hB[j].size(), cudaMemcpyDeviceToHost, st));
-        hU[j].resize(uflags[j].bytes());
-        PS_CUDA(cudaMemcpyAsync(hU[j].data(), uflags[j].get(), hU[j].size(), cudaMemcpyDeviceToHost, st));
+    for (int j = 1; j <= L; j++) {
+        hD[j].resize(dflags[j].bytes());
+        PS_CUDA(cudaMemcpyAsync(hD[j].data(), dflags[j].get(), hD[j].size(), cudaMemcpyDeviceToHost, st));
     }
     std::vector<uint8_t> hCov(n * npx), hSeam(n * npx);
     PS_CUDA(cudaMemcpyAsync(hCov.data(), cov, n * npx, cudaMemcpyDeviceToHost, st));
     PS_CUDA(cudaMemcpyAsync(hSeam.data(), seam, n * npx, cudaMemcpyDeviceToHost, st));
     PS_CUDA(cudaStreamSynchronize(st));
-    full_ = hTotal == (unsigned long long)npx;  // CudaMultibandBlend.cpp:616-617
-    weightCount_ = (long long)hc[0];
-    alphaCount_ = (long long)hc[1];
+    alphaCount_ = (long long)hAlpha;
     covCount_ = 0;
     for (uint8_t v : hCov) covCount_ += v != 0;
     packBits(hCov, covBits_);
@@ -472,7 +434,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     hCov.clear();
     hSeam.clear();
 
-    // work items
+    // work items of the remap and the pyrDown levels
     hRemap_.clear();
     if (xmap) {
         uint32_t t = 0;
@@ -493,59 +455,18 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
                         down.push_back({(uint8_t)c, (uint8_t)j, (uint16_t)tx, (uint16_t)ty, 0});
         downCnt_[j] = (int)down.size() - downOff_[j];
     }
-    std::vector<BlendItem> blend;
-    std::vector<uint8_t> cams;
-    for (int j = 0; j <= L; j++) {
-        const LevelGeom& g = geom_[j];
-        const int bX = divUp(g.w, kBlendTW), bY = divUp(g.h, kBlendTH);
-        blendOff_[j] = (int)blend.size();
-        for (int ty = 0; ty < bY; ty++)
-            for (int tx = 0; tx < bX; tx++) {
-                std::vector<uint8_t> list;
-                for (int c = 0; c < n; c++)
-                    if (hB[j][((size_t)c * bY + ty) * bX + tx]) list.push_back((uint8_t)c);
-                uint8_t cls = 0;
-                if (j == 0) {
-                    const int tw = std::min(kBlendTW, g.w - tx * kBlendTW), th = std::min(kBlendTH, g.h - ty * kBlendTH);
-                    const int cnt = hCounts[(size_t)ty * bX0 + tx];
-                    cls = cnt == 0 ? 0 : (cnt == tw * th ? 1 : 2);
-                }
-                BlendItem it;
-                std::memset(&it, 0, sizeof it);
-                it.level = (uint8_t)j;
-                it.cls = cls;
-                it.camCnt = (uint8_t)list.size();
-                if (list.size() == 1 && !hU[j][((size_t)list[0] * bY + ty) * bX + tx]) it.flags |= kTileUniform;
-                it.tx = (uint16_t)tx;
-                it.ty = (uint16_t)ty;
-                if (list.size() <= (size_t)kInlineCams) {
-                    for (size_t q = 0; q < list.size(); q++) it.cams[q] = list[q];
-                } else {
-                    const uint32_t off = (uint32_t)cams.size();
-                    std::memcpy(it.cams, &off, sizeof off);
-                    cams.insert(cams.end(), list.begin(), list.end());
-                }
-                blend.push_back(it);
-            }
-        blendCnt_[j] = (int)blend.size() - blendOff_[j];
-    }
-    if (cams.empty()) cams.push_back(0);
     hDown_ = down;
-    hBlend_ = blend;
-    hCams_ = cams;
+    // the weights' part: union coverage, fullMask, blend items
+    buildBlendState(cov, false, st);
     // levels with few tiles (from the top down) go to the tail kernel
     tailSplit(shape_.tailMaxItems, &tailDown_, &tailBlend_);
     dRemap_.alloc(std::max<size_t>(1, hRemap_.size()) * sizeof(RemapItem));
     dDown_.alloc(std::max<size_t>(1, down.size()) * sizeof(DownItem));
-    dBlend_.alloc(std::max<size_t>(1, blend.size()) * sizeof(BlendItem));
-    dCams_.alloc(cams.size());
     if (!hRemap_.empty())
         PS_CUDA(cudaMemcpyAsync(dRemap_.get(), hRemap_.data(), hRemap_.size() * sizeof(RemapItem),
                                 cudaMemcpyHostToDevice, st));
     if (!down.empty())
         PS_CUDA(cudaMemcpyAsync(dDown_.get(), down.data(), down.size() * sizeof(DownItem), cudaMemcpyHostToDevice, st));
-    PS_CUDA(cudaMemcpyAsync(dBlend_.get(), blend.data(), blend.size() * sizeof(BlendItem), cudaMemcpyHostToDevice, st));
-    PS_CUDA(cudaMemcpyAsync(dCams_.get(), cams.data(), cams.size(), cudaMemcpyHostToDevice, st));
 
     // tile-compact maps of the covered remap tiles
     if (xmap && !hRemap_.empty()) {
@@ -590,6 +511,161 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     hDesc_ = d;
     dDesc_.alloc(sizeof(RigDev) * slots_);
     writeDescriptors(st);
+    gen_ = g_generation++;
+}
+
+static void unpackBits(const std::vector<uint8_t>& bits, size_t count, std::vector<uint8_t>& out)
+{
+    out.resize(count);
+    for (size_t i = 0; i < count; i++) out[i] = (bits[i >> 3] >> (i & 7)) & 1 ? 255 : 0;
+}
+
+// The state that follows the weights: the union mask and the fullMask flag
+// from uniSrc (n device masks: the coverage, or the custom masks, whose
+// blend always normalises by the weight sums), the level-0 tile classes,
+// the count of non-zero weights and the blend items of every level
+// (CudaMultibandBlend.cpp:606-642; with custom masks :838-860, 888-892).
+void Rig::buildBlendState(const uint8_t* uniSrc, bool custom, cudaStream_t st)
+{
+    const int n = n_, L = L_, W = W_, H = H_;
+    const size_t npx = (size_t)W * H;
+    const int bX0 = divUp(W, kBlendTW), bY0 = divUp(H, kBlendTH);
+    DevBuf tileCounts((size_t)bX0 * bY0 * sizeof(int)), total(sizeof(unsigned long long));
+    total.zero(st);
+    PS_CUDA(launchUnion(uniSrc, n, W, H, (long long)npx, union_.as<uint8_t>(), geom_[0].pitch, kBlendTW, kBlendTH, bX0,
+                        tileCounts.as<int>(), total.as<unsigned long long>(), st));
+    std::vector<DevBuf> bflags(L + 1), uflags(L + 1);
+    DevBuf counts(sizeof(unsigned long long));
+    counts.zero(st);
+    for (int j = 0; j <= L; j++) {
+        const LevelGeom& g = geom_[j];
+        const long long stride = (long long)g.pitch * g.h;
+        const int bX = divUp(g.w, kBlendTW), bY = divUp(g.h, kBlendTH);
+        bflags[j].alloc((size_t)n * bX * bY);
+        bflags[j].zero(st);
+        uflags[j].alloc((size_t)n * bX * bY);
+        uflags[j].zero(st);
+        PS_CUDA(launchTileNot256(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kBlendTW, kBlendTH, bX, bY,
+                                 uflags[j].as<uint8_t>(), st));
+        PS_CUDA(launchTileFlags16(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n, kBlendTW, kBlendTH, bX, bY,
+                                  bflags[j].as<uint8_t>(), st));
+        PS_CUDA(launchCountNonzero16(lv_[j].Wt.as<uint16_t>(), g.w, g.h, g.pitch, stride, n,
+                                     counts.as<unsigned long long>(), st));
+    }
+    std::vector<int> hCounts((size_t)bX0 * bY0);
+    unsigned long long hTotal = 0, hWeights = 0;
+    std::vector<std::vector<uint8_t>> hB(L + 1), hU(L + 1);
+    PS_CUDA(cudaMemcpyAsync(hCounts.data(), tileCounts.get(), tileCounts.bytes(), cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaMemcpyAsync(&hTotal, total.get(), sizeof hTotal, cudaMemcpyDeviceToHost, st));
+    PS_CUDA(cudaMemcpyAsync(&hWeights, counts.get(), sizeof hWeights, cudaMemcpyDeviceToHost, st));
+    for (int j = 0; j <= L; j++) {
+        hB[j].resize(bflags[j].bytes());
+        PS_CUDA(cudaMemcpyAsync(hB[j].data(), bflags[j].get(), hB[j].size(), cudaMemcpyDeviceToHost, st));
+        hU[j].resize(uflags[j].bytes());
+        PS_CUDA(cudaMemcpyAsync(hU[j].data(), uflags[j].get(), hU[j].size(), cudaMemcpyDeviceToHost, st));
+    }
+    PS_CUDA(cudaStreamSynchronize(st));
+    full_ = !custom && hTotal == (unsigned long long)npx;  // CudaMultibandBlend.cpp:616-617
+    weightCount_ = (long long)hWeights;
+
+    std::vector<BlendItem> blend;
+    std::vector<uint8_t> cams;
+    for (int j = 0; j <= L; j++) {
+        const LevelGeom& g = geom_[j];
+        const int bX = divUp(g.w, kBlendTW), bY = divUp(g.h, kBlendTH);
+        blendOff_[j] = (int)blend.size();
+        for (int ty = 0; ty < bY; ty++)
+            for (int tx = 0; tx < bX; tx++) {
+                std::vector<uint8_t> list;
+                for (int c = 0; c < n; c++)
+                    if (hB[j][((size_t)c * bY + ty) * bX + tx]) list.push_back((uint8_t)c);
+                uint8_t cls = 0;
+                if (j == 0) {
+                    const int tw = std::min(kBlendTW, g.w - tx * kBlendTW), th = std::min(kBlendTH, g.h - ty * kBlendTH);
+                    const int cnt = hCounts[(size_t)ty * bX0 + tx];
+                    cls = cnt == 0 ? 0 : (cnt == tw * th ? 1 : 2);
+                }
+                BlendItem it;
+                std::memset(&it, 0, sizeof it);
+                it.level = (uint8_t)j;
+                it.cls = cls;
+                it.camCnt = (uint8_t)list.size();
+                if (list.size() == 1 && !hU[j][((size_t)list[0] * bY + ty) * bX + tx]) it.flags |= kTileUniform;
+                it.tx = (uint16_t)tx;
+                it.ty = (uint16_t)ty;
+                if (list.size() <= (size_t)kInlineCams) {
+                    for (size_t q = 0; q < list.size(); q++) it.cams[q] = list[q];
+                } else {
+                    const uint32_t off = (uint32_t)cams.size();
+                    std::memcpy(it.cams, &off, sizeof off);
+                    cams.insert(cams.end(), list.begin(), list.end());
+                }
+                blend.push_back(it);
+            }
+        blendCnt_[j] = (int)blend.size() - blendOff_[j];
+    }
+    if (cams.empty()) cams.push_back(0);
+    hBlend_ = blend;
+    hCams_ = cams;
+    dBlend_.alloc(std::max<size_t>(1, blend.size()) * sizeof(BlendItem));
+    dCams_.alloc(cams.size());
+    PS_CUDA(cudaMemcpyAsync(dBlend_.get(), blend.data(), blend.size() * sizeof(BlendItem), cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaMemcpyAsync(dCams_.get(), cams.data(), cams.size(), cudaMemcpyHostToDevice, st));
+}
+
+void Rig::setCustomMasks(const uint8_t* const* masks, cudaStream_t st)
+{
+    if (!ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+    if (linear_) fail(PS_EINVAL, "custom masks need the multiband blend (highQualityBlend != 0)");
+    if (masks)
+        for (int i = 0; i < n_; i++)
+            if (!masks[i]) fail(PS_EINVAL, "custom mask %d is NULL", i);
+    // the descriptors and work lists change under no run
+    waitIdle();
+    const int n = n_, L = L_, W = W_, H = H_;
+    const size_t npx = (size_t)W * H;
+    // weight masks: the custom masks, or the prepared unique masks back
+    DevBuf wm(n * npx), um;
+    std::vector<uint8_t> host;
+    if (masks) {
+        for (int i = 0; i < n; i++)
+            PS_CUDA(cudaMemcpyAsync(wm.as<uint8_t>() + i * npx, masks[i], npx, cudaMemcpyHostToDevice, st));
+    } else {
+        unpackBits(seamBits_, n * npx, host);
+        PS_CUDA(cudaMemcpyAsync(wm.get(), host.data(), n * npx, cudaMemcpyHostToDevice, st));
+        PS_CUDA(cudaStreamSynchronize(st));
+        um.alloc(n * npx);
+        unpackBits(covBits_, n * npx, host);
+        PS_CUDA(cudaMemcpyAsync(um.get(), host.data(), n * npx, cudaMemcpyHostToDevice, st));
+    }
+    // weight pyramids (pyramidDown16SC1To16SC1 of the 0/256 masks, CudaMultibandBlend.cpp:845-854)
+    {
+        const size_t plane0 = (size_t)geom_[0].pitch * H;
+        // the kernel also writes an alpha level 0 from its coverage input: given the same masks and the same
+        // output, both writes store the same value
+        PS_CUDA(launchInitLevel0(wm.as<uint8_t>(), wm.as<uint8_t>(), W, H, (long long)npx, lv_[0].Wt.as<uint16_t>(),
+                                 lv_[0].Wt.as<uint16_t>(), geom_[0].pitch, (long long)plane0, n, st));
+        for (int j = 0; j < L; j++) {
+            const LevelGeom& sg = geom_[j];
+            const LevelGeom& dg = geom_[j + 1];
+            PS_CUDA(launchWeightDown(lv_[j].Wt.as<uint16_t>(), sg.w, sg.h, sg.pitch, (long long)sg.pitch * sg.h,
+                                     lv_[j + 1].Wt.as<uint16_t>(), dg.w, dg.h, dg.pitch, (long long)dg.pitch * dg.h,
+                                     n, st));
+        }
+    }
+    buildBlendState(masks ? wm.as<uint8_t>() : um.as<uint8_t>(), masks != nullptr, st);
+    custom_ = masks != nullptr;
+    tailSplit(shape_.tailMaxItems, &tailDown_, &tailBlend_);
+    hDesc_.full = full_;
+    hDesc_.camLists = dCams_.as<uint8_t>();
+    hDesc_.blendItems = dBlend_.as<BlendItem>();
+    for (int j = 0; j <= L; j++) {
+        hDesc_.blendOff[j] = blendOff_[j];
+        hDesc_.blendCnt[j] = blendCnt_[j];
+    }
+    hDesc_.tailDown = tailDown_;
+    hDesc_.tailBlend = tailBlend_;
+    writeDescriptors(st);  // synchronises
     gen_ = g_generation++;
 }
 

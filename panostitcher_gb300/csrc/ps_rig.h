@@ -33,6 +33,15 @@ public:
                           int maxLevels, int minLength, cudaStream_t st);
     // Frees the resident state after the rig's runs in flight have finished.
     void clear();
+    // CudaTilingMultibandBlendFast::blend(images, masks, blendImage)
+    // (CudaMultibandBlend.cpp:825-893): the frames that follow are weighted by
+    // n host masks (W x H, non-zero = 256) instead of the unique masks, always
+    // normalised by the weight sums, and zeroed outside the masks' union.
+    // masks = NULL restores the prepared unique masks.  Waits for the rig's
+    // runs, rebuilds the weight pyramids and blend items, starts a new
+    // generation.  Synchronises.
+    void setCustomMasks(const uint8_t* const* masks, cudaStream_t st);
+    bool customMasks() const { return custom_; }
 
     bool ready() const { return n_ > 0; }
     int numImages() const { return n_; }
@@ -150,9 +159,10 @@ private:
     void prepareLinear(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
                        int radius, cudaStream_t st);
     void writeDescriptors(cudaStream_t st);
+    void buildBlendState(const uint8_t* uniSrcDev, bool custom, cudaStream_t st);
 
     int n_ = 0, W_ = 0, H_ = 0, L_ = 0, full_ = 0, srcW_ = 0, srcH_ = 0;
-    bool hasMaps_ = false, linear_ = false;
+    bool hasMaps_ = false, linear_ = false, custom_ = false;
     int nextSlot_ = 0, lastSlot_ = 0, slots_ = kIoSlots, slotsWanted_ = kIoSlots;
     cudaEvent_t slotComputed_[kIoSlots] = {}, slotDownloaded_[kIoSlots] = {};
     int numLinear_ = 0;

@@ -98,6 +98,14 @@ def _luts_arg(luts, n):
     return a, a.size // 768, a.ctypes.data
 
 
+def _mask_ptrs(masks):
+    """Host uint8 masks -> (kept arrays, void* array, count); None -> (None, None, 0)."""
+    if masks is None:
+        return None, None, 0
+    ms = [np.ascontiguousarray(m, np.uint8) for m in masks]
+    return ms, (C.c_void_p * len(ms))(*[m.ctypes.data for m in ms]), len(ms)
+
+
 class CudaPanoramaRender2:
     """CudaPanoramaRender2 (source/Task/RicohUtil.h:193-220) over libpanostitch."""
 
@@ -159,6 +167,13 @@ class CudaPanoramaRender2:
     def set_seam_rule(self, rule: int) -> None:
         """PS_SEAMS_NEAREST_AXIS (default) or PS_SEAMS_DISTANCE (getNonIntersectingMasks); next prepare."""
         check(lib().ps_render_set_seam_rule(self._h, rule))
+
+    def set_custom_masks(self, masks=None, stream=None, check: bool = False) -> bool:
+        """Weight the following frames by one host uint8 (H, W) mask per camera, as
+        CudaTilingMultibandBlendFast::blend(images, masks, blendImage) does; None returns to the unique
+        masks."""
+        keep, ptrs, n = _mask_ptrs(masks)
+        return self._status(lib().ps_render_set_custom_masks(self._h, ptrs, n, _stream_handle(stream)), check)
 
     def render(self, src: Sequence, dst, luts=None, stream=None, check: bool = False) -> bool:
         """render(src, dst, luts): src frames -> dst canvas (both host or device)."""
@@ -430,6 +445,16 @@ class CudaTilingMultibandBlendFast:
             self.last_error = lib().ps_last_error().decode(errors="replace")
             if check_:
                 raise PsError(st, self.last_error)
+            return False
+        return True
+
+    def set_custom_masks(self, masks=None, stream=None) -> bool:
+        """blend(images, masks, blendImage): later blends weight the cameras by these host uint8 (H, W)
+        masks; None returns to the unique masks."""
+        keep, ptrs, n = _mask_ptrs(masks)
+        st = lib().ps_blender_set_custom_masks(self._h, ptrs, n, _stream_handle(stream))
+        if st != L.PS_OK:
+            self.last_error = lib().ps_last_error().decode(errors="replace")
             return False
         return True
 

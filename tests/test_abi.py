@@ -173,3 +173,15 @@ def test_intersecting_seams_rejected_before_the_gpu(built_lib):
     small[1][:, 19:] = 255
     assert not b.prepare(list(cov), list(small), 3)
     assert "intersect at (19, 0)" in b.last_error and b.num_levels == 0
+
+
+def test_custom_masks_need_a_prepared_multiband_rig(built_lib):
+    assert built_lib.ps_render_set_custom_masks(None, None, 0, None) == L.PS_EINVAL
+    assert built_lib.ps_blender_set_custom_masks(None, None, 0, None) == L.PS_EINVAL
+    r = P.CudaPanoramaRender2()
+    m = np.zeros((8, 16), np.uint8)
+    assert not r.set_custom_masks([m, m])
+    assert "prepare" in r.last_error
+    b = P.CudaTilingMultibandBlendFast()
+    assert not b.set_custom_masks(None)
+    assert "prepare" in b.last_error

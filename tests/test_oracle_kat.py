@@ -340,3 +340,55 @@ def test_yuv_round_trip_of_block_constant_colours(oracle_lib):
     for fmt in (O.FMT_YUV420P, O.FMT_NV12):
         back = O.yuv_to_bgr32(O.bgr32_to_yuv(img, fmt), fmt)
         assert np.abs(back[..., :3].astype(int) - img[..., :3]).max() <= 2
+
+
+def test_custom_masks_blend_properties(oracle_lib):
+    """blend(images, masks, blendImage) (CudaMultibandBlend.cpp:825-893) in the oracle: with partial
+    coverage, custom masks equal to the unique masks change nothing; another partition of the coverage
+    blends as a blender prepared with it as its unique masks; masks narrower than the coverage zero the
+    pixels outside their union; None restores the prepared blend; with full coverage the custom blend
+    normalises by the weight sums."""
+    rng = np.random.default_rng(2024)
+    n, H, W, levels = 3, 40, 80, 4
+    cov = np.zeros((n, H, W), np.uint8)
+    cov[0][:, :34] = 255
+    cov[1][:, 26:60] = 255
+    cov[2][:, 52:] = 255
+    cov[:, :3, :4] = 0  # an uncovered corner
+    seams = np.zeros_like(cov)
+    seams[0][:, :30] = 255
+    seams[1][:, 30:56] = 255
+    seams[2][:, 56:] = 255
+    seams &= cov
+    other = np.zeros_like(cov)
+    other[0][:, :28] = 255
+    other[1][:, 28:58] = 255
+    other[2][:, 58:] = 255
+    other &= cov
+    imgs = []
+    for i in range(n):
+        im = rng.integers(0, 256, (H, W, 4)).astype(np.int16)
+        im[..., 3] = 0
+        im[cov[i] == 0] = 0
+        imgs.append(im)
+    b = O.Blender(cov, seams, levels)
+    assert not b.full_mask
+    ref = b.blend(imgs)
+    b.set_custom_masks(seams)
+    assert np.array_equal(b.blend(imgs), ref)
+    b.set_custom_masks(other)
+    assert np.array_equal(b.blend(imgs), O.Blender(cov, other, levels).blend(imgs))
+    narrow = other.copy()
+    narrow[:, :, :5] = 0
+    b.set_custom_masks(narrow)
+    out = b.blend(imgs)
+    assert not out[:, :5].any() and out[:, 5:].any()
+    b.set_custom_masks(None)
+    assert not b.full_mask and np.array_equal(b.blend(imgs), ref)
+    full = np.full_like(cov, 255)
+    bf = O.Blender(full, seams, levels)
+    assert bf.full_mask
+    bf.set_custom_masks(seams)
+    assert not bf.full_mask
+    bf.set_custom_masks(None)
+    assert bf.full_mask
