@@ -153,9 +153,11 @@ __device__ __forceinline__ int colHigh(int x, int W) { return x < W ? x : x % W;
 __device__ __forceinline__ int rowMap(int y, int H) { return y < 0 ? rowLow(y, H) : (y >= H ? rowHigh(y, H) : y); }
 __device__ __forceinline__ int colMap(int x, int W) { return x < 0 ? colLow(x, W) : (x >= W ? colHigh(x, W) : x); }
 
-// C truncating division a / d for |a| < 2^21 and 1 <= d < 2^16 given
-// rcp = __frcp_rn(d), exact: the fp32 quotient is within 1 of the true one,
-// and one remainder check fixes it.
+// C truncating division a / d given rcp = __frcp_rn(d), exact for |a| < 2^24
+// (exact in fp32), 1 <= d < 2^16 and |a| / d < 2^21: the fp32 quotient then
+// has a relative error below 2^-22, so it is within 1 of the true one, and one
+// remainder check fixes it.  The normalisation divides weighted sums of
+// Laplacians by their weight sums: |a| <= 255 d < 2^23, quotients <= 255.
 __device__ __forceinline__ int divTrunc(int a, int d, float rcp)
 {
     const int m = abs(a);
