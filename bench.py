@@ -14,7 +14,8 @@ The same line carries:
               decoder frames in as well (1.5 bytes per source pixel);
   roofline    the dominant kernel's algorithmic GB/s against the measured
               HBM copy bandwidth (CUDA events around every launch of a
-              profiled pass over the same workload);
+              profiled pass over the same workload), and its DRAM bytes per
+              launch from the committed ncu summary of the workload;
   launch_shape  the launch shape the autotuner chose after prepare (untimed)
               and its ms per frame against the default shape's;
   linear_blend  the linear-blend render mode (highQualityBlend 0) on the same rig;
@@ -24,6 +25,7 @@ The same line carries:
   cpu_baseline  the CPU restatement of the reference path on the host cores.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+                  [--workload c2|c5] [--scale K (profiler captures)]
 
 Under torchrun each rank stitches its own replica on its own GPU (weak
 scaling, no collective on the data path); rank 0 prints one JSON line.
