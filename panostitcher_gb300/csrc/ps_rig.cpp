@@ -237,6 +237,17 @@ static void distanceSeams(const uint8_t* cov, int n, int W, int H, uint8_t* seam
 static void checkSeamsDisjoint(const uint8_t* const* seams, int n, int W, int H)
 {
     const size_t npx = (size_t)W * H;
+    // branch-free count of the seams holding each pixel (n <= 64 fits a byte)
+    std::vector<uint8_t> count(npx, 0);
+    for (int i = 0; i < n; i++) {
+        const uint8_t* s = seams[i];
+        uint8_t* c = count.data();
+        for (size_t p = 0; p < npx; p++) c[p] = (uint8_t)(c[p] + (s[p] != 0));
+    }
+    uint8_t most = 0;
+    for (size_t p = 0; p < npx; p++) most = std::max(most, count[p]);
+    if (most <= 1) return;
+    // a shared pixel: name the first one, in camera order
     std::vector<uint8_t> owner(npx, 0);  // 1 + the camera whose seam holds the pixel
     for (int i = 0; i < n; i++) {
         const uint8_t* s = seams[i];
