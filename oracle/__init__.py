@@ -9,10 +9,11 @@ The C library (``ps_oracle.c``) restates, in plain C, the reference's
 CudaAccel integer semantics (``source/CudaAccel/CudaPyramid2.cu``,
 ``source/CudaAccel/CudaMultibandBlend.cpp``), its double-precision bilinear
 remap (``source/Warp/ZReproject.cpp:101-130``) and its PanoTools geometry
-(``source/Warp/Remap.cpp``).  Parity is unpinned against the reference
-binary, which cannot be built here (OpenCV 3.0, ticpp, EasyFFmpeg, MSBuild
-and CUDA texture references are all unavailable) and which ships no golden
-vectors; known-answer tests pin the restatement's consistency.
+(``source/Warp/Remap.cpp``).  It is pinned against the reference's own
+code: ``oracle/ref.py`` builds the reference's geometry, remap, pyramid and
+YUV sources unchanged into ``oracle/_ref/`` (where the reference tree is
+present), ``tests/test_ref_pin.py`` compares the two bit for bit, and the
+fixtures of ``tests/golden/`` are that build's outputs.
 """
 from __future__ import annotations
 

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY: the checker for the CUDA product path and the
  * timed CPU baseline.  Nothing in panostitcher_gb300/ links or calls it.
- * Parity is unpinned against the reference binary (it cannot be built here);
+ * Parity is pinned against the reference's own code built in oracle/_ref/;
  * see ps_oracle.h.
  *
  * Compile with -ffp-contract=off: the double-precision remap and geometry

@@ -5,13 +5,20 @@
  * product path in panostitcher_gb300/ is compared against; the product never
  * links, loads or calls it.  It is also the timed CPU baseline of bench.py.
  *
- * Parity status: UNPINNED against the reference binary.  The reference
- * (xpngzhng/PanoStitcher) cannot be built here: it needs OpenCV 3.0 (incl.
- * cudaarithm), ticpp, EasyFFmpeg and MSBuild, and its CUDA remap uses texture
- * references removed in CUDA 12.  It ships no golden vectors and no tests
- * with assertions.  Every function below restates the cited reference code
- * line by line in its integer / double semantics; known-answer tests in
- * tests/ pin the restatement's internal consistency.
+ * Parity status: PINNED against the reference's own code.  oracle/Makefile's
+ * `ref` target compiles the reference's geometry and CPU remap
+ * (source/Warp/Remap.cpp, ZReproject.cpp), its integer pyramid kernels and
+ * wrappers (source/CudaAccel/CudaPyramid2.cu) and its YUV conversions
+ * (source/CudaAccel/ImageProc.cu) unchanged into oracle/_ref/, against a
+ * small OpenCV subset and a CPU emulation of the CUDA runtime
+ * (oracle/ref/).  Every function below restates the cited reference code in
+ * its integer / double semantics and matches that build bit for bit
+ * (tests/test_ref_pin.py), except the documented right-edge tap of the
+ * bilinear remap; the fixtures in tests/golden/ are that build's outputs.
+ * Not pinned (no reference code to build): the LUT formula (getLUT, in a
+ * file that needs the exposure solvers), the distance-transform seams
+ * (OpenCV's distanceTransform), the linear-blend weights (OpenCV's Gaussian
+ * filter) and the nearest-optical-axis seam rule (the benchmark's own rule).
  *
  * Conventions
  *   - images are tightly packed row-major; 4-channel int16/int32 images store
