@@ -5,7 +5,8 @@ Headline: stitched output Mpix/s of the plain per-frame path on the
 6-camera rig (6 x 1920x1080 rectilinear, 100 deg -> 4096x2048 equirect,
 8-level multiband blend, per-camera LUT gains), frames resident in HBM,
 issued in turn on eight streams so eight frames are in flight (the
-single-stream figure is reported beside it).
+single-stream figure is reported beside it).  A step is one frame on each
+of the eight streams: eight stitched frames.
 The same line carries:
   e2e         the same metric through the C ABI with pinned host frames in
               and the host canvas out (H2D + D2H inside the timed region),
@@ -29,6 +30,8 @@ The same line carries:
 
 Under torchrun each rank stitches its own replica on its own GPU (weak
 scaling, no collective on the data path); rank 0 prints one JSON line.
+`--gpus N` without torchrun relaunches the script under torchrun with N
+ranks; under torchrun, N must equal WORLD_SIZE.
 """
 from __future__ import annotations
 
@@ -73,6 +76,29 @@ def dist_init(world, use_cuda):
     os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
     dist.init_process_group("nccl" if use_cuda else "gloo")
     return dist
+
+
+def rank_device(local: int, use_cuda: bool) -> str:
+    """The device a replica runs on: the GPU of its local rank."""
+    return f"cuda:{local}" if use_cuda else "cpu"
+
+
+def relaunch_cmd(argv, gpus: int, port: int):
+    """torchrun command that runs this script with `gpus` ranks (one per GPU) and the same arguments."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + list(argv)
+
+
+def measure_replica(replica, args, world: int, dist=None, device=None) -> dict:
+    """The headline measurement of one rank: W untimed warm-up steps, a barrier, K timed steps, then the
+    slowest rank's time and the whole job's Mpix/s (every rank stitched K steps of its own frames)."""
+    replica.run(args.warmup)
+    barrier(dist)
+    ms = replica.run(args.steps)
+    ms_max = reduce_max(ms, dist, device)
+    barrier(dist)
+    return {"ms": ms, "ms_max": ms_max,
+            "value": aggregate_mpix(world, args.steps * replica.frames_per_step, replica.canvas_px, ms_max)}
 
 
 def reduce_max(value: float, dist=None, device=None) -> float:
@@ -222,9 +248,10 @@ def link_bound(h2d_srcs, d2h_dsts, steps, dev):
     return go(steps)
 
 
-def link_fields(e2e, secs, steps, npx):
-    """The e2e line's host-link bound: the copy-only rate of the same bytes."""
-    bound = steps * npx / secs / 1e6
+def link_fields(e2e, secs, frames, npx, frames_per_step):
+    """The e2e line's host-link bound: the copy-only rate of the same bytes (`frames` frames' worth)."""
+    bound = frames * npx / secs / 1e6
+    steps = frames / frames_per_step
     return {"value": round(bound, 3), "unit": "Mpix/s",
             "h2d_gbs": round(steps * e2e["h2d_bytes_per_step"] / secs / 1e9, 1),
             "d2h_gbs": round(steps * e2e["d2h_bytes_per_step"] / secs / 1e9, 1),
@@ -233,96 +260,123 @@ def link_fields(e2e, secs, steps, npx):
 
 
 # ----------------------------------------------------------------------------- our arm
-def run_ours(args, world, rank, local, dist):
-    import torch
-    import panostitcher_gb300 as P
-    from panostitcher_gb300 import build as B
-    from panostitcher_gb300 import synth as S
-
-    B.build()
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    cfg = workload_rig(args)
+def workload_config(args, cfg, levels, frames_per_step, l2, parallelism):
+    """The `config` of both arms' lines: the same keys, the workload named by what it is."""
     W, H = cfg.dst_size
-    npx = W * H
-    r = P.CudaPanoramaRender2()
-    t = time.perf_counter()
-    r.prepare(cfg.cams, 1, cfg.levels, cfg.src_size, cfg.dst_size, check=True)
-    prepare_s = time.perf_counter() - t
-    # launch-shape autotuning (untimed, like prepare): frames issued the way
-    # the timed loop issues them
-    tune = None
-    if not args.no_tune:
+    c = {"workload": WORKLOADS[args.workload], "canvas": [W, H], "cams": cfg.num_cams, "src": list(cfg.src_size),
+         "levels": levels, "frames_per_step": frames_per_step, "l2": l2, "parallelism": parallelism}
+    if args.scale > 1:
+        c["workload"] += f"; every size divided by {args.scale}"
+    return c
+
+
+def l2_note(pool, frame_mb):
+    return f"inputs larger than L2: {pool} distinct {frame_mb:.1f} MB frames cycled"
+
+
+class CudaReplica:
+    """One rank's render on its own GPU: the rig prepared, a pool of frames in HBM, and a timed loop that
+    issues each step's frames in turn on `inflight` streams (one frame per stream per step), so up to
+    that many frames are in flight (the render keeps eight state slots)."""
+
+    def __init__(self, args, local):
+        import torch
+        import panostitcher_gb300 as P
+        from panostitcher_gb300 import synth as S
+        torch.cuda.set_device(local)
+        self.torch = torch
+        self.dev = torch.device(rank_device(local, True))
+        self.cfg = cfg = workload_rig(args)
+        W, H = cfg.dst_size
+        self.canvas_px = W * H
+        self.args = args
+        self.r = r = P.CudaPanoramaRender2()
         t = time.perf_counter()
-        tune = r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 8))
-        tune["seconds"] = round(time.perf_counter() - t, 2)
-    fs = S.FrameSource(cfg)
-    pool_host = [fs.frame(k) for k in range(args.pool)]
-    pool_dev = [[torch.from_numpy(f).to(dev) for f in fr] for fr in pool_host]
-    luts = S.luts(cfg)
-    dst = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+        r.prepare(cfg.cams, 1, cfg.levels, cfg.src_size, cfg.dst_size, check=True)
+        self.prepare_s = time.perf_counter() - t
+        # launch-shape autotuning (untimed, like prepare): frames issued the way
+        # the timed loop issues them
+        self.tune = None
+        if not args.no_tune:
+            t = time.perf_counter()
+            self.tune = r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 8))
+            self.tune["seconds"] = round(time.perf_counter() - t, 2)
+        fs = S.FrameSource(cfg)
+        self.pool_host = [fs.frame(k) for k in range(args.pool)]
+        self.pool_dev = [[torch.from_numpy(f).to(self.dev) for f in fr] for fr in self.pool_host]
+        self.luts = S.luts(cfg)
+        self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(args.inflight)]
+        self.dsts = [torch.empty((H, W, 4), dtype=torch.uint8, device=self.dev) for _ in range(args.inflight)]
+        self.frames_per_step = args.inflight
 
-    # ---- device-resident throughput (CUDA graph per frame).  Frames go out
-    # in turn on `inflight` streams, each with its own canvas, so up to that
-    # many frames are in flight (the render keeps eight state slots).
-    streams = [torch.cuda.Stream(device=dev) for _ in range(args.inflight)]
-    dsts = [dst] + [torch.empty_like(dst) for _ in range(args.inflight - 1)]
-
-    def timed(nsteps, nstreams):
+    def frames(self, nframes, nstreams):
+        """ms of device time for `nframes` frames issued round-robin on `nstreams` streams."""
+        torch = self.torch
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ends = [torch.cuda.Event() for _ in range(nstreams)]
         torch.cuda.synchronize()
         e0.record()
-        for st in streams[:nstreams]:
+        for st in self.streams[:nstreams]:
             st.wait_event(e0)
-        for k in range(nsteps):
+        for k in range(nframes):
             q = k % nstreams
-            r.render(pool_dev[k % args.pool], dsts[q], luts, stream=streams[q], check=True)
+            self.r.render(self.pool_dev[k % self.args.pool], self.dsts[q], self.luts, stream=self.streams[q],
+                          check=True)
         cur = torch.cuda.current_stream()
         for q in range(nstreams):
-            ends[q].record(streams[q])
+            ends[q].record(self.streams[q])
             cur.wait_event(ends[q])
         e1.record()
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
-    timed(args.warmup, args.inflight)
-    barrier(dist)
+    def run(self, steps):
+        return self.frames(steps * self.frames_per_step, self.frames_per_step)
+
+
+def run_ours(args, world, rank, local, dist):
+    import torch
+    import panostitcher_gb300 as P
+    from panostitcher_gb300 import build as B
+
+    B.build()
+    rep = CudaReplica(args, local)
+    r, cfg, dev = rep.r, rep.cfg, rep.dev
+    W, H = cfg.dst_size
+    npx = W * H
+    fps = rep.frames_per_step
+    pool_host, pool_dev, luts, dst = rep.pool_host, rep.pool_dev, rep.luts, rep.dsts[0]
+    tune = rep.tune
     sampler = ClockSampler(local)
     sampler.start()
-    ms = timed(args.steps, args.inflight)
+    m = measure_replica(rep, args, world, dist, dev)
     clocks = sampler.stop()
+    ms_max = m["ms_max"]
     # one frame at a time, with the launch shape tuned for that (cached after
     # the first call), then the in-flight shape again for the legs below
-    single_steps = max(10, args.steps // 2)
+    single_frames = max(10, args.steps)
     single_shape = r.launch_shape()
     if not args.no_tune:
         single_shape = r.autotune(frames_per_trial=20, in_flight=1)["shape"]
-    timed(args.warmup, 1)
-    single_ms = timed(single_steps, 1) / single_steps
+    rep.frames(args.warmup, 1)
+    single_ms = rep.frames(single_frames, 1) / single_frames
     if not args.no_tune:
         r.autotune(frames_per_trial=20, in_flight=min(args.inflight, 8))
-    ms_max = reduce_max(ms, dist, dev)
-    barrier(dist)
-    value = aggregate_mpix(world, args.steps, npx, ms_max)
+    value = m["value"]
     out = {"metric": METRICS[args.workload], "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 5), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
            "data": f"synthetic: seeded smooth field + per-frame noise, pool of {args.pool} frames in HBM",
-           "gpu_launches": args.steps * r.launches_per_frame,
-           "frames_in_flight": args.inflight,
-           "single_stream": {"value": round(npx / single_ms / 1e3, 3), "ms_per_step": round(single_ms, 5),
-                             "launch_shape": single_shape},
+           "gpu_launches": args.steps * fps * r.launches_per_frame,
+           "frames_per_step": fps, "ms_per_frame": round(ms_max / (args.steps * fps), 5),
+           "single_stream": {"value": round(npx / single_ms / 1e3, 3), "ms_per_frame": round(single_ms, 5),
+                             "frames": single_frames, "launch_shape": single_shape},
            "clocks": clocks}
     resident = r.resident_bytes
     frame_mb = sum(f.nbytes for f in pool_host[0]) / 1e6
-    out["config"] = {"workload": WORKLOADS[args.workload], "canvas": [W, H], "cams": cfg.num_cams,
-                     "src": list(cfg.src_size), "levels": r.num_levels, "full_mask": r.full_mask,
-                     "l2": f"inputs larger than L2: {args.pool} distinct {frame_mb:.1f} MB frames cycled, "
-                           f"rig state {resident / 1e6:.0f} MB resident", "parallelism": f"replicas x{world}",
-                     "prepare_s": round(prepare_s, 3)}
-    if args.scale > 1:
-        out["config"]["workload"] += f"; every size divided by {args.scale}"
+    out["config"] = workload_config(args, cfg, r.num_levels, fps, l2_note(args.pool, frame_mb), f"replicas x{world}")
+    out["setup"] = {"prepare_s": round(rep.prepare_s, 3), "full_mask": r.full_mask,
+                    "resident_mb": round(resident / 1e6)}
     out["launch_shape"] = tune if tune is not None else {"shape": r.launch_shape(), "tuned": False}
 
     # ---- e2e: pinned host frames in, host canvas out, through the C ABI
@@ -337,21 +391,22 @@ def run_ours(args, world, rank, local, dist):
         pinned_t.append(cams_t)
     hdst, hdst_t = pinned_copy(np.zeros((H, W, 4), np.uint8))
     e2e_steps = args.e2e_steps or args.steps
-    for k in range(2):
+    e2e_frames = e2e_steps * fps  # a step is fps frames, as in the device-resident loop
+    for k in range(max(2, args.warmup)):
         r.render(pinned[k % args.pool], hdst, luts, check=True)
     torch.cuda.synchronize()
     barrier(dist)
     t = time.perf_counter()
-    for k in range(e2e_steps):
+    for k in range(e2e_frames):
         r.render(pinned[k % args.pool], hdst, luts, check=True)
     torch.cuda.synchronize()
     e2e_s = reduce_max(time.perf_counter() - t, dist, dev)
-    out["e2e"] = {"value": round(world * e2e_steps * npx / e2e_s / 1e6, 3), "unit": "Mpix/s",
-                  "h2d_bytes_per_step": int(sum(f.nbytes for f in pinned[0])),
-                  "d2h_bytes_per_step": int(hdst.nbytes), "steps": e2e_steps,
+    out["e2e"] = {"value": round(world * e2e_frames * npx / e2e_s / 1e6, 3), "unit": "Mpix/s",
+                  "h2d_bytes_per_step": int(fps * sum(f.nbytes for f in pinned[0])),
+                  "d2h_bytes_per_step": int(fps * hdst.nbytes), "steps": e2e_steps, "frames_per_step": fps,
                   "path": "ps_render_render, pinned BGR32 host frames -> pinned BGR32 host canvas"}
-    out["e2e"]["link_bound"] = link_fields(out["e2e"], link_bound(pinned_t, [hdst_t], e2e_steps, dev), e2e_steps,
-                                           npx)
+    out["e2e"]["link_bound"] = link_fields(out["e2e"], link_bound(pinned_t, [hdst_t], e2e_frames, dev), e2e_frames,
+                                           npx, fps)
 
     # ---- e2e with the encoder handoff: NV12 planes downloaded (the Task layer's render + cvt + download)
     hy, hy_t = pinned_copy(np.zeros((H, W), np.uint8))
@@ -361,17 +416,18 @@ def run_ours(args, world, rank, local, dist):
     torch.cuda.synchronize()
     barrier(dist)
     t = time.perf_counter()
-    for k in range(e2e_steps):
+    for k in range(e2e_frames):
         r.render_yuv(pinned[k % args.pool], [hy, huv], luts, P.PS_FMT_NV12, check=True)
     torch.cuda.synchronize()
     nv12_s = reduce_max(time.perf_counter() - t, dist, dev)
-    out["e2e_nv12"] = {"value": round(world * e2e_steps * npx / nv12_s / 1e6, 3), "unit": "Mpix/s",
-                       "h2d_bytes_per_step": int(sum(f.nbytes for f in pinned[0])),
-                       "d2h_bytes_per_step": int(hy.nbytes + huv.nbytes), "steps": e2e_steps,
+    out["e2e_nv12"] = {"value": round(world * e2e_frames * npx / nv12_s / 1e6, 3), "unit": "Mpix/s",
+                       "h2d_bytes_per_step": int(fps * sum(f.nbytes for f in pinned[0])),
+                       "d2h_bytes_per_step": int(fps * (hy.nbytes + huv.nbytes)), "steps": e2e_steps,
+                       "frames_per_step": fps,
                        "path": "ps_render_render_yuv, pinned BGR32 host frames -> pinned NV12 host planes "
                                "(conversion fused into the level-0 blend)"}
-    out["e2e_nv12"]["link_bound"] = link_fields(out["e2e_nv12"], link_bound(pinned_t, [hy_t, huv_t], e2e_steps, dev),
-                                                e2e_steps, npx)
+    out["e2e_nv12"]["link_bound"] = link_fields(out["e2e_nv12"], link_bound(pinned_t, [hy_t, huv_t], e2e_frames, dev),
+                                                e2e_frames, npx, fps)
 
     # ---- e2e of the whole handoff: NV12 decoder frames in, NV12 encoder planes
     # out.  The input planes are made from the BGR pool by the library's own
@@ -397,19 +453,20 @@ def run_ours(args, world, rank, local, dist):
     torch.cuda.synchronize()
     barrier(dist)
     t = time.perf_counter()
-    for k in range(e2e_steps):
+    for k in range(e2e_frames):
         r.render_planar(nv12_h[k % args.pool], luts=luts, ydst=[hy, huv], check=True)
     torch.cuda.synchronize()
     pl_s = reduce_max(time.perf_counter() - t, dist, dev)
-    out["e2e_planar"] = {"value": round(world * e2e_steps * npx / pl_s / 1e6, 3), "unit": "Mpix/s",
-                         "h2d_bytes_per_step": int(sum(x.nbytes for x in nv12_t[0])),
-                         "d2h_bytes_per_step": int(hy.nbytes + huv.nbytes), "steps": e2e_steps,
+    out["e2e_planar"] = {"value": round(world * e2e_frames * npx / pl_s / 1e6, 3), "unit": "Mpix/s",
+                         "h2d_bytes_per_step": int(fps * sum(x.nbytes for x in nv12_t[0])),
+                         "d2h_bytes_per_step": int(fps * (hy.nbytes + huv.nbytes)), "steps": e2e_steps,
+                         "frames_per_step": fps,
                          "path": "ps_render_render_planar, pinned NV12 host frames -> pinned NV12 host planes "
                                  "(decoder frames converted on the device, encoder conversion fused into the "
                                  "level-0 blend)"}
     out["e2e_planar"]["link_bound"] = link_fields(out["e2e_planar"],
                                                   link_bound([nv12_t[k] for k in range(args.pool)], [hy_t, huv_t],
-                                                             e2e_steps, dev), e2e_steps, npx)
+                                                             e2e_frames, dev), e2e_frames, npx, fps)
     # the conversion kernel alone (device planes, profiled pass)
     r.profile(True)
     for k in range(10):
@@ -462,7 +519,7 @@ def run_ours(args, world, rank, local, dist):
                        "traffic": traffic,
                        "alg_bytes_per_launch": round(kernels[dom]["alg_bytes_per_launch"]),
                        "frame_alg_bytes": round(r.algorithmic_bytes(4, 4)),
-                       "frame_alg_gbs": round(r.algorithmic_bytes(4, 4) / (ms_max / args.steps) / 1e6, 1)}
+                       "frame_alg_gbs": round(r.algorithmic_bytes(4, 4) / (ms_max / (args.steps * fps)) / 1e6, 1)}
     out["kernels"] = {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                       for k, v in kernels.items()}
     out["kernels_by_level"] = {"columns": ["level", "us_per_frame", "alg_GBps"], **by_level}
@@ -480,7 +537,9 @@ def run_ours(args, world, rank, local, dist):
     if world == 1 and not args.no_serve and args.workload == "c2":
         out["serve"] = guarded(run_serve, args, dev)
     if world == 1 and rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = guarded(cpu_baseline, r, cfg, pool_host, luts, args.cpu_seconds)
+        res = guarded(cpu_baseline, args, r, cfg, pool_host, luts)
+        out["parity"] = res.pop("parity", None) if isinstance(res, dict) else None
+        out["cpu_baseline"] = res
     return out
 
 
@@ -518,13 +577,16 @@ def run_linear(args, dev):
 
 
 def run_batched(args, dev):
-    """Four rigs of uneven size (c3a..c3d) in one launch sequence per tick."""
+    """Four rigs of uneven size (c3a..c3d) in one launch sequence per tick, against the plain per-frame path
+    on the same rigs.  Both forms run their CUDA graphs with the same number of ticks in flight: tick k goes
+    out on stream k % inflight, with its own outputs; a plain tick is one render per rig on that stream."""
     import torch
     import panostitcher_gb300 as P
     from panostitcher_gb300 import synth as S
     names = ["c3a", "c3b", "c3c", "c3d"]
     cfgs = [S.rig(n) for n in names]
-    renders, pools, luts, dsts = [], [], [], []
+    nq = args.inflight
+    renders, pools, luts = [], [], []
     for c in cfgs:
         r = P.CudaPanoramaRender2()
         r.prepare(c.cams, 1, c.levels, c.src_size, c.dst_size, check=True)
@@ -532,40 +594,53 @@ def run_batched(args, dev):
         fs = S.FrameSource(c)
         pools.append([[torch.from_numpy(f).to(dev) for f in fs.frame(k)] for k in range(2)])
         luts.append(S.luts(c))
-        dsts.append(torch.empty((c.dst_size[1], c.dst_size[0], 4), dtype=torch.uint8, device=dev))
+    dsts = [[torch.empty((c.dst_size[1], c.dst_size[0], 4), dtype=torch.uint8, device=dev) for c in cfgs]
+            for _ in range(nq)]
+    streams = [torch.cuda.Stream(device=dev) for _ in range(nq)]
     px = sum(c.canvas_pixels for c in cfgs)
-    steps = max(5, args.steps // 2)
+    steps = max(20, args.steps)
     res = {"rigs": {n: f"{c.num_cams}x{c.src_size[0]}x{c.src_size[1]} -> {c.dst_size[0]}x{c.dst_size[1]}, "
-                       f"{r.num_levels} levels" for n, c, r in zip(names, cfgs, renders)}, "steps": steps}
-    # batched: one captured graph over all four rigs
-    for k in range(3):
-        P.render_batch(renders, [p[k % 2] for p in pools], dsts, luts)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for k in range(steps):
-        P.render_batch(renders, [p[k % 2] for p in pools], dsts, luts)
-    e1.record()
-    torch.cuda.synchronize()
-    bms = e0.elapsed_time(e1)
-    # plain per-frame path on the same rigs: one render per rig per tick, individual launches
+                       f"{r.num_levels} levels" for n, c, r in zip(names, cfgs, renders)},
+           "ticks": steps, "ticks_in_flight": nq}
+
+    def timed(tick, nticks):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for st in streams:
+            st.wait_event(e0)
+        for k in range(nticks):
+            tick(k, streams[k % nq], dsts[k % nq])
+        cur = torch.cuda.current_stream()
+        for st in streams:
+            cur.wait_stream(st)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    def batched(k, st, ds):
+        P.render_batch(renders, [p[k % 2] for p in pools], ds, luts, stream=st)
+
+    def plain(k, st, ds):
+        for r, p, lt, d in zip(renders, pools, luts, ds):
+            r.render(p[k % 2], d, lt, stream=st, check=True)
+
+    timed(batched, max(nq, args.warmup))
+    bms = timed(batched, steps)
+    timed(plain, max(nq, args.warmup))
+    pms = timed(plain, steps)
+    # the plain path one tick at a time (one stream), as a per-frame caller issues it
     for r in renders:
-        r.set_graph(False)
-    for k in range(3):
-        for r, p, lt, d in zip(renders, pools, luts, dsts):
-            r.render(p[k % 2], d, lt, check=True)
-    torch.cuda.synchronize()
-    e0.record()
-    for k in range(steps):
-        for r, p, lt, d in zip(renders, pools, luts, dsts):
-            r.render(p[k % 2], d, lt, check=True)
-    e1.record()
-    torch.cuda.synchronize()
-    pms = e0.elapsed_time(e1)
+        r.set_graph(True)
+    timed(lambda k, st, ds: plain(k, streams[0], dsts[0]), 3)
+    sms = timed(lambda k, st, ds: plain(k, streams[0], dsts[0]), steps)
     res.update({"mpix_s": round(steps * px / (bms / 1e3) / 1e6, 1),
                 "plain_mpix_s": round(steps * px / (pms / 1e3) / 1e6, 1),
+                "plain_one_stream_mpix_s": round(steps * px / (sms / 1e3) / 1e6, 1),
                 "ms_per_tick": round(bms / steps, 4), "plain_ms_per_tick": round(pms / steps, 4),
-                "speedup_vs_plain": round(pms / bms, 3)})
+                "speedup_vs_plain": round(pms / bms, 3),
+                "speedup_vs_plain_one_stream": round(sms / bms, 3),
+                "plain": "graph-captured renders, one per rig, same ticks in flight"})
     return res
 
 
@@ -623,70 +698,165 @@ def run_serve(args, dev, seconds=None):
         srv.close()
 
 
-def cpu_baseline(r, cfg, pool_host, luts, seconds):
-    """The oracle (CPU restatement of the reference path) on the host cores."""
+def cpu_baseline(args, r, cfg, pool_host, luts):
+    """The oracle (CPU restatement of the reference path, pinned to the reference's own code) on the host
+    cores, and the parity of the product against it on the same frames.
+
+    The oracle does what the reference's CPU render does: it derives its maps, coverage and seams from
+    the camera parameters (getReprojectMapsAndMasks at prepare, untimed), then per frame applies the
+    LUTs, remaps and blends (timed).  Parity, from the same run:
+      - geometry: map values whose float bits differ, coverage and seam pixels that differ, between the
+        product's FP64 device geometry and the oracle's;
+      - remap: the product's remap (ps_reproject_to_16s, the arithmetic of the render's k_remap) against
+        the oracle's double-precision bilinear through the same maps, every camera of one frame: the
+        histogram of per-channel differences;
+      - output: the product's render against the oracle's render of the same frame, each from its own
+        geometry: the histogram of per-channel differences.
+    Also times the oracle on the 2-camera fisheye rig (2048x1024, 100 frames) and on the 8-camera
+    7680x3840 rig (a few frames)."""
+    import torch
     import oracle as O
-    n = cfg.num_cams
-    maps = [r.maps(i, cfg.dst_size) for i in range(n)]
-    cov = np.stack([r.coverage(i, cfg.dst_size) for i in range(n)])
-    seams = np.stack([r.seam(i, cfg.dst_size) for i in range(n)])
-    ob = O.Blender(cov, seams, cfg.levels)
+    import panostitcher_gb300 as P
+    from panostitcher_gb300 import synth as S
     threads = os.cpu_count() or 1
+    n = cfg.num_cams
+    W, H = cfg.dst_size
+    t = time.perf_counter()
+    maps = [O.reproject_map(p, cfg.src_size, cfg.dst_size, threads=threads) for p in cfg.cams]
+    cov = np.stack([m[2] for m in maps])
+    seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov, threads=threads)
+    ob = O.Blender(cov, seams, cfg.levels)
+    geometry_s = time.perf_counter() - t
+    xm, ym = [m[0] for m in maps], [m[1] for m in maps]
+
+    def hist(a, b):
+        d = a.astype(np.int32) - b.astype(np.int32)
+        v, c = np.unique(d, return_counts=True)
+        return {str(int(x)): int(y) for x, y in zip(v, c)}
+
+    # ---- parity
+    pmaps = [r.maps(i, cfg.dst_size) for i in range(n)]
+    pcov = np.stack([r.coverage(i, cfg.dst_size) for i in range(n)])
+    pseams = np.stack([r.seam(i, cfg.dst_size) for i in range(n)])
+    map_diff = 0
+    for i in range(n):
+        both = (cov[i] > 0) & (pcov[i] > 0)
+        map_diff += int((both & ((pmaps[i][0].view(np.uint32) != xm[i].view(np.uint32)) |
+                                 (pmaps[i][1].view(np.uint32) != ym[i].view(np.uint32)))).sum())
+    frame = pool_host[0]
+    remap_hist = {}
+    for i in range(n):
+        dev_out = torch.empty((H, W, 4), dtype=torch.int16, device="cuda")
+        P.reproject_to_16s(torch.from_numpy(frame[i]).cuda(), torch.from_numpy(pmaps[i][0]).cuda(),
+                           torch.from_numpy(pmaps[i][1]).cuda(), dev_out,
+                           torch.from_numpy(np.ascontiguousarray(luts[i].reshape(-1))).cuda())
+        ref = O.reproject_16s(frame[i], pmaps[i][0], pmaps[i][1], luts[i])
+        got = dev_out.cpu().numpy()
+        for k, v in hist(got[..., :3][pcov[i] > 0], ref[..., :3][pcov[i] > 0]).items():
+            remap_hist[k] = remap_hist.get(k, 0) + v
+    got = np.zeros((H, W, 4), np.uint8)
+    r.render(frame, got, luts, check=True)
+    torch.cuda.synchronize()
+    ref = ob.render(frame, luts, xm, ym, threads)
+    parity = {"rig": WORKLOADS[args.workload],
+              "geometry": {"map_values_differing": map_diff,
+                           "coverage_px_differing": int(((cov > 0) != (pcov > 0)).sum()),
+                           "seam_px_differing": int(((seams > 0) != (pseams > 0)).sum()),
+                           "covered_px": int((cov > 0).sum())},
+              "remap_delta_histogram": remap_hist,
+              "output_delta_histogram": hist(got[..., :3], ref[..., :3]),
+              "bar": "remap within +-1 LSB of the double-precision bilinear; output bit-exact given the same "
+                     "geometry (tests/test_gpu_e2e_parity.py bounds the rest)",
+              "oracle": "C restatement pinned bit for bit to the reference's Remap.cpp, ZReproject.cpp, "
+                        "CudaPyramid2.cu (built here from the reference tree; tests/test_ref_pin.py)"}
+
+    # ---- timing
     frames = 0
     t = time.perf_counter()
     while True:
-        ob.render(pool_host[frames % len(pool_host)], luts, [m[0] for m in maps], [m[1] for m in maps], threads)
+        ob.render(pool_host[frames % len(pool_host)], luts, xm, ym, threads)
         frames += 1
         el = time.perf_counter() - t
-        if el >= seconds:
+        if el >= args.cpu_seconds:
             break
-    W, H = cfg.dst_size
-    return {"value": round(frames * W * H / el / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
-            "sample": f"{frames} full frames of the {cfg.num_cams}-camera {W}x{H} rig (LUT + bilinear remap + "
-                      f"multiband blend) in {el:.1f} s"}
+    res = {"value": round(frames * W * H / el / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
+           "sample": f"{frames} full frames of the {cfg.num_cams}-camera {W}x{H} rig (LUT + bilinear remap + "
+                     f"multiband blend) in {el:.1f} s; geometry from the camera parameters {geometry_s:.1f} s "
+                     f"before, untimed",
+           "parity": parity}
+    if args.scale == 1 and not args.no_cpu_rigs:
+        res["other_rigs"] = {"c1": cpu_rig_timing("c1", 100, threads), "c5": cpu_rig_timing("c5", 8, threads)}
+    return res
 
 
-# ----------------------------------------------------------------------------- reference arm
-def run_reference(args, world, rank):
-    """The reference path's CPU implementation (the oracle port) on the host cores."""
+def cpu_rig_timing(name, nframes, threads):
+    """The oracle's LUT + remap + blend on another benchmark rig: nframes frames on the host cores."""
     import oracle as O
     from panostitcher_gb300 import synth as S
-    O.build()
-    cfg = S.rig("c2")
+    cfg = S.rig(name)
     W, H = cfg.dst_size
-    n = cfg.num_cams
-    threads = os.cpu_count() or 1
-    from concurrent.futures import ThreadPoolExecutor
-    with ThreadPoolExecutor(max_workers=min(n, threads)) as ex:
-        maps = list(ex.map(lambda p: O.reproject_map(p, cfg.src_size, cfg.dst_size), cfg.cams))
+    maps = [O.reproject_map(p, cfg.src_size, cfg.dst_size, threads=threads) for p in cfg.cams]
     cov = np.stack([m[2] for m in maps])
-    seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov)
+    seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov, threads=threads)
     ob = O.Blender(cov, seams, cfg.levels)
     fs = S.FrameSource(cfg)
     pool = [fs.frame(k) for k in range(2)]
     luts = S.luts(cfg)
-    run = lambda k: ob.render(pool[k % 2], luts, [m[0] for m in maps], [m[1] for m in maps], threads)
-    budget = args.ref_seconds
+    ob.render(pool[0], luts, [m[0] for m in maps], [m[1] for m in maps], threads)
     t = time.perf_counter()
-    run(0)
+    for k in range(nframes):
+        ob.render(pool[k % 2], luts, [m[0] for m in maps], [m[1] for m in maps], threads)
+    el = time.perf_counter() - t
+    return {"value": round(nframes * W * H / el / 1e6, 4), "unit": "Mpix/s", "frames": nframes,
+            "ms_per_frame": round(el / nframes * 1e3, 2), "cores": threads,
+            "rig": f"{cfg.num_cams}x{cfg.src_size[0]}x{cfg.src_size[1]} -> {W}x{H}, {ob.levels} levels"}
+
+
+# ----------------------------------------------------------------------------- reference arm
+def run_reference(args, world, rank):
+    """The reference path's CPU implementation (the oracle port, pinned bit for bit to the reference's own
+    geometry and pyramid code) on all host cores: per step, the same frames_per_step frames of the same
+    workload as our arm; the number of timed steps is bounded by --ref-seconds."""
+    import oracle as O
+    from panostitcher_gb300 import synth as S
+    O.build()
+    cfg = workload_rig(args)
+    W, H = cfg.dst_size
+    threads = os.cpu_count() or 1
+    fps = args.inflight
+    maps = [O.reproject_map(p, cfg.src_size, cfg.dst_size, threads=threads) for p in cfg.cams]
+    cov = np.stack([m[2] for m in maps])
+    seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov, threads=threads)
+    ob = O.Blender(cov, seams, cfg.levels)
+    fs = S.FrameSource(cfg)
+    pool = [fs.frame(k) for k in range(args.pool)]
+    luts = S.luts(cfg)
+    xm, ym = [m[0] for m in maps], [m[1] for m in maps]
+
+    def step(k):
+        for f in range(fps):
+            ob.render(pool[(k * fps + f) % args.pool], luts, xm, ym, threads)
+
+    t = time.perf_counter()
+    step(0)
     one = time.perf_counter() - t
     warm = min(args.warmup, 1)
     for k in range(warm - 1):
-        run(k)
-    steps = max(1, min(args.steps, int(budget / max(one, 1e-3))))
+        step(k)
+    steps = max(1, min(args.steps, int(args.ref_seconds / max(one, 1e-3))))
     t = time.perf_counter()
     for k in range(steps):
-        run(k)
+        step(k)
     el = time.perf_counter() - t
-    value = steps * W * H / el / 1e6
-    sample = f"{steps} of {args.steps} steps (full 6-camera 4096x2048 frames, {threads} threads), " \
-             f"{warm} warm-up"
-    return {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mpix/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / steps * 1e3, 3),
+    value = steps * fps * W * H / el / 1e6
+    frame_mb = sum(f.nbytes for f in pool[0]) / 1e6
+    sample = f"{steps} of {args.steps} steps ({fps} full {cfg.num_cams}-camera {W}x{H} frames each, LUT + " \
+             f"bilinear remap + multiband blend, {threads} threads), {warm} warm-up"
+    return {"impl": "reference", "metric": METRICS[args.workload], "value": round(value, 4), "unit": "Mpix/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
             "data": "synthetic: seeded smooth field + per-frame noise",
-            "config": {"workload": WORKLOAD, "canvas": [W, H], "cams": n, "levels": ob.levels,
-                       "parallelism": "host threads"},
+            "config": workload_config(args, cfg, ob.levels, fps, l2_note(args.pool, frame_mb), f"replicas x{world}"),
             "cpu_baseline": {"value": round(value, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0,
@@ -713,9 +883,21 @@ def main(argv=None):
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu-rigs", action="store_true", help="skip the CPU timings of the c1 and c5 rigs")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        # one rank per GPU: run this script under torchrun with the same arguments
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        return subprocess.call(relaunch_cmd(sys.argv[1:] if argv is None else argv, args.gpus, port))
+    if world != args.gpus:
+        print(json.dumps({"error": f"--gpus {args.gpus} but WORLD_SIZE {world}: launch one rank per GPU"}),
+              flush=True)
+        return 2
     if args.impl == "reference":
         if rank != 0:
             return 0

@@ -196,6 +196,18 @@ int ps_render_set_custom_masks(ps_render* r, const uint8_t* const* masks, int nu
    save device memory; more let consecutive renders overlap on the GPU.
    No reference counterpart (the reference renders one frame at a time). */
 int ps_render_set_frames_in_flight(ps_render* r, int n);
+/* The reference's prepare estimates the device memory of its stream-based
+   render and, when the free memory exceeds it by less than 500 MB, renders
+   one camera at a time instead (source/Task/RicohUtil.cpp:1135-1170,
+   1315-1329).  Here the per-frame state is per frame in flight, so the
+   multiband prepare takes as many frames in flight (of those asked for) as
+   fit the free memory with that 500 MB margin, down to one, and reports the
+   fallback through ps_render_is_low_memory.  ps_render_set_memory_budget
+   caps that room further for the next prepare (bytes; 0 = free memory
+   only); ps_render_get_frames_in_flight gives the count taken.  Every count
+   stitches the same bytes. */
+int ps_render_set_memory_budget(ps_render* r, long long bytes);
+int ps_render_is_low_memory(const ps_render* r);
 /* The prepared render's frames in flight (0 before prepare). */
 int ps_render_get_frames_in_flight(const ps_render* r);
 /* CudaPanoramaRender2::render with decoder frames: src holds num_src YUV420P
@@ -214,6 +226,35 @@ int ps_render_render_planar(ps_render* r, const ps_planar_image* src, int num_sr
 /* Launch the per-frame kernels as one captured CUDA graph (default 1) or as
    individual launches (0).  No reference counterpart. */
 int ps_render_set_graph(ps_render* r, int enabled);
+
+/* The render's seam (unique) masks into num host buffers of dst_w * dst_h
+   bytes (0 / 255): what the reference's render keeps as dstUniqueMasksGPU
+   and its Tasks take from the blender's getUniqueMasks
+   (source/CudaAccel/CudaMultibandBlend.cpp:895-901). */
+int ps_render_get_unique_masks(const ps_render* r, uint8_t* const* masks, int num);
+/* The device bytes a render of this rig would hold with frames_in_flight
+   state slots (1..8), an upper bound that assumes every camera covers the
+   whole canvas; no allocation.  The reference's prepare makes the same kind
+   of estimate against the free device memory to choose its low-memory path
+   (source/Task/RicohUtil.cpp:1135-1170); ps_render_prepare makes it too
+   (see ps_render_set_frames_in_flight).  -1 on bad arguments. */
+long long ps_render_estimate_memory(const ps_photo_param* params, int num_params, int blend_param, int src_w,
+                                    int src_h, int dst_w, int dst_h, int frames_in_flight);
+
+/* Failure status of the render's kernels.  No reference counterpart (the
+   reference's kernels have no waits that can run out).  Every wait of the
+   blend kernels on the bulk-copy ring is bounded; one that runs out sets a
+   status bit on every frame of its launch and the kernel carries on, so the
+   device stays usable.  ps_render_check waits for the render's frames in
+   flight, reads and clears that status, and returns PS_ETIMEOUT if a wait ran
+   out since the last check (those frames may be wrong), else PS_OK. */
+int ps_render_check(ps_render* r);
+/* Failure-path test hook, no reference counterpart: with polls > 0 every
+   blend launch of this render makes one wait of that many polls on a
+   barrier that nothing completes, so that wait runs out and
+   ps_render_check reports PS_ETIMEOUT.  0 (default) turns it off.  Waits
+   for the frames in flight; the next render re-records its launches. */
+int ps_render_set_wait_probe(ps_render* r, int polls);
 
 /* CudaPanoramaRender2::clear / getNumImages (source/Task/RicohUtil.cpp:1341-1361).
    clear, like a new prepare, waits for the render's frames in flight before
@@ -364,10 +405,13 @@ int ps_cvt_yuv_to_bgr32(const ps_planar_image* src, const ps_image* dst, void* s
    scratch (parameters and coverage masks) lives in one fixed 16 MiB device
    array inside the library, held on every GPU that loads it until the
    process exits; num_params * dst_w * dst_h must not exceed
-   16 MiB - 64 KiB, else PS_EINVAL.  The first call on a device looks up the
-   array's address on that device, so make it before any stream capture.
-   All calls on a device share the array: calls whose work overlaps on the
-   GPU race.  Every scratch byte a call reads it has written itself. */
+   16 MiB - 64 KiB, and dst_h must not exceed 65535, else PS_EINVAL.  The
+   camera parameters reach the device as a kernel argument, so nothing of
+   the caller's host memory is read after the call returns.  The first call
+   on a device looks up the array's address on that device, so make it
+   before any stream capture.  All calls on a device share the array: calls
+   whose work overlaps on the GPU race.  Every scratch byte a call reads it
+   has written itself. */
 int ps_nearest_axis_seams_no_alloc(const ps_photo_param* params, int num_params, int src_w, int src_h, int dst_w,
                                    int dst_h, uint8_t* seams, void* stream);
 
@@ -390,6 +434,33 @@ int ps_blender_prepare(ps_blender* b, const uint8_t* const* masks, const uint8_t
 int ps_blender_blend(ps_blender* b, const void* const* images, const long long* pitches, int image_format,
                      ps_image* dst, void* stream);
 int ps_blender_get_num_levels(const ps_blender* b);
+/* CudaTilingMultibandBlendFast::begin / tile / end (source/CudaAccel/
+   CudaInterface.h:51-53, CudaMultibandBlend.cpp:737-783): the blend fed one
+   camera at a time, as the reference's render does when device memory is
+   short (source/Task/RicohUtil.cpp:1315-1329).  begin starts a blend; tile
+   takes camera `index`'s level-0 image (device int16 x4 or BGR32 uint8, as
+   ps_blender_blend; checked the same way, so it synchronises) and is done
+   with it when it returns, so one caller buffer can serve every camera; end
+   blends into dst (device, BGR32 or BGR24).  begin + a tile of every camera
+   + end gives exactly the bytes of ps_blender_blend.  A camera not tiled
+   contributes nothing while its weights still count in the normalisation,
+   as in the reference.  Stricter than the reference: a camera tiled twice
+   since begin, tile or end without begin, and another blend between begin
+   and end are errors (PS_EINVAL / PS_ESTATE). */
+int ps_blender_begin(ps_blender* b, void* stream);
+int ps_blender_tile(ps_blender* b, const void* image, long long pitch, int image_format, int index, void* stream);
+int ps_blender_end(ps_blender* b, ps_image* dst, void* stream);
+/* getUniqueMasks (CudaMultibandBlend.cpp:895-901): the seam (unique) masks,
+   into num host buffers of width * height bytes (0 / 255). */
+int ps_blender_get_unique_masks(const ps_blender* b, uint8_t* const* masks, int num);
+/* calcUsedMemorySize (:903-920): device bytes the blender holds. */
+long long ps_blender_used_memory(const ps_blender* b);
+/* estimateMemorySize (:922-926): device bytes a blender of this size would
+   hold at most, whatever the masks (no allocation); -1 on bad arguments. */
+long long ps_blender_estimate_memory(int width, int height, int num_images, int max_levels);
+/* As ps_render_check / ps_render_set_wait_probe, for the blender's blends. */
+int ps_blender_check(ps_blender* b);
+int ps_blender_set_wait_probe(ps_blender* b, int polls);
 /* blend(images, masks, blendImage) (:825-893): later blends use num host
    uint8 custom masks (width x height) as ps_render_set_custom_masks
    describes; masks = NULL returns to the unique masks.  Synchronises. */

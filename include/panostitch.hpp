@@ -210,6 +210,25 @@ public:
     {
         return ok(ps_blender_blend(b_, images.data(), pitches.data(), format, &dst, stream));
     }
+    // begin / tile(image, index) / end(blendImage) (CudaMultibandBlend.cpp:737-783):
+    // the blend fed one camera at a time
+    bool begin(void* stream = nullptr) { return ok(ps_blender_begin(b_, stream)); }
+    bool tile(const void* image, long long pitch, int format, int index, void* stream = nullptr)
+    {
+        return ok(ps_blender_tile(b_, image, pitch, format, index, stream));
+    }
+    bool end(ps_image& dst, void* stream = nullptr) { return ok(ps_blender_end(b_, &dst, stream)); }
+    // getUniqueMasks (:895-901): into host buffers of width * height bytes
+    bool getUniqueMasks(const std::vector<uint8_t*>& masks)
+    {
+        return ok(ps_blender_get_unique_masks(b_, masks.data(), (int)masks.size()));
+    }
+    // calcUsedMemorySize (:903-920) and estimateMemorySize (:922-926)
+    long long calcUsedMemorySize() const { return ps_blender_used_memory(b_); }
+    static long long estimateMemorySize(int width, int height, int numImages, int maxLevels = 16)
+    {
+        return ps_blender_estimate_memory(width, height, numImages, maxLevels);
+    }
     int numLevels() const { return ps_blender_get_num_levels(b_); }
     const std::string& lastError() const { return err_; }
 

@@ -74,6 +74,10 @@ def lib():
             vp = C.c_void_p
             L.orc_reproject_map.argtypes = [P(OrcParam), C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp]
             L.orc_nearest_axis_seams.argtypes = [P(OrcParam), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]
+            L.orc_reproject_map_rows.argtypes = [P(OrcParam), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                 vp, vp, vp, vp]
+            L.orc_nearest_axis_seams_rows.argtypes = [P(OrcParam), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                      C.c_int, C.c_int, vp, vp]
             L.orc_get_lut.argtypes = [C.c_double, vp]
             L.orc_reproject_bilinear_16s.argtypes = [vp, C.c_int, C.c_int, C.c_longlong, C.c_int, vp, vp, vp,
                                                      C.c_int, C.c_int, vp]
@@ -120,8 +124,23 @@ def _ptr_array(arrs):
 
 
 # ---------------------------------------------------------------- geometry
-def reproject_map(param: dict, cam_size, canvas_size, with_double: bool = False):
-    """getReprojectMap32FAndMask: float x/y maps (-1 sentinel) and 0/255 mask."""
+def _row_bands(H: int, threads: int):
+    k = max(1, min(threads, H))
+    return [(H * i // k, H * (i + 1) // k) for i in range(k)]
+
+
+def _run_bands(fn, H: int, threads: int):
+    bands = _row_bands(H, threads)
+    if len(bands) == 1:
+        fn(*bands[0])
+        return
+    from concurrent.futures import ThreadPoolExecutor  # ctypes calls release the GIL
+    with ThreadPoolExecutor(max_workers=len(bands)) as ex:
+        list(ex.map(lambda b: fn(*b), bands))
+
+
+def reproject_map(param: dict, cam_size, canvas_size, with_double: bool = False, threads: int = 1):
+    """getReprojectMap32FAndMask: float x/y maps (-1 sentinel) and 0/255 mask (row bands on `threads`)."""
     cw, ch = cam_size
     W, H = canvas_size
     xm = np.empty((H, W), np.float32)
@@ -129,18 +148,22 @@ def reproject_map(param: dict, cam_size, canvas_size, with_double: bool = False)
     mk = np.empty((H, W), np.uint8)
     m64 = np.empty((H, W, 2), np.float64) if with_double else None
     p = make_param(param)
-    lib().orc_reproject_map(C.byref(p), cw, ch, W, H, _ptr(m64) if with_double else None,
-                            _ptr(xm), _ptr(ym), _ptr(mk))
+    L = lib()
+    _run_bands(lambda r0, r1: L.orc_reproject_map_rows(C.byref(p), cw, ch, W, H, r0, r1,
+                                                       _ptr(m64) if with_double else None, _ptr(xm), _ptr(ym),
+                                                       _ptr(mk)), H, threads)
     return (xm, ym, mk, m64) if with_double else (xm, ym, mk)
 
 
-def nearest_axis_seams(params, cam_size, canvas_size, coverage: np.ndarray) -> np.ndarray:
+def nearest_axis_seams(params, cam_size, canvas_size, coverage: np.ndarray, threads: int = 1) -> np.ndarray:
     n = len(params)
     W, H = canvas_size
     arr = (OrcParam * n)(*[make_param(p) for p in params])
     cov = np.ascontiguousarray(coverage, dtype=np.uint8)
     seams = np.empty((n, H, W), np.uint8)
-    lib().orc_nearest_axis_seams(arr, n, cam_size[0], cam_size[1], W, H, _ptr(cov), _ptr(seams))
+    L = lib()
+    _run_bands(lambda r0, r1: L.orc_nearest_axis_seams_rows(arr, n, cam_size[0], cam_size[1], W, H, r0, r1,
+                                                            _ptr(cov), _ptr(seams)), H, threads)
     return seams
 
 

@@ -254,6 +254,12 @@ double orc_remap_axis_angle(const orc_remap* m, double cx, double cy)
 void orc_reproject_map(const orc_param* p, int camW, int camH, int canvasW, int canvasH,
                        double* map64, float* xmap, float* ymap, uint8_t* mask)
 {
+    orc_reproject_map_rows(p, camW, camH, canvasW, canvasH, 0, canvasH, map64, xmap, ymap, mask);
+}
+
+void orc_reproject_map_rows(const orc_param* p, int camW, int camH, int canvasW, int canvasH, int row0, int row1,
+                            double* map64, float* xmap, float* ymap, uint8_t* mask)
+{
     orc_remap m;
     orc_remap_init(p, canvasW, canvasH, camW, camH, &m);
     int circ = p->imageType == 2 || p->imageType == 3;
@@ -270,7 +276,7 @@ void orc_reproject_map(const orc_param* p, int camW, int camH, int canvasW, int 
                                                    : p->cropHeight * p->cropHeight * 0.25;
         }
     }
-    for (int h = 0; h < canvasH; h++) {
+    for (int h = row0; h < row1; h++) {
         for (int w = 0; w < canvasW; w++) {
             double sx, sy;
             orc_remap_point(&m, w, h, &sx, &sy);
@@ -300,11 +306,18 @@ void orc_reproject_map(const orc_param* p, int camW, int camH, int canvasW, int 
 void orc_nearest_axis_seams(const orc_param* params, int n, int camW, int camH, int canvasW, int canvasH,
                             const uint8_t* coverage, uint8_t* seams)
 {
+    orc_nearest_axis_seams_rows(params, n, camW, camH, canvasW, canvasH, 0, canvasH, coverage, seams);
+}
+
+void orc_nearest_axis_seams_rows(const orc_param* params, int n, int camW, int camH, int canvasW, int canvasH,
+                                 int row0, int row1, const uint8_t* coverage, uint8_t* seams)
+{
     size_t npx = (size_t)canvasW * canvasH;
     orc_remap* ms = (orc_remap*)malloc(sizeof(orc_remap) * (size_t)n);
     for (int i = 0; i < n; i++) orc_remap_init(&params[i], canvasW, canvasH, camW, camH, &ms[i]);
-    memset(seams, 0, npx * (size_t)n);
-    for (int h = 0; h < canvasH; h++) {
+    for (int i = 0; i < n; i++)
+        memset(seams + (size_t)i * npx + (size_t)row0 * canvasW, 0, (size_t)(row1 - row0) * canvasW);
+    for (int h = row0; h < row1; h++) {
         for (int w = 0; w < canvasW; w++) {
             size_t idx = (size_t)h * canvasW + w;
             int best = -1;

@@ -59,6 +59,12 @@ void orc_reproject_map(const orc_param* p, int camW, int camH, int canvasW, int 
                        double* map64 /* nullable, 2 per px */, float* xmap, float* ymap, uint8_t* mask);
 void orc_nearest_axis_seams(const orc_param* params, int n, int camW, int camH, int canvasW, int canvasH,
                             const uint8_t* coverage /* n*W*H */, uint8_t* seams /* n*W*H */);
+/* the same two on canvas rows [row0, row1) only (full-canvas buffers), so
+   that callers can split a canvas across threads */
+void orc_reproject_map_rows(const orc_param* p, int camW, int camH, int canvasW, int canvasH, int row0, int row1,
+                            double* map64, float* xmap, float* ymap, uint8_t* mask);
+void orc_nearest_axis_seams_rows(const orc_param* params, int n, int camW, int camH, int canvasW, int canvasH,
+                                 int row0, int row1, const uint8_t* coverage, uint8_t* seams);
 void orc_get_lut(double k, uint8_t lut[256]);
 
 /* ---- remap ------------------------------------------------------------- */

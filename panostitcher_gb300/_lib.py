@@ -99,9 +99,24 @@ _SIGS = [
     ("ps_blender_set_custom_masks", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int, C.c_void_p]),
     ("ps_render_set_frames_in_flight", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_get_frames_in_flight", C.c_int, [C.c_void_p]),
+    ("ps_render_set_memory_budget", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("ps_render_is_low_memory", C.c_int, [C.c_void_p]),
     ("ps_render_render_planar", C.c_int, [C.c_void_p, C.POINTER(PlanarImage), C.c_int, C.c_void_p, C.c_int,
                                           C.POINTER(Image), C.POINTER(PlanarImage), C.c_void_p]),
     ("ps_render_set_graph", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_render_check", C.c_int, [C.c_void_p]),
+    ("ps_render_set_wait_probe", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_blender_check", C.c_int, [C.c_void_p]),
+    ("ps_blender_begin", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("ps_blender_tile", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_int, C.c_void_p]),
+    ("ps_blender_end", C.c_int, [C.c_void_p, C.POINTER(Image), C.c_void_p]),
+    ("ps_blender_get_unique_masks", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int]),
+    ("ps_blender_used_memory", C.c_longlong, [C.c_void_p]),
+    ("ps_blender_estimate_memory", C.c_longlong, [C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("ps_render_get_unique_masks", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int]),
+    ("ps_render_estimate_memory", C.c_longlong, [C.POINTER(PhotoParam), C.c_int, C.c_int, C.c_int, C.c_int,
+                                                 C.c_int, C.c_int, C.c_int]),
+    ("ps_blender_set_wait_probe", C.c_int, [C.c_void_p, C.c_int]),
     ("ps_render_clear", None, [C.c_void_p]),
     ("ps_render_get_num_images", C.c_int, [C.c_void_p]),
     ("ps_render_get_num_levels", C.c_int, [C.c_void_p]),

@@ -61,8 +61,6 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         if force or _stale(obj, [path] + hdrs):
             cmd = [cc] + COMMON + extra + (["-Xptxas", "-v"] if ptxas_info and src.endswith(".cu") else []) + \
                   ["-c", path, "-o", obj]
-            if src.endswith(".cpp"):
-                cmd[1:1] = ["-x", "cu"] if False else []
             jobs.append(cmd)
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

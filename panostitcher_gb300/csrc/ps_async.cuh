@@ -48,9 +48,9 @@ __device__ __forceinline__ bool mbarTryWait(uint64_t* bar, uint32_t parity)
 }
 
 // Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity, long long maxPolls = kMaxPolls)
 {
-    for (long long i = 0; i < kMaxPolls; i++)
+    for (long long i = 0; i < maxPolls; i++)
         if (mbarTryWait(bar, parity)) return true;
     return false;
 }

@@ -22,6 +22,11 @@ struct ps_render {
 struct ps_blender {
     ps::Rig rig;
     std::unique_ptr<ps::Plan> plan;
+    // begin / tile / end in progress: the state slot the tiles go to and the
+    // cameras tiled so far
+    bool tiling = false;
+    int tileSlot = 0;
+    uint64_t tiled = 0;
 };
 
 namespace {
@@ -332,6 +337,17 @@ int ps_render_set_frames_in_flight(ps_render* r, int n)
 
 int ps_render_get_frames_in_flight(const ps_render* r) { return r && r->rig.ready() ? r->rig.slots() : 0; }
 
+int ps_render_set_memory_budget(ps_render* r, long long bytes)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (bytes < 0) fail(PS_EINVAL, "budget %lld is negative", bytes);
+        r->rig.setMemoryBudget(bytes);
+    });
+}
+
+int ps_render_is_low_memory(const ps_render* r) { return r && r->rig.ready() && r->rig.lowMemory() ? 1 : 0; }
+
 int ps_render_render_planar(ps_render* r, const ps_planar_image* src, int num_src, const uint8_t* luts,
                             int num_luts, const ps_image* dst, const ps_planar_image* ydst, void* stream)
 {
@@ -391,6 +407,54 @@ int ps_render_set_graph(ps_render* r, int enabled)
     return guarded([&] {
         if (!r) fail(PS_EINVAL, "render is NULL");
         r->useGraph = enabled != 0;
+    });
+}
+
+int ps_render_get_unique_masks(const ps_render* r, uint8_t* const* masks, int num)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (!r->rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        if (!masks || num != r->rig.numImages())
+            fail(PS_EINVAL, "%d mask buffers given, %d cameras prepared", num, r->rig.numImages());
+        const long long bytes = (long long)r->rig.width() * r->rig.height();
+        for (int i = 0; i < num; i++) {
+            if (!masks[i]) fail(PS_EINVAL, "mask buffer %d is NULL", i);
+            r->rig.exportState(3, i, 0, masks[i], bytes);
+        }
+    });
+}
+
+long long ps_render_estimate_memory(const ps_photo_param* params, int num_params, int blend_param, int src_w,
+                                    int src_h, int dst_w, int dst_h, int frames_in_flight)
+{
+    long long v = -1;
+    const int st = guarded([&] {
+        if (frames_in_flight < 1 || frames_in_flight > ps::Rig::kIoSlots)
+            fail(PS_EINVAL, "frames_in_flight %d out of range 1..%d", frames_in_flight, ps::Rig::kIoSlots);
+        v = ps::Rig::estimateBytes(params, num_params, blend_param, src_w, src_h, dst_w, dst_h, frames_in_flight);
+    });
+    return st == PS_OK ? v : -1;
+}
+
+int ps_render_check(ps_render* r)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (!r->rig.ready()) return;
+        const int st = r->rig.takeStatus();
+        if (st & 4)
+            fail(PS_ETIMEOUT, "a bounded wait of a blend kernel ran out: frames rendered since the last check "
+                              "may be wrong");
+    });
+}
+
+int ps_render_set_wait_probe(ps_render* r, int polls)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        if (!r->rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        r->rig.setWaitProbe(polls);
     });
 }
 
@@ -629,5 +693,94 @@ int ps_blender_blend(ps_blender* b, const void* const* images, const long long* 
 }
 
 int ps_blender_get_num_levels(const ps_blender* b) { return b && b->rig.ready() ? b->rig.numLevels() : 0; }
+
+int ps_blender_begin(ps_blender* b, void* stream)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        if (!b->rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        b->tileSlot = b->rig.peekSlot();  // the state slot the next run takes
+        PS_CUDA(cudaStreamWaitEvent(toStream(stream), b->rig.slotComputed(b->tileSlot), 0));
+        b->tiled = 0;
+        b->tiling = true;
+    });
+}
+
+int ps_blender_tile(ps_blender* b, const void* image, long long pitch, int image_format, int index, void* stream)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        if (!b->tiling) fail(PS_ESTATE, "tile without begin");
+        if (index < 0 || index >= b->rig.numImages())
+            fail(PS_EINVAL, "index %d out of range 0..%d", index, b->rig.numImages() - 1);
+        if (b->tiled >> index & 1) fail(PS_EINVAL, "camera %d was already tiled since begin", index);
+        if (image_format != 16 && image_format != 8) fail(PS_EINVAL, "image_format %d is neither 16 nor 8", image_format);
+        const int esz = image_format == 16 ? 8 : 4;
+        if (!image) fail(PS_EINVAL, "image is NULL");
+        if (pitch < (long long)b->rig.width() * esz || (pitch % esz) || (reinterpret_cast<uintptr_t>(image) % esz))
+            fail(PS_EINVAL, "image: bad pitch or alignment");
+        b->rig.imageToLevel0(image, pitch, image_format, index, b->tileSlot, toStream(stream));
+        b->tiled |= 1ull << index;
+    });
+}
+
+int ps_blender_end(ps_blender* b, ps_image* dst, void* stream)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        if (!b->tiling) fail(PS_ESTATE, "end without begin");
+        checkImage(dst, b->rig.width(), b->rig.height(), "dst", 0);
+        b->tiling = false;
+        if (b->rig.peekSlot() != b->tileSlot) fail(PS_ESTATE, "the blender ran another blend since begin");
+        for (int i = 0; i < b->rig.numImages(); i++)
+            if (!(b->tiled >> i & 1)) b->rig.zeroLevel0(i, b->tileSlot, toStream(stream));
+        if (!b->plan || !b->plan->matches({&b->rig})) b->plan.reset(new ps::Plan({&b->rig}));
+        b->plan->run({ps::FrameInput{nullptr, nullptr, dst}}, toStream(stream), false);
+    });
+}
+
+int ps_blender_get_unique_masks(const ps_blender* b, uint8_t* const* masks, int num)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        if (!b->rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        if (!masks || num != b->rig.numImages())
+            fail(PS_EINVAL, "%d mask buffers given, %d images prepared", num, b->rig.numImages());
+        const long long bytes = (long long)b->rig.width() * b->rig.height();
+        for (int i = 0; i < num; i++) {
+            if (!masks[i]) fail(PS_EINVAL, "mask buffer %d is NULL", i);
+            b->rig.exportState(3, i, 0, masks[i], bytes);
+        }
+    });
+}
+
+long long ps_blender_used_memory(const ps_blender* b) { return b && b->rig.ready() ? b->rig.residentBytes() : 0; }
+
+long long ps_blender_estimate_memory(int width, int height, int num_images, int max_levels)
+{
+    long long v = -1;
+    const int st = guarded([&] { v = ps::Rig::estimateBlenderBytes(width, height, num_images, max_levels); });
+    return st == PS_OK ? v : -1;
+}
+
+int ps_blender_check(ps_blender* b)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        if (!b->rig.ready()) return;
+        const int st = b->rig.takeStatus();
+        if (st & 4)
+            fail(PS_ETIMEOUT, "a bounded wait of a blend kernel ran out: blends since the last check may be wrong");
+    });
+}
+
+int ps_blender_set_wait_probe(ps_blender* b, int polls)
+{
+    return guarded([&] {
+        if (!b) fail(PS_EINVAL, "blender is NULL");
+        if (!b->rig.ready()) fail(PS_ESTATE, "have not prepared or prepare failed before");
+        b->rig.setWaitProbe(polls);
+    });
+}
 
 }  // extern "C"

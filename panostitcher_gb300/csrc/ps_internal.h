@@ -134,6 +134,10 @@ cudaError_t launchUnion(const uint8_t* cov, int n, int W, int H, long long maskS
                         int tw, int th, int tilesX, int* tileCounts, unsigned long long* total,
                         cudaStream_t st);
 // copy full-canvas maps into tile-compact float2 storage
+// per remap item (in item order), the box of source texels its taps read;
+// maps in tile-compact order (item k's tile is maps + k * 512: items are
+// numbered in mapTile order)
+cudaError_t launchRemapBoxes(const float2* maps, int nitems, int sw, int sh, RemapBox* boxes, cudaStream_t st);
 cudaError_t launchCompactMaps(const float* xmap, const float* ymap, int W, int H, long long maskStride,
                               const RemapItem* items, int nitems, float2* maps, cudaStream_t st);
 // int16x4 / uint8x4 images -> uchar4 level 0, checking range and zero outside coverage
@@ -169,7 +173,9 @@ struct LaunchShape {
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st);
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
 // counter: a zeroed int the launch hands its tiles out through
-cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st);
+// probePolls > 0: the failure-path test of the bounded waits (k_blend)
+cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, int probePolls,
+                        cudaStream_t st);
 // blend of few-tile levels above 0: two work items (the 64x8 halves) per tile
 cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st);
 // one cluster per segment: the rig's pyrDown levels tailDown..L and blend

@@ -577,6 +577,43 @@ __global__ void k_compact_maps(const float* __restrict__ xmap, const float* __re
     maps[(size_t)it.mapTile * (kRemapTW * kRemapTH) + threadIdx.x] = v;
 }
 
+// Source footprint of each remap tile: the bounding box of its taps
+// (x0, y0) .. (min(x0 + 1, sw - 1), min(y0 + 1, sh - 1)) over the valid
+// map values, columns widened to whole 16-byte chunks of BGR32 texels.
+__global__ void k_remap_boxes(const float2* __restrict__ maps, int nitems, int sw, int sh, RemapBox* boxes)
+{
+    __shared__ int s_box[4];
+    if (threadIdx.x < 4) s_box[threadIdx.x] = threadIdx.x < 2 ? 0x7FFFFFFF : -1;
+    __syncthreads();
+    const float2 m = maps[(size_t)blockIdx.x * (kRemapTW * kRemapTH) + threadIdx.x];
+    if (m.x >= 0.f && m.y >= 0.f && m.x < (float)sw && m.y < (float)sh) {
+        const int x0 = (int)m.x, y0 = (int)m.y;  // non-negative: truncation is the floor
+        atomicMin(&s_box[0], x0);
+        atomicMin(&s_box[1], y0);
+        atomicMax(&s_box[2], min(x0 + 1, sw - 1));
+        atomicMax(&s_box[3], min(y0 + 1, sh - 1));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        RemapBox b = {0, 0, 0, 0};
+        if (s_box[2] >= 0) {
+            const int ax0 = s_box[0] & ~3;
+            b.x0 = (uint16_t)ax0;
+            b.y0 = (uint16_t)s_box[1];
+            b.w = (uint16_t)min(65532, (s_box[2] + 1 - ax0 + 3) & ~3);
+            b.h = (uint16_t)min(65535, s_box[3] + 1 - s_box[1]);
+        }
+        boxes[blockIdx.x] = b;
+    }
+}
+
+cudaError_t launchRemapBoxes(const float2* maps, int nitems, int sw, int sh, RemapBox* boxes, cudaStream_t st)
+{
+    if (nitems <= 0) return cudaSuccess;
+    k_remap_boxes<<<nitems, kRemapTW * kRemapTH, 0, st>>>(maps, nitems, sw, sh, boxes);
+    return cudaGetLastError();
+}
+
 cudaError_t launchCompactMaps(const float* xmap, const float* ymap, int W, int H, long long maskStride,
                               const RemapItem* items, int nitems, float2* maps, cudaStream_t st)
 {
@@ -745,6 +782,20 @@ void* g_noallocPtr[64] = {};
 
 }  // namespace
 
+// The cameras' parameters travel to the device as the argument of a kernel
+// (by value, copied at launch), which writes them into the scratch array:
+// no host buffer is read after the call returns and no copy waits on the
+// host.  64 cameras x 288 bytes stay inside the 32 KB argument limit.
+struct NoAllocParams {
+    RemapDev cam[PS_MAX_CAMS];
+};
+static_assert(sizeof(NoAllocParams) <= 32000, "camera parameters exceed the kernel argument limit");
+
+__global__ void k_noalloc_params(const __grid_constant__ NoAllocParams p, int n, RemapDev* out)
+{
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = p.cam[i];
+}
+
 // coverage only (getReprojectMapAndMask's mask), as k_gen_map computes it
 __global__ void k_coverage(const RemapDev* __restrict__ prm, int W, int H, uint8_t* cov)
 {
@@ -766,6 +817,7 @@ extern "C" int ps_nearest_axis_seams_no_alloc(const ps_photo_param* params, int 
         if (!params || !seams || num_params <= 0) fail(PS_EINVAL, "NULL argument or no cameras");
         if (num_params > PS_MAX_CAMS) fail(PS_EINVAL, "%d cameras, at most %d supported", num_params, PS_MAX_CAMS);
         if (src_w <= 0 || src_h <= 0 || dst_w <= 0 || dst_h <= 0) fail(PS_EINVAL, "sizes must be positive");
+        if (dst_h > 65535) fail(PS_EINVAL, "dst_h %d exceeds 65535 (one grid row per canvas row)", dst_h);
         for (int i = 0; i < num_params; i++)
             if (params[i].image_type < 0 || params[i].image_type > 3)
                 fail(PS_EINVAL, "camera %d: image_type %d not in 0..3", i, params[i].image_type);
@@ -792,10 +844,10 @@ extern "C" int ps_nearest_axis_seams_no_alloc(const ps_photo_param* params, int 
         RemapDev* dParams = static_cast<RemapDev*>(base);
         uint8_t* cov = static_cast<uint8_t*>(base) + kNoAllocParamBytes;
         static_assert(sizeof(RemapDev) * PS_MAX_CAMS <= kNoAllocParamBytes, "parameter area too small");
-        std::vector<RemapDev> rp(num_params);
-        for (int i = 0; i < num_params; i++) remapInit(params[i], dst_w, dst_h, src_w, src_h, rp[i]);
-        // pageable source: the copy is staged before cudaMemcpyAsync returns
-        PS_CUDA(cudaMemcpyAsync(dParams, rp.data(), sizeof(RemapDev) * num_params, cudaMemcpyHostToDevice, st));
+        NoAllocParams rp;
+        for (int i = 0; i < num_params; i++) remapInit(params[i], dst_w, dst_h, src_w, src_h, rp.cam[i]);
+        k_noalloc_params<<<1, 64, 0, st>>>(rp, num_params, dParams);
+        PS_CUDA(cudaGetLastError());
         // every coverage byte is rewritten, so nothing of the last call's contents survives
         dim3 grid((dst_w + 127) / 128, dst_h, num_params);
         k_coverage<<<grid, 128, 0, st>>>(dParams, dst_w, dst_h, cov);

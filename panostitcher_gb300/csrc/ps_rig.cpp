@@ -122,6 +122,7 @@ void Rig::clear()
     }
     nextSlot_ = lastSlot_ = 0;
     maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset(); planar_.reset();
+    dRemapBox_.reset();
     imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
     hRemap_.clear();
     hDown_.clear();
@@ -182,7 +183,7 @@ long long Rig::residentBytes() const
     }
     b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
     b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
-    b += dLinear_.bytes() + linW_.bytes() + planar_.bytes();
+    b += dLinear_.bytes() + linW_.bytes() + planar_.bytes() + dRemapBox_.bytes();
     return b;
 }
 
@@ -198,6 +199,23 @@ static void validateParams(const ps_photo_param* params, int n, int srcW, int sr
     for (int i = 0; i < n; i++)
         if (params[i].image_type < 0 || params[i].image_type > 3)
             fail(PS_EINVAL, "camera %d: image_type %d not in 0..3", i, params[i].image_type);
+}
+
+long long Rig::estimateBlenderBytes(int W, int H, int n, int maxLevels, int slots)
+{
+    if (W <= 0 || H <= 0 || n <= 0 || n > PS_MAX_CAMS) fail(PS_EINVAL, "size (%d, %d) or %d images invalid", W, H, n);
+    if (slots < 1 || slots > kIoSlots) fail(PS_EINVAL, "%d state slots, 1..%d supported", slots, kIoSlots);
+    const int L = std::max(0, trueNumLevels(W, H, maxLevels, 2));
+    long long b = 0;
+    int w = W, h = H;
+    for (int j = 0; j <= L; j++) {
+        const long long px = (long long)roundUp(w, 64) * h;
+        b += px * n * (4 * slots + 2 + (j ? 2 : 0)) + (j ? px * 8 * slots : 0);
+        w = (w + 1) / 2;
+        h = (h + 1) / 2;
+    }
+    // coverage masks (input checks), union mask, output staging
+    return b + (long long)W * H * n + (long long)roundUp(W, 64) * H + (long long)W * H * 4 * slots;
 }
 
 long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
@@ -274,9 +292,25 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
             if (!seams[i]) fail(PS_EINVAL, "seam mask %d is NULL", i);
         checkSeamsDisjoint(seams, n, dstW, dstH);
     }
+    // The reference compares its estimate of the stream-based render's
+    // device memory with the free memory and, within 500 MB, falls back to
+    // one camera at a time (source/Task/RicohUtil.cpp:1135-1170).  Here the
+    // resident state is per frame in flight, so the fallback is fewer state
+    // slots: as many as fit with that margin, down to one.
+    // A caller's memory budget (setMemoryBudget) caps the same estimate.
+    int slots = slotsWanted_;
+    if (highQuality && slots > 1) {
+        size_t freeB = 0, totalB = 0;
+        PS_CUDA(cudaMemGetInfo(&freeB, &totalB));
+        long long room = (long long)freeB - 500000000LL;
+        if (budget_ > 0) room = std::min(room, budget_);
+        while (slots > 1 && estimateBytes(params, n, blendParam, srcW, srcH, dstW, dstH, slots) > room) slots--;
+    }
     try {
         // MIN_SIDE_LENGTH = 2, source/Task/RicohUtil.cpp:15
         setGeometry(n, dstW, dstH, highQuality ? std::max(0, trueNumLevels(dstW, dstH, blendParam, 2)) : 0);
+        lowMemory_ = slots < slots_;
+        slots_ = slots;
         srcW_ = srcW;
         srcH_ = srcH;
         const size_t npx = (size_t)dstW * dstH;
@@ -484,6 +518,10 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         maps_.alloc(hRemap_.size() * kRemapTW * kRemapTH * sizeof(float2));
         PS_CUDA(launchCompactMaps(xmap, ymap, W, H, (long long)npx, dRemap_.as<RemapItem>(), (int)hRemap_.size(),
                                   maps_.as<float2>(), st));
+        // item k has mapTile k here (items are numbered as they are listed)
+        dRemapBox_.alloc(hRemap_.size() * sizeof(RemapBox));
+        PS_CUDA(launchRemapBoxes(maps_.as<float2>(), (int)hRemap_.size(), srcW_, srcH_, dRemapBox_.as<RemapBox>(),
+                                 st));
     }
 
     // device descriptor
@@ -497,6 +535,7 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     d.srcW = srcW_;
     d.srcH = srcH_;
     d.maps = maps_.as<float2>();
+    d.remapBoxes = dRemapBox_.as<RemapBox>();
     d.unionMask = union_.as<uint8_t>();
     d.camLists = dCams_.as<uint8_t>();
     d.downItems = dDown_.as<DownItem>();
@@ -703,6 +742,25 @@ void Rig::waitIdle()
     }
 }
 
+int Rig::takeStatus()
+{
+    waitIdle();
+    if (!status_.get()) return 0;
+    int v = 0;
+    PS_CUDA(cudaMemcpy(&v, status_.get(), sizeof(int), cudaMemcpyDeviceToHost));
+    if (v) PS_CUDA(cudaMemset(status_.get(), 0, sizeof(int)));
+    return v;
+}
+
+void Rig::setWaitProbe(int polls)
+{
+    if (polls < 0 || polls > (1 << 24)) fail(PS_EINVAL, "wait probe of %d polls out of range 0..2^24", polls);
+    if (polls == probe_) return;
+    waitIdle();
+    probe_ = polls;
+    gen_++;  // plans re-record their launches
+}
+
 void Rig::waitIdleQuiet() noexcept
 {
     for (cudaEvent_t* es : {slotComputed_, slotDownloaded_})
@@ -836,16 +894,37 @@ void Rig::prepareLinear(const uint8_t* cov, const uint8_t* seam, const float* xm
 
 void Rig::imagesToLevel0(const void* const* images, const long long* pitches, int fmt, int slot, cudaStream_t st)
 {
-    const size_t n = n_;
+    toLevel0(images, pitches, fmt, 0, n_, slot, st);
+}
+
+void Rig::imageToLevel0(const void* image, long long pitch, int fmt, int cam, int slot, cudaStream_t st)
+{
+    if (cam < 0 || cam >= n_) fail(PS_EINVAL, "camera %d out of range 0..%d", cam, n_ - 1);
+    toLevel0(&image, &pitch, fmt, cam, 1, slot, st);
+}
+
+void Rig::zeroLevel0(int cam, int slot, cudaStream_t st)
+{
+    const LevelGeom& g = geom_[0];
+    PS_CUDA(cudaMemsetAsync(lv_[0].G[slot].as<uchar4>() + (size_t)cam * g.pitch * g.h, 0,
+                            (size_t)g.pitch * g.h * sizeof(uchar4), st));
+}
+
+void Rig::toLevel0(const void* const* images, const long long* pitches, int fmt, int cam0, int count, int slot,
+                   cudaStream_t st)
+{
+    const size_t n = count;
     std::vector<uint8_t> args((sizeof(void*) + sizeof(long long)) * n);
     std::memcpy(args.data(), images, sizeof(void*) * n);
     std::memcpy(args.data() + sizeof(void*) * n, pitches, sizeof(long long) * n);
     PS_CUDA(cudaMemcpyAsync(imgArgs_.get(), args.data(), args.size(), cudaMemcpyHostToDevice, st));
     PS_CUDA(cudaMemsetAsync(status_.get(), 0, sizeof(int), st));
     const LevelGeom& g = geom_[0];
+    const size_t npx = (size_t)W_ * H_;
     PS_CUDA(launchImagesToLevel0(imgArgs_.as<const void* const>(),
                                  reinterpret_cast<const long long*>(imgArgs_.as<uint8_t>() + sizeof(void*) * n), fmt,
-                                 n_, W_, H_, covDev_.as<uint8_t>(), (long long)W_ * H_, lv_[0].G[slot].as<uchar4>(), g.pitch,
+                                 count, W_, H_, covDev_.as<uint8_t>() + cam0 * npx, (long long)npx,
+                                 lv_[0].G[slot].as<uchar4>() + (size_t)cam0 * g.pitch * g.h, g.pitch,
                                  (long long)g.pitch * g.h, status_.as<int>(), st));
     int status = 0;
     PS_CUDA(cudaMemcpyAsync(&status, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1112,7 +1191,7 @@ void Plan::bind(const std::vector<Rig*>& rigs)
     gens_.clear();
     for (Rig* r : rigs) gens_.push_back(r->generation());
     lutOff_.clear();
-    size_t off = sizeof(FrameDev) * nr;
+    size_t off = (sizeof(FrameDev) * nr + 15) / 16 * 16;  // LUTs 16-byte aligned for bulk copies
     for (Rig* r : rigs) {
         lutOff_.push_back(off);
         off += (size_t)r->numImages() * 768;
@@ -1137,6 +1216,8 @@ void Plan::bind(const std::vector<Rig*>& rigs)
     };
     tailCluster_ = widest([](const LaunchShape& s) { return s.tailCluster; });
     for (int k = 0; k < 3; k++) perSm_[k] = widest([k](const LaunchShape& s) { return s.ctasPerSm[k]; });
+    probe_ = 0;
+    for (Rig* r : rigs) probe_ = std::max(probe_, r->waitProbe());
     auto addStep = [&](int kind, const std::vector<std::pair<int, std::pair<const void*, int>>>& parts, int step) {
         Step s{kind, (int)segs_.size(), 0, 0, -1, 0.0};
         for (const auto& p : parts) {
@@ -1253,7 +1334,7 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
         }
         if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, perSm_[0], counters + si, st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, perSm_[1], st));
-        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, st));
+        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, probe_, st));
         else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, tailCluster_, st));
         else if (s.kind == 6) PS_CUDA(launchBlendSmall(p, s.nsegs, s.total, st));
         else PS_CUDA(launchLinear(p, s.nsegs, s.total, maxCams_, st));

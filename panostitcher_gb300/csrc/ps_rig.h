@@ -68,6 +68,12 @@ public:
     // state slots of the next prepare (1..kIoSlots; default kIoSlots)
     void setSlots(int n) { slotsWanted_ = n < 1 ? 1 : (n > kIoSlots ? kIoSlots : n); }
     int slots() const { return slots_; }
+    // the last prepare found too little free device memory for the slots
+    // asked for and took fewer (the reference's low-memory path)
+    bool lowMemory() const { return lowMemory_; }
+    // device bytes the next prepare may take for the render (0: no limit
+    // but the free memory)
+    void setMemoryBudget(long long bytes) { budget_ = bytes > 0 ? bytes : 0; }
     uint8_t* inputBuffer(int cam, int slot = 0) const
     {
         return inputs_.as<uint8_t>() + ((size_t)slot * n_ + cam) * inPitch_ * srcH_;
@@ -87,6 +93,16 @@ public:
     }
     uint8_t* outputBuffer(int slot = 0) const { return output_.as<uint8_t>() + (size_t)slot * W_ * H_ * 4; }
     int* statusWord() const { return status_.as<int>(); }
+    // The status bits the kernels set since the last call (bit 4: a bounded
+    // wait of a blend kernel ran out), read and cleared after the rig's runs
+    // have finished.
+    int takeStatus();
+    // Failure-path test of the bounded waits: with polls > 0 every blend
+    // launch of this rig makes one wait of that many polls on a barrier that
+    // nothing completes, which therefore runs out.  0 (the default) is off.
+    // Waits for the rig's runs; the next run re-records its launches.
+    void setWaitProbe(int polls);
+    int waitProbe() const { return probe_; }
 
     void exportState(int what, int cam, int level, void* host, long long bytes) const;
     void exportCollapsed(int level, int16_t* host, long long bytes, cudaStream_t st) const;
@@ -138,6 +154,13 @@ public:
 
     // blender input: int16x4 / uint8x4 device images -> level 0 of a slot (checks)
     void imagesToLevel0(const void* const* images, const long long* pitches, int fmt, int slot, cudaStream_t st);
+    // the same for one camera (CudaTilingMultibandBlendFast::tile), and a
+    // camera left out of a tiled blend (its level 0 all zero: its Laplacians
+    // vanish, so it contributes nothing, while its weights still count)
+    void imageToLevel0(const void* image, long long pitch, int fmt, int cam, int slot, cudaStream_t st);
+    void zeroLevel0(int cam, int slot, cudaStream_t st);
+    // device bytes a blender of this size holds at most (any coverage)
+    static long long estimateBlenderBytes(int W, int H, int n, int maxLevels, int slots = kIoSlots);
 
     // Bytes a step must move at minimum (each input / output element once,
     // no halo re-reads): kind 0 remap, 1 pyrDown to `level`, 2 blend of
@@ -159,11 +182,13 @@ private:
     void prepareLinear(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
                        int radius, cudaStream_t st);
     void writeDescriptors(cudaStream_t st);
+    void toLevel0(const void* const* images, const long long* pitches, int fmt, int cam0, int count, int slot,
+                  cudaStream_t st);
     void buildBlendState(const uint8_t* uniSrcDev, bool custom, cudaStream_t st);
 
     int n_ = 0, W_ = 0, H_ = 0, L_ = 0, full_ = 0, srcW_ = 0, srcH_ = 0;
-    bool hasMaps_ = false, linear_ = false, custom_ = false;
-    int nextSlot_ = 0, lastSlot_ = 0, slots_ = kIoSlots, slotsWanted_ = kIoSlots;
+    bool hasMaps_ = false, linear_ = false, custom_ = false, lowMemory_ = false;
+    int nextSlot_ = 0, lastSlot_ = 0, slots_ = kIoSlots, slotsWanted_ = kIoSlots, probe_ = 0;
     cudaEvent_t slotComputed_[kIoSlots] = {}, slotDownloaded_[kIoSlots] = {};
     int numLinear_ = 0;
     DevBuf dLinear_, linW_;
@@ -171,8 +196,8 @@ private:
     std::vector<LevelGeom> geom_;
     LevelBufs lv_[PS_MAX_LEVELS + 1];
     DevBuf maps_, union_, inputs_, output_, covDev_, status_, imgArgs_, planar_;
-    long long inPitch_ = 0;
-    DevBuf dDesc_, dRemap_, dDown_, dBlend_, dCams_;
+    long long inPitch_ = 0, budget_ = 0;
+    DevBuf dDesc_, dRemap_, dRemapBox_, dDown_, dBlend_, dCams_;
     std::vector<RemapItem> hRemap_;
     int downOff_[PS_MAX_LEVELS + 1] = {}, downCnt_[PS_MAX_LEVELS + 1] = {};
     int blendOff_[PS_MAX_LEVELS + 1] = {}, blendCnt_[PS_MAX_LEVELS + 1] = {};
@@ -264,6 +289,7 @@ private:
     size_t segOff_ = 0, counterOff_ = 0, stageBytes_ = 0;
     int maxCams_ = 0;
     int tailCluster_ = 0, perSm_[3] = {0, 0, 0};  // launch widths (from the rigs' shapes)
+    int probe_ = 0;                                // wait probe of k_blend (Rig::setWaitProbe)
     IoSlot io_[Rig::kIoSlots];
     int nextIo_ = 0;
     // copy-in, compute and copy-out streams (non-blocking), the capture stream

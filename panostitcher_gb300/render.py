@@ -137,6 +137,7 @@ class CudaPanoramaRender2:
                 seams=None, stream=None, check: bool = False) -> bool:
         """prepare(params, highQualityBlend, blendParam, srcSize, dstSize); sizes are (w, h)."""
         arr = _params(params)
+        self._size = tuple(dst_size)
         if seams is None:
             st = lib().ps_render_prepare(self._h, arr, len(params), high_quality_blend, blend_param,
                                          src_size[0], src_size[1], dst_size[0], dst_size[1],
@@ -152,6 +153,7 @@ class CudaPanoramaRender2:
     def prepare_file(self, path: str, high_quality_blend: int, blend_param: int, src_size, dst_size, stream=None,
                      check: bool = False) -> bool:
         """prepare(path, highQualityBlend, blendParam, srcSize, dstSize) with a PTGui .pts camera file."""
+        self._size = tuple(dst_size)
         st = lib().ps_render_prepare_file(self._h, path.encode(), high_quality_blend, blend_param, src_size[0],
                                           src_size[1], dst_size[0], dst_size[1], _stream_handle(stream))
         return self._status(st, check)
@@ -163,6 +165,33 @@ class CudaPanoramaRender2:
     @property
     def frames_in_flight(self) -> int:
         return lib().ps_render_get_frames_in_flight(self._h)
+
+    def set_memory_budget(self, nbytes: int) -> None:
+        """Device bytes the next prepare may take (0: the free memory only); fewer frames in flight fit."""
+        check(lib().ps_render_set_memory_budget(self._h, int(nbytes)))
+
+    @property
+    def low_memory(self) -> bool:
+        """The last prepare took fewer frames in flight than asked for (the reference's low-memory path)."""
+        return bool(lib().ps_render_is_low_memory(self._h))
+
+    @staticmethod
+    def estimate_memory(params: Sequence[dict], blend_param: int, src_size, dst_size, frames_in_flight: int = 8):
+        """Device bytes a render of this rig would hold (upper bound, no allocation)."""
+        arr, n = _params(params), len(params)
+        v = lib().ps_render_estimate_memory(arr, n, blend_param, src_size[0], src_size[1], dst_size[0], dst_size[1],
+                                            frames_in_flight)
+        if v < 0:
+            raise PsError(L.PS_EINVAL, lib().ps_last_error().decode(errors="replace"))
+        return v
+
+    def get_unique_masks(self) -> list:
+        """The seam masks (uint8 (H, W), 0 / 255), one per camera."""
+        n = self.getNumImages()
+        W, H = self._size
+        out = [np.empty((H, W), np.uint8) for _ in range(n)]
+        check(lib().ps_render_get_unique_masks(self._h, (C.c_void_p * n)(*[o.ctypes.data for o in out]), n))
+        return out
 
     def set_seam_rule(self, rule: int) -> None:
         """PS_SEAMS_NEAREST_AXIS (default) or PS_SEAMS_DISTANCE (getNonIntersectingMasks); next prepare."""
@@ -213,6 +242,15 @@ class CudaPanoramaRender2:
         st = lib().ps_render_render_planar(self._h, arr, len(frames), lp, nl, d, y, _stream_handle(stream))
         del keep
         return self._status(st, check)
+
+    def check_status(self, check: bool = True) -> bool:
+        """Waits for the frames in flight and reports a bounded kernel wait that ran out since the last
+        check (PS_ETIMEOUT: those frames may be wrong)."""
+        return self._status(lib().ps_render_check(self._h), check)
+
+    def set_wait_probe(self, polls: int) -> None:
+        """Failure-path test hook: every blend launch makes one wait of `polls` polls that runs out."""
+        check(lib().ps_render_set_wait_probe(self._h, int(polls)))
 
     def clear(self) -> None:
         lib().ps_render_clear(self._h)
@@ -429,6 +467,7 @@ class CudaTilingMultibandBlendFast:
         sp = None if ss is None else (C.c_void_p * len(ss))(*[s.ctypes.data for s in ss])
         st = lib().ps_blender_prepare(self._h, mp, sp, len(ms), W, H, max_levels, min_length,
                                       _stream_handle(stream))
+        self._n = len(ms)
         if st != L.PS_OK:
             self.last_error = lib().ps_last_error().decode(errors="replace")
             return False
@@ -461,6 +500,49 @@ class CudaTilingMultibandBlendFast:
     @property
     def num_levels(self) -> int:
         return lib().ps_blender_get_num_levels(self._h)
+
+    def begin(self, stream=None) -> None:
+        """begin(): a blend fed one camera at a time."""
+        check(lib().ps_blender_begin(self._h, _stream_handle(stream)))
+
+    def tile(self, image, index: int, stream=None) -> None:
+        """tile(image, index): camera `index`'s CUDA int16 (H, W, 4) or uint8 (H, W, 4) level-0 image."""
+        fmt = 16 if image.element_size() == 2 else 8
+        check(lib().ps_blender_tile(self._h, image.data_ptr(), image.stride(0) * image.element_size(), fmt, index,
+                                    _stream_handle(stream)))
+
+    def end(self, dst, stream=None) -> None:
+        """end(blendImage): blends the tiled cameras into dst."""
+        d = as_image(dst)
+        check(lib().ps_blender_end(self._h, C.byref(d), _stream_handle(stream)))
+
+    def get_unique_masks(self, size) -> list:
+        """getUniqueMasks: the seam masks (uint8 (H, W), 0 / 255); size = (W, H)."""
+        W, H = size
+        n = self._n
+        out = [np.empty((H, W), np.uint8) for _ in range(n)]
+        check(lib().ps_blender_get_unique_masks(self._h, (C.c_void_p * n)(*[o.ctypes.data for o in out]), n))
+        return out
+
+    def calc_used_memory_size(self) -> int:
+        """calcUsedMemorySize: device bytes the blender holds."""
+        return lib().ps_blender_used_memory(self._h)
+
+    @staticmethod
+    def estimate_memory_size(width: int, height: int, num_images: int, max_levels: int = 16) -> int:
+        """estimateMemorySize: device bytes a blender of this size would hold at most."""
+        return lib().ps_blender_estimate_memory(width, height, num_images, max_levels)
+
+    def check_status(self) -> int:
+        """PS_OK, or PS_ETIMEOUT when a bounded kernel wait ran out since the last check."""
+        st = lib().ps_blender_check(self._h)
+        if st != L.PS_OK:
+            self.last_error = lib().ps_last_error().decode(errors="replace")
+        return st
+
+    def set_wait_probe(self, polls: int) -> None:
+        """Failure-path test hook: every blend launch makes one wait of `polls` polls that runs out."""
+        check(lib().ps_blender_set_wait_probe(self._h, int(polls)))
 
 
 def generate_reproject_map_and_mask(param: dict, src_size, dst_size, xmap, ymap, mask, stream=None) -> None:

@@ -33,10 +33,16 @@ def test_no_alloc_seams_equal_prepare(cuda, name, factor):
     r.prepare(cfg.cams, 1, cfg.levels, cfg.src_size, cfg.dst_size, check=True)
     ref = np.stack([r.seam(i, cfg.dst_size) for i in range(cfg.num_cams)])
     W, H = cfg.dst_size
-    for call in range(2):
-        out = torch.full((cfg.num_cams, H, W), 7, dtype=torch.uint8, device="cuda")
+    outs = [torch.full((cfg.num_cams, H, W), 7, dtype=torch.uint8, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    for call, out in enumerate(outs):
+        # the first call may load the library's device code (and its array);
+        # the second must leave the device's free memory as it found it
+        free_before = torch.cuda.mem_get_info()[0]
         L.check(_call(cfg, out))
         torch.cuda.synchronize()
+        if call == 1:
+            assert torch.cuda.mem_get_info()[0] == free_before, "the second call changed free device memory"
         assert np.array_equal(out.cpu().numpy(), ref), f"call {call}"
 
 
@@ -47,3 +53,13 @@ def test_no_alloc_rejects_oversize(cuda):
     st = _call(cfg, out)
     assert st == L.PS_EINVAL
     assert "scratch" in L.lib().ps_last_error().decode()
+
+
+def test_no_alloc_rejects_tall_canvas(cuda):
+    torch = cuda
+    cfg = S.scaled_rig(S.rig("c1"), 8)
+    cfg.dst_size = (64, 70000)            # 4.5 MB of coverage fits the scratch; 70000 rows do not fit a grid
+    out = torch.empty(16, dtype=torch.uint8, device="cuda")
+    st = _call(cfg, out)
+    assert st == L.PS_EINVAL
+    assert "65535" in L.lib().ps_last_error().decode()
