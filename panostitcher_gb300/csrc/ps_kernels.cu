@@ -152,12 +152,18 @@ __device__ __forceinline__ RemapSeg remapSeg(const Segment* segs, int nsegs, int
             sg.frame};
 }
 
-constexpr int kRStages = 2;
-constexpr int kRTexWords = 4096;  // 16 KB of source texels per stage
+#ifndef PS_REMAP_STAGES
+#define PS_REMAP_STAGES 2
+#endif
+#ifndef PS_REMAP_TEX_WORDS
+#define PS_REMAP_TEX_WORDS 4096
+#endif
+constexpr int kRStages = PS_REMAP_STAGES;
+constexpr int kRTexWords = PS_REMAP_TEX_WORDS;  // source texels per stage (16 KB; 0: gathers from global)
 struct alignas(16) RemapStage {
     float2 map[kRemapTW * kRemapTH];
     uint8_t lut[768];
-    uint32_t tex[kRTexWords];
+    uint32_t tex[kRTexWords > 0 ? kRTexWords : 4];
 };
 constexpr size_t kRemapSmem = sizeof(RemapStage) * kRStages;
 
@@ -259,7 +265,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
         ui.tx = item.tx;
         ui.ty = item.ty;
         const bool aligned = ((reinterpret_cast<uintptr_t>(ui.base) | (uintptr_t)ui.pitch) & 15) == 0;
-        ui.staged = ui.fmt == PS_FMT_BGR32 && aligned && box.w > 0 && box.x0 + box.w <= ui.sw &&
+        ui.staged = kRTexWords > 0 && ui.fmt == PS_FMT_BGR32 && aligned && box.w > 0 && box.x0 + box.w <= ui.sw &&
                     (int)box.w * box.h <= kRTexWords;
         ui.bx0 = box.x0;
         ui.by0 = box.y0;

@@ -201,6 +201,23 @@ static void validateParams(const ps_photo_param* params, int n, int srcW, int sr
             fail(PS_EINVAL, "camera %d: image_type %d not in 0..3", i, params[i].image_type);
 }
 
+// Upper bound of the work lists and descriptors a rig of this shape holds:
+// every pyrDown and blend tile listed (with its camera list), remap items and
+// boxes for every camera's level-0 tiles, one descriptor per state slot.
+static long long listBytes(int W, int H, int n, int L, int slots)
+{
+    long long b = (long long)sizeof(RigDev) * slots + 4096;
+    int w = W, h = H;
+    for (int j = 0; j <= L; j++) {
+        const long long down = (long long)divUp(w, kDownTW) * divUp(h, kDownTH) * n;
+        const long long blend = (long long)divUp(w, kBlendTW) * divUp(h, kBlendTH);
+        b += (j ? down * (long long)sizeof(DownItem) : 0) + blend * ((long long)sizeof(BlendItem) + n);
+        w = (w + 1) / 2;
+        h = (h + 1) / 2;
+    }
+    return b + (long long)divUp(W, kRemapTW) * divUp(H, kRemapTH) * n * (sizeof(RemapItem) + sizeof(RemapBox));
+}
+
 long long Rig::estimateBlenderBytes(int W, int H, int n, int maxLevels, int slots)
 {
     if (W <= 0 || H <= 0 || n <= 0 || n > PS_MAX_CAMS) fail(PS_EINVAL, "size (%d, %d) or %d images invalid", W, H, n);
@@ -214,8 +231,9 @@ long long Rig::estimateBlenderBytes(int W, int H, int n, int maxLevels, int slot
         w = (w + 1) / 2;
         h = (h + 1) / 2;
     }
-    // coverage masks (input checks), union mask, output staging
-    return b + (long long)W * H * n + (long long)roundUp(W, 64) * H + (long long)W * H * 4 * slots;
+    // coverage masks (input checks), union mask, output staging, input arguments, lists
+    return b + (long long)W * H * n + (long long)roundUp(W, 64) * H + (long long)W * H * 4 * slots + 16LL * n +
+           listBytes(W, H, n, L, slots);
 }
 
 long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
@@ -231,10 +249,10 @@ long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam
         w = (w + 1) / 2;
         h = (h + 1) / 2;
     }
-    // maps bounded by the full canvas per camera, inputs, output, union mask
+    // maps bounded by the full canvas per camera, inputs, output, union mask, lists
     b += (long long)dstW * dstH * 8 * n +
          ((long long)roundUp(srcW * 4, 256) * srcH * n + (long long)dstW * dstH * 4) * slots +
-         (long long)dstW * dstH;
+         (long long)roundUp(dstW, 64) * dstH + listBytes(dstW, dstH, n, L, slots);
     return b;
 }
 

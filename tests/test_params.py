@@ -1,5 +1,5 @@
-"""Camera parameter files: the PTGui .pts reader of loadPhotoParams
-(source/Warp/PhotoParam.cpp:681-771), and prepare(path, ...)."""
+"""Camera parameter files: the PTGui .pts and XML readers of loadPhotoParams
+(source/Warp/PhotoParam.cpp:17-506, 681-771), and prepare(path, ...)."""
 import os
 
 import numpy as np
@@ -43,10 +43,78 @@ def test_pts_without_header_or_global_has_no_cameras(built_lib, tmp_path):
     assert P.load_photo_params(_write(tmp_path, no_global, "b.pts")) == []
 
 
+# The per-camera layout (loadPhotoParamFromXML2): every field on each camera element.
+XML_PER_CAMERA = """<?xml version="1.0" encoding="utf-8"?>
+<!-- two cameras -->
+<Root>
+  <POSITION>
+    <IMAGETYPE>0</IMAGETYPE><CROPMODE>0</CROPMODE><HFOV>100</HFOV><VFOV>0</VFOV>
+    <Alpha>0.01</Alpha><Beta>-0.02</Beta><Gamma>0.03</Gamma><ShiftX>1.5</ShiftX><ShiftY>-2.5</ShiftY>
+    <ShearX>0</ShearX><ShearY>0</ShearY>
+    <CROPLEFT>10</CROPLEFT><CROPRIGHT>1910</CROPRIGHT><CROPTOP>20</CROPTOP><CROPBOTTOM>1060</CROPBOTTOM>
+    <CircleX>0</CircleX><CircleY>0</CircleY><CircleR>0</CircleR>
+    <YAW>10.5</YAW><PITCH>-2</PITCH><ROLL>1</ROLL>
+  </POSITION>
+  <POSITION note="attributes are ignored">
+    <IMAGETYPE>1</IMAGETYPE><CROPMODE>0</CROPMODE><HFOV>100</HFOV><VFOV>0</VFOV>
+    <Alpha>0.01</Alpha><Beta>-0.02</Beta><Gamma>0.03</Gamma><ShiftX>1.5</ShiftX><ShiftY>-2.5</ShiftY>
+    <ShearX>0</ShearX><ShearY>0</ShearY>
+    <CROPLEFT>0</CROPLEFT><CROPRIGHT>0</CROPRIGHT><CROPTOP>0</CROPTOP><CROPBOTTOM>0</CROPBOTTOM>
+    <CircleX>640</CircleX><CircleY>480</CircleY><CircleR>470</CircleR>
+    <YAW>180</YAW><PITCH>5</PITCH><ROLL>0</ROLL>
+  </POSITION>
+</Root>
+"""
+
+# The GlobalInfo layout (loadPhotoParamFromXML1): lens and crop once, the pose per camera element.
+XML_GLOBAL = """<Root>
+  <GlobalInfo>
+    <IMAGETYPE>0</IMAGETYPE><CROPMODE>0</CROPMODE><HFOV>100</HFOV><VFOV>0</VFOV>
+    <CROPLEFT>10</CROPLEFT><CROPRIGHT>1910</CROPRIGHT><CROPTOP>20</CROPTOP><CROPBOTTOM>1060</CROPBOTTOM>
+    <Alpha>0.01</Alpha><Beta>-0.02</Beta><Gamma>0.03</Gamma><ShiftX>1.5</ShiftX><ShiftY>-2.5</ShiftY>
+    <ShearX>0</ShearX><ShearY>0</ShearY>
+  </GlobalInfo>
+  <VIDEO><YAW>10.5</YAW><PITCH>-2</PITCH><ROLL>1</ROLL></VIDEO>
+  <VIDEO><YAW> 190 </YAW><PITCH>0</PITCH><ROLL>0</ROLL></VIDEO>
+</Root>
+"""
+
+
+def test_xml_per_camera_layout_equals_pts(built_lib, tmp_path):
+    xml = P.load_photo_params(_write(tmp_path, XML_PER_CAMERA, "rig.xml"))
+    pts = P.load_photo_params(_write(tmp_path, PTS))
+    assert len(xml) == 2
+    # the first camera is the .pts file's first camera, field for field
+    assert xml[0] == pts[0]
+    b = xml[1]
+    assert b["image_type"] == 1 and (b["yaw"], b["pitch"]) == (180, 5)
+    assert (b["circle_x"], b["circle_y"], b["circle_r"]) == (640, 480, 470)
+
+
+def test_xml_global_info_layout(built_lib, tmp_path):
+    cams = P.load_photo_params(_write(tmp_path, XML_GLOBAL, "rig.cfg"))  # any extension but .pts is XML
+    assert len(cams) == 2
+    pts = P.load_photo_params(_write(tmp_path, PTS))
+    assert cams[0] == pts[0]
+    assert cams[1]["yaw"] == 190 and cams[1]["crop_width"] == 1900
+    for c in cams:
+        assert (c["hfov"], c["shift_x"], c["alpha"]) == (100, 1.5, 0.01)
+
+
+def test_xml_layouts_fall_back_and_fail(built_lib, tmp_path):
+    # a camera element without IMAGETYPE: not the per-camera layout, and no GlobalInfo either
+    broken = XML_PER_CAMERA.replace("<IMAGETYPE>1</IMAGETYPE>", "")
+    assert P.load_photo_params(_write(tmp_path, broken, "a.xml")) == []
+    # not a number, unclosed elements, no Root: no cameras
+    assert P.load_photo_params(_write(tmp_path, XML_GLOBAL.replace(">100<", ">x<"), "b.xml")) == []
+    assert P.load_photo_params(_write(tmp_path, "<Root><POSITION>", "c.xml")) == []
+    assert P.load_photo_params(_write(tmp_path, "<Other/>", "d.xml")) == []
+    r = P.CudaPanoramaRender2()
+    assert not r.prepare_file(_write(tmp_path, "<Root/>", "e.xml"), 1, 8, (1920, 1080), (2048, 1024))
+    assert "load photo params failed" in r.last_error
+
+
 def test_other_files_are_rejected(built_lib, tmp_path):
-    with pytest.raises(P.PsError) as e:
-        P.load_photo_params(_write(tmp_path, "<Root/>", "rig.xml"))
-    assert "ticpp" in str(e.value)
     with pytest.raises(P.PsError):
         P.load_photo_params(_write(tmp_path, PTS, "noextension"))
     with pytest.raises(P.PsError):
@@ -59,6 +127,20 @@ def test_other_files_are_rejected(built_lib, tmp_path):
 @pytest.mark.gpu
 def test_prepare_file_equals_prepare(cuda, tmp_path):
     path = _write(tmp_path, PTS)
+    params = P.load_photo_params(path)
+    a, b = P.CudaPanoramaRender2(), P.CudaPanoramaRender2()
+    assert a.prepare_file(path, 1, 6, (1920, 1080), (512, 256), check=True)
+    assert b.prepare(params, 1, 6, (1920, 1080), (512, 256), check=True)
+    for i in range(len(params)):
+        for what in (0, 1, 3):
+            ea = a.export(what, i, 0, (256, 512), np.float32 if what < 2 else np.uint8)
+            eb = b.export(what, i, 0, (256, 512), np.float32 if what < 2 else np.uint8)
+            assert np.array_equal(ea, eb)
+
+
+@pytest.mark.gpu
+def test_prepare_xml_file_equals_prepare(cuda, tmp_path):
+    path = _write(tmp_path, XML_PER_CAMERA, "rig.xml")
     params = P.load_photo_params(path)
     a, b = P.CudaPanoramaRender2(), P.CudaPanoramaRender2()
     assert a.prepare_file(path, 1, 6, (1920, 1080), (512, 256), check=True)
