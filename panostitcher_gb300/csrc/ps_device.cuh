@@ -43,11 +43,7 @@ struct LevelDev {
 
 // Work items (one per tile), resident per rig and built at prepare time.
 struct RemapItem { uint16_t cam, pad; uint16_t tx, ty; uint32_t mapTile; };
-// The source texels a remap tile's bilinear taps read: columns x0 .. x0 + w - 1
-// (x0 a multiple of 4, w a multiple of 4, so every row of BGR32 texels is a
-// whole number of 16-byte chunks) and rows y0 .. y0 + h - 1.  w = 0: no
-// valid map value in the tile.  Built at prepare, one per remap item.
-struct RemapBox { uint16_t x0, y0, w, h; };
+
 struct DownItem { uint8_t cam, level; uint16_t tx, ty; uint16_t pad; };   // level = output level
 // A blend tile lists the cameras whose weight touches it: up to 8 inline,
 // more through RigDev::camLists (cams[0..3] then hold the uint32 offset).
@@ -82,7 +78,6 @@ struct RigDev {
     // linear-blend mode: the remap items (tile-major) and their weights,
     // 512 floats per item in the layout of the maps
     const RemapItem* remapItems;
-    const RemapBox* remapBoxes;  // multiband mode: one per remap item, in item order
     const float* linWeights;
 };
 

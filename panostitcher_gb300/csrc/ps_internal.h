@@ -134,10 +134,6 @@ cudaError_t launchUnion(const uint8_t* cov, int n, int W, int H, long long maskS
                         int tw, int th, int tilesX, int* tileCounts, unsigned long long* total,
                         cudaStream_t st);
 // copy full-canvas maps into tile-compact float2 storage
-// per remap item (in item order), the box of source texels its taps read;
-// maps in tile-compact order (item k's tile is maps + k * 512: items are
-// numbered in mapTile order)
-cudaError_t launchRemapBoxes(const float2* maps, int nitems, int sw, int sh, RemapBox* boxes, cudaStream_t st);
 cudaError_t launchCompactMaps(const float* xmap, const float* ymap, int W, int H, long long maskStride,
                               const RemapItem* items, int nitems, float2* maps, cudaStream_t st);
 // int16x4 / uint8x4 images -> uchar4 level 0, checking range and zero outside coverage

@@ -127,17 +127,11 @@ __device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, lo
 }
 
 // Level-0 remap over the covered 32x16 tiles of every camera; each thread
-// remaps two pixels (rows ly and ly + 8).  Tiles flow through a ring of
-// shared-memory stages.  Warp 0 takes the next tile from a per-launch
-// counter and stages it with bulk asynchronous copies (the TMA engine's
-// non-tensor mode) completing on the stage's "full" mbarrier: the tile's
-// map (512 float2, contiguous in the tile-compact layout), its camera's LUT,
-// and -- for BGR32 sources whose rows are 16-byte aligned -- every row of the
-// tile's source box (the texels its taps read, prepared as RemapBox), so the
-// gathers read shared memory instead of waiting on HBM.  A tile whose box
-// does not fit a stage, or whose source is BGR24 or unaligned, gathers from
-// global memory as before.  All eight warps compute; each releases a stage
-// on its "empty" mbarrier.  Every wait is bounded (status bit 4 on timeout).
+// remaps two pixels (rows ly and ly + 8) so two independent gathers are in
+// flight; the tile's map is 512 consecutive float2.  A CTA walks a
+// contiguous run of items (camera-major, so the camera rarely changes): the
+// camera's constants and LUT are reloaded only when it does, and the next
+// item's map is loaded before the current item's gathers.
 struct RemapSeg {
     const RemapItem* items;
     int prefix, end;
@@ -152,194 +146,100 @@ __device__ __forceinline__ RemapSeg remapSeg(const Segment* segs, int nsegs, int
             sg.frame};
 }
 
-#ifndef PS_REMAP_STAGES
-#define PS_REMAP_STAGES 2
-#endif
-#ifndef PS_REMAP_TEX_WORDS
-#define PS_REMAP_TEX_WORDS 4096
-#endif
-constexpr int kRStages = PS_REMAP_STAGES;
-constexpr int kRTexWords = PS_REMAP_TEX_WORDS;  // source texels per stage (16 KB; 0: gathers from global)
-struct alignas(16) RemapStage {
-    float2 map[kRemapTW * kRemapTH];
-    uint8_t lut[768];
-    uint32_t tex[kRTexWords > 0 ? kRTexWords : 4];
-};
-constexpr size_t kRemapSmem = sizeof(RemapStage) * kRStages;
+// Items are handed out in chunks of kRemapChunk through `counter` (zero at
+// launch); the next chunk is fetched one chunk ahead, so the next item and
+// its map are always known before the current item is gathered.
+constexpr int kRemapChunk = 8;
 
-// What the compute warps need of a staged tile besides the stage itself.
-struct RemapUnit {
-    const uint8_t* base;  // source frame (direct gathers)
-    uint32_t* G;          // the camera's level 0
-    long long pitch;
-    int gpitch, W, H, sw, sh, fmt;
-    int tx, ty;
-    int valid, staged;
-    int bx0, by0, bw;     // staged box: origin and row length in texels
-};
-
-// One pixel's taps from the staged box (coordinates relative to its origin).
-__device__ __forceinline__ void remapFetchStaged(float2 m, const uint32_t* tex, int bx0, int by0, int bw, int sw,
-                                                 int sh, RemapTap& p)
-{
-    p.x0 = -1;
-    if (!(m.x >= 0.f && m.y >= 0.f && m.x < (float)sw && m.y < (float)sh)) return;
-    const float tx = __fadd_rz(m.x, 8388608.f), ty = __fadd_rz(m.y, 8388608.f);  // 2^23 + floor
-    const int x0 = __float_as_int(tx) - 0x4B000000, y0 = __float_as_int(ty) - 0x4B000000;
-    const int x1 = min(x0 + 1, sw - 1), y1 = min(y0 + 1, sh - 1);
-    const uint32_t* r0 = tex + (y0 - by0) * bw - bx0;
-    const uint32_t* r1 = tex + (y1 - by0) * bw - bx0;
-    p.t00 = r0[x0];
-    p.t01 = r0[x1];
-    p.t10 = r1[x0];
-    p.t11 = r1[x1];
-    p.fx = m.x - (tx - 8388608.f);
-    p.fy = m.y - (ty - 8388608.f);
-    p.x0 = x0;
-    p.y0 = y0;
-}
-
-__global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict__ gsegs, int nsegs, int total,
+__global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict__ segs, int nsegs, int total,
                                                        int* __restrict__ counter)
 {
-    extern __shared__ __align__(16) unsigned char r_smem[];
-    RemapStage* stage = reinterpret_cast<RemapStage*>(r_smem);
-    __shared__ RemapUnit info[kRStages];
-    __shared__ uint64_t full[kRStages], empty[kRStages];
-    __shared__ int s_timeout;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < kRStages; k++) {
-            mbarInit(&full[k], 1);
-            mbarInit(&empty[k], kThreads / 32);
-        }
-        s_timeout = 0;
-    }
-    __syncthreads();
-
-    // ---- the staging warp's state (warp 0)
-    int s = 0, srcRows = 0, done = 0;
-    RemapSeg cur{};
-    if (warp == 0 && total > 0) {
-        s = 0;
-        cur = remapSeg(gsegs, nsegs, 0, total);
-    }
-    // Stage u: take an item, write its unit, expect its bytes, copy its map
-    // and LUT.  The source rows follow in stageRows (after the wait for the
-    // previous kernel, which may have written the source frames).
-    RemapBox box{};
-    auto stageHead = [&](int u) {
-        const int stg = u % kRStages;
-        if (u >= kRStages && !mbarWait(&empty[stg], ((u / kRStages) - 1) & 1)) s_timeout = 1;
-        int it = 0;
-        if (lane == 0) it = atomicAdd(counter, 1);
-        it = __shfl_sync(0xffffffffu, it, 0);
-        RemapUnit ui{};
-        srcRows = 0;
-        if (it >= total) {
-            done = 1;
-            if (lane == 0) {
-                info[stg] = ui;  // valid = 0: the end
-                mbarArrive(&full[stg]);
-            }
-            return;
-        }
-        if (it >= cur.end) {
-            s = findSegment(gsegs, nsegs, it, s);
-            cur = remapSeg(gsegs, nsegs, s, total);
-        }
-        const RemapItem item = cur.items[it - cur.prefix];
-        const RigDev& R = *cur.R;
-        const FrameDev& F = *cur.F;
-        box = R.remapBoxes[it - cur.prefix];
-        ui.valid = 1;
-        ui.base = F.src[item.cam];
-        ui.pitch = F.srcPitch[item.cam];
-        ui.fmt = F.srcFmt;
-        ui.G = reinterpret_cast<uint32_t*>(R.lv[0].G) + (size_t)item.cam * R.lv[0].camStride;
-        ui.gpitch = R.lv[0].pitch;
-        ui.W = R.W;
-        ui.H = R.H;
-        ui.sw = R.srcW;
-        ui.sh = R.srcH;
-        ui.tx = item.tx;
-        ui.ty = item.ty;
-        const bool aligned = ((reinterpret_cast<uintptr_t>(ui.base) | (uintptr_t)ui.pitch) & 15) == 0;
-        ui.staged = kRTexWords > 0 && ui.fmt == PS_FMT_BGR32 && aligned && box.w > 0 && box.x0 + box.w <= ui.sw &&
-                    (int)box.w * box.h <= kRTexWords;
-        ui.bx0 = box.x0;
-        ui.by0 = box.y0;
-        ui.bw = box.w;
-        if (ui.staged) srcRows = box.h;
-        const uint32_t bytes = sizeof(float2) * kRemapTW * kRemapTH + 768 + (uint32_t)srcRows * box.w * 4;
-        fenceProxyAsync();
-        if (lane == 0) {
-            info[stg] = ui;
-            mbarArriveExpectTx(&full[stg], bytes);
-        }
-        __syncwarp();
-        if (lane == 0)
-            bulkCopy(stage[stg].map, R.maps + (size_t)item.mapTile * (kRemapTW * kRemapTH),
-                     sizeof(float2) * kRemapTW * kRemapTH, &full[stg]);
-        else if (lane == 1)
-            bulkCopy(stage[stg].lut, F.luts + item.cam * 768, 768, &full[stg]);
+    __shared__ uint8_t lut[3 * 256];
+    __shared__ int s_grab;
+    auto grab = [&] {  // all threads together
+        __syncthreads();
+        if (threadIdx.x == 0) s_grab = atomicAdd(counter, kRemapChunk);
+        __syncthreads();
+        return s_grab;
     };
-    auto stageRows = [&](int u) {
-        const int stg = u % kRStages;
-        if (!srcRows) return;
-        const RemapUnit& ui = info[stg];
-        for (int r = lane; r < srcRows; r += 32)
-            bulkCopy(stage[stg].tex + r * ui.bw, ui.base + (size_t)(ui.by0 + r) * ui.pitch + (size_t)ui.bx0 * 4,
-                     (uint32_t)ui.bw * 4, &full[stg]);
-    };
-
-    // The hand-out counter, items, boxes, maps and LUTs are written before
-    // the launch sequence, not by a kernel: the first tile's map and LUT are
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    // The hand-out counter, items, descriptors and maps are written before
+    // the launch sequence, not by a kernel: the first chunk and its map are
     // fetched while the previous kernel finishes.
-    if (warp == 0) stageHead(0);
+    int it = grab(), end = 0, nextBegin = total, s = 0;
+    RemapSeg cur{};
+    RemapItem item{};
+    float2 m0{}, m1{};
+    if (it < total) {
+        end = min(it + kRemapChunk, total);
+        nextBegin = grab();
+        s = findSegment(segs, nsegs, it, 0);
+        cur = remapSeg(segs, nsegs, s, total);
+        item = cur.items[it - cur.prefix];
+        const float2* mt = cur.R->maps + (size_t)item.mapTile * (kRemapTW * kRemapTH);
+        m0 = __ldg(mt + threadIdx.x);
+        m1 = __ldg(mt + threadIdx.x + kThreads);
+    }
     waitPrevGrid();
     allowNextGrid();
-    if (warp == 0) {
-        __syncwarp();
-        stageRows(0);
+    if (it >= total) return;
+    // constants of the loaded camera
+    int camSeg = -1, cam = -1;
+    const uint8_t* base = nullptr;
+    long long pitch = 0;
+    int fmt = 0, sw = 0, sh = 0, W = 0, H = 0, gpitch = 0;
+    uint32_t* G = nullptr;
+    for (;;) {
+        if (item.cam != cam || s != camSeg) {  // uniform across the block
+            const FrameDev& F = *cur.F;
+            const RigDev& R = *cur.R;
+            cam = item.cam;
+            camSeg = s;
+            base = F.src[cam];
+            pitch = F.srcPitch[cam];
+            fmt = F.srcFmt;
+            sw = R.srcW;
+            sh = R.srcH;
+            W = R.W;
+            H = R.H;
+            gpitch = R.lv[0].pitch;
+            G = reinterpret_cast<uint32_t*>(R.lv[0].G) + (size_t)cam * R.lv[0].camStride;
+            __syncthreads();
+            const uint8_t* src = F.luts + cam * 768;
+            for (int k = threadIdx.x; k < 768; k += kThreads) lut[k] = __ldg(src + k);
+            __syncthreads();
+        }
+        // the next item (the rest of this chunk, else the next chunk's first) and its map
+        const int nit = it + 1 < end ? it + 1 : (nextBegin < total ? nextBegin : -1);
+        RemapItem nitem = item;
+        float2 n0 = m0, n1 = m1;
+        if (nit >= 0) {
+            if (nit >= cur.end) {
+                s = findSegment(segs, nsegs, nit, s);
+                cur = remapSeg(segs, nsegs, s, total);
+            }
+            nitem = cur.items[nit - cur.prefix];
+            const float2* nt = cur.R->maps + (size_t)nitem.mapTile * (kRemapTW * kRemapTH);
+            n0 = __ldg(nt + threadIdx.x);
+            n1 = __ldg(nt + threadIdx.x + kThreads);
+        }
+        const uint32_t v0 = remapPixel(m0, base, pitch, fmt, sw, sh, lut);
+        const uint32_t v1 = remapPixel(m1, base, pitch, fmt, sw, sh, lut);
+        const int x = item.tx * kRemapTW + lx, y0 = item.ty * kRemapTH + ly, y1 = y0 + 8;
+        if (x < W) {
+            if (y0 < H) G[(size_t)y0 * gpitch + x] = v0;
+            if (y1 < H) G[(size_t)y1 * gpitch + x] = v1;
+        }
+        if (nit < 0) break;
+        if (it + 1 >= end) {  // into the next chunk; fetch the one after it
+            end = min(nextBegin + kRemapChunk, total);
+            nextBegin = grab();
+        }
+        it = nit;
+        item = nitem;
+        m0 = n0;
+        m1 = n1;
     }
-    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
-    for (int u = 0;; u++) {
-        if (warp == 0 && !done) {
-            stageHead(u + kRStages - 1);
-            __syncwarp();
-            stageRows(u + kRStages - 1);
-        }
-        const int stg = u % kRStages;
-        if (!mbarWait(&full[stg], (u / kRStages) & 1)) s_timeout = 1;
-        const RemapUnit& ui = info[stg];  // rewritten only after every warp releases the stage
-        if (!ui.valid) break;
-        const RemapStage& S = stage[stg];
-        const float2 m0 = S.map[threadIdx.x], m1 = S.map[threadIdx.x + kThreads];
-        RemapTap p0, p1;
-        if (ui.staged) {
-            remapFetchStaged(m0, S.tex, ui.bx0, ui.by0, ui.bw, ui.sw, ui.sh, p0);
-            remapFetchStaged(m1, S.tex, ui.bx0, ui.by0, ui.bw, ui.sw, ui.sh, p1);
-        } else {
-            remapFetch(m0, ui.base, ui.pitch, ui.fmt, ui.sw, ui.sh, p0);
-            remapFetch(m1, ui.base, ui.pitch, ui.fmt, ui.sw, ui.sh, p1);
-        }
-        const uint32_t v0 = remapFinish(p0, m0, S.lut);
-        const uint32_t v1 = remapFinish(p1, m1, S.lut);
-        const int x = ui.tx * kRemapTW + lx, y0 = ui.ty * kRemapTH + ly, y1 = y0 + 8;
-        if (x < ui.W) {
-            if (y0 < ui.H) ui.G[(size_t)y0 * ui.gpitch + x] = v0;
-            if (y1 < ui.H) ui.G[(size_t)y1 * ui.gpitch + x] = v1;
-        }
-        __syncwarp();
-        if (lane == 0) mbarArrive(&empty[stg]);
-    }
-    // Timeouts of the staging warp precede its terminal arrive, which every
-    // warp has waited on; the others' meet here.
-    __syncthreads();
-    if (s_timeout && threadIdx.x == 0)
-        for (int k = 0; k < nsegs; k++)
-            if (gsegs[k].frame->status) atomicOr(gsegs[k].frame->status, 4);
 }
 
 // ============================================================================
@@ -1279,6 +1179,7 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
         mbarInit(&never, 1);
         s_timeout = 0;
     }
+    if (threadIdx.x < kBStages) info[threadIdx.x].valid = 0;  // a stage read after a wait ran out ends the loop
     __syncthreads();
     const int lane = threadIdx.x & 31;
 
@@ -1774,27 +1675,10 @@ static cudaError_t launchPdl(void (*kernel)(Args...), int grid, int block, cudaS
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
-template <class... Args>
-static cudaError_t launchPdlSmem(void (*kernel)(Args...), int grid, int block, size_t smem, cudaStream_t st,
-                                 Args... args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, args...);
-}
-
 int residentCtasPerSm(int kind)
 {
     switch (kind) {
-    case 0: return residentPerSm<k_remap>(kThreads, kRemapSmem);
+    case 0: return residentPerSm<k_remap>(kThreads);
     case 1: return residentPerSm<k_pyrdown>(kThreads);
     case 2: return residentPerSm<k_blend>(kBlendThreads);
     default: return 1;
@@ -1804,11 +1688,8 @@ int residentCtasPerSm(int kind)
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_remap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRemapSmem);
-    if (attr != cudaSuccess) return attr;
-    return launchPdlSmem(k_remap, gridFor(total, residentPerSm<k_remap>(kThreads, kRemapSmem), perSm), kThreads,
-                         kRemapSmem, st, segs, nsegs, total, counter);
+    return launchPdl(k_remap, gridFor(total, residentPerSm<k_remap>(kThreads), perSm), kThreads, st, segs, nsegs,
+                     total, counter);
 }
 
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st)

@@ -577,43 +577,6 @@ __global__ void k_compact_maps(const float* __restrict__ xmap, const float* __re
     maps[(size_t)it.mapTile * (kRemapTW * kRemapTH) + threadIdx.x] = v;
 }
 
-// Source footprint of each remap tile: the bounding box of its taps
-// (x0, y0) .. (min(x0 + 1, sw - 1), min(y0 + 1, sh - 1)) over the valid
-// map values, columns widened to whole 16-byte chunks of BGR32 texels.
-__global__ void k_remap_boxes(const float2* __restrict__ maps, int nitems, int sw, int sh, RemapBox* boxes)
-{
-    __shared__ int s_box[4];
-    if (threadIdx.x < 4) s_box[threadIdx.x] = threadIdx.x < 2 ? 0x7FFFFFFF : -1;
-    __syncthreads();
-    const float2 m = maps[(size_t)blockIdx.x * (kRemapTW * kRemapTH) + threadIdx.x];
-    if (m.x >= 0.f && m.y >= 0.f && m.x < (float)sw && m.y < (float)sh) {
-        const int x0 = (int)m.x, y0 = (int)m.y;  // non-negative: truncation is the floor
-        atomicMin(&s_box[0], x0);
-        atomicMin(&s_box[1], y0);
-        atomicMax(&s_box[2], min(x0 + 1, sw - 1));
-        atomicMax(&s_box[3], min(y0 + 1, sh - 1));
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        RemapBox b = {0, 0, 0, 0};
-        if (s_box[2] >= 0) {
-            const int ax0 = s_box[0] & ~3;
-            b.x0 = (uint16_t)ax0;
-            b.y0 = (uint16_t)s_box[1];
-            b.w = (uint16_t)min(65532, (s_box[2] + 1 - ax0 + 3) & ~3);
-            b.h = (uint16_t)min(65535, s_box[3] + 1 - s_box[1]);
-        }
-        boxes[blockIdx.x] = b;
-    }
-}
-
-cudaError_t launchRemapBoxes(const float2* maps, int nitems, int sw, int sh, RemapBox* boxes, cudaStream_t st)
-{
-    if (nitems <= 0) return cudaSuccess;
-    k_remap_boxes<<<nitems, kRemapTW * kRemapTH, 0, st>>>(maps, nitems, sw, sh, boxes);
-    return cudaGetLastError();
-}
-
 cudaError_t launchCompactMaps(const float* xmap, const float* ymap, int W, int H, long long maskStride,
                               const RemapItem* items, int nitems, float2* maps, cudaStream_t st)
 {

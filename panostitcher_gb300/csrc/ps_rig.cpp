@@ -122,7 +122,6 @@ void Rig::clear()
     }
     nextSlot_ = lastSlot_ = 0;
     maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset(); planar_.reset();
-    dRemapBox_.reset();
     imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
     hRemap_.clear();
     hDown_.clear();
@@ -183,7 +182,7 @@ long long Rig::residentBytes() const
     }
     b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
     b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
-    b += dLinear_.bytes() + linW_.bytes() + planar_.bytes() + dRemapBox_.bytes();
+    b += dLinear_.bytes() + linW_.bytes() + planar_.bytes();
     return b;
 }
 
@@ -202,8 +201,8 @@ static void validateParams(const ps_photo_param* params, int n, int srcW, int sr
 }
 
 // Upper bound of the work lists and descriptors a rig of this shape holds:
-// every pyrDown and blend tile listed (with its camera list), remap items and
-// boxes for every camera's level-0 tiles, one descriptor per state slot.
+// every pyrDown and blend tile listed (with its camera list), remap items for
+// every camera's level-0 tiles, one descriptor per state slot.
 static long long listBytes(int W, int H, int n, int L, int slots)
 {
     long long b = (long long)sizeof(RigDev) * slots + 4096;
@@ -215,7 +214,7 @@ static long long listBytes(int W, int H, int n, int L, int slots)
         w = (w + 1) / 2;
         h = (h + 1) / 2;
     }
-    return b + (long long)divUp(W, kRemapTW) * divUp(H, kRemapTH) * n * (sizeof(RemapItem) + sizeof(RemapBox));
+    return b + (long long)divUp(W, kRemapTW) * divUp(H, kRemapTH) * n * sizeof(RemapItem);
 }
 
 long long Rig::estimateBlenderBytes(int W, int H, int n, int maxLevels, int slots)
@@ -536,10 +535,6 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         maps_.alloc(hRemap_.size() * kRemapTW * kRemapTH * sizeof(float2));
         PS_CUDA(launchCompactMaps(xmap, ymap, W, H, (long long)npx, dRemap_.as<RemapItem>(), (int)hRemap_.size(),
                                   maps_.as<float2>(), st));
-        // item k has mapTile k here (items are numbered as they are listed)
-        dRemapBox_.alloc(hRemap_.size() * sizeof(RemapBox));
-        PS_CUDA(launchRemapBoxes(maps_.as<float2>(), (int)hRemap_.size(), srcW_, srcH_, dRemapBox_.as<RemapBox>(),
-                                 st));
     }
 
     // device descriptor
@@ -553,7 +548,6 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     d.srcW = srcW_;
     d.srcH = srcH_;
     d.maps = maps_.as<float2>();
-    d.remapBoxes = dRemapBox_.as<RemapBox>();
     d.unionMask = union_.as<uint8_t>();
     d.camLists = dCams_.as<uint8_t>();
     d.downItems = dDown_.as<DownItem>();

@@ -197,7 +197,7 @@ private:
     LevelBufs lv_[PS_MAX_LEVELS + 1];
     DevBuf maps_, union_, inputs_, output_, covDev_, status_, imgArgs_, planar_;
     long long inPitch_ = 0, budget_ = 0;
-    DevBuf dDesc_, dRemap_, dRemapBox_, dDown_, dBlend_, dCams_;
+    DevBuf dDesc_, dRemap_, dDown_, dBlend_, dCams_;
     std::vector<RemapItem> hRemap_;
     int downOff_[PS_MAX_LEVELS + 1] = {}, downCnt_[PS_MAX_LEVELS + 1] = {};
     int blendOff_[PS_MAX_LEVELS + 1] = {}, blendCnt_[PS_MAX_LEVELS + 1] = {};
