@@ -208,6 +208,20 @@ int ps_render_set_frames_in_flight(ps_render* r, int n);
    stitches the same bytes. */
 int ps_render_set_memory_budget(ps_render* r, long long bytes);
 int ps_render_is_low_memory(const ps_render* r);
+/* The map-free remap of the reference's low-memory path
+   (cudaReprojectTo16S(src, dst, dstSize, param), source/CudaAccel/
+   CudaReproject.cu:559-602,722-742, which computes dstToSrc per pixel).
+   With enable != 0 the next multiband prepare keeps no maps: the remap
+   computes each pixel's source coordinate in fp32 from the camera
+   parameters (the reference's dstToSrc does it in double, which GB300 runs
+   at a small fraction of its fp32 rate), and takes the coverage from the
+   FP64 geometry of prepare.  Level 0 is then within +-1 of the exact remap
+   per channel, not bit for bit, and the blend of it is exact.  prepare also
+   turns it on by itself when even one frame in flight with resident maps
+   does not fit (ps_render_is_low_memory).  ps_render_is_map_free reports
+   the mode of the last prepare.  The maps cannot be exported then. */
+int ps_render_set_map_free(ps_render* r, int enable);
+int ps_render_is_map_free(const ps_render* r);
 /* The prepared render's frames in flight (0 before prepare). */
 int ps_render_get_frames_in_flight(const ps_render* r);
 /* CudaPanoramaRender2::render with decoder frames: src holds num_src YUV420P
@@ -276,7 +290,8 @@ int ps_render_get_input_buffer(ps_render* r, int cam, void** data, long long* pi
    2 coverage mask (uint8 0/255), 3 seam mask (uint8 0/255),
    4 weight pyramid level `level` (int16), 5 alpha pyramid level `level`
    (int32, the raw 5x5 sum as pyrDown16SC1To32SC1 writes it; level >= 1),
-   6 linear-blend weight (float, linear-blend mode). */
+   6 linear-blend weight (float, linear-blend mode), 7 level 0 of the last
+   render (uint8 x4 B,G,R,0 per pixel: the remap's output; synchronises). */
 int ps_render_export(const ps_render* r, int what, int cam, int level, void* host_out, long long bytes);
 /* Debug copy of the collapsed result at level `level` >= 1 of the last
    render (int16 x4 per pixel), for bit-exact checks of the pipeline. */
@@ -414,6 +429,13 @@ int ps_cvt_yuv_to_bgr32(const ps_planar_image* src, const ps_image* dst, void* s
    has written itself. */
 int ps_nearest_axis_seams_no_alloc(const ps_photo_param* params, int num_params, int src_w, int src_h, int dst_w,
                                    int dst_h, uint8_t* seams, void* stream);
+
+/* The bounds-checked build (no reference counterpart): libpanostitch_checked.so
+   is the same library with every global access of the stitch kernels checked
+   against the extent of its buffer; an access outside is not made and is
+   counted.  Returns the count since the last reset (waits for the device),
+   or -1 in the normal build.  reset != 0 sets it back to 0. */
+long long ps_debug_bounds_violations(int reset);
 
 /* ==== multiband blender: CudaTilingMultibandBlendFast (CudaInterface.h:45-82) ==== */
 typedef struct ps_blender ps_blender;

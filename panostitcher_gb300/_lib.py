@@ -11,7 +11,10 @@ import os
 import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpanostitch.so")
+# PS_LIBRARY=checked selects the bounds-checked build (libpanostitch_checked.so,
+# every kernel access checked against its buffer; see ps_debug_bounds_violations).
+LIB_PATH = os.path.join(HERE, "libpanostitch_checked.so" if os.environ.get("PS_LIBRARY") == "checked"
+                        else "libpanostitch.so")
 
 PS_OK, PS_EINVAL, PS_ENOMEM, PS_ECUDA, PS_ETIMEOUT, PS_ESTATE = 0, 1, 2, 3, 4, 5
 PS_MAX_LEVELS, PS_MAX_CAMS, PS_MAX_IN_FLIGHT = 16, 64, 8
@@ -19,7 +22,8 @@ PS_FMT_BGR24, PS_FMT_BGR32 = 24, 32
 PS_FMT_YUV420P, PS_FMT_NV12 = 420, 12
 PS_SEAMS_NEAREST_AXIS, PS_SEAMS_DISTANCE = 0, 1
 PS_MEM_HOST, PS_MEM_DEVICE = 0, 1
-EXPORT_XMAP, EXPORT_YMAP, EXPORT_COVERAGE, EXPORT_SEAM, EXPORT_WEIGHT, EXPORT_ALPHA, EXPORT_LINEAR_WEIGHT = range(7)
+(EXPORT_XMAP, EXPORT_YMAP, EXPORT_COVERAGE, EXPORT_SEAM, EXPORT_WEIGHT, EXPORT_ALPHA, EXPORT_LINEAR_WEIGHT,
+ EXPORT_LEVEL0) = range(8)
 
 _STATUS_NAMES = {PS_EINVAL: "PS_EINVAL", PS_ENOMEM: "PS_ENOMEM", PS_ECUDA: "PS_ECUDA",
                  PS_ETIMEOUT: "PS_ETIMEOUT", PS_ESTATE: "PS_ESTATE"}
@@ -101,6 +105,9 @@ _SIGS = [
     ("ps_render_get_frames_in_flight", C.c_int, [C.c_void_p]),
     ("ps_render_set_memory_budget", C.c_int, [C.c_void_p, C.c_longlong]),
     ("ps_render_is_low_memory", C.c_int, [C.c_void_p]),
+    ("ps_render_set_map_free", C.c_int, [C.c_void_p, C.c_int]),
+    ("ps_debug_bounds_violations", C.c_longlong, [C.c_int]),
+    ("ps_render_is_map_free", C.c_int, [C.c_void_p]),
     ("ps_render_render_planar", C.c_int, [C.c_void_p, C.POINTER(PlanarImage), C.c_int, C.c_void_p, C.c_int,
                                           C.POINTER(Image), C.POINTER(PlanarImage), C.c_void_p]),
     ("ps_render_set_graph", C.c_int, [C.c_void_p, C.c_int]),

@@ -15,6 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpanostitch.so")
+# the bounds-checked build: the kernels' translation unit again with
+# -DPS_CHECK_BOUNDS, linked with the same other objects
+LIB_CHECKED = os.path.join(HERE, "libpanostitch_checked.so")
+CHECKED_SRC = "csrc/ps_kernels.cu"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "csrc/ps_kernels.cu": [],
@@ -49,6 +53,7 @@ def _headers():
 
 
 def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
+    """Builds libpanostitch.so and its bounds-checked twin libpanostitch_checked.so."""
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
@@ -62,6 +67,11 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
             cmd = [cc] + COMMON + extra + (["-Xptxas", "-v"] if ptxas_info and src.endswith(".cu") else []) + \
                   ["-c", path, "-o", obj]
             jobs.append(cmd)
+    checked_obj = os.path.join(BUILD, "ps_kernels_checked.cu.o")
+    checked_path = os.path.join(HERE, CHECKED_SRC)
+    checked_new = force or _stale(checked_obj, [checked_path] + hdrs)
+    if checked_new:
+        jobs.append([cc] + COMMON + SOURCES[CHECKED_SRC] + ["-DPS_CHECK_BOUNDS", "-c", checked_path, "-o", checked_obj])
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
         return cmd, r
@@ -71,8 +81,11 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed on {cmd[-3]}")
-    if force or jobs or not os.path.exists(LIB):
-        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static", "-Xlinker", "-z,defs"] + \
+    kernels_obj = os.path.join(BUILD, os.path.basename(CHECKED_SRC) + ".o")
+    for lib, lib_objs in ((LIB, objs), (LIB_CHECKED, [checked_obj if o == kernels_obj else o for o in objs])):
+        if not (force or jobs or not os.path.exists(lib)):
+            continue
+        cmd = [cc] + ARCH + ["-shared", "-o", lib] + lib_objs + ["-cudart", "static", "-Xlinker", "-z,defs"] + \
               ["-lpthread", "-ldl", "-lrt"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if verbose or r.returncode != 0:

@@ -348,6 +348,16 @@ int ps_render_set_memory_budget(ps_render* r, long long bytes)
 
 int ps_render_is_low_memory(const ps_render* r) { return r && r->rig.ready() && r->rig.lowMemory() ? 1 : 0; }
 
+int ps_render_set_map_free(ps_render* r, int enable)
+{
+    return guarded([&] {
+        if (!r) fail(PS_EINVAL, "render is NULL");
+        r->rig.setMapFree(enable != 0);
+    });
+}
+
+int ps_render_is_map_free(const ps_render* r) { return r && r->rig.ready() && r->rig.mapFree() ? 1 : 0; }
+
 int ps_render_render_planar(ps_render* r, const ps_planar_image* src, int num_src, const uint8_t* luts,
                             int num_luts, const ps_image* dst, const ps_planar_image* ydst, void* stream)
 {
@@ -625,6 +635,8 @@ int ps_cvt_yuv_to_bgr32(const ps_planar_image* src, const ps_image* dst, void* s
         PS_CUDA(ps::launchYuvToBgr32(f, toStream(stream)));
     });
 }
+
+long long ps_debug_bounds_violations(int reset) { return ps::boundsViolations(reset != 0); }
 
 int ps_get_lut(double k, uint8_t* lut256)
 {

@@ -58,11 +58,28 @@ constexpr int kTileUniform = 1;
 // [first, first + count) of remap items (cameras in index order) covering it.
 struct LinearItem { uint16_t tx, ty; uint32_t first, count; };
 
+// Remap::remapImage's parameters in fp32, for the map-free remap (the
+// reference's dstToSrc, source/CudaAccel/CudaReproject.cu:81-264, keeps them
+// in double).
+struct RemapParamF {
+    int type;  // 0 rectilinear, else fisheye
+    float srcTX, srcTY, destTX, destTY;
+    float scale0, scale1, shear0, shear1, rot0, rot1;
+    float rad[6];
+    float mt[9];
+    float distance, horizontal, vertical;
+};
+
 struct RigDev {
     int n, L, W, H;
     int full;                 // union of coverages == whole canvas
     int srcW, srcH;
-    const float2* maps;       // tile-compact maps of all cameras
+    const float2* maps;       // tile-compact maps of all cameras (NULL when map-free)
+    int numRemapItems;        // tiles of the maps (and of the map-free coverage words)
+    // map-free remap: per camera its parameters, per remap tile (in map-tile
+    // order) its coverage as 16 words of 32 bits, one word per tile row
+    const RemapParamF* camsF;
+    const uint32_t* covTiles;
     const uint8_t* unionMask; // level-0 union coverage (0/255), pitch = lv[0].pitch
     const uint8_t* camLists;  // camera indices of blend tiles with more than 8 cameras
     LevelDev lv[PS_MAX_LEVELS + 1];

@@ -134,6 +134,11 @@ cudaError_t launchUnion(const uint8_t* cov, int n, int W, int H, long long maskS
                         int tw, int th, int tilesX, int* tileCounts, unsigned long long* total,
                         cudaStream_t st);
 // copy full-canvas maps into tile-compact float2 storage
+// map-free remap: coverage bits per remap tile (16 words each, map-tile
+// order) and the fp32 parameters of a camera
+cudaError_t launchCovTiles(const uint8_t* cov, int W, int H, long long maskStride, const RemapItem* items,
+                           int nitems, uint32_t* words, cudaStream_t st);
+RemapParamF remapParamF(const RemapDev& r);
 cudaError_t launchCompactMaps(const float* xmap, const float* ymap, int W, int H, long long maskStride,
                               const RemapItem* items, int nitems, float2* maps, cudaStream_t st);
 // int16x4 / uint8x4 images -> uchar4 level 0, checking range and zero outside coverage
@@ -169,6 +174,9 @@ struct LaunchShape {
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st);
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
 // counter: a zeroed int the launch hands its tiles out through
+// Accesses the checked build's kernels refused since the last reset
+// (waits for the device); -1 in the normal build, -2 on a CUDA error.
+long long boundsViolations(bool reset);
 // probePolls > 0: the failure-path test of the bounded waits (k_blend)
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, int probePolls,
                         cudaStream_t st);

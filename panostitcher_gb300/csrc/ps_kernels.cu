@@ -25,6 +25,66 @@ namespace ps {
 
 __constant__ int c_k5[5] = {1, 4, 6, 4, 1};
 
+// ---- the checked build ---------------------------------------------------------
+// Compiled with -DPS_CHECK_BOUNDS (libpanostitch_checked.so), every global
+// access of the stitch kernels is checked against the extent of the buffer
+// it belongs to.  An access outside is not made -- a load reads 0, a store
+// is dropped, a bulk copy reads from the buffer's start instead, so its
+// byte count still completes its barrier -- and the device-wide violation
+// counter goes up (ps_debug_bounds_violations).  Nothing traps.  In the
+// normal build every check is a constant true.
+#ifdef PS_CHECK_BOUNDS
+__device__ unsigned long long g_boundsViolations;
+#endif
+
+template <class T>
+__device__ __forceinline__ bool inside(const T* p, const void* base, long long bytes)
+{
+#ifdef PS_CHECK_BOUNDS
+    const char* c = reinterpret_cast<const char*>(p);
+    const char* b = static_cast<const char*>(base);
+    if (!base || c < b || c + sizeof(T) > b + bytes) {
+        atomicAdd(&g_boundsViolations, 1ull);
+        return false;
+    }
+#endif
+    return true;
+}
+
+// [p, p + n) inside [base, base + bytes)
+__device__ __forceinline__ bool insideRange(const void* p, long long n, const void* base, long long bytes)
+{
+#ifdef PS_CHECK_BOUNDS
+    const char* c = static_cast<const char*>(p);
+    const char* b = static_cast<const char*>(base);
+    if (!base || c < b || c + n > b + bytes) {
+        atomicAdd(&g_boundsViolations, 1ull);
+        return false;
+    }
+#endif
+    return true;
+}
+
+template <class T>
+__device__ __forceinline__ T ldChecked(const T* p, const void* base, long long bytes)
+{
+    return inside(p, base, bytes) ? __ldg(p) : T{};
+}
+
+// A bulk copy whose source range is checked: outside its buffer it copies
+// from the buffer's start instead, so the barrier still receives its bytes.
+__device__ __forceinline__ void bulkCopyChecked(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                                const void* base, long long ext)
+{
+    if (!insideRange(src, bytes, base, ext)) src = base;
+    bulkCopy(dst, src, bytes, bar);
+}
+
+// Extents of a rig's buffers.
+__device__ __forceinline__ long long gBytes(const RigDev& R, const LevelDev& L) { return (long long)R.n * L.camStride * 4; }
+__device__ __forceinline__ long long wBytes(const RigDev& R, const LevelDev& L) { return (long long)R.n * L.camStride * 2; }
+__device__ __forceinline__ long long cBytes(const LevelDev& L) { return (long long)L.pitch * L.h * 8; }
+
 // ============================================================================
 // Remap of one canvas pixel: cudaTransform (source/CudaAccel/
 // CudaGainAdjust.cu:57-101) fused with the bilinear map remap.  The
@@ -36,10 +96,11 @@ __constant__ int c_k5[5] = {1, 4, 6, 4, 1};
 // is recomputed with the reference's exact sequence of IEEE double
 // operations, so the stored byte equals the double-precision one.
 // ============================================================================
-__device__ __forceinline__ uint32_t loadTexel(const uint8_t* row, int x, int fmt)
+__device__ __forceinline__ uint32_t loadTexel(const uint8_t* row, int x, int fmt, const uint8_t* base, long long bytes)
 {
-    if (fmt == PS_FMT_BGR32) return __ldg(reinterpret_cast<const uint32_t*>(row) + x);
+    if (fmt == PS_FMT_BGR32) return ldChecked(reinterpret_cast<const uint32_t*>(row) + x, base, bytes);
     const uint8_t* p = row + 3 * x;
+    if (!insideRange(p, 3, base, bytes)) return 0;
     return (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8) | ((uint32_t)__ldg(p + 2) << 16);
 }
 
@@ -81,10 +142,11 @@ __device__ __forceinline__ void remapFetch(float2 m, const uint8_t* base, long l
     const int x1 = min(x0 + 1, sw - 1), y1 = min(y0 + 1, sh - 1);
     const uint8_t* r0 = base + (size_t)y0 * pitch;
     const uint8_t* r1 = base + (size_t)y1 * pitch;
-    p.t00 = loadTexel(r0, x0, fmt);
-    p.t01 = loadTexel(r0, x1, fmt);
-    p.t10 = loadTexel(r1, x0, fmt);
-    p.t11 = loadTexel(r1, x1, fmt);
+    const long long bytes = pitch * sh;
+    p.t00 = loadTexel(r0, x0, fmt, base, bytes);
+    p.t01 = loadTexel(r0, x1, fmt, base, bytes);
+    p.t10 = loadTexel(r1, x0, fmt, base, bytes);
+    p.t11 = loadTexel(r1, x1, fmt, base, bytes);
     p.fx = m.x - (tx - 8388608.f);  // exact
     p.fy = m.y - (ty - 8388608.f);
     p.x0 = x0;
@@ -116,6 +178,63 @@ __device__ __forceinline__ uint32_t remapFinish(const RemapTap& p, float2 m, con
         out |= (uint32_t)v << (8 * c);
     }
     return out;
+}
+
+// Map-free remap: the source coordinate of canvas pixel (cx, cy) in fp32,
+// the steps of Remap::remapImage (source/Warp/Remap.cpp:356-514) as the
+// reference's dstToSrc takes them (source/CudaAccel/CudaReproject.cu:81-264),
+// which keeps them in double.  Within about 1e-3 px of the FP64 maps; the
+// caller clamps the result into the frame, coverage comes from the FP64
+// geometry of prepare.
+__device__ __forceinline__ float2 remapPointF(const RemapParamF& m, float cx, float cy)
+{
+    constexpr float kPiF = 3.14159265358979323846f;
+    const float xs = cx - (m.srcTX - 0.5f), ys = cy - (m.srcTY - 0.5f);
+    float xd = xs + m.rot1;
+    while (xd < -m.rot0) xd += 2.f * m.rot0;
+    while (xd > m.rot0) xd -= 2.f * m.rot0;
+    float phi = xd / m.distance;
+    float theta = -ys / m.distance + kPiF / 2.f;
+    if (theta < 0.f) { theta = -theta; phi += kPiF; }
+    if (theta > kPiF) { theta = kPiF - (theta - kPiF); phi += kPiF; }
+    float st, ct, sp, cp;
+    sincosf(theta, &st, &ct);
+    sincosf(phi, &sp, &cp);
+    const float u0 = st * sp, u1 = ct, u2 = st * cp;
+    const float v0 = m.mt[0] * u0 + m.mt[3] * u1 + m.mt[6] * u2;
+    const float v1 = m.mt[1] * u0 + m.mt[4] * u1 + m.mt[7] * u2;
+    const float v2 = m.mt[2] * u0 + m.mt[5] * u1 + m.mt[8] * u2;
+    const float r = sqrtf(v0 * v0 + v1 * v1);
+    const float th0 = r == 0.f ? 0.f : m.distance * atan2f(r, v2) / r;
+    float x = th0 * v0, y = th0 * v1;
+    if (m.type == 0) {
+        const float rr = sqrtf(x * x + y * y);
+        const float th = rr / m.distance;
+        const float rho = th >= kPiF / 2.f ? 1.6e16f : (th == 0.f ? 1.f : tanf(th) / th);
+        x *= rho;
+        y *= rho;
+    }
+    x *= m.scale0;
+    y *= m.scale1;
+    const float rt = sqrtf(x * x + y * y) / m.rad[4];
+    const float sc = rt < m.rad[5] ? ((m.rad[3] * rt + m.rad[2]) * rt + m.rad[1]) * rt + m.rad[0] : 1000.f;
+    x *= sc;
+    y *= sc;
+    y += m.vertical;
+    x += m.horizontal;
+    const float xo = x + m.shear0 * y, yo = y + m.shear1 * x;
+    return make_float2(xo + (m.destTX - 0.5f), yo + (m.destTY - 0.5f));
+}
+
+// The map value of a map-free pixel: -1 where the camera does not cover it,
+// else the fp32 coordinate clamped into the frame.
+__device__ __forceinline__ float2 mapFreeValue(const RemapParamF& m, uint32_t covWord, int lx, int cx, int cy, int sw,
+                                               int sh)
+{
+    if (!((covWord >> lx) & 1u)) return make_float2(-1.f, -1.f);
+    const float2 v = remapPointF(m, (float)cx, (float)cy);
+    return make_float2(fminf(fmaxf(v.x, 0.f), __int_as_float(__float_as_int((float)sw) - 1)),
+                       fminf(fmaxf(v.y, 0.f), __int_as_float(__float_as_int((float)sh) - 1)));
 }
 
 __device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, long long pitch, int fmt, int sw,
@@ -166,6 +285,25 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
     // The hand-out counter, items, descriptors and maps are written before
     // the launch sequence, not by a kernel: the first chunk and its map are
     // fetched while the previous kernel finishes.
+    // The tile's two map values of this thread: from the resident maps, or,
+    // map-free, from the coverage bits (the FP64 coverage of prepare) and the
+    // fp32 geometry.
+    auto loadMap = [&](const RigDev& R, const RemapItem& itm, float2& a, float2& b) {
+        const long long tiles = R.numRemapItems;
+        if (R.maps) {
+            const float2* mt = R.maps + (size_t)itm.mapTile * (kRemapTW * kRemapTH);
+            const long long mb = tiles * kRemapTW * kRemapTH * (long long)sizeof(float2);
+            a = ldChecked(mt + threadIdx.x, R.maps, mb);
+            b = ldChecked(mt + threadIdx.x + kThreads, R.maps, mb);
+        } else {
+            const uint32_t* cw = R.covTiles + (size_t)itm.mapTile * kRemapTH;
+            const RemapParamF& pf = R.camsF[itm.cam];
+            const int cx = itm.tx * kRemapTW + lx, cy = itm.ty * kRemapTH + ly;
+            const long long cb = tiles * kRemapTH * 4;
+            a = mapFreeValue(pf, ldChecked(cw + ly, R.covTiles, cb), lx, cx, cy, R.srcW, R.srcH);
+            b = mapFreeValue(pf, ldChecked(cw + ly + 8, R.covTiles, cb), lx, cx, cy + 8, R.srcW, R.srcH);
+        }
+    };
     int it = grab(), end = 0, nextBegin = total, s = 0;
     RemapSeg cur{};
     RemapItem item{};
@@ -176,9 +314,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
         s = findSegment(segs, nsegs, it, 0);
         cur = remapSeg(segs, nsegs, s, total);
         item = cur.items[it - cur.prefix];
-        const float2* mt = cur.R->maps + (size_t)item.mapTile * (kRemapTW * kRemapTH);
-        m0 = __ldg(mt + threadIdx.x);
-        m1 = __ldg(mt + threadIdx.x + kThreads);
+        loadMap(*cur.R, item, m0, m1);
     }
     waitPrevGrid();
     allowNextGrid();
@@ -189,6 +325,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
     long long pitch = 0;
     int fmt = 0, sw = 0, sh = 0, W = 0, H = 0, gpitch = 0;
     uint32_t* G = nullptr;
+    const void* gLo = nullptr;  // the level-0 buffer of the camera's rig and its extent (checked build)
+    long long gExt = 0;
     for (;;) {
         if (item.cam != cam || s != camSeg) {  // uniform across the block
             const FrameDev& F = *cur.F;
@@ -204,6 +342,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
             H = R.H;
             gpitch = R.lv[0].pitch;
             G = reinterpret_cast<uint32_t*>(R.lv[0].G) + (size_t)cam * R.lv[0].camStride;
+            gLo = R.lv[0].G;
+            gExt = gBytes(R, R.lv[0]);
             __syncthreads();
             const uint8_t* src = F.luts + cam * 768;
             for (int k = threadIdx.x; k < 768; k += kThreads) lut[k] = __ldg(src + k);
@@ -219,16 +359,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
                 cur = remapSeg(segs, nsegs, s, total);
             }
             nitem = cur.items[nit - cur.prefix];
-            const float2* nt = cur.R->maps + (size_t)nitem.mapTile * (kRemapTW * kRemapTH);
-            n0 = __ldg(nt + threadIdx.x);
-            n1 = __ldg(nt + threadIdx.x + kThreads);
+            loadMap(*cur.R, nitem, n0, n1);
         }
         const uint32_t v0 = remapPixel(m0, base, pitch, fmt, sw, sh, lut);
         const uint32_t v1 = remapPixel(m1, base, pitch, fmt, sw, sh, lut);
         const int x = item.tx * kRemapTW + lx, y0 = item.ty * kRemapTH + ly, y1 = y0 + 8;
         if (x < W) {
-            if (y0 < H) G[(size_t)y0 * gpitch + x] = v0;
-            if (y1 < H) G[(size_t)y1 * gpitch + x] = v1;
+            if (y0 < H && inside(G + (size_t)y0 * gpitch + x, gLo, gExt)) G[(size_t)y0 * gpitch + x] = v0;
+            if (y1 < H && inside(G + (size_t)y1 * gpitch + x, gLo, gExt)) G[(size_t)y1 * gpitch + x] = v1;
         }
         if (nit < 0) break;
         if (it + 1 >= end) {  // into the next chunk; fetch the one after it
@@ -253,9 +391,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
 // each thread two pixels (rows ly and ly + 8).  The LUTs of all cameras of
 // the current rig are staged in shared memory.
 // ============================================================================
-__device__ __forceinline__ void storeBgr(const FrameDev& F, int x, int y, uint32_t v)
+__device__ __forceinline__ void storeBgr(const FrameDev& F, int x, int y, int H, uint32_t v)
 {
     uint8_t* row = F.out + (size_t)y * F.outPitch;
+    if (!insideRange(row + (F.outFmt == PS_FMT_BGR32 ? 4 : 3) * x, F.outFmt == PS_FMT_BGR32 ? 4 : 3, F.out,
+                     F.outPitch * H))
+        return;
     if (F.outFmt == PS_FMT_BGR32) {
         reinterpret_cast<uint32_t*>(row)[x] = v;
     } else {
@@ -296,8 +437,11 @@ __global__ void __launch_bounds__(kThreads) k_linear(const Segment* __restrict__
         for (uint32_t q = 0; q < item.count; q++) {
             const RemapItem ri = R.remapItems[item.first + q];
             const size_t base = (size_t)ri.mapTile * (kRemapTW * kRemapTH) + threadIdx.x;
-            const float2 m0 = __ldg(R.maps + base), m1 = __ldg(R.maps + base + kThreads);
-            const float w0 = __ldg(R.linWeights + base), w1 = __ldg(R.linWeights + base + kThreads);
+            const long long tilePx = (long long)R.numRemapItems * kRemapTW * kRemapTH;
+            const float2 m0 = ldChecked(R.maps + base, R.maps, tilePx * 8);
+            const float2 m1 = ldChecked(R.maps + base + kThreads, R.maps, tilePx * 8);
+            const float w0 = ldChecked(R.linWeights + base, R.linWeights, tilePx * 4);
+            const float w1 = ldChecked(R.linWeights + base + kThreads, R.linWeights, tilePx * 4);
             const uint8_t* src = F.src[ri.cam];
             const long long pitch = F.srcPitch[ri.cam];
             const uint8_t* lut = luts + ri.cam * 768;
@@ -311,8 +455,8 @@ __global__ void __launch_bounds__(kThreads) k_linear(const Segment* __restrict__
         }
         const int x = item.tx * kRemapTW + lx, y0 = item.ty * kRemapTH + ly, y1 = y0 + 8;
         if (x < R.W) {
-            if (y0 < R.H) storeBgr(F, x, y0, roundSaturate3(a0));
-            if (y1 < R.H) storeBgr(F, x, y1, roundSaturate3(a1));
+            if (y0 < R.H) storeBgr(F, x, y0, R.H, roundSaturate3(a0));
+            if (y1 < R.H) storeBgr(F, x, y1, R.H, roundSaturate3(a1));
         }
     }
 }
@@ -411,18 +555,21 @@ __device__ __forceinline__ void downLoad(const RigDev& R, const DownItem& item, 
     // the lane's outputs (X, Y), (X + 1, Y): X is even, so both divisors are
     // one aligned 4-byte load (X + 1 stays inside the row pitch)
     const int X = ox0 + 2 * (lane & 15), Y = oy0 + 2 * w + (lane >> 4);
-    g.m = X < Ld.w && Y < Ld.h
-              ? __ldg(reinterpret_cast<const uint32_t*>(Ld.Am + (size_t)item.cam * Ld.camStride + (size_t)Y * Ld.pitch + X))
-              : 0u;
+    g.m = X < Ld.w && Y < Ld.h ? ldChecked(reinterpret_cast<const uint32_t*>(Ld.Am + (size_t)item.cam * Ld.camStride +
+                                                                           (size_t)Y * Ld.pitch + X),
+                                           Ld.Am, wBytes(R, Ld))
+                               : 0u;
     const bool extra = lane < kDInW - 64;
+    const long long ext = gBytes(R, Ls);
     if (downInterior(R, item)) {
         const uint32_t* row = G + (size_t)iy0 * Ls.pitch + ix0;
 #pragma unroll
         for (int r = 0; r < kDRows; r++, row += Ls.pitch) {
-            const uint2 v = ldLevel<kFresh>(reinterpret_cast<const uint2*>(row) + lane);
+            const uint2* q = reinterpret_cast<const uint2*>(row) + lane;
+            const uint2 v = inside(q, Ls.G, ext) ? ldLevel<kFresh>(q) : make_uint2(0, 0);
             g.a[r] = v.x;
             g.b[r] = v.y;
-            g.c[r] = extra ? ldLevel<kFresh>(row + 64 + lane) : 0u;
+            g.c[r] = extra && inside(row + 64 + lane, Ls.G, ext) ? ldLevel<kFresh>(row + 64 + lane) : 0u;
         }
         return;
     }
@@ -431,9 +578,9 @@ __device__ __forceinline__ void downLoad(const RigDev& R, const DownItem& item, 
 #pragma unroll
     for (int r = 0; r < kDRows; r++) {
         const uint32_t* row = G + (size_t)rowMap(iy0 + r, Ls.h) * Ls.pitch;
-        g.a[r] = ldLevel<kFresh>(row + c0);
-        g.b[r] = ldLevel<kFresh>(row + c1);
-        g.c[r] = extra ? ldLevel<kFresh>(row + c2) : 0u;
+        g.a[r] = inside(row + c0, Ls.G, ext) ? ldLevel<kFresh>(row + c0) : 0u;
+        g.b[r] = inside(row + c1, Ls.G, ext) ? ldLevel<kFresh>(row + c1) : 0u;
+        g.c[r] = extra && inside(row + c2, Ls.G, ext) ? ldLevel<kFresh>(row + c2) : 0u;
     }
 }
 
@@ -506,8 +653,12 @@ __device__ __forceinline__ void downHorizontal(const RigDev& R, const DownItem& 
     const int X = item.tx * kDownTW + 2 * k, Y = item.ty * kDownTH + 2 * w + rsel;
     if (X < Ld.w && Y < Ld.h) {
         uint32_t* dst = reinterpret_cast<uint32_t*>(Ld.G) + (size_t)item.cam * Ld.camStride + (size_t)Y * Ld.pitch + X;
-        if (X + 1 < Ld.w) *reinterpret_cast<uint2*>(dst) = make_uint2(out0, out1);
-        else dst[0] = out0;
+        const long long ext = gBytes(R, Ld);
+        if (X + 1 < Ld.w) {
+            if (inside(reinterpret_cast<uint2*>(dst), Ld.G, ext)) *reinterpret_cast<uint2*>(dst) = make_uint2(out0, out1);
+        } else if (inside(dst, Ld.G, ext)) {
+            dst[0] = out0;
+        }
     }
 }
 
@@ -710,6 +861,7 @@ __device__ __forceinline__ void storeYuv(const UnitGeo& G, int x, int y, const u
     for (int r = 0; r < 2; r++) {
         uint8_t* yrow = G.out + (size_t)(y + r) * G.outPitch + x;
         const uint32_t yy = packSat2(yuvLumaRaw(o[2 * r]), yuvLumaRaw(o[2 * r + 1]));
+        if (!insideRange(yrow, 2, G.out, G.outPitch * G.h)) continue;
         if ((reinterpret_cast<uintptr_t>(yrow) & 1) == 0) {
             *reinterpret_cast<uint16_t*>(yrow) = (uint16_t)yy;
         } else {
@@ -721,8 +873,10 @@ __device__ __forceinline__ void storeYuv(const UnitGeo& G, int x, int y, const u
     const uint32_t uv = packSat2((c.x + d.x) >> (kYuvShift + 1), (c.y + d.y) >> (kYuvShift + 1));
     const uint8_t u = (uint8_t)uv, v = (uint8_t)(uv >> 8);
     const size_t cy = (size_t)(y >> 1);
+    const long long cext = G.outCPitch * (G.h / 2);
     if (G.outFmt == PS_FMT_NV12) {
         uint8_t* p = G.outU + cy * G.outCPitch + x;
+        if (!insideRange(p, 2, G.outU, cext)) return;
         if ((reinterpret_cast<uintptr_t>(p) & 1) == 0) {
             *reinterpret_cast<uint16_t*>(p) = (uint16_t)uv;
         } else {
@@ -730,8 +884,9 @@ __device__ __forceinline__ void storeYuv(const UnitGeo& G, int x, int y, const u
             p[1] = v;
         }
     } else {
-        G.outU[cy * G.outCPitch + (x >> 1)] = u;
-        G.outV[cy * G.outVPitch + (x >> 1)] = v;
+        if (inside(G.outU + cy * G.outCPitch + (x >> 1), G.outU, cext)) G.outU[cy * G.outCPitch + (x >> 1)] = u;
+        if (inside(G.outV + cy * G.outVPitch + (x >> 1), G.outV, G.outVPitch * (G.h / 2)))
+            G.outV[cy * G.outVPitch + (x >> 1)] = v;
     }
 }
 
@@ -787,8 +942,10 @@ __device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const
             uint32_t w = 0;
             if (y + r < Lj.h) {  // columns up to the pitch are allocated (and zero beyond the width)
                 const size_t o = (size_t)cam * Lj.camStride + (size_t)(y + r) * Lj.pitch + x;
-                g = ldLevel<kFresh>(reinterpret_cast<const uint2*>(Lj.G + o));
-                w = __ldg(reinterpret_cast<const uint32_t*>(Lj.Wt + o));
+                const uint2* gp = reinterpret_cast<const uint2*>(Lj.G + o);
+                const uint32_t* wp = reinterpret_cast<const uint32_t*>(Lj.Wt + o);
+                if (inside(gp, Lj.G, gBytes(R, Lj))) g = ldLevel<kFresh>(gp);
+                if (inside(wp, Lj.Wt, wBytes(R, Lj))) w = __ldg(wp);
             }
             *reinterpret_cast<uint2*>(&S.gj[q][ly + r][lx]) = g;
             *reinterpret_cast<uint32_t*>(&S.w[q][ly + r][lx]) = w;
@@ -804,14 +961,15 @@ __device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const
             const int q = k / elems, e = k - q * elems;
             const int r = rb + e / kFW, c = e % kFW;
             const int cam = tileCam(raw, R.camLists, c0 + q);
-            S.fp[q][r][c + 3] = ldLevel<kFresh>(reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
-                                                (size_t)fRow[r] * Lu.pitch + fCol[c]);
+            const uint32_t* gp = reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
+                                 (size_t)fRow[r] * Lu.pitch + fCol[c];
+            S.fp[q][r][c + 3] = inside(gp, Lu.G, gBytes(R, Lu)) ? ldLevel<kFresh>(gp) : 0u;
         }
         if (last)
             for (int k = threadIdx.x; k < elems; k += kConsumers) {
                 const int r = rb + k / kFW, c = k % kFW;
-                S.cf[r][c + 1] =
-                    ldLevel<kFresh>(reinterpret_cast<const uint2*>(Lu.C + (size_t)fRow[r] * Lu.pitch + fCol[c]));
+                const uint2* cp = reinterpret_cast<const uint2*>(Lu.C + (size_t)fRow[r] * Lu.pitch + fCol[c]);
+                S.cf[r][c + 1] = inside(cp, Lu.C, cBytes(Lu)) ? ldLevel<kFresh>(cp) : make_uint2(0, 0);
             }
     }
 }
@@ -971,6 +1129,7 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
         }
     }
     if (j > 0) {
+        const long long cext = (long long)G.pitch * G.h * 8;
 #pragma unroll
         for (int r = 0; r < 2; r++) {
             if (y + r >= G.h) break;
@@ -978,12 +1137,13 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
             const int* a = n[2 * r];
             const int* b = n[2 * r + 1];
             if (x + 1 < G.w) {
-                *reinterpret_cast<int4*>(Cj) =
-                    make_int4((int)((uint32_t)(uint16_t)a[0] | ((uint32_t)(uint16_t)a[1] << 16)),
-                              (int)(uint32_t)(uint16_t)a[2],
-                              (int)((uint32_t)(uint16_t)b[0] | ((uint32_t)(uint16_t)b[1] << 16)),
-                              (int)(uint32_t)(uint16_t)b[2]);
-            } else if (x < G.w) {
+                if (inside(reinterpret_cast<int4*>(Cj), G.C, cext))
+                    *reinterpret_cast<int4*>(Cj) =
+                        make_int4((int)((uint32_t)(uint16_t)a[0] | ((uint32_t)(uint16_t)a[1] << 16)),
+                                  (int)(uint32_t)(uint16_t)a[2],
+                                  (int)((uint32_t)(uint16_t)b[0] | ((uint32_t)(uint16_t)b[1] << 16)),
+                                  (int)(uint32_t)(uint16_t)b[2]);
+            } else if (x < G.w && inside(Cj, G.C, cext)) {
                 Cj[0] = make_short4((short)a[0], (short)a[1], (short)a[2], 0);
             }
         }
@@ -998,10 +1158,11 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
         for (int p = 0; p < 4; p++)
             o[p] = packSatBgr(n[p][0], n[p][1], n[p][2]);
         if (cls == 2) {
+            const long long uext = (long long)G.pitch * G.h;
             for (int r = 0; r < rows; r++) {
                 const uint8_t* um = G.um + (size_t)(y + r) * G.pitch + x;
-                if (!um[0]) o[2 * r] = 0;
-                if (cols == 2 && !um[1]) o[2 * r + 1] = 0;
+                if (!(inside(um, G.um, uext) ? um[0] : 0)) o[2 * r] = 0;
+                if (cols == 2 && !(inside(um + 1, G.um, uext) ? um[1] : 0)) o[2 * r + 1] = 0;
             }
         }
     }
@@ -1009,18 +1170,23 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
         storeYuv(G, x, y, o);
         return;
     }
+    const long long oext = G.outPitch * G.h;
     for (int r = 0; r < rows; r++) {
         uint8_t* orow = G.out + (size_t)(y + r) * G.outPitch;
         if (G.outFmt == PS_FMT_BGR32) {
             if (cols == 2 && (reinterpret_cast<uintptr_t>(orow) & 7) == 0) {
-                reinterpret_cast<uint2*>(orow)[x / 2] = make_uint2(o[2 * r], o[2 * r + 1]);
+                if (inside(reinterpret_cast<uint2*>(orow) + x / 2, G.out, oext))
+                    reinterpret_cast<uint2*>(orow)[x / 2] = make_uint2(o[2 * r], o[2 * r + 1]);
             } else {
-                reinterpret_cast<uint32_t*>(orow)[x] = o[2 * r];
-                if (cols == 2) reinterpret_cast<uint32_t*>(orow)[x + 1] = o[2 * r + 1];
+                if (inside(reinterpret_cast<uint32_t*>(orow) + x, G.out, oext))
+                    reinterpret_cast<uint32_t*>(orow)[x] = o[2 * r];
+                if (cols == 2 && inside(reinterpret_cast<uint32_t*>(orow) + x + 1, G.out, oext))
+                    reinterpret_cast<uint32_t*>(orow)[x + 1] = o[2 * r + 1];
             }
         } else {
             for (int i = 0; i < cols; i++) {
                 const uint32_t v = o[2 * r + i];
+                if (!insideRange(orow + 3 * (x + i), 3, G.out, oext)) continue;
                 orow[3 * (x + i)] = v & 0xFF;
                 orow[3 * (x + i) + 1] = (v >> 8) & 0xFF;
                 orow[3 * (x + i) + 2] = (v >> 16) & 0xFF;
@@ -1140,12 +1306,15 @@ __device__ __forceinline__ void computeUnitRows(const Stage& S, const UnitGeo& G
     }
     if (y >= G.h || j == 0) return;  // level 0 goes through computeUnit
     short4* Cj = G.C + (size_t)y * G.pitch + x;
+    const long long cext = (long long)G.pitch * G.h * 8;
     if (x + 1 < G.w) {
-        *reinterpret_cast<int4*>(Cj) = make_int4((int)((uint32_t)(uint16_t)n0[0] | ((uint32_t)(uint16_t)n0[1] << 16)),
-                                                 (int)(uint32_t)(uint16_t)n0[2],
-                                                 (int)((uint32_t)(uint16_t)n1[0] | ((uint32_t)(uint16_t)n1[1] << 16)),
-                                                 (int)(uint32_t)(uint16_t)n1[2]);
-    } else if (x < G.w) {
+        if (inside(reinterpret_cast<int4*>(Cj), G.C, cext))
+            *reinterpret_cast<int4*>(Cj) =
+                make_int4((int)((uint32_t)(uint16_t)n0[0] | ((uint32_t)(uint16_t)n0[1] << 16)),
+                          (int)(uint32_t)(uint16_t)n0[2],
+                          (int)((uint32_t)(uint16_t)n1[0] | ((uint32_t)(uint16_t)n1[1] << 16)),
+                          (int)(uint32_t)(uint16_t)n1[2]);
+    } else if (x < G.w && inside(Cj, G.C, cext)) {
         Cj[0] = make_short4((short)n0[0], (short)n0[1], (short)n0[2], 0);
     }
 }
@@ -1261,30 +1430,30 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                         int r = k - q * cb;
                         const int cam = tileCam(raw, R->camLists, chunk * kCamsPerUnit + q);
                         if (r < kBlendTH) {
-                            bulkCopy(&st[stg].gj[q][r][0],
-                                     Lj.G + (size_t)cam * Lj.camStride + (size_t)(ty * kBlendTH + r) * Lj.pitch +
-                                         tx * kBlendTW,
-                                     kBlendTW * 4, &full[stg]);
+                            bulkCopyChecked(&st[stg].gj[q][r][0],
+                                            Lj.G + (size_t)cam * Lj.camStride + (size_t)(ty * kBlendTH + r) * Lj.pitch +
+                                                tx * kBlendTW,
+                                            kBlendTW * 4, &full[stg], Lj.G, gBytes(*R, Lj));
                             continue;
                         }
                         r -= kBlendTH;
                         if (!uni) {
                             if (r < kBlendTH) {
-                                bulkCopy(&st[stg].w[q][r][0],
-                                         Lj.Wt + (size_t)cam * Lj.camStride + (size_t)(ty * kBlendTH + r) * Lj.pitch +
-                                             tx * kBlendTW,
-                                         kBlendTW * 2, &full[stg]);
+                                bulkCopyChecked(&st[stg].w[q][r][0],
+                                                Lj.Wt + (size_t)cam * Lj.camStride +
+                                                    (size_t)(ty * kBlendTH + r) * Lj.pitch + tx * kBlendTW,
+                                                kBlendTW * 2, &full[stg], Lj.Wt, wBytes(*R, Lj));
                                 continue;
                             }
                             r -= kBlendTH;
                         }
-                        bulkCopy(&st[stg].fp[q][r][0],
-                                 Lu.G + (size_t)cam * Lu.camStride + (size_t)(fy0 + r) * Lu.pitch + (fx0 - 3), kFpW * 4,
-                                 &full[stg]);
+                        bulkCopyChecked(&st[stg].fp[q][r][0],
+                                        Lu.G + (size_t)cam * Lu.camStride + (size_t)(fy0 + r) * Lu.pitch + (fx0 - 3),
+                                        kFpW * 4, &full[stg], Lu.G, gBytes(*R, Lu));
                     } else {
                         const int r = k - nc * cb;
-                        bulkCopy(&st[stg].cf[r][0], Lu.C + (size_t)(fy0 + r) * Lu.pitch + (fx0 - 1), kCfW * 8,
-                                 &full[stg]);
+                        bulkCopyChecked(&st[stg].cf[r][0], Lu.C + (size_t)(fy0 + r) * Lu.pitch + (fx0 - 1), kCfW * 8,
+                                        &full[stg], Lu.C, cBytes(Lu));
                     }
                 }
             } else if (lane == 0) {
@@ -1844,4 +2013,24 @@ cudaError_t launchReprojectTo16S(const uint8_t* src, long long srcPitch, int src
     return cudaGetLastError();
 }
 
+}  // namespace ps
+
+// ---- the checked build's counter ------------------------------------------------
+namespace ps {
+long long boundsViolations(bool reset)
+{
+#ifdef PS_CHECK_BOUNDS
+    unsigned long long v = 0;
+    if (cudaDeviceSynchronize() != cudaSuccess) return -2;  // the renders run on their own streams
+    if (cudaMemcpyFromSymbol(&v, g_boundsViolations, sizeof v) != cudaSuccess) return -2;
+    if (reset) {
+        const unsigned long long z = 0;
+        if (cudaMemcpyToSymbol(g_boundsViolations, &z, sizeof z) != cudaSuccess) return -2;
+    }
+    return (long long)v;
+#else
+    (void)reset;
+    return -1;
+#endif
+}
 }  // namespace ps

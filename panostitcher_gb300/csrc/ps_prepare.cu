@@ -577,6 +577,49 @@ __global__ void k_compact_maps(const float* __restrict__ xmap, const float* __re
     maps[(size_t)it.mapTile * (kRemapTW * kRemapTH) + threadIdx.x] = v;
 }
 
+// Coverage of each remap tile as 16 words (one per tile row, bit = column),
+// for the map-free remap: one warp per row, one ballot per word.
+__global__ void k_cov_tiles(const uint8_t* __restrict__ cov, int W, int H, long long maskStride,
+                            const RemapItem* __restrict__ items, uint32_t* words)
+{
+    const RemapItem it = items[blockIdx.x];
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    const int x = it.tx * kRemapTW + lx, y = it.ty * kRemapTH + ly;
+    const bool c = x < W && y < H && cov[(size_t)it.cam * maskStride + (size_t)y * W + x] != 0;
+    const uint32_t w = __ballot_sync(0xffffffffu, c);
+    if (lx == 0) words[(size_t)it.mapTile * kRemapTH + ly] = w;
+}
+
+cudaError_t launchCovTiles(const uint8_t* cov, int W, int H, long long maskStride, const RemapItem* items,
+                           int nitems, uint32_t* words, cudaStream_t st)
+{
+    if (nitems <= 0) return cudaSuccess;
+    k_cov_tiles<<<nitems, kRemapTW * kRemapTH, 0, st>>>(cov, W, H, maskStride, items, words);
+    return cudaGetLastError();
+}
+
+RemapParamF remapParamF(const RemapDev& r)
+{
+    RemapParamF f;
+    f.type = r.type;
+    f.srcTX = (float)r.srcTX;
+    f.srcTY = (float)r.srcTY;
+    f.destTX = (float)r.destTX;
+    f.destTY = (float)r.destTY;
+    f.scale0 = (float)r.scale0;
+    f.scale1 = (float)r.scale1;
+    f.shear0 = (float)r.shear0;
+    f.shear1 = (float)r.shear1;
+    f.rot0 = (float)r.rot0;
+    f.rot1 = (float)r.rot1;
+    for (int i = 0; i < 6; i++) f.rad[i] = (float)r.rad[i];
+    for (int i = 0; i < 9; i++) f.mt[i] = (float)r.mt[i];
+    f.distance = (float)r.distance;
+    f.horizontal = (float)r.horizontal;
+    f.vertical = (float)r.vertical;
+    return f;
+}
+
 cudaError_t launchCompactMaps(const float* xmap, const float* ymap, int W, int H, long long maskStride,
                               const RemapItem* items, int nitems, float2* maps, cudaStream_t st)
 {

@@ -122,6 +122,7 @@ void Rig::clear()
     }
     nextSlot_ = lastSlot_ = 0;
     maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset(); planar_.reset();
+    camsF_.reset(); covTiles_.reset();
     imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
     hRemap_.clear();
     hDown_.clear();
@@ -182,7 +183,7 @@ long long Rig::residentBytes() const
     }
     b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
     b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
-    b += dLinear_.bytes() + linW_.bytes() + planar_.bytes();
+    b += dLinear_.bytes() + linW_.bytes() + planar_.bytes() + camsF_.bytes() + covTiles_.bytes();
     return b;
 }
 
@@ -236,7 +237,7 @@ long long Rig::estimateBlenderBytes(int W, int H, int n, int maxLevels, int slot
 }
 
 long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
-                             int dstH, int slots)
+                             int dstH, int slots, bool mapFree)
 {
     validateParams(params, n, srcW, srcH, dstW, dstH);
     const int L = std::max(0, trueNumLevels(dstW, dstH, blendParam, 2));
@@ -248,8 +249,10 @@ long long Rig::estimateBytes(const ps_photo_param* params, int n, int blendParam
         w = (w + 1) / 2;
         h = (h + 1) / 2;
     }
-    // maps bounded by the full canvas per camera, inputs, output, union mask, lists
-    b += (long long)dstW * dstH * 8 * n +
+    // maps (or, map-free, coverage bits) bounded by the full canvas per
+    // camera, inputs, output, union mask, lists
+    const long long tiles = (long long)divUp(dstW, kRemapTW) * divUp(dstH, kRemapTH) * n;
+    b += (mapFree ? tiles * kRemapTH * 4 + (long long)sizeof(RemapParamF) * n : (long long)dstW * dstH * 8 * n) +
          ((long long)roundUp(srcW * 4, 256) * srcH * n + (long long)dstW * dstH * 4) * slots +
          (long long)roundUp(dstW, 64) * dstH + listBytes(dstW, dstH, n, L, slots);
     return b;
@@ -315,24 +318,32 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
     // resident state is per frame in flight, so the fallback is fewer state
     // slots: as many as fit with that margin, down to one.
     // A caller's memory budget (setMemoryBudget) caps the same estimate.
+    // When even one slot does not fit, the maps stop being resident: the
+    // remap computes each source coordinate (the reference's map-free
+    // remap, RicohUtil.cpp:1315-1329).
     int slots = slotsWanted_;
-    if (highQuality && slots > 1) {
+    mapFree_ = highQuality && mapFreeWanted_;
+    if (highQuality) {
         size_t freeB = 0, totalB = 0;
         PS_CUDA(cudaMemGetInfo(&freeB, &totalB));
         long long room = (long long)freeB - 500000000LL;
         if (budget_ > 0) room = std::min(room, budget_);
-        while (slots > 1 && estimateBytes(params, n, blendParam, srcW, srcH, dstW, dstH, slots) > room) slots--;
+        while (slots > 1 && estimateBytes(params, n, blendParam, srcW, srcH, dstW, dstH, slots, mapFree_) > room)
+            slots--;
+        if (!mapFree_ && estimateBytes(params, n, blendParam, srcW, srcH, dstW, dstH, slots, false) > room)
+            mapFree_ = true;
     }
     try {
         // MIN_SIDE_LENGTH = 2, source/Task/RicohUtil.cpp:15
         setGeometry(n, dstW, dstH, highQuality ? std::max(0, trueNumLevels(dstW, dstH, blendParam, 2)) : 0);
-        lowMemory_ = slots < slots_;
+        lowMemory_ = slots < slots_ || (mapFree_ && !mapFreeWanted_);
         slots_ = slots;
         srcW_ = srcW;
         srcH_ = srcH;
         const size_t npx = (size_t)dstW * dstH;
         DevBuf xmap(n * npx * 4), ymap(n * npx * 4), cov(n * npx), seam(n * npx);
-        std::vector<RemapDev> rp(n);
+        std::vector<RemapDev>& rp = hParams_;
+        rp.assign(n, RemapDev{});
         for (int i = 0; i < n; i++) remapInit(params[i], dstW, dstH, srcW, srcH, rp[i]);
         DevBuf dParams(sizeof(RemapDev) * n);
         PS_CUDA(cudaMemcpyAsync(dParams.get(), rp.data(), sizeof(RemapDev) * n, cudaMemcpyHostToDevice, st));
@@ -531,10 +542,20 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
         PS_CUDA(cudaMemcpyAsync(dDown_.get(), down.data(), down.size() * sizeof(DownItem), cudaMemcpyHostToDevice, st));
 
     // tile-compact maps of the covered remap tiles
-    if (xmap && !hRemap_.empty()) {
+    if (xmap && !hRemap_.empty() && !mapFree_) {
         maps_.alloc(hRemap_.size() * kRemapTW * kRemapTH * sizeof(float2));
         PS_CUDA(launchCompactMaps(xmap, ymap, W, H, (long long)npx, dRemap_.as<RemapItem>(), (int)hRemap_.size(),
                                   maps_.as<float2>(), st));
+    }
+    if (xmap && !hRemap_.empty() && mapFree_) {  // coverage bits and fp32 parameters instead of maps
+        covTiles_.alloc(hRemap_.size() * kRemapTH * sizeof(uint32_t));
+        PS_CUDA(launchCovTiles(cov, W, H, (long long)npx, dRemap_.as<RemapItem>(), (int)hRemap_.size(),
+                               covTiles_.as<uint32_t>(), st));
+        std::vector<RemapParamF> pf(n);
+        for (int i = 0; i < n; i++) pf[i] = remapParamF(hParams_[i]);
+        camsF_.alloc(sizeof(RemapParamF) * n);
+        PS_CUDA(cudaMemcpyAsync(camsF_.get(), pf.data(), sizeof(RemapParamF) * n, cudaMemcpyHostToDevice, st));
+        PS_CUDA(cudaStreamSynchronize(st));  // pf is a host temporary
     }
 
     // device descriptor
@@ -547,7 +568,10 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     d.full = full_;
     d.srcW = srcW_;
     d.srcH = srcH_;
-    d.maps = maps_.as<float2>();
+    d.maps = mapFree_ ? nullptr : maps_.as<float2>();
+    d.numRemapItems = (int)hRemap_.size();
+    d.camsF = camsF_.as<RemapParamF>();
+    d.covTiles = covTiles_.as<uint32_t>();
     d.unionMask = union_.as<uint8_t>();
     d.camLists = dCams_.as<uint8_t>();
     d.downItems = dDown_.as<DownItem>();
@@ -950,8 +974,17 @@ void Rig::exportState(int what, int cam, int level, void* host, long long bytes)
     if (!ready()) fail(PS_ESTATE, "not prepared");
     if (cam < 0 || cam >= n_) fail(PS_EINVAL, "camera %d out of range", cam);
     const size_t npx = (size_t)W_ * H_;
+    if (what == 7) {  // level 0 of the last run (the remap's output; uint8 x4, the fourth byte 0)
+        if ((size_t)bytes < npx * 4) fail(PS_EINVAL, "buffer too small");
+        const_cast<Rig*>(this)->waitIdle();  // the runs are on the render's own streams
+        const LevelGeom& g = geom_[0];
+        PS_CUDA(cudaMemcpy2D(host, (size_t)W_ * 4, lv_[0].G[lastSlot_].as<uchar4>() + (size_t)cam * g.pitch * g.h,
+                             (size_t)g.pitch * 4, (size_t)W_ * 4, H_, cudaMemcpyDeviceToHost));
+        return;
+    }
     if (what == 0 || what == 1) {
         if (!hasMaps_) fail(PS_EINVAL, "no maps (prepared from masks)");
+        if (mapFree_) fail(PS_EINVAL, "map-free render: the maps are not resident");
         if ((size_t)bytes < npx * 4) fail(PS_EINVAL, "buffer too small");
         float* out = static_cast<float*>(host);
         std::fill(out, out + npx, -1.f);

@@ -59,7 +59,12 @@ public:
     long long residentBytes() const;
     // resident bytes a rig of this shape would hold (no allocation)
     static long long estimateBytes(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH,
-                                   int dstW, int dstH, int slots = kIoSlots);
+                                   int dstW, int dstH, int slots = kIoSlots, bool mapFree = false);
+    // Map-free remap (next prepare): no resident maps; the remap computes
+    // each source coordinate in fp32 (within +-1 of the exact level 0).
+    // Taken by itself when even one slot with maps does not fit.
+    void setMapFree(bool on) { mapFreeWanted_ = on; }
+    bool mapFree() const { return mapFree_; }
 
     // Device staging of host frames and of a host canvas: one set per state
     // slot, so consecutive renders with host buffers overlap their copies (slot 0's
@@ -188,6 +193,9 @@ private:
 
     int n_ = 0, W_ = 0, H_ = 0, L_ = 0, full_ = 0, srcW_ = 0, srcH_ = 0;
     bool hasMaps_ = false, linear_ = false, custom_ = false, lowMemory_ = false;
+    bool mapFree_ = false, mapFreeWanted_ = false;
+    std::vector<RemapDev> hParams_;  // the cameras' Remap parameters of the last prepare
+    DevBuf camsF_, covTiles_;
     int nextSlot_ = 0, lastSlot_ = 0, slots_ = kIoSlots, slotsWanted_ = kIoSlots, probe_ = 0;
     cudaEvent_t slotComputed_[kIoSlots] = {}, slotDownloaded_[kIoSlots] = {};
     int numLinear_ = 0;

@@ -170,6 +170,19 @@ class CudaPanoramaRender2:
         """Device bytes the next prepare may take (0: the free memory only); fewer frames in flight fit."""
         check(lib().ps_render_set_memory_budget(self._h, int(nbytes)))
 
+    def set_map_free(self, enable: bool) -> None:
+        """Next multiband prepare keeps no maps: fp32 coordinates per pixel (level 0 within +-1)."""
+        check(lib().ps_render_set_map_free(self._h, int(bool(enable))))
+
+    @property
+    def map_free(self) -> bool:
+        return bool(lib().ps_render_is_map_free(self._h))
+
+    def level0(self, cam: int) -> np.ndarray:
+        """Level 0 of the last render for one camera (uint8 (H, W, 4)): the remap's output."""
+        W, H = self._size
+        return self.export(L.EXPORT_LEVEL0, cam, 0, (H, W, 4), np.uint8)
+
     @property
     def low_memory(self) -> bool:
         """The last prepare took fewer frames in flight than asked for (the reference's low-memory path)."""

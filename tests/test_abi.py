@@ -35,6 +35,15 @@ def test_library_exports_every_declared_symbol(built_lib):
     assert decl <= set(L.exported_symbols())
 
 
+def test_checked_build_exports_the_same_abi(built_lib):
+    path = os.path.join(ROOT, "panostitcher_gb300", "libpanostitch_checked.so")
+    checked = C.CDLL(path)
+    missing = [n for n in sorted(declared_functions()) if not hasattr(checked, n)]
+    assert not missing, missing
+    built_lib.ps_debug_bounds_violations.restype = C.c_longlong
+    assert built_lib.ps_debug_bounds_violations(0) == -1  # the normal build checks nothing
+
+
 def test_version_and_empty_error(built_lib):
     assert b"sm_103a" in built_lib.ps_version()
 
