@@ -914,6 +914,7 @@ void Rig::prepareLinear(const uint8_t* cov, const uint8_t* seam, const float* xm
     d.srcH = srcH_;
     d.maps = maps_.as<float2>();
     d.remapItems = dRemap_.as<RemapItem>();
+    d.numRemapItems = (int)hRemap_.size();
     d.linWeights = linW_.as<float>();
     d.tailDown = d.tailBlend = 1;
     d.lv[0].w = W;
