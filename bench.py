@@ -711,9 +711,15 @@ def cpu_baseline(args, r, cfg, pool_host, luts):
         the oracle's double-precision bilinear through the same maps, every camera of one frame: the
         histogram of per-channel differences;
       - output: the product's render against the oracle's render of the same frame, each from its own
-        geometry: the histogram of per-channel differences.
-    Also times the oracle on the 2-camera fisheye rig (2048x1024, 100 frames) and on the 8-camera
-    7680x3840 rig (a few frames)."""
+        geometry: the histogram of per-channel differences;
+      - secondary: the product's render against the reference's CPU render semantics
+        (TilingMultibandBlendFast: x255 masked pyrDown, R >> 8 normalisation), which the reference's
+        CPU and CUDA blends do not share: the histogram of per-channel differences.
+    The timed value is the reference's CPU render (CPUPanoramaRender: LUT, bilinear remap, the CPU
+    multiband blend) restated in the oracle and pinned bit for bit to the reference's own
+    TilingMultibandBlendFast; the CudaAccel-semantics oracle is timed beside it.  Also times the CPU
+    render on the 2-camera fisheye rig (2048x1024, 100 frames) and on the 8-camera 7680x3840 rig (a few
+    frames)."""
     import torch
     import oracle as O
     import panostitcher_gb300 as P
@@ -726,6 +732,7 @@ def cpu_baseline(args, r, cfg, pool_host, luts):
     cov = np.stack([m[2] for m in maps])
     seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov, threads=threads)
     ob = O.Blender(cov, seams, cfg.levels)
+    cb = O.CpuBlender(cov, seams, cfg.levels)
     geometry_s = time.perf_counter() - t
     xm, ym = [m[0] for m in maps], [m[1] for m in maps]
 
@@ -758,6 +765,7 @@ def cpu_baseline(args, r, cfg, pool_host, luts):
     r.render(frame, got, luts, check=True)
     torch.cuda.synchronize()
     ref = ob.render(frame, luts, xm, ym, threads)
+    cref = cb.render(frame, luts, xm, ym, threads)
     parity = {"rig": WORKLOADS[args.workload],
               "geometry": {"map_values_differing": map_diff,
                            "coverage_px_differing": int(((cov > 0) != (pcov > 0)).sum()),
@@ -765,24 +773,33 @@ def cpu_baseline(args, r, cfg, pool_host, luts):
                            "covered_px": int((cov > 0).sum())},
               "remap_delta_histogram": remap_hist,
               "output_delta_histogram": hist(got[..., :3], ref[..., :3]),
+              "cpu_semantics_delta_histogram": hist(got[..., :3], cref[..., :3]),
               "bar": "remap within +-1 LSB of the double-precision bilinear; output bit-exact given the same "
                      "geometry (tests/test_gpu_e2e_parity.py bounds the rest)",
               "oracle": "C restatement pinned bit for bit to the reference's Remap.cpp, ZReproject.cpp, "
-                        "CudaPyramid2.cu (built here from the reference tree; tests/test_ref_pin.py)"}
+                        "CudaPyramid2.cu, MultiBandBlend.cpp and Pyramid.cpp (built here from the reference "
+                        "tree; tests/test_ref_pin.py)"}
 
     # ---- timing
-    frames = 0
-    t = time.perf_counter()
-    while True:
-        ob.render(pool_host[frames % len(pool_host)], luts, xm, ym, threads)
-        frames += 1
-        el = time.perf_counter() - t
-        if el >= args.cpu_seconds:
-            break
+    def timed(render):
+        frames = 0
+        t = time.perf_counter()
+        while True:
+            render(pool_host[frames % len(pool_host)], luts, xm, ym, threads)
+            frames += 1
+            el = time.perf_counter() - t
+            if el >= args.cpu_seconds:
+                return frames, el
+
+    frames, el = timed(cb.render)
+    cframes, cel = timed(ob.render)
     res = {"value": round(frames * W * H / el / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
-           "sample": f"{frames} full frames of the {cfg.num_cams}-camera {W}x{H} rig (LUT + bilinear remap + "
-                     f"multiband blend) in {el:.1f} s; geometry from the camera parameters {geometry_s:.1f} s "
-                     f"before, untimed",
+           "sample": f"{frames} full frames of the {cfg.num_cams}-camera {W}x{H} rig through the reference's "
+                     f"CPU render (LUT + bilinear remap + TilingMultibandBlendFast) in {el:.1f} s; geometry "
+                     f"from the camera parameters {geometry_s:.1f} s before, untimed",
+           "cudaaccel_semantics": {"value": round(cframes * W * H / cel / 1e6, 4), "unit": "Mpix/s",
+                                   "sample": f"{cframes} frames of the oracle of the product's own semantics "
+                                             f"(CudaTilingMultibandBlendFast) in {cel:.1f} s"},
            "parity": parity}
     if args.scale == 1 and not args.no_cpu_rigs:
         res["other_rigs"] = {"c1": cpu_rig_timing("c1", 100, threads), "c5": cpu_rig_timing("c5", 8, threads)}
@@ -790,7 +807,8 @@ def cpu_baseline(args, r, cfg, pool_host, luts):
 
 
 def cpu_rig_timing(name, nframes, threads):
-    """The oracle's LUT + remap + blend on another benchmark rig: nframes frames on the host cores."""
+    """The reference's CPU render (LUT + remap + TilingMultibandBlendFast, restated in the oracle) on
+    another benchmark rig: nframes frames on the host cores."""
     import oracle as O
     from panostitcher_gb300 import synth as S
     cfg = S.rig(name)
@@ -798,7 +816,7 @@ def cpu_rig_timing(name, nframes, threads):
     maps = [O.reproject_map(p, cfg.src_size, cfg.dst_size, threads=threads) for p in cfg.cams]
     cov = np.stack([m[2] for m in maps])
     seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov, threads=threads)
-    ob = O.Blender(cov, seams, cfg.levels)
+    ob = O.CpuBlender(cov, seams, cfg.levels)
     fs = S.FrameSource(cfg)
     pool = [fs.frame(k) for k in range(2)]
     luts = S.luts(cfg)
@@ -814,9 +832,10 @@ def cpu_rig_timing(name, nframes, threads):
 
 # ----------------------------------------------------------------------------- reference arm
 def run_reference(args, world, rank):
-    """The reference path's CPU implementation (the oracle port, pinned bit for bit to the reference's own
-    geometry and pyramid code) on all host cores: per step, the same frames_per_step frames of the same
-    workload as our arm; the number of timed steps is bounded by --ref-seconds."""
+    """The reference's own CPU implementation of the path, CPUPanoramaRender::render (LUT, bilinear remap,
+    TilingMultibandBlendFast), as the oracle restates it and pins bit for bit to the reference's own code,
+    on all host cores: per step, the same frames_per_step frames of the same workload as our arm; the
+    number of timed steps is bounded by --ref-seconds."""
     import oracle as O
     from panostitcher_gb300 import synth as S
     O.build()
@@ -827,7 +846,7 @@ def run_reference(args, world, rank):
     maps = [O.reproject_map(p, cfg.src_size, cfg.dst_size, threads=threads) for p in cfg.cams]
     cov = np.stack([m[2] for m in maps])
     seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov, threads=threads)
-    ob = O.Blender(cov, seams, cfg.levels)
+    ob = O.CpuBlender(cov, seams, cfg.levels)
     fs = S.FrameSource(cfg)
     pool = [fs.frame(k) for k in range(args.pool)]
     luts = S.luts(cfg)
@@ -850,8 +869,9 @@ def run_reference(args, world, rank):
     el = time.perf_counter() - t
     value = steps * fps * W * H / el / 1e6
     frame_mb = sum(f.nbytes for f in pool[0]) / 1e6
-    sample = f"{steps} of {args.steps} steps ({fps} full {cfg.num_cams}-camera {W}x{H} frames each, LUT + " \
-             f"bilinear remap + multiband blend, {threads} threads), {warm} warm-up"
+    sample = f"{steps} of {args.steps} steps ({fps} full {cfg.num_cams}-camera {W}x{H} frames each through " \
+             f"the reference's CPU render: LUT + bilinear remap + TilingMultibandBlendFast, {threads} threads), " \
+             f"{warm} warm-up"
     return {"impl": "reference", "metric": METRICS[args.workload], "value": round(value, 4), "unit": "Mpix/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32",
@@ -876,7 +896,7 @@ def main(argv=None):
     ap.add_argument("--inflight", type=int, default=8, help="caller streams of the device-resident loop")
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-linear", action="store_true")

@@ -59,7 +59,7 @@ def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
     if force or not os.path.exists(_LIB_PATH) or \
             os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(os.path.join(_HERE, f))
-                                              for f in ("ps_oracle.c", "ps_oracle.h", "Makefile")):
+                                              for f in ("ps_oracle.c", "ps_oracle_cpu.c", "ps_oracle.h", "Makefile")):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -101,6 +101,17 @@ def lib():
             L.orc_mb_blend.argtypes = [vp, vp, vp, vp, vp]
             L.orc_mb_blend_mt.argtypes = [vp, vp, vp, C.c_int]
             L.orc_render.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int]
+            L.orc_cpu_mb_prepare.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+            L.orc_cpu_mb_prepare.restype = vp
+            L.orc_cpu_mb_free.argtypes = [vp]
+            L.orc_cpu_mb_num_levels.argtypes = [vp]
+            L.orc_cpu_mb_num_levels.restype = C.c_int
+            L.orc_cpu_mb_full_mask.argtypes = [vp]
+            L.orc_cpu_mb_full_mask.restype = C.c_int
+            L.orc_cpu_mb_get_weight.argtypes = [vp, C.c_int, C.c_int, vp]
+            L.orc_cpu_mb_get_alpha.argtypes = [vp, C.c_int, C.c_int, vp]
+            L.orc_cpu_mb_blend.argtypes = [vp, vp, vp, vp, C.c_int]
+            L.orc_cpu_render.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int]
             L.orc_linear_weights.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp]
             L.orc_linear_render.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int,
                                             vp]
@@ -414,4 +425,74 @@ class Blender:
         dst = np.empty((self.H, self.W, 4), np.uint8)
         lib().orc_render(self._h, _ptr_array(srcs), sw, sh, chn, None if lt is None else _ptr(lt),
                          _ptr_array(xm), _ptr_array(ym), _ptr(dst), nthreads)
+        return dst
+
+
+class CpuBlender:
+    """TilingMultibandBlendFast restated (the reference's CPU twin of the blend,
+    source/Blend/MultiBandBlend.cpp:906-1031): prepare(masks) + blend(images).
+
+    Its arithmetic differs from the CudaAccel semantics that Blender restates
+    and the product computes (x255 masked pyrDown, R >> 8 full-mask
+    normalisation, saturating Laplacian, OpenCV borders); it serves the
+    secondary difference histogram and the timed reference CPU path."""
+
+    def __init__(self, masks: np.ndarray, seams: np.ndarray, max_levels: int, min_length: int = 2):
+        masks = np.ascontiguousarray(masks, np.uint8)
+        seams = np.ascontiguousarray(seams, np.uint8)
+        self.n, self.H, self.W = masks.shape
+        self._h = lib().orc_cpu_mb_prepare(_ptr(masks), _ptr(seams), self.n, self.W, self.H, max_levels,
+                                           min_length)
+        if not self._h:
+            raise ValueError("oracle prepare failed")
+        self.levels = lib().orc_cpu_mb_num_levels(self._h)
+        self.full_mask = bool(lib().orc_cpu_mb_full_mask(self._h))
+        self.sizes = level_sizes(self.W, self.H, self.levels)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().orc_cpu_mb_free(h)
+            self._h = None
+
+    def weight(self, cam: int, level: int) -> np.ndarray:
+        w, h = self.sizes[level]
+        out = np.empty((h, w), np.int16)
+        lib().orc_cpu_mb_get_weight(self._h, cam, level, _ptr(out))
+        return out
+
+    def alpha(self, cam: int, level: int) -> np.ndarray:
+        w, h = self.sizes[level]
+        out = np.empty((h, w), np.int32)
+        lib().orc_cpu_mb_get_alpha(self._h, cam, level, _ptr(out))
+        return out
+
+    def blend(self, images, pyramids: bool = False, nthreads: int = 1):
+        """BGR32 (H, W, 4) blend of n (H, W, 4) int16 level-0 images; with ``pyramids`` also the
+        collapsed int32x3 result pyramid, level by level."""
+        imgs = [np.ascontiguousarray(im, np.int16) for im in images]
+        assert len(imgs) == self.n
+        dst = np.empty((self.H, self.W, 4), np.uint8)
+        if not pyramids:
+            lib().orc_cpu_mb_blend(self._h, _ptr_array(imgs), _ptr(dst), None, nthreads)
+            return dst
+        tot = sum(w * h for (w, h) in self.sizes)
+        coll = np.empty((tot, 3), np.int32)
+        lib().orc_cpu_mb_blend(self._h, _ptr_array(imgs), _ptr(dst), _ptr(coll), nthreads)
+        out, off = [], 0
+        for (w, h) in self.sizes:
+            out.append(coll[off:off + w * h].reshape(h, w, 3))
+            off += w * h
+        return dst, out
+
+    def render(self, srcs, luts, xmaps, ymaps, nthreads: int = 1) -> np.ndarray:
+        """CPUPanoramaRender::render: LUT -> bilinear remap to int16 -> this blend."""
+        srcs = [np.ascontiguousarray(s, np.uint8) for s in srcs]
+        sh, sw, chn = srcs[0].shape
+        xm = [np.ascontiguousarray(x, np.float32) for x in xmaps]
+        ym = [np.ascontiguousarray(y, np.float32) for y in ymaps]
+        lt = None if luts is None else np.ascontiguousarray(luts, np.uint8).reshape(self.n, 3, 256)
+        dst = np.empty((self.H, self.W, 4), np.uint8)
+        lib().orc_cpu_render(self._h, _ptr_array(srcs), sw, sh, chn, None if lt is None else _ptr(lt),
+                             _ptr_array(xm), _ptr_array(ym), _ptr(dst), nthreads)
         return dst

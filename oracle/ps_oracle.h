@@ -108,6 +108,34 @@ void orc_mb_blend(orc_blender* b, const int16_t* const* images, uint8_t* dst, in
 /* same arithmetic, camera pyramids built on nthreads threads */
 void orc_mb_blend_mt(orc_blender* b, const int16_t* const* images, uint8_t* dst, int nthreads);
 
+/* ---- multiband blend, CPU semantics (TilingMultibandBlendFast) ------------ */
+/* The reference's CPU twin of the blend (source/Blend/MultiBandBlend.cpp:
+   906-1031 with source/Blend/Pyramid.cpp), restated in ps_oracle_cpu.c.  It
+   differs from the CudaAccel semantics above, which the product computes:
+   the masked pyrDown divides ((S << 8) - S) by the alpha sum, the full-mask
+   normalisation is R >> 8, the Laplacian subtract saturates, and its borders
+   are OpenCV's (reflect-101 rows, wrapped columns).  Same inputs as
+   orc_mb_prepare: coverage masks and unique masks, n*W*H each.  coll_out
+   (nullable) receives the collapsed result pyramid, int32x3 per pixel,
+   levels 0..L packed.  nthreads host threads; the result does not depend on
+   them. */
+typedef struct orc_cpu_blender orc_cpu_blender;
+orc_cpu_blender* orc_cpu_mb_prepare(const uint8_t* masks, const uint8_t* seams, int n, int W, int H, int maxLevels,
+                                    int minLength);
+void orc_cpu_mb_free(orc_cpu_blender* b);
+int orc_cpu_mb_num_levels(const orc_cpu_blender* b);
+int orc_cpu_mb_full_mask(const orc_cpu_blender* b);
+void orc_cpu_mb_get_weight(const orc_cpu_blender* b, int cam, int level, int16_t* out);
+void orc_cpu_mb_get_alpha(const orc_cpu_blender* b, int cam, int level, int32_t* out);
+void orc_cpu_mb_blend(orc_cpu_blender* b, const int16_t* const* images, uint8_t* dst, int32_t* coll_out,
+                      int nthreads);
+/* CPUPanoramaRender::render (source/Task/RicohUtil.cpp:1481-1587): per camera
+   LUT, row-parallel bilinear remap to int16, then the CPU blend; arguments as
+   orc_render. */
+void orc_cpu_render(orc_cpu_blender* b, const uint8_t* const* srcs, int srcW, int srcH, int channels,
+                    const uint8_t* luts, const float* const* xmaps, const float* const* ymaps, uint8_t* dst,
+                    int nthreads);
+
 /* ---- whole render (CPUPanoramaRender / CudaPanoramaRender2 dataflow) ---- */
 /* srcs: n BGR24/BGR32 frames; luts: n*3*256 or NULL; maps: n float x/y maps.
    Writes BGR32 dst.  nthreads>1 uses the row-parallel remap and the

@@ -4,8 +4,9 @@
 lie in the reference tree, the reference's geometry and CPU remap
 (``source/Warp/Remap.cpp``, ``source/Warp/ZReproject.cpp``), its integer
 pyramid kernels with their host wrappers (``source/CudaAccel/CudaPyramid2.cu``,
-``CudaUtil.cuh``) and its YUV conversions (``source/CudaAccel/ImageProc.cu``)
-into ``oracle/_ref/libpsref.so``.  OpenCV is replaced by ``oracle/ref/cv_shim``
+``CudaUtil.cuh``), its YUV conversions (``source/CudaAccel/ImageProc.cu``) and
+its CPU multiband blend (``source/Blend/MultiBandBlend.cpp`` with
+``Pyramid.cpp``) into ``oracle/_ref/libpsref.so``.  OpenCV is replaced by ``oracle/ref/cv_shim``
 and the CUDA runtime by ``oracle/ref/cuda_emu``, which runs the kernels on host
 cores.  ``oracle/ref/ref_driver.cpp`` chains them as the reference's callers do.
 
@@ -72,9 +73,10 @@ def lib():
             L.psref_reproject_map.argtypes = [C.POINTER(OrcParam), i, i, i, i, vp, vp]
             L.psref_reproject_16s.argtypes = [vp, i, i, i, vp, i, i, vp]
             L.psref_mb_blend.argtypes = [i, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
+            L.psref_cpu_mb_blend.argtypes = [i, i, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
             L.psref_bgr32_to_yuv.argtypes = [vp, i, i, i, vp, vp, vp]
             L.psref_yuv_to_bgr32.argtypes = [vp, vp, vp, i, i, i, vp]
-            for name in ("psref_reproject_map", "psref_reproject_16s", "psref_mb_blend",
+            for name in ("psref_reproject_map", "psref_reproject_16s", "psref_mb_blend", "psref_cpu_mb_blend",
                          "psref_bgr32_to_yuv", "psref_yuv_to_bgr32"):
                 getattr(L, name).restype = i
             _lib = L
@@ -170,6 +172,38 @@ def mb_blend(masks: np.ndarray, seams: np.ndarray, images, levels: int, pyramids
     return out, {
         "norm": _split(norm, sizes, 4),
         "coll": _split(coll, sizes, 4),
+        "weight": [_split(wts[i], sizes, 1) for i in range(n)],
+        "alpha": [_split(als[i], sizes, 1) for i in range(n)],
+    }
+
+
+def cpu_mb_blend(masks: np.ndarray, seams: np.ndarray, images, max_levels: int, min_length: int = 2):
+    """The reference's TilingMultibandBlendFast: prepare(masks, max_levels, min_length) + blend(images).
+
+    masks / seams: (n, H, W) coverage and unique masks; images: n (H, W, 4)
+    int16 level-0 images (B, G, R used).  Returns the BGR32 (H, W, 4) blend
+    and a dict of the collapsed int32x3 result pyramid and the per-camera
+    weight (int16) and alpha (int32) pyramids.
+    """
+    masks = np.ascontiguousarray(masks, np.uint8)
+    seams = np.ascontiguousarray(seams, np.uint8)
+    n, H, W = masks.shape
+    imgs = np.ascontiguousarray(np.stack([np.asarray(im, np.int16) for im in images]))
+    assert imgs.shape == (n, H, W, 4)
+    from . import num_levels
+    sizes = _level_sizes(W, H, num_levels(W, H, max_levels, min_length))
+    tot = sum(w * h for (w, h) in sizes)
+    out = np.empty((H, W, 4), np.uint8)
+    coll = np.empty((tot, 3), np.int32)
+    wts = np.empty((n, tot), np.int16)
+    als = np.empty((n, tot), np.int32)
+    levels = C.c_int(-1)
+    _check(_need().psref_cpu_mb_blend(n, W, H, max_levels, min_length, _ptr(masks), _ptr(seams), _ptr(imgs),
+                                      _ptr(out), _ptr(coll), _ptr(wts), _ptr(als), C.byref(levels)),
+           "TilingMultibandBlendFast")
+    assert levels.value == len(sizes) - 1
+    return out, {
+        "coll": _split(coll, sizes, 3),
         "weight": [_split(wts[i], sizes, 1) for i in range(n)],
         "alpha": [_split(als[i], sizes, 1) for i in range(n)],
     }

@@ -13,7 +13,14 @@
  *   - Mat::convertTo(dst, depth): saturate_cast<dst depth> per element
  *     (alpha = 1, beta = 0 only);
  *   - Mat::setTo(s, mask): every channel of the elements whose mask byte is
- *     non-zero (all elements without a mask) takes saturate_cast(s[c]).
+ *     non-zero (all elements without a mask) takes saturate_cast(s[c]);
+ *   - add / subtract: saturate_cast<depth>(a +- b) per element, where the
+ *     sum is formed in int for the integer depths (so 32-bit sums wrap);
+ *   - bitwise operators on 8-bit masks, countNonZero;
+ *   - borderInterpolate: OpenCV's documented mapping of an outside index p
+ *     (reflect-101 and reflect mirror about the edge, with or without
+ *     repeating it, and map every index to 0 when len == 1; wrap takes p
+ *     modulo len; replicate clamps).
  * Images are continuous: step = cols * elemSize, so rows are packed.
  */
 #ifndef PSEMU_OPENCV2_CORE_HPP
@@ -26,6 +33,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <ostream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -62,12 +70,25 @@
 #define CV_64FC1 CV_MAKETYPE(CV_64F, 1)
 #define CV_64FC2 CV_MAKETYPE(CV_64F, 2)
 
+#define CV_CN_MAX 512
+#define CV_CPU_SSE 1
+#define CV_CPU_SSE2 2
+#define CV_StsUnsupportedFormat (-210)
+#define CV_Error(code, msg) throw std::runtime_error(std::string("CV_Error: ") + (msg))
+
 #define CV_Assert(expr) \
     do { if (!(expr)) throw std::runtime_error(std::string("CV_Assert failed: ") + #expr); } while (0)
 
 typedef unsigned char uchar;
 typedef signed char schar;
 typedef unsigned short ushort;
+
+/* MSVC's bounded sprintf into a char array, which the reference's
+   debugging helpers call. */
+template <size_t N, class... A> inline int sprintf_s(char (&buf)[N], const char* fmt, A... a)
+{
+    return std::snprintf(buf, N, fmt, a...);
+}
 
 namespace cv {
 
@@ -76,6 +97,43 @@ typedef signed char schar;
 typedef unsigned short ushort;
 
 inline int cvRound(double v) { return (int)std::nearbyint(v); }
+
+enum { BORDER_CONSTANT = 0, BORDER_REPLICATE = 1, BORDER_REFLECT = 2, BORDER_WRAP = 3, BORDER_REFLECT_101 = 4,
+       BORDER_REFLECT101 = 4, BORDER_DEFAULT = 4 };
+
+inline int borderInterpolate(int p, int len, int borderType)
+{
+    if (p >= 0 && p < len) return p;
+    switch (borderType) {
+    case BORDER_REPLICATE: return p < 0 ? 0 : len - 1;
+    case BORDER_REFLECT:
+    case BORDER_REFLECT_101: {
+        const int skipEdge = borderType == BORDER_REFLECT_101;
+        if (len == 1) return 0;
+        while (p < 0 || p >= len) p = p < 0 ? -p - 1 + skipEdge : 2 * len - 1 - p - skipEdge;
+        return p;
+    }
+    case BORDER_WRAP:
+        if (len <= 0) throw std::runtime_error("borderInterpolate: empty range");
+        p %= len;
+        return p < 0 ? p + len : p;
+    default: return -1;
+    }
+}
+
+inline bool checkHardwareSupport(int) { return true; }
+inline size_t alignSize(size_t sz, int n) { return (sz + n - 1) & ~(size_t)(n - 1); }
+template <class T> inline T* alignPtr(T* p, int n) { return (T*)(((size_t)p + n - 1) & ~(size_t)(n - 1)); }
+
+/* Heap buffer of n elements (value-initialised). */
+template <class T, size_t = 0> class AutoBuffer {
+public:
+    explicit AutoBuffer(size_t n) : v_(n ? n : 1) {}
+    operator T*() { return v_.data(); }
+    operator const T*() const { return v_.data(); }
+private:
+    std::vector<T> v_;
+};
 
 template <class T> inline T saturate_cast(int v)
 {
@@ -137,6 +195,26 @@ typedef Vec<float, 3> Vec3f;
 typedef Vec<float, 4> Vec4f;
 typedef Vec<double, 2> Vec2d;
 typedef Vec<double, 3> Vec3d;
+
+template <class T> struct Rect_ {
+    T x = 0, y = 0, width = 0, height = 0;
+    Rect_() {}
+    Rect_(T vx, T vy, T w, T h) : x(vx), y(vy), width(w), height(h) {}
+    Size size() const { return Size((int)width, (int)height); }
+    T area() const { return width * height; }
+};
+typedef Rect_<int> Rect;
+template <class T> inline bool operator==(const Rect_<T>& a, const Rect_<T>& b)
+{
+    return a.x == b.x && a.y == b.y && a.width == b.width && a.height == b.height;
+}
+template <class T> inline Rect_<T> operator&(const Rect_<T>& a, const Rect_<T>& b)
+{
+    const T x0 = std::max(a.x, b.x), y0 = std::max(a.y, b.y);
+    const T x1 = std::min(a.x + a.width, b.x + b.width), y1 = std::min(a.y + a.height, b.y + b.height);
+    if (x1 <= x0 || y1 <= y0) return Rect_<T>();
+    return Rect_<T>(x0, y0, x1 - x0, y1 - y0);
+}
 
 struct Range {
     int start = 0, end = 0;
@@ -262,6 +340,14 @@ public:
         dst.create(rows, cols, type_);
         for (int r = 0; r < rows; ++r) std::memcpy(dst.ptr(r), ptr(r), (size_t)cols * elemSize());
     }
+    void copyTo(Mat& dst, const Mat& mask) const
+    {
+        dst.create(rows, cols, type_);
+        const size_t es = elemSize();
+        for (int r = 0; r < rows; ++r)
+            for (int c = 0; c < cols; ++c)
+                if (mask.ptr(r)[c]) std::memcpy(dst.ptr(r) + c * es, ptr(r) + c * es, es);
+    }
     Mat clone() const { Mat m; copyTo(m); return m; }
     void convertTo(Mat& dst, int rtype, double alpha = 1, double beta = 0) const
     {
@@ -280,6 +366,73 @@ private:
     int type_ = 0;
     std::shared_ptr<uchar> buf_;
 };
+
+namespace detail {
+template <class T> inline void binaryOp(const Mat& a, const Mat& b, Mat& dst, int sign)
+{
+    CV_Assert(a.size() == b.size() && a.type() == b.type());
+    const Mat sa = a, sb = b;  /* dst may alias either operand */
+    dst.create(a.rows, a.cols, a.type());
+    const size_t n = (size_t)a.cols * a.channels();
+    for (int r = 0; r < a.rows; ++r) {
+        const T* pa = sa.ptr<T>(r);
+        const T* pb = sb.ptr<T>(r);
+        T* pd = dst.ptr<T>(r);
+        for (size_t i = 0; i < n; ++i) {
+            if (std::numeric_limits<T>::is_integer && sizeof(T) < sizeof(int))
+                pd[i] = saturate_cast<T>(sign > 0 ? (int)pa[i] + (int)pb[i] : (int)pa[i] - (int)pb[i]);
+            else
+                pd[i] = (T)(sign > 0 ? pa[i] + pb[i] : pa[i] - pb[i]);
+        }
+    }
+}
+inline void arith(const Mat& a, const Mat& b, Mat& dst, int sign)
+{
+    switch (a.depth()) {
+    case CV_8U: binaryOp<uchar>(a, b, dst, sign); break;
+    case CV_8S: binaryOp<schar>(a, b, dst, sign); break;
+    case CV_16U: binaryOp<ushort>(a, b, dst, sign); break;
+    case CV_16S: binaryOp<short>(a, b, dst, sign); break;
+    case CV_32S: binaryOp<int>(a, b, dst, sign); break;
+    case CV_32F: binaryOp<float>(a, b, dst, sign); break;
+    case CV_64F: binaryOp<double>(a, b, dst, sign); break;
+    }
+}
+template <class F> inline Mat bytewise(const Mat& a, const Mat* b, F f)
+{
+    if (b) CV_Assert(a.size() == b->size() && a.type() == b->type());
+    Mat out(a.rows, a.cols, a.type());
+    const size_t n = (size_t)a.cols * a.elemSize();
+    for (int r = 0; r < a.rows; ++r)
+        for (size_t i = 0; i < n; ++i) out.ptr(r)[i] = f(a.ptr(r)[i], b ? b->ptr(r)[i] : (uchar)0);
+    return out;
+}
+}  // namespace detail
+
+inline void add(const Mat& a, const Mat& b, Mat& dst) { detail::arith(a, b, dst, 1); }
+inline void subtract(const Mat& a, const Mat& b, Mat& dst) { detail::arith(a, b, dst, -1); }
+inline void bitwise_not(const Mat& a, Mat& dst) { dst = detail::bytewise(a, nullptr, [](uchar x, uchar) { return (uchar)~x; }); }
+inline Mat operator~(const Mat& a) { return detail::bytewise(a, nullptr, [](uchar x, uchar) { return (uchar)~x; }); }
+inline Mat operator&(const Mat& a, const Mat& b) { return detail::bytewise(a, &b, [](uchar x, uchar y) { return (uchar)(x & y); }); }
+inline Mat operator|(const Mat& a, const Mat& b) { return detail::bytewise(a, &b, [](uchar x, uchar y) { return (uchar)(x | y); }); }
+inline Mat& operator&=(Mat& a, const Mat& b) { a = a & b; return a; }
+inline Mat& operator|=(Mat& a, const Mat& b) { a = a | b; return a; }
+inline Mat& operator-=(Mat& a, const Mat& b) { subtract(a, b, a); return a; }
+inline int countNonZero(const Mat& a)
+{
+    CV_Assert(a.channels() == 1);
+    int c = 0;
+    const size_t es = a.elemSize();
+    for (int r = 0; r < a.rows; ++r)
+        for (int x = 0; x < a.cols; ++x) {
+            const uchar* p = a.ptr(r) + x * es;
+            bool nz = false;
+            for (size_t k = 0; k < es; ++k) nz |= p[k] != 0;
+            c += nz;
+        }
+    return c;
+}
+inline std::ostream& operator<<(std::ostream& o, const Mat&) { return o << "[Mat]"; }
 
 inline void split(const Mat& m, Mat* out)
 {

@@ -20,6 +20,9 @@ frames, LUTs and random masks.  Everything else is the reference's output:
   - out, coll, norm1, alpha1, weight1: the blend, its collapsed pyramid
     (every level), the normalised level 1 and the level-1 alpha and weight
     pyramids;
+  - cpu_out: the reference's CPU blend, TilingMultibandBlendFast
+    (source/Blend/MultiBandBlend.cpp:906-1031 with Pyramid.cpp), of the same
+    level-0 images and masks;
   - yuv_*: cvtBGR32ToYUV420P / cvtBGR32ToNV12 and the inverse conversions.
 
   python tests/golden/make_golden.py
@@ -66,13 +69,14 @@ def rig_case(name, factor, frame):
         level0.append(R.reproject_16s(apply_luts(frames[i], luts[i]), m64))
         quirk.append((cov[i] > 0) & (np.floor(xm) == sw - 1))
     out, pyr = R.mb_blend(cov, seams, level0, levels, pyramids=True)
+    cpu_out, _ = R.cpu_mb_blend(cov, seams, level0, cfg.levels)
     n = cfg.num_cams
     coll = np.concatenate([c.reshape(-1, 4) for c in pyr["coll"]])
     return dict(source=np.array("reference"), params=json.dumps(cfg.cams), src_size=np.array(cfg.src_size),
                 dst_size=np.array(cfg.dst_size), levels=np.array(cfg.levels), num_levels=np.array(levels),
                 frames=np.stack(frames), luts=luts, xmaps=np.stack([m[0] for m in maps]),
                 ymaps=np.stack([m[1] for m in maps]), cov=cov, seams=seams, level0=np.stack(level0),
-                quirk=np.stack(quirk), out=out, coll=coll, norm1=pyr["norm"][1],
+                quirk=np.stack(quirk), out=out, cpu_out=cpu_out, coll=coll, norm1=pyr["norm"][1],
                 alpha1=np.stack([pyr["alpha"][i][1] for i in range(n)]),
                 weight1=np.stack([pyr["weight"][i][1] for i in range(n)]))
 
@@ -93,8 +97,9 @@ def partition_case(W, H, n, levels, seed):
     imgs[cov == 0] = 0
     nl = O.num_levels(W, H, levels)
     out = R.mb_blend(cov, seams, list(imgs), nl)
+    cpu_out, _ = R.cpu_mb_blend(cov, seams, list(imgs), levels)
     return dict(source=np.array("reference"), cov=cov, seams=seams, level0=imgs, levels=np.array(levels),
-                out=out, num_levels=np.array(nl))
+                out=out, cpu_out=cpu_out, num_levels=np.array(nl))
 
 
 def yuv_case(W, H, seed):

@@ -3,8 +3,10 @@
 oracle/_ref/libpsref.so is the reference's geometry and CPU remap
 (source/Warp/Remap.cpp, ZReproject.cpp), its integer pyramid kernels and
 wrappers (source/CudaAccel/CudaPyramid2.cu) chained as
-CudaTilingMultibandBlendFast::prepare/blend chains them, and its YUV
-conversions (source/CudaAccel/ImageProc.cu), compiled unchanged by
+CudaTilingMultibandBlendFast::prepare/blend chains them, its YUV
+conversions (source/CudaAccel/ImageProc.cu) and its CPU multiband blend
+class TilingMultibandBlendFast (source/Blend/MultiBandBlend.cpp with
+Pyramid.cpp), compiled unchanged by
 `make -C oracle ref`; the kernels run on host cores under oracle/ref/cuda_emu.
 It can only be built where the reference tree is present, so these tests
 skip elsewhere; the committed fixtures of tests/golden/ carry the same pin
@@ -123,6 +125,57 @@ def test_partition_blend_bit_exact(oracle_lib, W, H, n, levels, full):
     ob = blend_case(cov, seams, imgs, levels)
     if full:
         assert ob.full_mask
+
+
+def cpu_blend_case(cov, seams, level0, max_levels, min_length=2):
+    """The CPU-semantics restatement against the reference's own TilingMultibandBlendFast: output,
+    collapsed pyramid, weight and alpha pyramids, at one and at several host threads."""
+    ob = O.CpuBlender(cov, seams, max_levels, min_length)
+    rout, rp = R.cpu_mb_blend(cov, seams, level0, max_levels, min_length)
+    for nthreads in (1, 4):
+        out, coll = ob.blend(level0, pyramids=True, nthreads=nthreads)
+        assert np.array_equal(out, rout), f"output, {nthreads} threads"
+        for j in range(ob.levels + 1):
+            assert np.array_equal(coll[j], rp["coll"][j]), f"collapsed level {j}, {nthreads} threads"
+    for i in range(cov.shape[0]):
+        for j in range(ob.levels + 1):
+            assert np.array_equal(ob.weight(i, j), rp["weight"][i][j]), f"weight {i} level {j}"
+            if j:
+                assert np.array_equal(ob.alpha(i, j), rp["alpha"][i][j]), f"alpha {i} level {j}"
+    return ob
+
+
+@pytest.mark.parametrize("name,factor", SCALED)
+def test_rig_cpu_blend_bit_exact(oracle_lib, name, factor):
+    cfg = S.scaled_rig(S.rig(name), factor)
+    frames = S.FrameSource(cfg).frame(1)
+    luts = S.luts(cfg)
+    geo = [geometry_pair(cfg, i) for i in range(cfg.num_cams)]
+    cov = np.stack([g[1] for g in geo])
+    seams = O.nearest_axis_seams(cfg.cams, cfg.src_size, cfg.dst_size, cov)
+    level0 = [O.reproject_16s(frames[i], geo[i][4], geo[i][5], luts[i]) for i in range(cfg.num_cams)]
+    cpu_blend_case(cov, seams, level0, cfg.levels)
+
+
+@pytest.mark.parametrize("W,H,n,levels,full", [(33, 17, 3, 5, False), (130, 67, 4, 8, False),
+                                               (257, 129, 5, 8, True), (96, 48, 12, 6, False),
+                                               (512, 256, 2, 8, False)])
+def test_partition_cpu_blend_bit_exact(oracle_lib, W, H, n, levels, full):
+    rng = np.random.default_rng(W * 31 + H + n)
+    cov, seams, imgs = random_partition(rng, W, H, n, full)
+    ob = cpu_blend_case(cov, seams, imgs, levels)
+    if full:
+        assert ob.full_mask
+
+
+@pytest.mark.parametrize("W,H", [(1, 1), (2, 1), (1, 6), (3, 2), (5, 3), (7, 5), (9, 4), (4, 4)])
+def test_tiny_cpu_blend_bit_exact(oracle_lib, W, H):
+    """Sizes down to one pixel with the shortest side length 1, so that every level's border mapping
+    (wrapped columns, reflected rows, the one-pixel cases) is exercised."""
+    rng = np.random.default_rng(W * 7 + H)
+    for full in (True, False):
+        cov, seams, imgs = random_partition(rng, W, H, 2, full)
+        cpu_blend_case(cov, seams, imgs, 16, 1)
 
 
 @pytest.mark.parametrize("W,H", [(2, 2), (66, 34), (130, 66), (640, 360)])
