@@ -165,7 +165,29 @@ struct orc_cpu_blender {
     int32_t* alpha;   /* n * total: alphaPyrs (levels >= 1; level 0 unused) */
     int32_t* wsum;    /* total: resultWeightPyr (only if !full) */
     uint8_t* masknot; /* W*H: maskNot (only if !full) */
+    /* Working memory, allocated once and reused by every blend, as the
+       reference allocates its pyramids at prepare (:929-930): returning it
+       to the system after each frame makes every frame fault it in again,
+       which costs far more than the blend on hosts that keep device page
+       tables coherent with the CPU's. */
+    int16_t* g;       /* 3 * total: one camera's image pyramid (imagePyr) */
+    int32_t* res;     /* 3 * total: resultPyr */
+    int16_t* level0;  /* n * W*H*4: the render's remapped images */
+    uint8_t* lutted;  /* the render's LUT'd source frame */
+    size_t luttedBytes;
+    pool_t* pool;
+    int poolThreads;
 };
+
+static pool_t* blender_pool(orc_cpu_blender* b, int nthreads)
+{
+    if (!b->pool || b->poolThreads != nthreads) {
+        if (b->pool) pool_destroy(b->pool);
+        b->pool = pool_create(nthreads);
+        b->poolThreads = nthreads;
+    }
+    return b->pool;
+}
 
 static size_t cpu_total(const orc_cpu_blender* b) { return b->off[b->L + 1]; }
 
@@ -202,6 +224,8 @@ orc_cpu_blender* orc_cpu_mb_prepare(const uint8_t* masks, const uint8_t* seams, 
     b->off[0] = 0;
     for (int j = 0; j <= b->L; j++) b->off[j + 1] = b->off[j] + (size_t)b->ws[j] * b->hs[j];
     const size_t tot = cpu_total(b), npx = (size_t)W * H;
+    b->g = (int16_t*)malloc(sizeof(int16_t) * 3 * tot);
+    b->res = (int32_t*)malloc(sizeof(int32_t) * 3 * tot);
     b->weight = (int16_t*)calloc((size_t)n * tot, sizeof(int16_t));
     b->alpha = (int32_t*)calloc((size_t)n * tot, sizeof(int32_t));
     int16_t* tmp = (int16_t*)malloc(sizeof(int16_t) * tot);
@@ -258,6 +282,11 @@ void orc_cpu_mb_free(orc_cpu_blender* b)
     free(b->alpha);
     free(b->wsum);
     free(b->masknot);
+    free(b->g);
+    free(b->res);
+    free(b->level0);
+    free(b->lutted);
+    if (b->pool) pool_destroy(b->pool);
     free(b);
 }
 
@@ -394,6 +423,13 @@ static void pass_up_lap(void* arg, int y0, int y1)
     free(h);
 }
 
+/* resultPyr[i].setTo(0) (:999-1000), over the packed pixels of all levels */
+static void pass_zero(void* arg, int p0, int p1)
+{
+    blend_ctx* c = (blend_ctx*)arg;
+    memset(c->res + 3 * (size_t)p0, 0, sizeof(int32_t) * 3 * (size_t)(p1 - p0));
+}
+
 /* the top level, a Gaussian, accumulated as it is */
 static void pass_top(void* arg, int y0, int y1)
 {
@@ -481,9 +517,11 @@ static void cpu_blend_pool(orc_cpu_blender* b, const int16_t* const* images, uin
     blend_ctx c;
     memset(&c, 0, sizeof(c));
     c.b = b;
-    c.g = (int16_t*)malloc(sizeof(int16_t) * 3 * tot);
-    c.res = (int32_t*)calloc(3 * tot, sizeof(int32_t));  /* resultPyr[i].setTo(0) (:999-1000) */
+    c.g = b->g;
+    c.res = b->res;
     c.dst = dst;
+    const int chunkPx = (int)(tot / (8 * (size_t)nthreads) + 1);
+    pool_for(pool, (int)tot, chunkPx, pass_zero, &c);
     const int L = b->L;
     for (int i = 0; i < b->n; i++) {
         c.cam = i;
@@ -499,24 +537,20 @@ static void cpu_blend_pool(orc_cpu_blender* b, const int16_t* const* images, uin
         }
         pool_for(pool, b->hs[L], row_chunk(b->hs[L], nthreads), pass_top, &c);
     }
-    pool_for(pool, (int)tot, (int)(tot / (8 * (size_t)nthreads) + 1), pass_norm, &c);  /* :1021-1024 */
+    pool_for(pool, (int)tot, chunkPx, pass_norm, &c);  /* :1021-1024 */
     for (int j = L - 1; j >= 0; j--) {  /* :1025 */
         c.j = j;
         pool_for(pool, b->hs[j + 1], row_chunk(b->hs[j + 1], nthreads), pass_collapse, &c);
     }
     if (coll_out) memcpy(coll_out, c.res, sizeof(int32_t) * 3 * tot);
     pool_for(pool, b->H, row_chunk(b->H, nthreads), pass_out, &c);
-    free(c.g);
-    free(c.res);
 }
 
 void orc_cpu_mb_blend(orc_cpu_blender* b, const int16_t* const* images, uint8_t* dst, int32_t* coll_out,
                       int nthreads)
 {
     if (nthreads < 1) nthreads = 1;
-    pool_t* pool = pool_create(nthreads);
-    cpu_blend_pool(b, images, dst, coll_out, pool, nthreads);
-    pool_destroy(pool);
+    cpu_blend_pool(b, images, dst, coll_out, blender_pool(b, nthreads), nthreads);
 }
 
 /* ======================================================================== */
@@ -560,14 +594,21 @@ void orc_cpu_render(orc_cpu_blender* b, const uint8_t* const* srcs, int srcW, in
                     int nthreads)
 {
     if (nthreads < 1) nthreads = 1;
-    pool_t* pool = pool_create(nthreads);
+    pool_t* pool = blender_pool(b, nthreads);
     const size_t npx = (size_t)b->W * b->H;
+    if (!b->level0) b->level0 = (int16_t*)malloc(sizeof(int16_t) * 4 * npx * (size_t)b->n);
+    const size_t lb = (size_t)srcW * srcH * channels;
+    if (luts && b->luttedBytes < lb) {
+        free(b->lutted);
+        b->lutted = (uint8_t*)malloc(lb);
+        b->luttedBytes = lb;
+    }
     int16_t** imgs = (int16_t**)calloc((size_t)b->n, sizeof(int16_t*));
     render_ctx c;
     memset(&c, 0, sizeof(c));
-    c.lutted = luts ? (uint8_t*)malloc((size_t)srcW * srcH * channels) : NULL;
+    c.lutted = b->lutted;
     for (int i = 0; i < b->n; i++) {
-        imgs[i] = (int16_t*)malloc(sizeof(int16_t) * 4 * npx);
+        imgs[i] = b->level0 + 4 * npx * (size_t)i;
         c.src = srcs[i];
         c.lut = luts ? luts + (size_t)i * 768 : NULL;
         c.srcW = srcW;
@@ -581,8 +622,5 @@ void orc_cpu_render(orc_cpu_blender* b, const uint8_t* const* srcs, int srcW, in
         pool_for(pool, b->H, row_chunk(b->H, nthreads), pass_remap, &c);
     }
     cpu_blend_pool(b, (const int16_t* const*)imgs, dst, NULL, pool, nthreads);
-    for (int i = 0; i < b->n; i++) free(imgs[i]);
     free(imgs);
-    free(c.lutted);
-    pool_destroy(pool);
 }
