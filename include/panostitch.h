@@ -303,8 +303,7 @@ int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out,
    one kernel kind (0 remap, 1 pyrDown, 2 blend, 3 the tail kernel that runs
    the few-tile top levels, reported at its lowest blend level, 4 the
    linear-blend render, 5 the conversion of decoder frames, at level 0, 6
-   the blend of few-tile levels in half tiles, 7 the deferred level-0 blend
-   that stores its normalised sums, 8 the level-0 collapse that finishes it) at
+   the blend of few-tile levels in half tiles) at
    one level (-1 = all levels): launch count, summed device milliseconds
    and summed algorithmic bytes (each input and output element counted
    once).
@@ -339,13 +338,6 @@ typedef struct ps_launch_shape {
     int small_blend_max_items; /* blend levels above 0 (below the tail) with at
                              most this many tiles run as 64x8 half tiles, up to
                              eight cameras staged at once; 0 = none (default 0) */
-    int defer_level0;     /* 1: the level-0 blend computes its normalised sums as
-                             soon as level 1 exists, beside the rest of the pyramid
-                             (a second branch of the frame's launch graph), and a
-                             last launch adds the collapsed level 1 and writes the
-                             output; for one frame at a time.  Costs 4 bytes per
-                             canvas pixel per frame in flight.  Same bytes either
-                             way (default 0) */
 } ps_launch_shape;
 typedef struct ps_tune_report {
     double ms_per_frame_default;  /* device ms per frame of the default shape */

@@ -81,10 +81,6 @@ struct RigDev {
     const RemapParamF* camsF;
     const uint32_t* covTiles;
     const uint8_t* unionMask; // level-0 union coverage (0/255), pitch = lv[0].pitch
-    // deferred collapse of level 0: the packed normalised sums N_0 (3 x 10
-    // bits, pitch = lv[0].pitch), written by k_blend in N mode and finished by
-    // k_collapse0; NULL when the launch shape does not defer it
-    uint32_t* N0;
     const uint8_t* camLists;  // camera indices of blend tiles with more than 8 cameras
     LevelDev lv[PS_MAX_LEVELS + 1];
     // work items of every level (used by the tail kernel)

@@ -158,12 +158,11 @@ struct LaunchShape {
     int tailHalf = 1;              // the tail blends levels above 0 in 64x8 half tiles
     int ctasPerSm[3] = {0, 0, 0};  // k_remap, k_pyrdown, k_blend; 0 = as many as fit
     int smallBlendMaxItems = 0;    // blend levels above 0 with at most this many tiles run in k_blend_small
-    int deferLevel0 = 0;           // level 0's blend split: N_0 beside the upper levels, then k_collapse0
     bool operator==(const LaunchShape& o) const
     {
         return tailMaxItems == o.tailMaxItems && tailCluster == o.tailCluster && tailHalf == o.tailHalf &&
                ctasPerSm[0] == o.ctasPerSm[0] && ctasPerSm[1] == o.ctasPerSm[1] && ctasPerSm[2] == o.ctasPerSm[2] &&
-               smallBlendMaxItems == o.smallBlendMaxItems && deferLevel0 == o.deferLevel0;
+               smallBlendMaxItems == o.smallBlendMaxItems;
     }
     bool operator!=(const LaunchShape& o) const { return !(*this == o); }
 };
@@ -178,12 +177,9 @@ cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, 
 // Accesses the checked build's kernels refused since the last reset
 // (waits for the device); -1 in the normal build, -2 on a CUDA error.
 long long boundsViolations(bool reset);
-// probePolls > 0: the failure-path test of the bounded waits (k_blend);
-// nMode != 0: level 0 of the deferred collapse (store N_0, no collapse)
+// probePolls > 0: the failure-path test of the bounded waits (k_blend)
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, int probePolls,
-                        int nMode, cudaStream_t st);
-// level 0 of the deferred collapse: N_0 + pyrUp32(C_1) -> the 8-bit output
-cudaError_t launchCollapse0(const Segment* segs, int nsegs, int total, cudaStream_t st);
+                        cudaStream_t st);
 // blend of few-tile levels above 0: two work items (the 64x8 halves) per tile
 cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st);
 // one cluster per segment: the rig's pyrDown levels tailDown..L and blend

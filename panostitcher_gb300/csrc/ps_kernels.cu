@@ -771,7 +771,6 @@ constexpr int kTailCamsPerUnit = 8;
 struct UnitGeo {
     int w, h, pitch, full, hasUp, outFmt;
     short4* C;              // collapsed result of the unit's level (j >= 1)
-    uint32_t* N0;           // deferred collapse: level 0's packed normalised sums (else NULL)
     const uint8_t* um;      // union mask (level 0, partially covered tiles)
     uint8_t* out;           // BGR canvas or Y plane
     uint8_t* outU;          // U (YUV420P) or UV (NV12) plane
@@ -779,10 +778,9 @@ struct UnitGeo {
     long long outPitch, outCPitch, outVPitch;
 };
 
-__device__ __forceinline__ void fillGeo(UnitGeo& g, const RigDev& R, const FrameDev& F, int j, bool nMode = false)
+__device__ __forceinline__ void fillGeo(UnitGeo& g, const RigDev& R, const FrameDev& F, int j)
 {
     const LevelDev& Lj = R.lv[j];
-    g.N0 = nMode && j == 0 ? R.N0 : nullptr;
     g.w = Lj.w;
     g.h = Lj.h;
     g.pitch = Lj.pitch;
@@ -921,7 +919,7 @@ struct BlendAcc {
 // its eight rows and footprint rows 4*half .. 4*half+5.
 template <bool kFresh, class Stage, class Sync>
 __device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const uint4& raw, int chunk, int* fRow,
-                                                int* fCol, Sync sync, int half = -1, bool withC = true)
+                                                int* fCol, Sync sync, int half = -1)
 {
     const int lx = (threadIdx.x & 31) * 2;
     const int ly = half < 0 ? (threadIdx.x >> 5) * 2 : 8 * half + (threadIdx.x >> 5);
@@ -967,7 +965,7 @@ __device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const
                                  (size_t)fRow[r] * Lu.pitch + fCol[c];
             S.fp[q][r][c + 3] = inside(gp, Lu.G, gBytes(R, Lu)) ? ldLevel<kFresh>(gp) : 0u;
         }
-        if (last && withC)
+        if (last)
             for (int k = threadIdx.x; k < elems; k += kConsumers) {
                 const int r = rb + k / kFW, c = k % kFW;
                 const uint2* cp = reinterpret_cast<const uint2*>(Lu.C + (size_t)fRow[r] * Lu.pitch + fCol[c]);
@@ -1131,34 +1129,91 @@ __device__ __forceinline__ Lap laplacian(uint32_t gpx, uint32_t ulo, uint32_t uh
     return l;
 }
 
-// Level 0 of the deferred-collapse mode: the normalised sum N_0 of a thread's
-// 2x2 block, packed as three 10-bit fields B | G << 10 | R << 20, each
-// N + 256 (|N_0| <= 255: a normalised sum of Laplacians of bytes), stored
-// in RigDev::N0 (pitch lv[0].pitch) for k_collapse0.
-__device__ __forceinline__ uint32_t packN(const int* n)
-{
-    uint32_t v = 0;
-#pragma unroll
-    for (int c = 0; c < 3; c++) v |= (uint32_t)min(max(n[c] + 256, 0), 1023) << (10 * c);
-    return v;
-}
-
-__device__ __forceinline__ void unpackN(uint32_t v, int* n)
-{
-#pragma unroll
-    for (int c = 0; c < 3; c++) n[c] = (int)((v >> (10 * c)) & 1023u) - 256;
-}
-
-// The end of a tile at level j for a thread's 2x2 block (pixel p = 2 * row +
-// column at (x, y)): add pyrUp32 of the C_{j+1} footprint staged in cf (rows
-// of kCfW short4, column 1 = footprint column 0) to the normalised sums n,
-// then store C_j (j >= 1) or the 8-bit level-0 output (tile class cls).
-__device__ __forceinline__ void collapseStore(const uint2* cf0, const UnitGeo& G, int j, int cls, bool withUp, int x,
-                                              int y, int (&n)[4][3])
+template <class Stage>
+__device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, const uint4& raw, int chunk,
+                                            bool staged, BlendAcc& acc)
 {
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    if (withUp) {
-        const uint2* cf = cf0 + wp * kCfW + 1 + lane;
+    const int lx = 2 * lane, ly = 2 * wp;
+    const int j = raw.x & 0xFF, cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
+    const bool uni = ((raw.x >> 24) & kTileUniform) != 0;
+    const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
+    const bool hasUp = G.hasUp != 0;
+    const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
+    const bool active = !(j == 0 && cls == 0);
+    constexpr int NC = Stage::kCams;
+    const int c0 = chunk * NC;
+    const int nc = max(0, min(NC, camCnt - c0));
+    const bool first = chunk == 0, last = chunk == unitChunks<NC>(raw) - 1;
+    const bool fast = uni && staged;  // weights were not staged
+    if (first) {
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            acc.r[p][0] = acc.r[p][1] = acc.r[p][2] = 0;
+            acc.wsum[p] = 0;
+        }
+    }
+    if (active) {
+        for (int q = 0; q < nc; q++) {
+            uint32_t ulo[4] = {0, 0, 0, 0}, uhi[4] = {0, 0, 0, 0};
+            if (hasUp) upsample2x2(&S.fp[q][wp][3 + lane], kFpW, ulo, uhi);
+            const uint2 gt = *reinterpret_cast<const uint2*>(&S.gj[q][ly][lx]);
+            const uint2 gb = *reinterpret_cast<const uint2*>(&S.gj[q][ly + 1][lx]);
+            const uint32_t gp[4] = {gt.x, gt.y, gb.x, gb.y};
+            uint32_t wq[2] = {0, 0};
+            if (!fast) {
+                wq[0] = *reinterpret_cast<const uint32_t*>(&S.w[q][ly][lx]);
+                wq[1] = *reinterpret_cast<const uint32_t*>(&S.w[q][ly + 1][lx]);
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                const Lap l = laplacian(gp[p], ulo[p], uhi[p]);
+                if (fast) {
+                    acc.r[p][0] = (int)(l.br & 0xFFFFu) - 256;
+                    acc.r[p][1] = l.g;
+                    acc.r[p][2] = (int)(l.br >> 16) - 256;
+                } else {
+                    // B and R accumulate w * (256 + L); the 256 * sum(w) comes off at normalisation
+                    const int w = (int)((wq[p >> 1] >> (16 * (p & 1))) & 0xFFFFu);
+                    acc.r[p][0] += w * (int)(l.br & 0xFFFFu);
+                    acc.r[p][1] += w * l.g;
+                    acc.r[p][2] += w * (int)(l.br >> 16);
+                    acc.wsum[p] += w;
+                }
+            }
+        }
+    }
+    if (!last) return;
+    if (!fast) {
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            acc.r[p][0] -= acc.wsum[p] << 8;
+            acc.r[p][2] -= acc.wsum[p] << 8;
+        }
+    }
+    int n[4][3];
+    if (fast) {
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) n[p][c] = acc.r[p][c];
+    } else if (G.full) {
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) n[p][c] = (acc.r[p][c] + 128) >> 8;
+    } else {
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int d = acc.wsum[p] ? acc.wsum[p] : 1;
+            const float inv = __frcp_rn((float)d);
+#pragma unroll
+            for (int c = 0; c < 3; c++) n[p][c] = divTrunc(acc.r[p][c], d, inv);
+        }
+    }
+    // collapse: + pyrUp32(C_{j+1})
+    if (hasUp && active) {
+        const uint2* cf = &S.cf[wp][1 + lane];
         int e[3][3], o[3][3];  // vertical sums per footprint column, even / odd row
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -1245,110 +1300,6 @@ __device__ __forceinline__ void collapseStore(const uint2* cf0, const UnitGeo& G
             }
         }
     }
-}
-
-// nMode (level 0 of the deferred-collapse mode): at the tile's last unit
-// store the packed normalised sums in N0 and stop; k_collapse0 finishes the
-// tile once C_1 exists.
-template <class Stage>
-__device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, const uint4& raw, int chunk,
-                                            bool staged, BlendAcc& acc, uint32_t* N0 = nullptr)
-{
-    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    const int lx = 2 * lane, ly = 2 * wp;
-    const int j = raw.x & 0xFF, cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
-    const bool uni = ((raw.x >> 24) & kTileUniform) != 0;
-    const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
-    const bool hasUp = G.hasUp != 0;
-    const int x = tx * kBlendTW + lx, y = ty * kBlendTH + ly;
-    const bool active = !(j == 0 && cls == 0);
-    constexpr int NC = Stage::kCams;
-    const int c0 = chunk * NC;
-    const int nc = max(0, min(NC, camCnt - c0));
-    const bool first = chunk == 0, last = chunk == unitChunks<NC>(raw) - 1;
-    const bool fast = uni && staged;  // weights were not staged
-    if (first) {
-#pragma unroll
-        for (int p = 0; p < 4; p++) {
-            acc.r[p][0] = acc.r[p][1] = acc.r[p][2] = 0;
-            acc.wsum[p] = 0;
-        }
-    }
-    if (active) {
-        for (int q = 0; q < nc; q++) {
-            uint32_t ulo[4] = {0, 0, 0, 0}, uhi[4] = {0, 0, 0, 0};
-            if (hasUp) upsample2x2(&S.fp[q][wp][3 + lane], kFpW, ulo, uhi);
-            const uint2 gt = *reinterpret_cast<const uint2*>(&S.gj[q][ly][lx]);
-            const uint2 gb = *reinterpret_cast<const uint2*>(&S.gj[q][ly + 1][lx]);
-            const uint32_t gp[4] = {gt.x, gt.y, gb.x, gb.y};
-            uint32_t wq[2] = {0, 0};
-            if (!fast) {
-                wq[0] = *reinterpret_cast<const uint32_t*>(&S.w[q][ly][lx]);
-                wq[1] = *reinterpret_cast<const uint32_t*>(&S.w[q][ly + 1][lx]);
-            }
-#pragma unroll
-            for (int p = 0; p < 4; p++) {
-                const Lap l = laplacian(gp[p], ulo[p], uhi[p]);
-                if (fast) {
-                    acc.r[p][0] = (int)(l.br & 0xFFFFu) - 256;
-                    acc.r[p][1] = l.g;
-                    acc.r[p][2] = (int)(l.br >> 16) - 256;
-                } else {
-                    // B and R accumulate w * (256 + L); the 256 * sum(w) comes off at normalisation
-                    const int w = (int)((wq[p >> 1] >> (16 * (p & 1))) & 0xFFFFu);
-                    acc.r[p][0] += w * (int)(l.br & 0xFFFFu);
-                    acc.r[p][1] += w * l.g;
-                    acc.r[p][2] += w * (int)(l.br >> 16);
-                    acc.wsum[p] += w;
-                }
-            }
-        }
-    }
-    if (!last) return;
-    if (!fast) {
-#pragma unroll
-        for (int p = 0; p < 4; p++) {
-            acc.r[p][0] -= acc.wsum[p] << 8;
-            acc.r[p][2] -= acc.wsum[p] << 8;
-        }
-    }
-    int n[4][3];
-    if (fast) {
-#pragma unroll
-        for (int p = 0; p < 4; p++)
-#pragma unroll
-            for (int c = 0; c < 3; c++) n[p][c] = acc.r[p][c];
-    } else if (G.full) {
-#pragma unroll
-        for (int p = 0; p < 4; p++)
-#pragma unroll
-            for (int c = 0; c < 3; c++) n[p][c] = (acc.r[p][c] + 128) >> 8;
-    } else {
-#pragma unroll
-        for (int p = 0; p < 4; p++) {
-            const int d = acc.wsum[p] ? acc.wsum[p] : 1;
-            const float inv = __frcp_rn((float)d);
-#pragma unroll
-            for (int c = 0; c < 3; c++) n[p][c] = divTrunc(acc.r[p][c], d, inv);
-        }
-    }
-    if (N0) {  // deferred collapse (level 0 only)
-        if (!active || y >= G.h || x >= G.w) return;
-        const long long next = (long long)G.pitch * G.h * 4;
-#pragma unroll
-        for (int r = 0; r < 2; r++) {
-            if (y + r >= G.h) break;
-            uint32_t* np = N0 + (size_t)(y + r) * G.pitch + x;
-            if (x + 1 < G.w) {
-                if (inside(reinterpret_cast<uint2*>(np), N0, next))
-                    *reinterpret_cast<uint2*>(np) = make_uint2(packN(n[2 * r]), packN(n[2 * r + 1]));
-            } else if (inside(np, N0, next)) {
-                np[0] = packN(n[2 * r]);
-            }
-        }
-        return;
-    }
-    collapseStore(&S.cf[0][0], G, j, cls, hasUp && active, x, y, n);
 }
 
 // The tail kernel's variant for levels above 0: one 64x8 half of a tile
@@ -1483,7 +1434,7 @@ __device__ __forceinline__ void computeUnitRows(const Stage& S, const UnitGeo& G
 // on, so the wait runs out, and the timeout is reported as any other
 // (status bit 4 of every frame in the launch).
 __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total,
-                                                            int* __restrict__ counter, int probePolls, int nMode)
+                                                            int* __restrict__ counter, int probePolls)
 {
     __shared__ BlendStage st[kBStages];
     __shared__ UnitInfo info[kBStages];
@@ -1542,7 +1493,7 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
             if (valid) {
                 R = segs[seg].rig;
                 j = raw.x & 0xFF;
-                if (lane == 0) fillGeo(ui.geo, *R, *segs[seg].frame, j, nMode != 0);
+                if (lane == 0) fillGeo(ui.geo, *R, *segs[seg].frame, j);
                 const int cls = (raw.x >> 8) & 0xFF, camCnt = (raw.x >> 16) & 0xFF;
                 uni = ((raw.x >> 24) & kTileUniform) != 0;
                 tx = raw.y & 0xFFFF;
@@ -1551,7 +1502,7 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                 const LevelDev& Lj = R->lv[j];
                 const LevelDev& Lu = R->lv[hasUp ? j + 1 : j];
                 nc = max(0, min(kCamsPerUnit, camCnt - chunk * kCamsPerUnit));
-                last = chunk == unitChunks(raw) - 1 && !nMode;  // nMode: no C_{j+1} footprint
+                last = chunk == unitChunks(raw) - 1;
                 const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
                 const bool rowsIn = (ty + 1) * kBlendTH <= Lj.h;
                 const bool fpIn = !hasUp || (fx0 - 3 >= 0 && fx0 - 3 + kFpW <= Lu.w && fy0 >= 0 && fy0 + kFH <= Lu.h);
@@ -1647,10 +1598,10 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
         const bool active = !((raw.x & 0xFF) == 0 && ((raw.x >> 8) & 0xFF) == 0);
         if (active && !staged) {
             stageUnitDirect<false>(st[stg], *segs[ui.seg].rig, raw, chunk, fRow, fCol,
-                                   [] { namedBarrier(1, kConsumers); }, -1, nMode == 0);
+                                   [] { namedBarrier(1, kConsumers); });
             namedBarrier(1, kConsumers);
         }
-        computeUnit(st[stg], ui.geo, raw, chunk, staged, acc, ui.geo.N0);
+        computeUnit(st[stg], ui.geo, raw, chunk, staged, acc);
         if (active && !staged) fenceProxyAsync();  // our stage writes precede later bulk copies into it
         __syncwarp();
         if (lane == 0) mbarArrive(&empty[stg]);  // this warp is done with the stage
@@ -1662,99 +1613,6 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
     if (s_timeout && threadIdx.x == 0)
         for (int k = 0; k < nsegs; k++)
             if (segs[k].frame->status) atomicOr(segs[k].frame->status, 4);
-}
-
-// ============================================================================
-// k_collapse0: level 0 of the deferred-collapse mode.  k_blend in N mode has
-// stored each covered level-0 tile's normalised sums N_0 (packed) while the
-// upper levels were still being built; once C_1 exists, this kernel adds
-// pyrUp32(C_1) and stores the 8-bit output (restoreImageFromLaplacePyramid's
-// last step, then convertTo(CV_8U) and setTo(0, maskNot),
-// CudaMultibandBlend.cpp:220-231,820-822), with the same arithmetic as the
-// undeferred k_blend.  One 64x16 level-0 tile per work item (the level-0
-// blend items); a CTA walks a contiguous run of items.  The tile's C_1
-// footprint is staged row by row across the warps, with the border mapping
-// per row and per lane's column.
-// ============================================================================
-__global__ void __launch_bounds__(kThreads) k_collapse0(const Segment* __restrict__ segs, int nsegs, int total)
-{
-    __shared__ uint2 cf[kFH][kCfW];
-    constexpr int kWarps = kThreads / 32;
-    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    int s = 0, begin, end;
-    itemRange(total, begin, end);
-    uint4 raw = make_uint4(0, 0, 0, 0);
-    UnitGeo geo;
-    if (begin < end) {
-        s = findSegment(segs, nsegs, begin, s);
-        raw = __ldg(static_cast<const uint4*>(segs[s].items) + (begin - segs[s].prefix));
-        fillGeo(geo, *segs[s].rig, *segs[s].frame, 0, true);
-    }
-    waitPrevGrid();
-    allowNextGrid();
-    for (int it = begin; it < end; it++) {
-        if (it != begin) {
-            const int sn = findSegment(segs, nsegs, it, s);
-            raw = __ldg(static_cast<const uint4*>(segs[sn].items) + (it - segs[sn].prefix));
-            if (sn != s) fillGeo(geo, *segs[sn].rig, *segs[sn].frame, 0, true);
-            s = sn;
-        }
-        const RigDev& R = *segs[s].rig;
-        const int cls = (raw.x >> 8) & 0xFF;
-        const int tx = raw.y & 0xFFFF, ty = raw.y >> 16;
-        const int x = tx * kBlendTW + 2 * lane, y = ty * kBlendTH + 2 * wp;
-        const bool withUp = R.L > 0 && cls != 0;
-        __syncthreads();  // readers of the previous tile's footprint are done
-        int n[4][3];
-        {
-            // N_0 of the thread's block and the tile's C_1 footprint rows
-            uint2 nv[2] = {make_uint2(0, 0), make_uint2(0, 0)};
-            const long long next = (long long)geo.pitch * geo.h * 4;
-            if (cls != 0 && x < geo.w)
-#pragma unroll
-                for (int r = 0; r < 2; r++)
-                    if (y + r < geo.h) {
-                        const uint32_t* np = geo.N0 + (size_t)(y + r) * geo.pitch + x;
-                        if (x + 1 < geo.w) {
-                            if (inside(reinterpret_cast<const uint2*>(np), geo.N0, next))
-                                nv[r] = __ldg(reinterpret_cast<const uint2*>(np));
-                        } else if (inside(np, geo.N0, next)) {
-                            nv[r].x = __ldg(np);
-                        }
-                    }
-            constexpr int kRows = (kFH + kWarps - 1) / kWarps;
-            uint2 ca[kRows], cb[kRows];
-            const LevelDev& Lu = R.lv[withUp ? 1 : 0];
-            const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
-            const bool hasB = lane < kFW - 32;
-            const int colA = withUp ? colMap(fx0 + lane, Lu.w) : 0;
-            const int colB = withUp && hasB ? colMap(fx0 + 32 + lane, Lu.w) : 0;
-#pragma unroll
-            for (int i = 0; i < kRows; i++) {
-                const int r = wp + i * kWarps;
-                ca[i] = cb[i] = make_uint2(0, 0);
-                if (withUp && r < kFH) {
-                    const uint2* row = reinterpret_cast<const uint2*>(Lu.C + (size_t)rowMap(fy0 + r, Lu.h) * Lu.pitch);
-                    if (inside(row + colA, Lu.C, cBytes(Lu))) ca[i] = __ldg(row + colA);
-                    if (hasB && inside(row + colB, Lu.C, cBytes(Lu))) cb[i] = __ldg(row + colB);
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < kRows; i++) {
-                const int r = wp + i * kWarps;
-                if (withUp && r < kFH) {
-                    cf[r][lane + 1] = ca[i];
-                    if (hasB) cf[r][32 + lane + 1] = cb[i];
-                }
-            }
-            unpackN(nv[0].x, n[0]);
-            unpackN(nv[0].y, n[1]);
-            unpackN(nv[1].x, n[2]);
-            unpackN(nv[1].y, n[3]);
-        }
-        __syncthreads();
-        collapseStore(&cf[0][0], geo, 0, cls, withUp, x, y, n);
-    }
 }
 
 // ============================================================================
@@ -2075,17 +1933,8 @@ static int residentPerSm(int threads, size_t dynSmem = 0)
 
 // Every per-frame kernel is launched with programmatic stream serialisation,
 // so its prologue overlaps the previous kernel's tail (see waitPrevGrid).
-// pdl = false: a plain launch (the first kernel of a graph's side branch,
-// and the one that joins it), whose griddepcontrol.wait returns at once.
 template <class... Args>
 static cudaError_t launchPdl(void (*kernel)(Args...), int grid, int block, cudaStream_t st, Args... args)
-{
-    return launchMaybePdl(true, kernel, grid, block, st, args...);
-}
-
-template <class... Args>
-static cudaError_t launchMaybePdl(bool pdl, void (*kernel)(Args...), int grid, int block, cudaStream_t st,
-                                  Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
@@ -2096,7 +1945,7 @@ static cudaError_t launchMaybePdl(bool pdl, void (*kernel)(Args...), int grid, i
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = pdl ? 1 : 0;
+    cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
@@ -2141,18 +1990,11 @@ cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams,
 }
 
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, int probePolls,
-                        int nMode, cudaStream_t st)
+                        cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchMaybePdl(nMode == 0, k_blend, gridFor(total, residentPerSm<k_blend>(kBlendThreads), perSm),
-                          kBlendThreads, st, segs, nsegs, total, counter, probePolls, nMode);
-}
-
-cudaError_t launchCollapse0(const Segment* segs, int nsegs, int total, cudaStream_t st)
-{
-    if (total <= 0) return cudaSuccess;
-    return launchMaybePdl(false, k_collapse0, gridFor(total, residentPerSm<k_collapse0>(kThreads)), kThreads, st,
-                          segs, nsegs, total);
+    return launchPdl(k_blend, gridFor(total, residentPerSm<k_blend>(kBlendThreads), perSm), kBlendThreads, st, segs,
+                     nsegs, total, counter, probePolls);
 }
 
 cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st)

@@ -121,7 +121,6 @@ void Rig::clear()
         l.Am.reset();
     }
     nextSlot_ = lastSlot_ = 0;
-    for (DevBuf& b : N0_) b.reset();
     maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset(); planar_.reset();
     camsF_.reset(); covTiles_.reset();
     imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
@@ -182,7 +181,6 @@ long long Rig::residentBytes() const
         for (int k = 0; k < kIoSlots; k++) b += l.G[k].bytes() + l.C[k].bytes();
         b += l.Wt.bytes() + l.Am.bytes();
     }
-    for (const DevBuf& n0 : N0_) b += n0.bytes();
     b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
     b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
     b += dLinear_.bytes() + linW_.bytes() + planar_.bytes() + camsF_.bytes() + covTiles_.bytes();
@@ -598,7 +596,6 @@ void Rig::preparePyramids(const uint8_t* cov, const uint8_t* seam, const float* 
     }
     hDesc_ = d;
     dDesc_.alloc(sizeof(RigDev) * slots_);
-    allocDeferred();
     writeDescriptors(st);
     gen_ = g_generation++;
 }
@@ -758,24 +755,12 @@ void Rig::setCustomMasks(const uint8_t* const* masks, cudaStream_t st)
     gen_ = g_generation++;
 }
 
-// The deferred level-0 collapse keeps N_0 (4 bytes per level-0 pixel) per
-// state slot while the shape asks for it; otherwise the buffers are freed.
-void Rig::allocDeferred()
-{
-    const bool want = shape_.deferLevel0 && !linear_ && L_ >= 1 && !geom_.empty();
-    for (int k = 0; k < kIoSlots; k++) {
-        if (want && k < slots_) N0_[k].alloc((size_t)geom_[0].pitch * geom_[0].h * 4);
-        else N0_[k].reset();
-    }
-}
-
 // One descriptor per state slot, differing in the pyramid pointers.
 void Rig::writeDescriptors(cudaStream_t st)
 {
     RigDev ds[kIoSlots];
     for (int k = 0; k < slots_; k++) {
         ds[k] = hDesc_;
-        ds[k].N0 = N0_[k].as<uint32_t>();
         for (int j = 0; j <= L_; j++) {
             ds[k].lv[j].G = lv_[j].G[k].as<uchar4>();
             ds[k].lv[j].C = lv_[j].C[k].as<short4>();
@@ -839,9 +824,7 @@ void Rig::setShape(const LaunchShape& s)
     for (int k = 0; k < 3; k++)
         if (s.ctasPerSm[k] < 0 || s.ctasPerSm[k] > 64)
             fail(PS_EINVAL, "ctas_per_sm[%d] = %d out of range 0..64", k, s.ctasPerSm[k]);
-    if (s.deferLevel0 != 0 && s.deferLevel0 != 1) fail(PS_EINVAL, "defer_level0 must be 0 or 1 (got %d)", s.deferLevel0);
     if (s == shape_) return;
-    const LaunchShape old = shape_;
     shape_ = s;
     if (!ready() || linear_) return;
     // the descriptors change under no run: launch lists follow the new
@@ -851,18 +834,6 @@ void Rig::setShape(const LaunchShape& s)
     hDesc_.tailDown = tailDown_;
     hDesc_.tailBlend = tailBlend_;
     hDesc_.tailHalf = shape_.tailHalf;
-    try {
-        allocDeferred();
-    } catch (...) {
-        shape_ = old;  // not enough memory for N_0: keep the previous shape
-        allocDeferred();
-        tailSplit(shape_.tailMaxItems, &tailDown_, &tailBlend_);
-        hDesc_.tailDown = tailDown_;
-        hDesc_.tailBlend = tailBlend_;
-        hDesc_.tailHalf = shape_.tailHalf;
-        writeDescriptors(nullptr);
-        throw;
-    }
     writeDescriptors(nullptr);
     gen_ = g_generation++;
 }
@@ -1130,19 +1101,6 @@ double Rig::stepBytes(int kind, int level) const
         }
         return b;
     }
-    if (kind == 7 || kind == 8) {
-        // the deferred level-0 collapse.  7, k_blend storing N_0: per camera in the tile's list weight
-        // (2 B) + G_0 (4 B) + a quarter of G_1 (1 B), N_0 out (4 B).  8, k_collapse0: N_0 in (4 B), a
-        // quarter of C_1 (2 B), the canvas out (4 B) and, in partly covered tiles, the union mask (1 B)
-        const LevelGeom& g0 = geom_[0];
-        for (int k = blendOff_[0]; k < blendOff_[0] + blendCnt_[0]; k++) {
-            const BlendItem& it = hBlend_[k];
-            const int tw = std::min(kBlendTW, g0.w - it.tx * kBlendTW), th = std::min(kBlendTH, g0.h - it.ty * kBlendTH);
-            if (it.cls == 0) { b += kind == 8 ? (double)tw * th * 4 : 0; continue; }
-            b += (double)tw * th * (kind == 7 ? it.camCnt * 7 + 4 : 10 + (it.cls == 2 ? 1 : 0));
-        }
-        return b;
-    }
     // blend: per camera in the tile's list weight (2 B) + G_j (4 B) + a quarter of G_{j+1} (1 B);
     // a quarter of C_{j+1} (2 B); out C_j (8 B) or the canvas (4 B)
     const LevelGeom& g = geom_[level];
@@ -1248,10 +1206,7 @@ void Plan::ensureStreams()
     for (cudaStream_t& c : sComp_) PS_CUDA(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
     PS_CUDA(cudaStreamCreateWithFlags(&sOut_, cudaStreamNonBlocking));
     PS_CUDA(cudaStreamCreateWithFlags(&capStream_, cudaStreamNonBlocking));
-    PS_CUDA(cudaStreamCreateWithFlags(&capSide_, cudaStreamNonBlocking));
     PS_CUDA(cudaEventCreateWithFlags(&callerEv_, cudaEventDisableTiming));
-    PS_CUDA(cudaEventCreateWithFlags(&forkEv_, cudaEventDisableTiming));
-    PS_CUDA(cudaEventCreateWithFlags(&joinEv_, cudaEventDisableTiming));
     for (IoSlot& sl : io_) {
         PS_CUDA(cudaEventCreateWithFlags(&sl.argsCopied, cudaEventDisableTiming));
         PS_CUDA(cudaEventCreateWithFlags(&sl.computed, cudaEventDisableTiming));
@@ -1334,39 +1289,11 @@ void Plan::bind(const std::vector<Rig*>& rigs)
     for (int r = 0; r < nr; r++)
         if (!rigs[r]->linear()) parts.push_back({r, {rigs[r]->remapItems(), rigs[r]->numRemapItems()}});
     addStep(0, parts, 0);
-    // The deferred level-0 collapse (every pyramid rig's shape asks for it):
-    // level 0's blend without its collapse runs on a side branch once pyrDown
-    // level 1 is done, beside the upper levels; k_collapse0 closes the frame.
-    bool defer = false;
-    for (Rig* r : rigs)
-        if (!r->linear()) defer = true;
-    for (Rig* r : rigs)
-        if (!r->linear() && !r->deferLevel0()) defer = false;
-    auto level0Step = [&](int kind) {
-        Step s{kind, (int)segs_.size(), 0, 0, 0, 0.0};
-        for (int r = 0; r < nr; r++) {
-            if (rigs[r]->linear()) continue;
-            segRig_.push_back(r);
-            segs_.push_back({rigs[r]->blendItems(0), rigs[r]->deviceDesc(),
-                             reinterpret_cast<const FrameDev*>(sizeof(FrameDev) * r), rigs[r]->numBlendItems(0),
-                             s.total});
-            s.total += rigs[r]->numBlendItems(0);
-            s.bytes += rigs[r]->stepBytes(kind, 0);
-        }
-        s.nsegs = (int)segs_.size() - s.segOff;
-        return s;
-    };
     for (int J = 1; J <= maxL; J++) {
         parts.clear();
         for (int r = 0; r < nr; r++)
             if (J < rigs[r]->tailDown()) parts.push_back({r, {rigs[r]->downItems(J), rigs[r]->numDownItems(J)}});
         addStep(1, parts, J);
-        if (J == 1 && defer) {
-            steps_.push_back(Step{11, (int)segs_.size(), 0, 0, 0, 0.0});
-            Step s = level0Step(7);
-            s.side = true;
-            steps_.push_back(s);
-        }
     }
     {
         // the tail: one cluster per rig that has one (segment count 1)
@@ -1393,17 +1320,13 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         for (int r = 0; r < nr; r++) {
             if (rigs[r]->linear()) continue;
             const int j = rigs[r]->tailBlend() - 1 - s;
-            if (j < 0 || (j == 0 && defer)) continue;
+            if (j < 0) continue;
             const int cnt = rigs[r]->numBlendItems(j);
             if (j > 0 && cnt <= rigs[r]->shape().smallBlendMaxItems) small.push_back({r, {rigs[r]->blendItems(j), 2 * cnt}});
             else parts.push_back({r, {rigs[r]->blendItems(j), cnt}});
         }
         addStep(6, small, s);
         addStep(2, parts, s);
-    }
-    if (defer) {
-        steps_.push_back(Step{12, (int)segs_.size(), 0, 0, 0, 0.0});
-        steps_.push_back(level0Step(8));
     }
     // one work counter per step after the segments, zeroed in every run's staged copy
     counterOff_ = (segOff_ + segs_.size() * sizeof(Segment) + 15) / 16 * 16;
@@ -1424,12 +1347,11 @@ Plan::~Plan()
     for (cudaStream_t st : sComp_)
         if (st) cudaStreamSynchronize(st);
     dropGraph();
-    for (cudaStream_t st : {sIn_, sOut_, capStream_, capSide_})
+    for (cudaStream_t st : {sIn_, sOut_, capStream_})
         if (st) cudaStreamDestroy(st);
     for (cudaStream_t st : sComp_)
         if (st) cudaStreamDestroy(st);
-    for (cudaEvent_t e : {callerEv_, forkEv_, joinEv_})
-        if (e) cudaEventDestroy(e);
+    if (callerEv_) cudaEventDestroy(callerEv_);
     for (IoSlot& sl : io_)
         for (cudaEvent_t e : {sl.argsCopied, sl.computed, sl.downloaded})
             if (e) cudaEventDestroy(e);
@@ -1447,23 +1369,9 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
 {
     const Segment* segs = reinterpret_cast<const Segment*>(static_cast<const uint8_t*>(slot.dArgs.get()) + segOff_);
     int* counters = reinterpret_cast<int*>(static_cast<uint8_t*>(slot.dArgs.get()) + counterOff_);
-    // The side branch forks only under graph capture; run directly (or
-    // profiled), its steps take their place in order on the one stream.
-    const bool fork = st == capStream_;
     for (size_t si = 0; si < steps_.size(); si++) {
         const Step& s = steps_[si];
-        if (s.kind == 11 || s.kind == 12) {
-            if (fork && s.kind == 11) {
-                PS_CUDA(cudaEventRecord(forkEv_, st));
-                PS_CUDA(cudaStreamWaitEvent(capSide_, forkEv_, 0));
-            } else if (fork) {
-                PS_CUDA(cudaEventRecord(joinEv_, capSide_));
-                PS_CUDA(cudaStreamWaitEvent(st, joinEv_, 0));
-            }
-            continue;
-        }
         const Segment* p = segs + s.segOff;
-        cudaStream_t ls = fork && s.side ? capSide_ : st;
         cudaEvent_t a = nullptr, b = nullptr;
         if (prof) {
             a = prof->event();
@@ -1472,9 +1380,7 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
         }
         if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, perSm_[0], counters + si, st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, perSm_[1], st));
-        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, probe_, 0, st));
-        else if (s.kind == 7) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, probe_, 1, ls));
-        else if (s.kind == 8) PS_CUDA(launchCollapse0(p, s.nsegs, s.total, st));
+        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, probe_, st));
         else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, tailCluster_, st));
         else if (s.kind == 6) PS_CUDA(launchBlendSmall(p, s.nsegs, s.total, st));
         else PS_CUDA(launchLinear(p, s.nsegs, s.total, maxCams_, st));

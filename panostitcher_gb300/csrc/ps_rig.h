@@ -150,9 +150,6 @@ public:
     // new generation.
     void setShape(const LaunchShape& s);
     const LaunchShape& shape() const { return shape_; }
-    // the shape defers level 0's collapse, and this rig's split allows it
-    // (level 0 blended below the tail, pyrDown level 1 its own launch)
-    bool deferLevel0() const { return shape_.deferLevel0 && N0_[0].get() && tailDown_ >= 2 && tailBlend_ >= 1; }
     // the tail levels a tail_max_items value gives: pyrDown down..L, blend L..blend
     void tailSplit(int maxItems, int* down, int* blend) const;
     // pyrDown levels tailDown()..L and blend levels L..tailBlend() run in the tail kernel
@@ -190,7 +187,6 @@ private:
     void prepareLinear(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
                        int radius, cudaStream_t st);
     void writeDescriptors(cudaStream_t st);
-    void allocDeferred();  // N0_ per slot when the shape defers level 0, else none
     void toLevel0(const void* const* images, const long long* pitches, int fmt, int cam0, int count, int slot,
                   cudaStream_t st);
     void buildBlendState(const uint8_t* uniSrcDev, bool custom, cudaStream_t st);
@@ -208,7 +204,6 @@ private:
     std::vector<LevelGeom> geom_;
     LevelBufs lv_[PS_MAX_LEVELS + 1];
     DevBuf maps_, union_, inputs_, output_, covDev_, status_, imgArgs_, planar_;
-    DevBuf N0_[kIoSlots];  // deferred level-0 collapse: packed N_0 per state slot
     long long inPitch_ = 0, budget_ = 0;
     DevBuf dDesc_, dRemap_, dDown_, dBlend_, dCams_;
     std::vector<RemapItem> hRemap_;
@@ -269,23 +264,15 @@ public:
     void bind(const std::vector<Rig*>& rigs);
     // stage frame arguments, upload host inputs, run, download host outputs
     void run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph, Profiler* prof = nullptr);
-    int launchesPerRun() const
-    {
-        int n = 0;
-        for (const Step& s : steps_) n += s.kind != 11 && s.kind != 12;
-        return n;
-    }
+    int launchesPerRun() const { return (int)steps_.size(); }
     bool matches(const std::vector<Rig*>& rigs) const;
 
 private:
     struct Step {
-        // 0 remap, 1 pyrDown, 2 blend, 3 tail, 4 linear-blend render, 6 few-tile blend, 7 level-0 blend
-        // storing N_0, 8 level-0 collapse; 11 / 12 open / close the side branch of the frame's graph
-        int kind;
+        int kind;  // 0 remap, 1 pyrDown, 2 blend, 3 tail, 4 linear-blend render, 6 few-tile blend
         int segOff, nsegs, total;
-        int level;        // level of the first rig in the step
-        double bytes;     // algorithmic bytes of the step (all rigs)
-        bool side = false;  // launched on the side branch (graph capture only)
+        int level;      // level of the first rig in the step
+        double bytes;   // algorithmic bytes of the step (all rigs)
     };
     // Per-run state in kIoSlots copies: run k uses slot k % kIoSlots, so while
     // run k computes, run k + 1 uploads and run k - 1 downloads.
@@ -316,16 +303,12 @@ private:
     // copy-in, compute and copy-out streams (non-blocking), the capture stream
     cudaStream_t sIn_ = nullptr, sComp_[Rig::kIoSlots] = {}, sOut_ = nullptr, capStream_ = nullptr;
     cudaEvent_t callerEv_ = nullptr;
-    // the side branch of a captured frame (the deferred level-0 blend): its
-    // capture stream and the fork / join events
-    cudaStream_t capSide_ = nullptr;
-    cudaEvent_t forkEv_ = nullptr, joinEv_ = nullptr;
 };
 
 // The autotuner (ps_tune.cpp): times launch shapes on a prepared rig by
 // coordinate descent from the default shape (tail split, the levels run as
-// half tiles by k_blend_small, the deferred level-0 collapse, tail tile
-// split, tail cluster width, CTAs per SM of k_blend, k_pyrdown, k_remap), frames
+// half tiles by k_blend_small, tail tile split, tail cluster width, CTAs per
+// SM of k_blend, k_pyrdown, k_remap), frames
 // issued round-robin on `inflight` streams, and leaves the fastest set on
 // the rig and bound to the plan.  Results are kept per rig geometry, GPU and
 // concurrency, so a later call for the same geometry times nothing unless

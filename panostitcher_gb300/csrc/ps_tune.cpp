@@ -192,13 +192,6 @@ std::vector<LaunchShape> neighbours(const Rig& rig, const LaunchShape& cur, int 
         }
         break;
     }
-    case 7:  // level 0's blend deferred beside the upper levels (or not)
-        if (L >= 1) {
-            LaunchShape s = cur;
-            s.deferLevel0 = 1 - cur.deferLevel0;
-            out.push_back(s);
-        }
-        break;
     default: {  // CTAs per SM of k_blend (3), k_pyrdown (4), k_remap (5)
         const int k = 5 - knob;
         const int resident = residentCtasPerSm(k);
@@ -259,7 +252,7 @@ LaunchShape autotune(Rig& rig, Plan& plan, int framesPerTrial, int inflight, boo
         // coordinate descent, two passes; a move must gain 1%
         for (int pass = 0; pass < 2; pass++) {
             bool moved = false;
-            for (int knob : {0, 6, 7, 1, 2, 3, 4, 5})
+            for (int knob : {0, 6, 1, 2, 3, 4, 5})
                 for (const LaunchShape& s : neighbours(rig, best, knob)) {
                     const double t = trials.time(s);
                     report.trials++;

@@ -307,13 +307,13 @@ class CudaPanoramaRender2:
         return lib().ps_render_algorithmic_bytes(self._h, bytes_in_per_px, bytes_out_per_px)
 
     SHAPE_DEFAULT = {"tail_max_items": 16, "tail_cluster": 0, "tail_half_tiles": 1, "ctas_per_sm": (0, 0, 0),
-                     "small_blend_max_items": 0, "defer_level0": 0}
+                     "small_blend_max_items": 0}
 
     @staticmethod
     def _shape_dict(s: "L.LaunchShape") -> dict:
         return {"tail_max_items": s.tail_max_items, "tail_cluster": s.tail_cluster,
                 "tail_half_tiles": s.tail_half_tiles, "ctas_per_sm": tuple(s.ctas_per_sm),
-                "small_blend_max_items": s.small_blend_max_items, "defer_level0": s.defer_level0}
+                "small_blend_max_items": s.small_blend_max_items}
 
     def launch_shape(self) -> dict:
         """The render's launch shape (ps_launch_shape fields)."""
@@ -329,7 +329,7 @@ class CudaPanoramaRender2:
             raise ValueError(f"unknown launch-shape fields {sorted(unknown)}")
         cur.update(fields)
         s = L.LaunchShape(cur["tail_max_items"], cur["tail_cluster"], cur["tail_half_tiles"],
-                          (C.c_int * 3)(*cur["ctas_per_sm"]), cur["small_blend_max_items"], cur["defer_level0"])
+                          (C.c_int * 3)(*cur["ctas_per_sm"]), cur["small_blend_max_items"])
         check(lib().ps_render_set_launch_shape(self._h, C.byref(s)))
 
     def autotune(self, frames_per_trial: int = 0, in_flight: int = 0, force: bool = False) -> dict:

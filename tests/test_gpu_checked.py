@@ -44,8 +44,7 @@ def check(tag):
 def same(a, b, tag):
     assert np.array_equal(a[..., :3], b[..., :3]), tag
 
-shapes = [dict(), dict(tail_max_items=0, small_blend_max_items=128), dict(tail_half_tiles=0, tail_cluster=8),
-          dict(tail_max_items=0, small_blend_max_items=128, defer_level0=1)]
+shapes = [dict(), dict(tail_max_items=0, small_blend_max_items=128), dict(tail_half_tiles=0, tail_cluster=8)]
 for name, f in (("c2", 4), ("c1", 4), ("ricoh", 4), ("c3c", 8)):
     p = Prepared(S.scaled_rig(S.rig(name), f))
     W, H = p.cfg.dst_size

@@ -2,16 +2,14 @@
 
 Every launch shape must stitch the same bytes: the tail split only moves
 pyramid levels between kernels that run the same per-tile code, the tail's
-half tiles change which threads own which pixels, grid widths change which
-CTA takes which tile, and the deferred level-0 collapse stores level 0's
-normalised sums and adds the collapsed level 1 in a later launch.  Each shape's frames are compared with the
+half tiles change which threads own which pixels, and grid widths change
+which CTA takes which tile.  Each shape's frames are compared with the
 oracle, as are the frames after autotuning and a batch of rigs whose shapes
 differ.
 """
 import numpy as np
 import pytest
 
-import oracle as O
 import panostitcher_gb300 as P
 from panostitcher_gb300 import synth as S
 
@@ -33,9 +31,6 @@ SHAPES = [
     {"small_blend_max_items": 1 << 20},        # every blend level above 0 below the tail in half tiles
     {"small_blend_max_items": 64},
     {"tail_max_items": 0, "small_blend_max_items": 1 << 20},  # no tail: k_blend_small up to the top level
-    {"defer_level0": 1},                       # level 0's collapse deferred (a side branch in the graph)
-    {"defer_level0": 1, "tail_max_items": 0, "small_blend_max_items": 128},
-    {"defer_level0": 1, "tail_max_items": 1 << 20},  # the tail runs every level: nothing to defer
 ]
 
 
@@ -106,27 +101,3 @@ def test_batch_of_rigs_with_different_shapes(cuda, oracle_lib):
         cuda.cuda.synchronize()
         for d, ref in zip(dsts, refs):
             assert np.array_equal(d[..., :3], ref), diff_histogram(d[..., :3], ref)
-
-
-@pytest.mark.parametrize("graph", [True, False], ids=["graph", "direct"])
-def test_deferred_collapse_outputs(cuda, oracle_lib, graph):
-    """The deferred level-0 collapse on every output of the level-0 store: BGR32, BGR24 and the encoder
-    planes, captured (the side branch forks) and launched directly (one stream, in step order)."""
-    import torch
-    p = Prepared(S.scaled_rig(S.rig("c2"), 8), graph=graph)
-    p.r.set_launch_shape(defer_level0=1, tail_max_items=0, small_blend_max_items=128)
-    assert p.r.launch_shape()["defer_level0"] == 1
-    W, H = p.cfg.dst_size
-    for k in range(3):
-        f = p.frames.frame(k)
-        ref = p.oracle_render(f, p.luts)
-        for ch in (4, 3):
-            out = p.product_render(f, p.luts, channels_out=ch)
-            assert np.array_equal(out[..., :3], ref[..., :3]), diff_histogram(out[..., :3], ref[..., :3])
-        for fmt in (P.PS_FMT_YUV420P, P.PS_FMT_NV12):
-            planes = O.bgr32_to_yuv(ref, fmt)
-            got = [np.zeros_like(x) for x in planes]
-            p.r.render_yuv(f, got, p.luts, fmt=fmt, check=True)
-            torch.cuda.synchronize()
-            for a, b in zip(got, planes):
-                assert np.array_equal(a, b)
