@@ -8,10 +8,22 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "ps_device.cuh"
 
 namespace ps {
+
+// An NVTX range over a scope of host code (prepare, each render run, the
+// autotuner, each launch issued outside a graph), so a profiler's timeline
+// shows the library's phases beside the kernels.  NVTX calls cost nothing
+// measurable unless a tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ---- errors -------------------------------------------------------------------
 // Internal code throws ps::Error; the C ABI converts it to a status code and

@@ -302,6 +302,7 @@ static void checkSeamsDisjoint(const uint8_t* const* seams, int n, int W, int H)
 void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam, int srcW, int srcH, int dstW,
                             int dstH, const uint8_t* const* seams, cudaStream_t st, int seamRule, int highQuality)
 {
+    NvtxRange range("ps.prepare");
     clear();
     validateParams(params, n, srcW, srcH, dstW, dstH);
     if (blendParam <= 0) fail(PS_EINVAL, "blendParam = %d, should be positive", blendParam);  // RicohUtil.cpp:1105
@@ -376,6 +377,7 @@ void Rig::prepareFromParams(const ps_photo_param* params, int n, int blendParam,
 void Rig::prepareFromMasks(const uint8_t* const* masks, const uint8_t* const* seams, int n, int W, int H,
                            int maxLevels, int minLength, cudaStream_t st)
 {
+    NvtxRange range("ps.prepare");
     clear();
     // CudaTilingMultibandBlendFast::prepare, source/CudaAccel/CudaMultibandBlend.cpp:549-568
     if (!masks || n <= 0) fail(PS_EINVAL, "no masks");
@@ -1372,6 +1374,9 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
     for (size_t si = 0; si < steps_.size(); si++) {
         const Step& s = steps_[si];
         const Segment* p = segs + s.segOff;
+        static const char* const kRangeName[] = {"ps.remap", "ps.pyrdown", "ps.blend", "ps.tail",
+                                                 "ps.linear", "ps.cvt", "ps.blend_small"};
+        NvtxRange range(kRangeName[s.kind >= 0 && s.kind <= 6 ? s.kind : 5]);
         cudaEvent_t a = nullptr, b = nullptr;
         if (prof) {
             a = prof->event();
@@ -1401,6 +1406,7 @@ static int bytesPerPixel(int fmt) { return fmt == PS_FMT_BGR24 ? 3 : 4; }
 // stream.  The caller's stream waits for the run's completion.
 void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph, Profiler* prof)
 {
+    NvtxRange range("ps.run");
     if (prof && !prof->on()) prof = nullptr;
     if (prof) useGraph = false;
     if (in.size() != rigs_.size()) fail(PS_EINVAL, "plan input count mismatch");

@@ -212,6 +212,7 @@ std::vector<LaunchShape> neighbours(const Rig& rig, const LaunchShape& cur, int 
 LaunchShape autotune(Rig& rig, Plan& plan, int framesPerTrial, int inflight, bool useGraph, bool force,
                      TuneReport* rep)
 {
+    NvtxRange range("ps.autotune");
     if (!rig.ready()) fail(PS_ESTATE, "render not prepared");
     if (rig.linear()) fail(PS_EINVAL, "the linear-blend mode has one launch and nothing to tune");
     if (framesPerTrial < 0 || framesPerTrial > 10000) fail(PS_EINVAL, "frames_per_trial must be in 0..10000");
