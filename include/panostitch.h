@@ -353,10 +353,11 @@ int ps_render_get_launch_shape(const ps_render* r, ps_launch_shape* shape);
 /* Times launch shapes on the prepared render (frames_per_trial frames per
    timed run, 0 = 20; issued round-robin on in_flight streams, 0 = the
    render's frames in flight) by coordinate descent from the default
-   shape, and keeps the fastest.  The render's slot-0 input buffers are
-   overwritten with a test pattern.  A geometry tuned before in this
-   process is not timed again unless force is non-zero.  Blocks (about a
-   second at 4096x2048).  chosen and report may be NULL. */
+   shape, and keeps the fastest.  The render's input staging (every state
+   slot) is overwritten with test patterns, and the trials cycle through
+   them as distinct frames would.  A geometry tuned before in this
+   process is not timed again unless force is non-zero.  Blocks (a few
+   seconds at 4096x2048).  chosen and report may be NULL. */
 int ps_render_autotune(ps_render* r, int frames_per_trial, int in_flight, int force, ps_launch_shape* chosen,
                        ps_tune_report* report);
 

@@ -40,8 +40,10 @@ std::string tuneKey(const Rig& r, int inflight, bool useGraph)
 }
 
 // Frames issued round-robin on `inflight` caller streams, with device
-// inputs (the rig's slot-0 frame staging, filled with a fixed pattern) and
-// one device canvas per stream.
+// inputs and one device canvas per stream.  The inputs are the rig's frame
+// staging of every state slot, each filled with its own pattern, and frame k
+// reads slot k's: with eight slots the trial cycles through more input bytes
+// than L2 holds, as a stream of distinct frames does.
 class Trials {
 public:
     Trials(Rig& rig, Plan& plan, int frames, int inflight, bool useGraph)
@@ -51,16 +53,19 @@ public:
         const long long pitch = rig.inputPitch();
         std::vector<uint8_t> pattern((size_t)pitch * rig.srcH());
         uint32_t x = 0x9E3779B9u;
-        for (uint8_t& b : pattern) {  // xorshift32
-            x ^= x << 13;
-            x ^= x >> 17;
-            x ^= x << 5;
-            b = (uint8_t)(x >> 24);
-        }
-        src_.resize(n);
-        for (int c = 0; c < n; c++) {
-            PS_CUDA(cudaMemcpy(rig.inputBuffer(c, 0), pattern.data(), pattern.size(), cudaMemcpyHostToDevice));
-            src_[c] = {rig.inputBuffer(c, 0), pitch, rig.srcW(), rig.srcH(), PS_FMT_BGR32, PS_MEM_DEVICE};
+        src_.resize(rig.slots());
+        for (int sl = 0; sl < rig.slots(); sl++) {
+            for (uint8_t& b : pattern) {  // xorshift32, continued from slot to slot
+                x ^= x << 13;
+                x ^= x >> 17;
+                x ^= x << 5;
+                b = (uint8_t)(x >> 24);
+            }
+            src_[sl].resize(n);
+            for (int c = 0; c < n; c++) {
+                PS_CUDA(cudaMemcpy(rig.inputBuffer(c, sl), pattern.data(), pattern.size(), cudaMemcpyHostToDevice));
+                src_[sl][c] = {rig.inputBuffer(c, sl), pitch, rig.srcW(), rig.srcH(), PS_FMT_BGR32, PS_MEM_DEVICE};
+            }
         }
         luts_.resize((size_t)n * 768);
         for (size_t k = 0; k < luts_.size(); k++) luts_[k] = (uint8_t)std::min<size_t>(255, (k % 256) * 9 / 8);
@@ -90,17 +95,18 @@ public:
         if (t1_) cudaEventDestroy(t1_);
     }
 
-    // ms per frame of a shape: the median of three timed runs
+    // ms per frame of a shape: the median of five timed runs (a 1% move must
+    // stand out of run-to-run noise of about that size)
     double time(const LaunchShape& shape)
     {
         rig_.setShape(shape);
         plan_.bind({&rig_});
         for (int k = 0; k < 2 * Rig::kIoSlots; k++) issue(k);  // every argument slot captures its graph
         for (cudaStream_t s : streams_) PS_CUDA(cudaStreamSynchronize(s));
-        double t[3];
+        double t[5];
         for (double& v : t) v = timed();
-        std::sort(t, t + 3);
-        return t[1];
+        std::sort(t, t + 5);
+        return t[2];
     }
     void setFrames(int f) { frames_ = f; }
     int frames() const { return frames_; }
@@ -108,7 +114,7 @@ public:
 private:
     void issue(int k)
     {
-        const FrameInput in{src_.data(), luts_.data(), &dst_[k % inflight_]};
+        const FrameInput in{src_[k % src_.size()].data(), luts_.data(), &dst_[k % inflight_]};
         plan_.run({in}, streams_[k % inflight_], useGraph_);
     }
     double timed()
@@ -131,7 +137,8 @@ private:
     Plan& plan_;
     int frames_, inflight_;
     bool useGraph_;
-    std::vector<ps_image> src_, dst_;
+    std::vector<std::vector<ps_image>> src_;  // per state slot: the cameras' inputs
+    std::vector<ps_image> dst_;
     std::vector<uint8_t> luts_;
     std::vector<DevBuf> out_;
     std::vector<cudaStream_t> streams_;
@@ -158,6 +165,15 @@ std::vector<LaunchShape> neighbours(const Rig& rig, const LaunchShape& cur, int 
             LaunchShape s = cur;
             s.tailMaxItems = v;
             out.push_back(s);
+            // the blend levels a smaller tail hands back run best as half tiles
+            // together with it, so the split is also tried with those levels in
+            // k_blend_small (each knob alone can measure slower than the pair)
+            int most = 0;
+            for (int j = std::max(1, b); j < curBlend; j++) most = std::max(most, rig.numBlendItems(j));
+            if (most > cur.smallBlendMaxItems && most <= 512) {
+                s.smallBlendMaxItems = most;
+                out.push_back(s);
+            }
         }
         break;
     }
@@ -242,8 +258,8 @@ LaunchShape autotune(Rig& rig, Plan& plan, int framesPerTrial, int inflight, boo
         Trials trials(rig, plan, framesPerTrial, inflight, useGraph);
         double tBest = trials.time(best);
         report.trials = 1;
-        // at least ~2 ms of device time per timed run
-        const int want = (int)std::min(2000.0, std::max((double)framesPerTrial, 2.0 / std::max(tBest, 1e-4)));
+        // at least ~4 ms of device time per timed run
+        const int want = (int)std::min(4000.0, std::max((double)framesPerTrial, 4.0 / std::max(tBest, 1e-4)));
         if (want > trials.frames()) {
             trials.setFrames(want);
             tBest = trials.time(best);
