@@ -352,8 +352,8 @@ int ps_render_set_launch_shape(ps_render* r, const ps_launch_shape* shape);
 int ps_render_get_launch_shape(const ps_render* r, ps_launch_shape* shape);
 /* Times launch shapes on the prepared render (frames_per_trial frames per
    timed run, 0 = 20; issued round-robin on in_flight streams, 0 = the
-   render's frames in flight) by coordinate descent from the default
-   shape, and keeps the fastest.  The render's input staging (every state
+   render's frames in flight) over a small grid of the interacting
+   choices, then by coordinate descent from the best, and keeps the fastest.  The render's input staging (every state
    slot) is overwritten with test patterns, and the trials cycle through
    them as distinct frames would.  A geometry tuned before in this
    process is not timed again unless force is non-zero.  Blocks (a few

@@ -258,14 +258,54 @@ LaunchShape autotune(Rig& rig, Plan& plan, int framesPerTrial, int inflight, boo
         Trials trials(rig, plan, framesPerTrial, inflight, useGraph);
         double tBest = trials.time(best);
         report.trials = 1;
-        // at least ~4 ms of device time per timed run
-        const int want = (int)std::min(4000.0, std::max((double)framesPerTrial, 4.0 / std::max(tBest, 1e-4)));
+        // at least ~4 ms of device time and eight frames per stream per timed
+        // run: a short run is mostly the pipeline filling and draining, which
+        // hides what a shape changes in the steady state of frames in flight
+        const int want = (int)std::min(4000.0, std::max({(double)framesPerTrial, 4.0 / std::max(tBest, 1e-4),
+                                                          8.0 * inflight}));
         if (want > trials.frames()) {
             trials.setFrames(want);
             tBest = trials.time(best);
             report.trials++;
         }
         report.msDefault = tBest;
+        // The knobs interact: with frames in flight, dropping the tail kernel,
+        // running the few-tile levels as half tiles and narrowing the blend
+        // grid pay off together while each alone measures slower.  So a small
+        // grid over those three seeds the descent.
+        {
+            std::vector<LaunchShape> seen{best};
+            const int L = rig.numLevels();
+            for (int tail : {0, 2, 16})
+                for (int small : {0, 32, 128})
+                    for (int ctas : {0, 1, 2}) {
+                        LaunchShape s;
+                        s.tailMaxItems = tail;
+                        s.smallBlendMaxItems = small;
+                        s.ctasPerSm[2] = ctas;
+                        // shapes that launch the same work the same way are timed once
+                        int d = 0, b = 0;
+                        rig.tailSplit(tail, &d, &b);
+                        int smallLevels = 0;
+                        for (int j = 1; j < b && j <= L; j++) smallLevels += rig.numBlendItems(j) <= small;
+                        bool dup = false;
+                        for (const LaunchShape& o : seen) {
+                            int od = 0, ob = 0;
+                            rig.tailSplit(o.tailMaxItems, &od, &ob);
+                            int os = 0;
+                            for (int j = 1; j < ob && j <= L; j++) os += rig.numBlendItems(j) <= o.smallBlendMaxItems;
+                            if (od == d && ob == b && os == smallLevels && o.ctasPerSm[2] == ctas) dup = true;
+                        }
+                        if (dup) continue;
+                        seen.push_back(s);
+                        const double t = trials.time(s);
+                        report.trials++;
+                        if (t < tBest * 0.99) {
+                            tBest = t;
+                            best = s;
+                        }
+                    }
+        }
         // coordinate descent, two passes; a move must gain 1%
         for (int pass = 0; pass < 2; pass++) {
             bool moved = false;
