@@ -66,6 +66,28 @@ __device__ __forceinline__ void bulkCopy(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
+// Bulk tensor copies (TMA, tile mode, no swizzle) of one box of a 3-D or
+// 2-D tensor map into shared memory, completing on an mbarrier.  The map
+// (a CUtensorMap) lives in global memory; dst must be 128-byte aligned and
+// the box's first coordinate times the element size a multiple of 16 bytes.
+__device__ __forceinline__ void tmaLoad3d(void* dst, const void* tmap, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smemAddr(dst)),
+        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smemAddr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tmaLoad2d(void* dst, const void* tmap, int x, int y, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smemAddr(dst)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smemAddr(bar))
+        : "memory");
+}
+
 // Named barrier over the first `count` threads of the CTA (id 1..15).
 __device__ __forceinline__ void namedBarrier(int id, int count)
 {

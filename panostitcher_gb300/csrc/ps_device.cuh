@@ -70,6 +70,13 @@ struct RemapParamF {
     float distance, horizontal, vertical;
 };
 
+// The tensor maps of one level for k_blend's producer (boxes of the bulk
+// tensor copies): the level's G tile (64 x 16 x 1 of uint32 over pitch x h x
+// cameras), its G footprint as the level above a blend (40 x 10 x 1), its
+// collapsed C footprint (36 x 10 of 8-byte pixels over pitch x h) and its
+// weight tile (64 x 16 x 1 of uint16).
+constexpr int kTmG = 0, kTmGfp = 1, kTmC = 2, kTmW = 3, kTmapsPerLevel = 4;
+
 struct RigDev {
     int n, L, W, H;
     int full;                 // union of coverages == whole canvas
@@ -82,6 +89,10 @@ struct RigDev {
     const uint32_t* covTiles;
     const uint8_t* unionMask; // level-0 union coverage (0/255), pitch = lv[0].pitch
     const uint8_t* camLists;  // camera indices of blend tiles with more than 8 cameras
+    // TMA tensor maps of this state slot (CUtensorMap, 128 bytes each, 64-byte
+    // aligned in device memory), kTmapsPerLevel per level: see kTmG ... kTmW;
+    // NULL when they could not be encoded (k_blend then copies row by row)
+    const void* tmaps;
     LevelDev lv[PS_MAX_LEVELS + 1];
     // work items of every level (used by the tail kernel)
     const DownItem* downItems;

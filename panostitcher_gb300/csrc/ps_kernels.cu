@@ -16,6 +16,7 @@
 // ~36 per frame over full-canvas int16/int32 images
 // (source/CudaAccel/CudaMultibandBlend.cpp:785-823).
 #include <algorithm>
+#include <cstddef>
 
 #include "ps_async.cuh"
 #include "ps_device.cuh"
@@ -754,15 +755,23 @@ constexpr int kBlendThreads = kConsumers + 32;  // + the producer warp
 
 // One unit's shared-memory stage: NC cameras of one tile (k_blend stages
 // two cameras per unit in a ring; the tail kernel stages up to eight at once).
+// Every camera's part starts on a 128-byte boundary, as the bulk tensor
+// copies into it require: the footprint of a camera is kFH rows of kFpW
+// words (a dense box), padded to kFpCam words.
 template <int NC>
-struct alignas(16) BlendStageT {
+struct alignas(128) BlendStageT {
     static constexpr int kCams = NC;
+    static constexpr int kFpCam = (kFH * kFpW + 31) / 32 * 32;
     uint32_t gj[NC][kBlendTH][kBlendTW];  // G_j, uchar4
     uint16_t w[NC][kBlendTH][kBlendTW];   // weights
-    uint32_t fp[NC][kFH][kFpW];           // G_{j+1} footprint
+    uint32_t fpw[NC][kFpCam];             // G_{j+1} footprint: row r, column c at [r * kFpW + c]
     uint2 cf[kFH][kCfW];                  // C_{j+1} footprint (short4 bits)
 };
 using BlendStage = BlendStageT<kCamsPerUnit>;
+static_assert(offsetof(BlendStage, w) % 128 == 0 && offsetof(BlendStage, fpw) % 128 == 0 &&
+                  offsetof(BlendStage, cf) % 128 == 0 && sizeof(BlendStage::gj[0]) % 128 == 0 &&
+                  sizeof(BlendStage::w[0]) % 128 == 0 && sizeof(BlendStage::fpw[0]) % 128 == 0,
+              "every bulk tensor copy destination starts on a 128-byte boundary");
 constexpr int kTailCamsPerUnit = 8;
 
 // What the consumers need of a unit besides its stage: the level geometry
@@ -963,7 +972,7 @@ __device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const
             const int cam = tileCam(raw, R.camLists, c0 + q);
             const uint32_t* gp = reinterpret_cast<const uint32_t*>(Lu.G) + (size_t)cam * Lu.camStride +
                                  (size_t)fRow[r] * Lu.pitch + fCol[c];
-            S.fp[q][r][c + 3] = inside(gp, Lu.G, gBytes(R, Lu)) ? ldLevel<kFresh>(gp) : 0u;
+            S.fpw[q][r * kFpW + c + 3] = inside(gp, Lu.G, gBytes(R, Lu)) ? ldLevel<kFresh>(gp) : 0u;
         }
         if (last)
             for (int k = threadIdx.x; k < elems; k += kConsumers) {
@@ -1067,8 +1076,8 @@ __device__ __forceinline__ void stageUnitRows(Stage& S, const RigDev& R, const u
         const int t = wp + i * kWarps;
         if (t < gTasks) {
             const int q = t / nr, r = rb + (t - q * nr);
-            S.fp[q][r][lane + 3] = fa[i];
-            if (hasB) S.fp[q][r][32 + lane + 3] = fb[i];
+            S.fpw[q][r * kFpW + lane + 3] = fa[i];
+            if (hasB) S.fpw[q][r * kFpW + 32 + lane + 3] = fb[i];
         }
     }
 #pragma unroll
@@ -1156,7 +1165,7 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
     if (active) {
         for (int q = 0; q < nc; q++) {
             uint32_t ulo[4] = {0, 0, 0, 0}, uhi[4] = {0, 0, 0, 0};
-            if (hasUp) upsample2x2(&S.fp[q][wp][3 + lane], kFpW, ulo, uhi);
+            if (hasUp) upsample2x2(&S.fpw[q][wp * kFpW + 3 + lane], kFpW, ulo, uhi);
             const uint2 gt = *reinterpret_cast<const uint2*>(&S.gj[q][ly][lx]);
             const uint2 gb = *reinterpret_cast<const uint2*>(&S.gj[q][ly + 1][lx]);
             const uint32_t gp[4] = {gt.x, gt.y, gb.x, gb.y};
@@ -1337,7 +1346,7 @@ __device__ __forceinline__ void computeUnitRows(const Stage& S, const UnitGeo& G
     for (int q = 0; q < nc; q++) {
         uint32_t u0lo = 0, u0hi = 0, u1lo = 0, u1hi = 0;
         if (hasUp) {
-            const uint32_t* g = &S.fp[q][0][0] + 3;
+            const uint32_t* g = &S.fpw[q][0] + 3;
             uint32_t vlo[3], vhi[3];
 #pragma unroll
             for (int k = 0; k < 3; k++) {
@@ -1531,6 +1540,28 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                 }
                 __syncwarp();
                 const int fx0 = tx * (kBlendTW / 2) - 1, fy0 = ty * (kBlendTH / 2) - 1;
+#ifndef PS_CHECK_BOUNDS
+                if (R->tmaps) {
+                    // one bulk tensor copy per camera and array: the G_j tile,
+                    // its weights, its G_{j+1} footprint; then the C_{j+1} footprint
+                    if (lane == 0) {
+                        const uint8_t* tm = static_cast<const uint8_t*>(R->tmaps);
+                        const uint8_t* tmJ = tm + (size_t)j * kTmapsPerLevel * 128;
+                        const uint8_t* tmU = tm + (size_t)(j + 1) * kTmapsPerLevel * 128;
+                        for (int q = 0; q < nc; q++) {
+                            const int cam = tileCam(raw, R->camLists, chunk * kCamsPerUnit + q);
+                            tmaLoad3d(&st[stg].gj[q][0][0], tmJ + kTmG * 128, tx * kBlendTW, ty * kBlendTH, cam,
+                                      &full[stg]);
+                            if (!uni)
+                                tmaLoad3d(&st[stg].w[q][0][0], tmJ + kTmW * 128, tx * kBlendTW, ty * kBlendTH, cam,
+                                          &full[stg]);
+                            if (hasUp) tmaLoad3d(&st[stg].fpw[q][0], tmU + kTmGfp * 128, fx0 - 3, fy0, cam, &full[stg]);
+                        }
+                        if (hasUp && last) tmaLoad2d(&st[stg].cf[0][0], tmU + kTmC * 128, fx0 - 1, fy0, &full[stg]);
+                    }
+                    nCopies = 0;
+                }
+#endif
                 for (int k = lane; k < nCopies; k += 32) {
                     if (k < nc * cb) {
                         const int q = k / cb;
@@ -1554,7 +1585,7 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                             }
                             r -= kBlendTH;
                         }
-                        bulkCopyChecked(&st[stg].fp[q][r][0],
+                        bulkCopyChecked(&st[stg].fpw[q][r * kFpW],
                                         Lu.G + (size_t)cam * Lu.camStride + (size_t)(fy0 + r) * Lu.pitch + (fx0 - 3),
                                         kFpW * 4, &full[stg], Lu.G, gBytes(*R, Lu));
                     } else {
@@ -1638,7 +1669,7 @@ union TailSmem {
 
 __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ segs, int nsegs, int cluster)
 {
-    extern __shared__ __align__(16) uint8_t tailSmem[];  // a TailSmem (dynamic: above the 48 KB static limit)
+    extern __shared__ __align__(128) uint8_t tailSmem[];  // a TailSmem (dynamic: above the 48 KB static limit)
     TailSmem& sm = *reinterpret_cast<TailSmem*>(tailSmem);
     
     const int rig = blockIdx.x / cluster, rank = blockIdx.x % cluster;
@@ -1691,7 +1722,7 @@ using SmallStage = BlendStageT<kTailCamsPerUnit>;
 
 __global__ void __launch_bounds__(kThreads) k_blend_small(const Segment* __restrict__ segs, int nsegs, int total)
 {
-    extern __shared__ __align__(16) uint8_t smallSmem[];  // a SmallStage (dynamic: above the 48 KB static limit)
+    extern __shared__ __align__(128) uint8_t smallSmem[];  // a SmallStage (dynamic: above the 48 KB static limit)
     SmallStage& st = *reinterpret_cast<SmallStage*>(smallSmem);
     
     // Items and descriptors are written before the launch sequence, not by

@@ -2,6 +2,9 @@
 // launch plans that stitch frames with it.
 #include "ps_rig.h"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 #include <atomic>
@@ -124,6 +127,7 @@ void Rig::clear()
     maps_.reset(); union_.reset(); inputs_.reset(); output_.reset(); covDev_.reset(); status_.reset(); planar_.reset();
     camsF_.reset(); covTiles_.reset();
     imgArgs_.reset(); dDesc_.reset(); dRemap_.reset(); dDown_.reset(); dBlend_.reset(); dCams_.reset();
+    tmaps_.reset();
     hRemap_.clear();
     hDown_.clear();
     hBlend_.clear();
@@ -183,6 +187,7 @@ long long Rig::residentBytes() const
     }
     b += maps_.bytes() + union_.bytes() + inputs_.bytes() + output_.bytes() + covDev_.bytes() + status_.bytes();
     b += imgArgs_.bytes() + dDesc_.bytes() + dRemap_.bytes() + dDown_.bytes() + dBlend_.bytes() + dCams_.bytes();
+    b += tmaps_.bytes();
     b += dLinear_.bytes() + linW_.bytes() + planar_.bytes() + camsF_.bytes() + covTiles_.bytes();
     return b;
 }
@@ -757,12 +762,75 @@ void Rig::setCustomMasks(const uint8_t* const* masks, cudaStream_t st)
     gen_ = g_generation++;
 }
 
+// The driver's tensor-map encoder, looked up once through the runtime.
+static PFN_cuTensorMapEncodeTiled_v12000 tensorMapEncoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// The tensor maps of k_blend's producer for every state slot and level (see
+// kTmG ... kTmW): G and W as pitch x h x cameras, C as pitch x h.  Boxes lie
+// inside the level wherever the producer uses them (interior tiles); the
+// maps still bound them, filling zeros outside.
+bool Rig::encodeTensorMaps()
+{
+    tmaps_.reset();
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensorMapEncoder();
+    if (!encode || linear_) return false;
+    const int perSlot = (L_ + 1) * kTmapsPerLevel;
+    std::vector<CUtensorMap> maps((size_t)slots_ * perSlot);
+    std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+    auto tiled = [&](CUtensorMap* m, CUtensorMapDataType type, size_t esz, void* base, int rank, cuuint64_t w,
+                     cuuint64_t h, cuuint64_t cams, cuuint32_t bw, cuuint32_t bh, long long pitch, long long camStride) {
+        const cuuint64_t dims[3] = {w, h, cams};
+        const cuuint64_t strides[2] = {(cuuint64_t)pitch * esz, (cuuint64_t)camStride * esz};
+        const cuuint32_t box[3] = {bw, bh, 1};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        return encode(m, type, (cuuint32_t)rank, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
+    for (int k = 0; k < slots_; k++)
+        for (int j = 0; j <= L_; j++) {
+            const LevelGeom& g = geom_[j];
+            const long long cs = (long long)g.pitch * g.h;
+            CUtensorMap* m = maps.data() + (size_t)k * perSlot + (size_t)j * kTmapsPerLevel;
+            bool ok = tiled(m + kTmG, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, lv_[j].G[k].get(), 3, g.pitch, g.h, n_,
+                            kBlendTW, kBlendTH, g.pitch, cs) &&
+                      tiled(m + kTmGfp, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, lv_[j].G[k].get(), 3, g.pitch, g.h, n_,
+                            kBlendTW / 2 + 8, kBlendTH / 2 + 2, g.pitch, cs) &&
+                      tiled(m + kTmW, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv_[j].Wt.get(), 3, g.pitch, g.h, n_,
+                            kBlendTW, kBlendTH, g.pitch, cs);
+            if (ok && j > 0)
+                ok = tiled(m + kTmC, CU_TENSOR_MAP_DATA_TYPE_UINT64, 8, lv_[j].C[k].get(), 2, g.pitch, g.h, 1,
+                           kBlendTW / 2 + 4, kBlendTH / 2 + 2, g.pitch, cs);
+            if (!ok) return false;
+        }
+    tmaps_.alloc(maps.size() * sizeof(CUtensorMap));
+    PS_CUDA(cudaMemcpy(tmaps_.get(), maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+    return true;
+}
+
 // One descriptor per state slot, differing in the pyramid pointers.
 void Rig::writeDescriptors(cudaStream_t st)
 {
     RigDev ds[kIoSlots];
+    const bool tma = encodeTensorMaps();
     for (int k = 0; k < slots_; k++) {
         ds[k] = hDesc_;
+        ds[k].tmaps = tma ? static_cast<const uint8_t*>(tmaps_.get()) +
+                                (size_t)k * (L_ + 1) * kTmapsPerLevel * sizeof(CUtensorMap)
+                          : nullptr;
         for (int j = 0; j <= L_; j++) {
             ds[k].lv[j].G = lv_[j].G[k].as<uchar4>();
             ds[k].lv[j].C = lv_[j].C[k].as<short4>();

@@ -187,6 +187,7 @@ private:
     void prepareLinear(const uint8_t* covDev, const uint8_t* seamDev, const float* xmapDev, const float* ymapDev,
                        int radius, cudaStream_t st);
     void writeDescriptors(cudaStream_t st);
+    bool encodeTensorMaps();  // tmaps_ for every slot and level; false when the driver cannot
     void toLevel0(const void* const* images, const long long* pitches, int fmt, int cam0, int count, int slot,
                   cudaStream_t st);
     void buildBlendState(const uint8_t* uniSrcDev, bool custom, cudaStream_t st);
@@ -206,6 +207,7 @@ private:
     DevBuf maps_, union_, inputs_, output_, covDev_, status_, imgArgs_, planar_;
     long long inPitch_ = 0, budget_ = 0;
     DevBuf dDesc_, dRemap_, dDown_, dBlend_, dCams_;
+    DevBuf tmaps_;  // slots x (L + 1) x kTmapsPerLevel CUtensorMap
     std::vector<RemapItem> hRemap_;
     int downOff_[PS_MAX_LEVELS + 1] = {}, downCnt_[PS_MAX_LEVELS + 1] = {};
     int blendOff_[PS_MAX_LEVELS + 1] = {}, blendCnt_[PS_MAX_LEVELS + 1] = {};
@@ -306,7 +308,8 @@ private:
 };
 
 // The autotuner (ps_tune.cpp): times launch shapes on a prepared rig by
-// coordinate descent from the default shape (tail split, the levels run as
+// a grid over the tail split, the half-tile levels and the blend's CTAs per
+// SM, then coordinate descent from the best of it (tail split, the levels run as
 // half tiles by k_blend_small, tail tile split, tail cluster width, CTAs per
 // SM of k_blend, k_pyrdown, k_remap), frames
 // issued round-robin on `inflight` streams, and leaves the fastest set on
