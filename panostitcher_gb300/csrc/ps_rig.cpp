@@ -208,10 +208,11 @@ static void validateParams(const ps_photo_param* params, int n, int srcW, int sr
 
 // Upper bound of the work lists and descriptors a rig of this shape holds:
 // every pyrDown and blend tile listed (with its camera list), remap items for
-// every camera's level-0 tiles, one descriptor per state slot.
+// every camera's level-0 tiles, one descriptor and one set of tensor maps per
+// state slot.
 static long long listBytes(int W, int H, int n, int L, int slots)
 {
-    long long b = (long long)sizeof(RigDev) * slots + 4096;
+    long long b = (long long)(sizeof(RigDev) + (size_t)(L + 1) * kTmapsPerLevel * sizeof(CUtensorMap)) * slots + 4096;
     int w = W, h = H;
     for (int j = 0; j <= L; j++) {
         const long long down = (long long)divUp(w, kDownTW) * divUp(h, kDownTH) * n;
