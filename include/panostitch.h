@@ -303,7 +303,8 @@ int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out,
    one kernel kind (0 remap, 1 pyrDown, 2 blend, 3 the tail kernel that runs
    the few-tile top levels, reported at its lowest blend level, 4 the
    linear-blend render, 5 the conversion of decoder frames, at level 0, 6
-   the blend of few-tile levels in half tiles) at
+   the blend of few-tile levels in half tiles, 7 the exact recompute of the
+   remap tiles whose fp32 result lies near a rounding tie, at level 0) at
    one level (-1 = all levels): launch count, summed device milliseconds
    and summed algorithmic bytes (each input and output element counted
    once).
@@ -338,6 +339,11 @@ typedef struct ps_launch_shape {
     int small_blend_max_items; /* blend levels above 0 (below the tail) with at
                              most this many tiles run as 64x8 half tiles, up to
                              eight cameras staged at once; 0 = none (default 0) */
+    int remap_defer_ties; /* 1: the remap lists the pixels whose fp32 result lies
+                             near a rounding tie and a short second launch
+                             recomputes them exactly (faster with frames in
+                             flight); 0: the remap recomputes them itself (the
+                             shortest single frame) (default 1) */
 } ps_launch_shape;
 typedef struct ps_tune_report {
     double ms_per_frame_default;  /* device ms per frame of the default shape */

@@ -69,7 +69,7 @@ class LaunchShape(C.Structure):
     """ps_launch_shape: the launch choices that can change after prepare."""
 
     _fields_ = [("tail_max_items", C.c_int), ("tail_cluster", C.c_int), ("tail_half_tiles", C.c_int),
-                ("ctas_per_sm", C.c_int * 3), ("small_blend_max_items", C.c_int)]
+                ("ctas_per_sm", C.c_int * 3), ("small_blend_max_items", C.c_int), ("remap_defer_ties", C.c_int)]
 
 
 class TuneReport(C.Structure):

@@ -233,7 +233,7 @@ int ps_render_profile_read(ps_render* r, int kind, int level, long long* launche
 {
     return guarded([&] {
         if (!r) fail(PS_EINVAL, "render is NULL");
-        if (kind < 0 || kind > 6) fail(PS_EINVAL, "kind %d not in 0..6", kind);
+        if (kind < 0 || kind > 7) fail(PS_EINVAL, "kind %d not in 0..7", kind);
         r->prof.read(kind, level, launches, total_ms, bytes);
     });
 }
@@ -260,6 +260,7 @@ ps::LaunchShape fromAbi(const ps_launch_shape& s)
     o.tailHalf = s.tail_half_tiles;
     for (int k = 0; k < 3; k++) o.ctasPerSm[k] = s.ctas_per_sm[k];
     o.smallBlendMaxItems = s.small_blend_max_items;
+    o.remapDefer = s.remap_defer_ties;
     return o;
 }
 
@@ -270,6 +271,7 @@ void toAbi(const ps::LaunchShape& s, ps_launch_shape* o)
     o->tail_half_tiles = s.tailHalf;
     for (int k = 0; k < 3; k++) o->ctas_per_sm[k] = s.ctasPerSm[k];
     o->small_blend_max_items = s.smallBlendMaxItems;
+    o->remap_defer_ties = s.remapDefer;
 }
 
 }  // namespace

@@ -151,6 +151,17 @@ struct Segment {
     int count, prefix;
 };
 
+// A level-0 pixel whose fp32 remap lies near a rounding tie, listed by the
+// remap for its exact recompute: everything the recompute needs without
+// looking the tile up again.
+struct RemapTie {
+    const FrameDev* frame;
+    const RigDev* rig;
+    float mx, my;    // the map value
+    uint32_t pixel;  // y * pitch + x in the camera's level-0 plane
+    int cam;
+};
+
 #ifdef __CUDACC__
 // Item `it` of a launch -> its segment, scanning forward from a hint (each
 // CTA visits its items in increasing order).

@@ -170,11 +170,12 @@ struct LaunchShape {
     int tailHalf = 1;              // the tail blends levels above 0 in 64x8 half tiles
     int ctasPerSm[3] = {0, 0, 0};  // k_remap, k_pyrdown, k_blend; 0 = as many as fit
     int smallBlendMaxItems = 0;    // blend levels above 0 with at most this many tiles run in k_blend_small
+    int remapDefer = 1;            // near-tie remap pixels recomputed by k_remap_fix (1) or inside k_remap (0)
     bool operator==(const LaunchShape& o) const
     {
         return tailMaxItems == o.tailMaxItems && tailCluster == o.tailCluster && tailHalf == o.tailHalf &&
                ctasPerSm[0] == o.ctasPerSm[0] && ctasPerSm[1] == o.ctasPerSm[1] && ctasPerSm[2] == o.ctasPerSm[2] &&
-               smallBlendMaxItems == o.smallBlendMaxItems;
+               smallBlendMaxItems == o.smallBlendMaxItems && remapDefer == o.remapDefer;
     }
     bool operator!=(const LaunchShape& o) const { return !(*this == o); }
 };
@@ -183,7 +184,16 @@ struct LaunchShape {
 // perSm > 0 caps the CTAs per SM of the one-wave persistent grid; counter
 // (remap and blend) is a zeroed int through which the launch hands out its
 // work items
-cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st);
+// defer: near-tie pixels go on the list (tieCount, ties) for launchRemapFix;
+// otherwise k_remap recomputes them itself
+cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, int* tieCount,
+                        RemapTie* ties, bool defer, cudaStream_t st);
+// the pixels k_remap listed as lying near a rounding tie, recomputed exactly;
+// ties has room for kRemapTiesPerTile entries per remap tile of the launch,
+// and tieCount is a zeroed int
+cudaError_t launchRemapFix(const Segment* segs, int nsegs, int total, const int* tieCount, const RemapTie* ties,
+                           cudaStream_t st);
+constexpr int kRemapTiesPerTile = 2;
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st);
 // counter: a zeroed int the launch hands its tiles out through
 // Accesses the checked build's kernels refused since the last reset

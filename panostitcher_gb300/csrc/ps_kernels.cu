@@ -17,6 +17,7 @@
 // (source/CudaAccel/CudaMultibandBlend.cpp:785-823).
 #include <algorithm>
 #include <cstddef>
+#include <cstdlib>
 
 #include "ps_async.cuh"
 #include "ps_device.cuh"
@@ -155,7 +156,12 @@ __device__ __forceinline__ void remapFetch(float2 m, const uint8_t* base, long l
 }
 
 // Returns B | G << 8 | R << 16 (0 where the map is invalid).
-__device__ __forceinline__ uint32_t remapFinish(const RemapTap& p, float2 m, const uint8_t* lut)
+// The fp32 result of a pixel's three channels.  Where a channel lies within
+// 2e-4 of a rounding tie, fp32 cannot decide the byte: with exact, that
+// channel is recomputed with the reference's double sequence; without,
+// nearTie is set and the caller has the pixel recomputed (k_remap_fix).
+template <bool kExact>
+__device__ __forceinline__ uint32_t remapFinish(const RemapTap& p, float2 m, const uint8_t* lut, bool& nearTie)
 {
     if (p.x0 < 0) return 0;
     const float gx = 1.f - p.fx, gy = 1.f - p.fy;
@@ -174,8 +180,12 @@ __device__ __forceinline__ uint32_t remapFinish(const RemapTap& p, float2 m, con
         // nearest integer, ties to even, in the low mantissa bits
         const float t = r + 12582912.f;
         int v = __float_as_int(t) - 0x4B400000;
-        if (fabsf(r - (t - 12582912.f)) > 0.4998f)  // within 2e-4 of a tie: exact recompute
-            v = bilinearExact((double)m.x, (double)m.y, p.x0, p.y0, p00, p01, p10, p11);
+        const bool tie = fabsf(r - (t - 12582912.f)) > 0.4998f;  // within 2e-4 of a tie
+        if (kExact) {
+            if (tie) v = bilinearExact((double)m.x, (double)m.y, p.x0, p.y0, p00, p01, p10, p11);
+        } else {
+            nearTie |= tie;
+        }
         out |= (uint32_t)v << (8 * c);
     }
     return out;
@@ -238,12 +248,21 @@ __device__ __forceinline__ float2 mapFreeValue(const RemapParamF& m, uint32_t co
                        fminf(fmaxf(v.y, 0.f), __int_as_float(__float_as_int((float)sh) - 1)));
 }
 
+// The remap of one pixel, exact (kExact) or fp32 with the near-tie flag.
+template <bool kExact = true>
 __device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, long long pitch, int fmt, int sw,
-                                               int sh, const uint8_t* lut)
+                                               int sh, const uint8_t* lut, bool& nearTie)
 {
     RemapTap p;
     remapFetch(m, base, pitch, fmt, sw, sh, p);
-    return remapFinish(p, m, lut);
+    return remapFinish<kExact>(p, m, lut, nearTie);
+}
+
+__device__ __forceinline__ uint32_t remapPixel(float2 m, const uint8_t* base, long long pitch, int fmt, int sw,
+                                               int sh, const uint8_t* lut)
+{
+    bool unused = false;
+    return remapPixel<true>(m, base, pitch, fmt, sw, sh, lut, unused);
 }
 
 // Level-0 remap over the covered 32x16 tiles of every camera; each thread
@@ -271,8 +290,45 @@ __device__ __forceinline__ RemapSeg remapSeg(const Segment* segs, int nsegs, int
 // its map are always known before the current item is gathered.
 constexpr int kRemapChunk = 8;
 
+// The map value of pixel (lx, row) of a remap tile: from the resident maps,
+// or, map-free, from the coverage bits (the FP64 coverage of prepare) and the
+// fp32 geometry.
+__device__ __forceinline__ float2 remapMapValue(const RigDev& R, const RemapItem& itm, int lx, int row)
+{
+    const long long tiles = R.numRemapItems;
+    if (R.maps) {
+        const float2* mt = R.maps + (size_t)itm.mapTile * (kRemapTW * kRemapTH) + row * kRemapTW + lx;
+        return ldChecked(mt, R.maps, tiles * kRemapTW * kRemapTH * (long long)sizeof(float2));
+    }
+    const uint32_t* cw = R.covTiles + (size_t)itm.mapTile * kRemapTH;
+    const uint32_t bits = ldChecked(cw + row, R.covTiles, tiles * kRemapTH * 4);
+    return mapFreeValue(R.camsF[itm.cam], bits, lx, itm.tx * kRemapTW + lx, itm.ty * kRemapTH + row, R.srcW,
+                        R.srcH);
+}
+
+// The exact pixel: the reference's double sequence where fp32 lies near a
+// tie; the camera's LUT is read from global memory.
+__device__ __forceinline__ void remapFixPixel(const FrameDev& F, const RigDev& R, float2 m, uint32_t pixel, int cam)
+{
+    const uint32_t pitch = (uint32_t)R.lv[0].pitch;
+    if (pixel % pitch >= (uint32_t)R.W || pixel / pitch >= (uint32_t)R.H) return;  // a tile's part off the canvas
+    const uint32_t v = remapPixel(m, F.src[cam], F.srcPitch[cam], F.srcFmt, R.srcW, R.srcH, F.luts + cam * 768);
+    uint32_t* g = reinterpret_cast<uint32_t*>(R.lv[0].G) + (size_t)cam * R.lv[0].camStride + pixel;
+    if (inside(g, R.lv[0].G, gBytes(R, R.lv[0]))) *g = v;
+}
+
+// The rare pixels whose fp32 remap lies near a rounding tie (about 0.1% of
+// them) get the reference's double sequence.  Inline (kDefer false), the
+// check with its out-of-line double call costs every pixel (a quarter of the
+// kernel's instructions; keeping the double sequence inline spills).
+// Deferred, a warp appends such pixels to the launch's list (tieCount, ties:
+// room for tieCap entries, one atomic per warp) and k_remap_fix recomputes
+// them before anything reads level 0: the remap is faster, and the short
+// extra launch costs latency only when nothing else is in flight.
+template <bool kDefer>
 __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict__ segs, int nsegs, int total,
-                                                       int* __restrict__ counter)
+                                                       int* __restrict__ counter, int* __restrict__ tieCount,
+                                                       RemapTie* __restrict__ ties, int tieCap)
 {
     __shared__ uint8_t lut[3 * 256];
     __shared__ int s_grab;
@@ -286,25 +342,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
     // The hand-out counter, items, descriptors and maps are written before
     // the launch sequence, not by a kernel: the first chunk and its map are
     // fetched while the previous kernel finishes.
-    // The tile's two map values of this thread: from the resident maps, or,
-    // map-free, from the coverage bits (the FP64 coverage of prepare) and the
-    // fp32 geometry.
-    auto loadMap = [&](const RigDev& R, const RemapItem& itm, float2& a, float2& b) {
-        const long long tiles = R.numRemapItems;
-        if (R.maps) {
-            const float2* mt = R.maps + (size_t)itm.mapTile * (kRemapTW * kRemapTH);
-            const long long mb = tiles * kRemapTW * kRemapTH * (long long)sizeof(float2);
-            a = ldChecked(mt + threadIdx.x, R.maps, mb);
-            b = ldChecked(mt + threadIdx.x + kThreads, R.maps, mb);
-        } else {
-            const uint32_t* cw = R.covTiles + (size_t)itm.mapTile * kRemapTH;
-            const RemapParamF& pf = R.camsF[itm.cam];
-            const int cx = itm.tx * kRemapTW + lx, cy = itm.ty * kRemapTH + ly;
-            const long long cb = tiles * kRemapTH * 4;
-            a = mapFreeValue(pf, ldChecked(cw + ly, R.covTiles, cb), lx, cx, cy, R.srcW, R.srcH);
-            b = mapFreeValue(pf, ldChecked(cw + ly + 8, R.covTiles, cb), lx, cx, cy + 8, R.srcW, R.srcH);
-        }
-    };
     int it = grab(), end = 0, nextBegin = total, s = 0;
     RemapSeg cur{};
     RemapItem item{};
@@ -315,13 +352,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
         s = findSegment(segs, nsegs, it, 0);
         cur = remapSeg(segs, nsegs, s, total);
         item = cur.items[it - cur.prefix];
-        loadMap(*cur.R, item, m0, m1);
+        m0 = remapMapValue(*cur.R, item, lx, ly);
+        m1 = remapMapValue(*cur.R, item, lx, ly + 8);
     }
     waitPrevGrid();
     allowNextGrid();
     if (it >= total) return;
     // constants of the loaded camera
     int camSeg = -1, cam = -1;
+    const FrameDev* camF = nullptr;  // the frame and rig of the loaded camera
+    const RigDev* camR = nullptr;
     const uint8_t* base = nullptr;
     long long pitch = 0;
     int fmt = 0, sw = 0, sh = 0, W = 0, H = 0, gpitch = 0;
@@ -334,6 +374,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
             const RigDev& R = *cur.R;
             cam = item.cam;
             camSeg = s;
+            camF = &F;
+            camR = &R;
             base = F.src[cam];
             pitch = F.srcPitch[cam];
             fmt = F.srcFmt;
@@ -360,11 +402,25 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
                 cur = remapSeg(segs, nsegs, s, total);
             }
             nitem = cur.items[nit - cur.prefix];
-            loadMap(*cur.R, nitem, n0, n1);
+            n0 = remapMapValue(*cur.R, nitem, lx, ly);
+            n1 = remapMapValue(*cur.R, nitem, lx, ly + 8);
         }
-        const uint32_t v0 = remapPixel(m0, base, pitch, fmt, sw, sh, lut);
-        const uint32_t v1 = remapPixel(m1, base, pitch, fmt, sw, sh, lut);
+        bool tie0 = false, tie1 = false;
+        const uint32_t v0 = remapPixel<!kDefer>(m0, base, pitch, fmt, sw, sh, lut, tie0);
+        const uint32_t v1 = remapPixel<!kDefer>(m1, base, pitch, fmt, sw, sh, lut, tie1);
         const int x = item.tx * kRemapTW + lx, y0 = item.ty * kRemapTH + ly, y1 = y0 + 8;
+        if (kDefer) {
+            const uint32_t b0 = __ballot_sync(0xffffffffu, tie0), b1 = __ballot_sync(0xffffffffu, tie1);
+            if (b0 | b1) {  // the warp's near-tie pixels, one atomic for the warp
+                int e = 0;
+                if (lx == 0) e = atomicAdd(tieCount, __popc(b0) + __popc(b1));
+                e = __shfl_sync(0xffffffffu, e, 0);
+                const uint32_t below = (1u << lx) - 1u;
+                const int e0 = e + __popc(b0 & below), e1 = e + __popc(b0) + __popc(b1 & below);
+                if (tie0 && e0 < tieCap) ties[e0] = {camF, camR, m0.x, m0.y, (uint32_t)((size_t)y0 * gpitch + x), cam};
+                if (tie1 && e1 < tieCap) ties[e1] = {camF, camR, m1.x, m1.y, (uint32_t)((size_t)y1 * gpitch + x), cam};
+            }
+        }
         if (x < W) {
             if (y0 < H && inside(G + (size_t)y0 * gpitch + x, gLo, gExt)) G[(size_t)y0 * gpitch + x] = v0;
             if (y1 < H && inside(G + (size_t)y1 * gpitch + x, gLo, gExt)) G[(size_t)y1 * gpitch + x] = v1;
@@ -378,6 +434,40 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
         item = nitem;
         m0 = n0;
         m1 = n1;
+    }
+}
+
+// The exact recompute of the pixels k_remap put on the launch's list
+// (ties[0 .. *tieCount)), one thread per entry.  An entry carries its frame,
+// rig, map value and pixel, so the recompute is a short chain of loads.
+// Most frames list none.  A list that overflowed (more than tieCap entries)
+// has every pixel of the launch recomputed, tile by tile.
+__global__ void __launch_bounds__(kThreads) k_remap_fix(const Segment* __restrict__ segs, int nsegs, int total,
+                                                        const int* __restrict__ tieCount,
+                                                        const RemapTie* __restrict__ ties, int tieCap)
+{
+    waitPrevGrid();
+    allowNextGrid();
+    const int listed = __ldcg(tieCount);
+    const long long stride = (long long)gridDim.x * kThreads;
+    const long long first = blockIdx.x * (long long)kThreads + threadIdx.x;
+    if (listed <= tieCap) {
+        for (long long e = first; e < listed; e += stride) {
+            const RemapTie t = ties[e];
+            remapFixPixel(*t.frame, *t.rig, make_float2(t.mx, t.my), t.pixel, t.cam);
+        }
+        return;
+    }
+    for (long long e = first; e < (long long)total * kThreads * 2; e += stride) {  // the list overflowed
+        const int it = (int)(e / (kThreads * 2)), t = (int)(e % (kThreads * 2)) >> 1, half = (int)(e & 1);
+        const int s = findSegment(segs, nsegs, it, 0);
+        const RemapSeg cur = remapSeg(segs, nsegs, s, total);
+        const RemapItem item = cur.items[it - cur.prefix];
+        const int lx = t & 31, row = (t >> 5) + half * 8;
+        const int x = item.tx * kRemapTW + lx, y = item.ty * kRemapTH + row;
+        if (x < cur.R->W && y < cur.R->H)
+            remapFixPixel(*cur.F, *cur.R, remapMapValue(*cur.R, item, lx, row),
+                          (uint32_t)((size_t)y * cur.R->lv[0].pitch + x), item.cam);
     }
 }
 
@@ -1983,18 +2073,45 @@ static cudaError_t launchPdl(void (*kernel)(Args...), int grid, int block, cudaS
 int residentCtasPerSm(int kind)
 {
     switch (kind) {
-    case 0: return residentPerSm<k_remap>(kThreads);
+    case 0: return std::min(residentPerSm<k_remap<true>>(kThreads), residentPerSm<k_remap<false>>(kThreads));
     case 1: return residentPerSm<k_pyrdown>(kThreads);
     case 2: return residentPerSm<k_blend>(kBlendThreads);
     default: return 1;
     }
 }
 
-cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, cudaStream_t st)
+// Entries the launch's tie list has room for.
+static int tieListCap(int total)
+{
+#ifdef PS_CHECK_BOUNDS
+    // the checked build's tests may lower it (0: k_remap_fix takes its overflow path)
+    static const int perTile = [] {
+        const char* v = std::getenv("PS_CHECKED_TIE_LIST_PER_TILE");
+        return v ? std::max(0, std::min(std::atoi(v), kRemapTiesPerTile)) : kRemapTiesPerTile;
+    }();
+    return perTile * total;
+#else
+    return kRemapTiesPerTile * total;
+#endif
+}
+
+cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, int* tieCount,
+                        RemapTie* ties, bool defer, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
-    return launchPdl(k_remap, gridFor(total, residentPerSm<k_remap>(kThreads), perSm), kThreads, st, segs, nsegs,
-                     total, counter);
+    if (defer)
+        return launchPdl(k_remap<true>, gridFor(total, residentPerSm<k_remap<true>>(kThreads), perSm), kThreads, st,
+                         segs, nsegs, total, counter, tieCount, ties, tieListCap(total));
+    return launchPdl(k_remap<false>, gridFor(total, residentPerSm<k_remap<false>>(kThreads), perSm), kThreads, st,
+                     segs, nsegs, total, counter, tieCount, ties, 0);
+}
+
+cudaError_t launchRemapFix(const Segment* segs, int nsegs, int total, const int* tieCount, const RemapTie* ties,
+                           cudaStream_t st)
+{
+    if (total <= 0) return cudaSuccess;
+    return launchPdl(k_remap_fix, 2 * smCount(), kThreads, st, segs, nsegs, total, tieCount, ties,
+                     tieListCap(total));
 }
 
 cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, cudaStream_t st)

@@ -221,7 +221,9 @@ static long long listBytes(int W, int H, int n, int L, int slots)
         w = (w + 1) / 2;
         h = (h + 1) / 2;
     }
-    return b + (long long)divUp(W, kRemapTW) * divUp(H, kRemapTH) * n * sizeof(RemapItem);
+    // remap items and each state slot's tie list
+    return b + (long long)divUp(W, kRemapTW) * divUp(H, kRemapTH) * n *
+                   (sizeof(RemapItem) + sizeof(RemapTie) * kRemapTiesPerTile * slots);
 }
 
 long long Rig::estimateBlenderBytes(int W, int H, int n, int maxLevels, int slots)
@@ -890,6 +892,8 @@ void Rig::setShape(const LaunchShape& s)
     if (s.tailCluster != 0 && s.tailCluster != 8 && s.tailCluster != 16)
         fail(PS_EINVAL, "tail_cluster must be 0, 8 or 16 (got %d)", s.tailCluster);
     if (s.tailHalf != 0 && s.tailHalf != 1) fail(PS_EINVAL, "tail_half_tiles must be 0 or 1 (got %d)", s.tailHalf);
+    if (s.remapDefer != 0 && s.remapDefer != 1)
+        fail(PS_EINVAL, "remap_defer_ties must be 0 or 1 (got %d)", s.remapDefer);
     if (s.smallBlendMaxItems < 0 || s.smallBlendMaxItems > (1 << 24))
         fail(PS_EINVAL, "small_blend_max_items %d out of range", s.smallBlendMaxItems);
     for (int k = 0; k < 3; k++)
@@ -1333,6 +1337,8 @@ void Plan::bind(const std::vector<Rig*>& rigs)
     };
     tailCluster_ = widest([](const LaunchShape& s) { return s.tailCluster; });
     for (int k = 0; k < 3; k++) perSm_[k] = widest([k](const LaunchShape& s) { return s.ctasPerSm[k]; });
+    remapDefer_ = false;  // deferred when any rig of the launch asks for it
+    for (Rig* r : rigs) remapDefer_ = remapDefer_ || r->shape().remapDefer;
     probe_ = 0;
     for (Rig* r : rigs) probe_ = std::max(probe_, r->waitProbe());
     auto addStep = [&](int kind, const std::vector<std::pair<int, std::pair<const void*, int>>>& parts, int step) {
@@ -1360,6 +1366,14 @@ void Plan::bind(const std::vector<Rig*>& rigs)
     for (int r = 0; r < nr; r++)
         if (!rigs[r]->linear()) parts.push_back({r, {rigs[r]->remapItems(), rigs[r]->numRemapItems()}});
     addStep(0, parts, 0);
+    int remapTotal = 0;
+    if (remapDefer_ && !steps_.empty() && steps_.back().kind == 0) {  // its exact recompute, same segments
+        Step f = steps_.back();
+        f.kind = 7;
+        f.bytes = 0;
+        remapTotal = f.total;
+        steps_.push_back(f);
+    }
     for (int J = 1; J <= maxL; J++) {
         parts.clear();
         for (int r = 0; r < nr; r++)
@@ -1400,15 +1414,19 @@ void Plan::bind(const std::vector<Rig*>& rigs)
         addStep(2, parts, s);
     }
     // one work counter per step after the segments, zeroed in every run's staged copy
+    // and the remap's tie count after them
     counterOff_ = (segOff_ + segs_.size() * sizeof(Segment) + 15) / 16 * 16;
-    const size_t need = counterOff_ + std::max<size_t>(1, steps_.size()) * sizeof(int);
+    const size_t need = counterOff_ + (steps_.size() + 1) * sizeof(int);
     for (IoSlot& sl : io_)
         if (need > sl.dArgs.bytes()) {
             const size_t cap = need + need / 2;
             sl.dArgs.alloc(cap);
             sl.stage.alloc(cap);
         }
-    stageBytes_ = counterOff_ + steps_.size() * sizeof(int);
+    stageBytes_ = counterOff_ + (steps_.size() + 1) * sizeof(int);
+    for (IoSlot& sl : io_)
+        if ((size_t)remapTotal * kRemapTiesPerTile * sizeof(RemapTie) > sl.ties.bytes())
+            sl.ties.alloc((size_t)remapTotal * kRemapTiesPerTile * sizeof(RemapTie));
 }
 
 Plan::~Plan()
@@ -1444,15 +1462,19 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
         const Step& s = steps_[si];
         const Segment* p = segs + s.segOff;
         static const char* const kRangeName[] = {"ps.remap", "ps.pyrdown", "ps.blend", "ps.tail",
-                                                 "ps.linear", "ps.cvt", "ps.blend_small"};
-        NvtxRange range(kRangeName[s.kind >= 0 && s.kind <= 6 ? s.kind : 5]);
+                                                 "ps.linear", "ps.cvt", "ps.blend_small", "ps.remap_fix"};
+        NvtxRange range(kRangeName[s.kind >= 0 && s.kind <= 7 ? s.kind : 5]);
         cudaEvent_t a = nullptr, b = nullptr;
         if (prof) {
             a = prof->event();
             b = prof->event();
             PS_CUDA(cudaEventRecord(a, st));
         }
-        if (s.kind == 0) PS_CUDA(launchRemap(p, s.nsegs, s.total, perSm_[0], counters + si, st));
+        int* tieCount = counters + steps_.size();  // the remap's count of listed near-tie pixels
+        if (s.kind == 0)
+            PS_CUDA(launchRemap(p, s.nsegs, s.total, perSm_[0], counters + si, tieCount, slot.ties.as<RemapTie>(),
+                                remapDefer_, st));
+        else if (s.kind == 7) PS_CUDA(launchRemapFix(p, s.nsegs, s.total, tieCount, slot.ties.as<RemapTie>(), st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, perSm_[1], st));
         else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, probe_, st));
         else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, tailCluster_, st));
@@ -1654,7 +1676,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
             sg[k].rig = rigs_[segRig_[k]]->deviceDesc(rs[segRig_[k]]);
         }
     }
-    std::memset(stage + counterOff_, 0, steps_.size() * sizeof(int));
+    std::memset(stage + counterOff_, 0, (steps_.size() + 1) * sizeof(int));
     PS_CUDA(cudaMemcpyAsync(dArgs, stage, stageBytes_, cudaMemcpyHostToDevice, sIn_));
     PS_CUDA(cudaEventRecord(S.argsCopied, sIn_));
 

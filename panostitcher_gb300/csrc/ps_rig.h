@@ -271,7 +271,8 @@ public:
 
 private:
     struct Step {
-        int kind;  // 0 remap, 1 pyrDown, 2 blend, 3 tail, 4 linear-blend render, 6 few-tile blend
+        int kind;  // 0 remap, 1 pyrDown, 2 blend, 3 tail, 4 linear-blend render, 6 few-tile blend,
+                   // 7 the exact recompute of the remap tiles near rounding ties
         int segOff, nsegs, total;
         int level;      // level of the first rig in the step
         double bytes;   // algorithmic bytes of the step (all rigs)
@@ -281,6 +282,7 @@ private:
     struct IoSlot {
         DevBuf dArgs;   // [FrameDev x nr][LUTs][Segment x nseg]
         HostBuf stage;  // pinned staging copy of dArgs
+        DevBuf ties;    // the remap's list of tiles to recompute exactly (k_remap_fix)
         cudaGraphExec_t graph = nullptr;
         cudaEvent_t argsCopied = nullptr, computed = nullptr, downloaded = nullptr;
         bool used = false;
@@ -299,6 +301,7 @@ private:
     size_t segOff_ = 0, counterOff_ = 0, stageBytes_ = 0;
     int maxCams_ = 0;
     int tailCluster_ = 0, perSm_[3] = {0, 0, 0};  // launch widths (from the rigs' shapes)
+    bool remapDefer_ = true;                      // k_remap lists near-tie pixels for k_remap_fix
     int probe_ = 0;                                // wait probe of k_blend (Rig::setWaitProbe)
     IoSlot io_[Rig::kIoSlots];
     int nextIo_ = 0;

@@ -208,6 +208,12 @@ std::vector<LaunchShape> neighbours(const Rig& rig, const LaunchShape& cur, int 
         }
         break;
     }
+    case 7: {  // near-tie remap pixels: a second launch, or inside k_remap
+        LaunchShape s = cur;
+        s.remapDefer = 1 - cur.remapDefer;
+        out.push_back(s);
+        break;
+    }
     default: {  // CTAs per SM of k_blend (3), k_pyrdown (4), k_remap (5)
         const int k = 5 - knob;
         const int resident = residentCtasPerSm(k);
@@ -309,7 +315,7 @@ LaunchShape autotune(Rig& rig, Plan& plan, int framesPerTrial, int inflight, boo
         // coordinate descent, two passes; a move must gain 1%
         for (int pass = 0; pass < 2; pass++) {
             bool moved = false;
-            for (int knob : {0, 6, 1, 2, 3, 4, 5})
+            for (int knob : {0, 6, 1, 2, 3, 4, 5, 7})
                 for (const LaunchShape& s : neighbours(rig, best, knob)) {
                     const double t = trials.time(s);
                     report.trials++;

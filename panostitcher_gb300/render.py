@@ -291,7 +291,7 @@ class CudaPanoramaRender2:
         check(lib().ps_render_profile(self._h, int(bool(enabled))))
 
     KERNELS = {0: "k_remap", 1: "k_pyrdown", 2: "k_blend", 3: "k_tail", 4: "k_linear", 5: "k_yuv_to_bgr32",
-               6: "k_blend_small"}
+               6: "k_blend_small", 7: "k_remap_fix"}
 
     def profile_read(self, kind: int, level: int = -1):
         """(launches, total_ms, algorithmic_bytes) of finished profiled launches."""
@@ -307,13 +307,13 @@ class CudaPanoramaRender2:
         return lib().ps_render_algorithmic_bytes(self._h, bytes_in_per_px, bytes_out_per_px)
 
     SHAPE_DEFAULT = {"tail_max_items": 16, "tail_cluster": 0, "tail_half_tiles": 1, "ctas_per_sm": (0, 0, 0),
-                     "small_blend_max_items": 0}
+                     "small_blend_max_items": 0, "remap_defer_ties": 1}
 
     @staticmethod
     def _shape_dict(s: "L.LaunchShape") -> dict:
         return {"tail_max_items": s.tail_max_items, "tail_cluster": s.tail_cluster,
                 "tail_half_tiles": s.tail_half_tiles, "ctas_per_sm": tuple(s.ctas_per_sm),
-                "small_blend_max_items": s.small_blend_max_items}
+                "small_blend_max_items": s.small_blend_max_items, "remap_defer_ties": s.remap_defer_ties}
 
     def launch_shape(self) -> dict:
         """The render's launch shape (ps_launch_shape fields)."""
@@ -329,7 +329,7 @@ class CudaPanoramaRender2:
             raise ValueError(f"unknown launch-shape fields {sorted(unknown)}")
         cur.update(fields)
         s = L.LaunchShape(cur["tail_max_items"], cur["tail_cluster"], cur["tail_half_tiles"],
-                          (C.c_int * 3)(*cur["ctas_per_sm"]), cur["small_blend_max_items"])
+                          (C.c_int * 3)(*cur["ctas_per_sm"]), cur["small_blend_max_items"], cur["remap_defer_ties"])
         check(lib().ps_render_set_launch_shape(self._h, C.byref(s)))
 
     def autotune(self, frames_per_trial: int = 0, in_flight: int = 0, force: bool = False) -> dict:

@@ -132,16 +132,16 @@ def test_launch_shape_validation_before_the_gpu(built_lib):
     r = P.CudaPanoramaRender2()
     assert r.launch_shape() == P.CudaPanoramaRender2.SHAPE_DEFAULT
     for bad in ({"tail_cluster": 5}, {"tail_half_tiles": 2}, {"tail_max_items": -1}, {"ctas_per_sm": (0, -1, 0)},
-                {"ctas_per_sm": (0, 0, 65)}, {"small_blend_max_items": -3}):
+                {"ctas_per_sm": (0, 0, 65)}, {"small_blend_max_items": -3}, {"remap_defer_ties": 2}):
         with pytest.raises(P.PsError) as e:
             r.set_launch_shape(**bad)
         assert e.value.code == L.PS_EINVAL
     assert r.launch_shape() == P.CudaPanoramaRender2.SHAPE_DEFAULT  # rejected shapes leave it unchanged
     # before prepare the shape is only stored (it applies at prepare)
     r.set_launch_shape(tail_max_items=0, tail_cluster=8, tail_half_tiles=0, ctas_per_sm=(1, 2, 3),
-                       small_blend_max_items=256)
+                       small_blend_max_items=256, remap_defer_ties=0)
     assert r.launch_shape() == {"tail_max_items": 0, "tail_cluster": 8, "tail_half_tiles": 0,
-                                "ctas_per_sm": (1, 2, 3), "small_blend_max_items": 256}
+                                "ctas_per_sm": (1, 2, 3), "small_blend_max_items": 256, "remap_defer_ties": 0}
     with pytest.raises(ValueError):
         r.set_launch_shape(tile=64)
     with pytest.raises(P.PsError) as e:

@@ -10,6 +10,12 @@ and half tiles, border tiles of odd sizes, the encoder and decoder handoffs,
 the linear-blend mode, a batch of two rigs and the streaming blender -- and
 requires zero refused accesses and the oracle's bytes.  Nothing is made to
 go out of bounds on purpose.
+
+The checked build keeps one near-tie pixel per warp in the remap's own list,
+so the launch's list and k_remap_fix run on every frame; a second run sets
+that list's room to zero (PS_CHECKED_TIE_LIST_PER_TILE=0), which sends every
+frame with a listed pixel down k_remap_fix's overflow path (every pixel
+recomputed exactly).
 """
 import os
 import subprocess
@@ -129,5 +135,36 @@ def test_checked_build_refuses_nothing(cuda):
     env = dict(os.environ, PS_LIBRARY="checked")
     r = subprocess.run([sys.executable, "-c", SCRIPT.replace("ROOT", repr(ROOT))], env=env, capture_output=True,
                        text=True, timeout=900)
+    sys.stdout.write(r.stdout[-3000:])
+    assert r.returncode == 0 and "ALL OK" in r.stdout, r.stderr[-4000:]
+
+
+OVERFLOW_SCRIPT = r"""
+import sys
+import numpy as np
+sys.path.insert(0, ROOT)
+sys.path.insert(0, ROOT + "/tests")
+import torch
+import panostitcher_gb300 as P
+from panostitcher_gb300 import _lib as L
+from panostitcher_gb300 import synth as S
+from _util import Prepared
+assert L.LIB_PATH.endswith("libpanostitch_checked.so"), L.LIB_PATH
+assert L.lib().ps_debug_bounds_violations(1) == 0
+torch.cuda.set_device(0)
+for name, f in (("c2", 4), ("ricoh", 4), ("c3c", 8)):
+    p = Prepared(S.scaled_rig(S.rig(name), f))
+    for k in (1, 2):
+        fr = p.frames.frame(k)
+        assert np.array_equal(p.product_render(fr, p.luts)[..., :3], p.oracle_render(fr, p.luts)[..., :3]), name
+    assert L.lib().ps_debug_bounds_violations(1) == 0, name
+print("ALL OK", flush=True)
+"""
+
+
+def test_checked_build_tie_list_overflow(cuda):
+    env = dict(os.environ, PS_LIBRARY="checked", PS_CHECKED_TIE_LIST_PER_TILE="0")
+    r = subprocess.run([sys.executable, "-c", OVERFLOW_SCRIPT.replace("ROOT", repr(ROOT))], env=env,
+                       capture_output=True, text=True, timeout=600)
     sys.stdout.write(r.stdout[-3000:])
     assert r.returncode == 0 and "ALL OK" in r.stdout, r.stderr[-4000:]

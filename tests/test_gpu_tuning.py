@@ -31,6 +31,7 @@ SHAPES = [
     {"small_blend_max_items": 1 << 20},        # every blend level above 0 below the tail in half tiles
     {"small_blend_max_items": 64},
     {"tail_max_items": 0, "small_blend_max_items": 1 << 20},  # no tail: k_blend_small up to the top level
+    {"remap_defer_ties": 0},                   # near-tie remap pixels recomputed inside k_remap
 ]
 
 
@@ -93,6 +94,7 @@ def test_batch_of_rigs_with_different_shapes(cuda, oracle_lib):
     ps[1].r.set_launch_shape(tail_cluster=8, tail_half_tiles=0)
     ps[2].r.set_launch_shape(tail_max_items=1 << 20, ctas_per_sm=(2, 2, 2))
     ps[0].r.set_launch_shape(small_blend_max_items=1 << 20)  # one rig's levels in k_blend_small, the others not
+    ps[2].r.set_launch_shape(remap_defer_ties=0)  # the launch still defers: the other rigs ask for it
     frames = [p.frames.frame(3) for p in ps]
     refs = [p.oracle_render(f, p.luts)[..., :3] for p, f in zip(ps, frames)]
     dsts = [np.zeros((c.dst_size[1], c.dst_size[0], 4), np.uint8) for c in cfgs]
