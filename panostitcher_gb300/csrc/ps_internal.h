@@ -185,9 +185,11 @@ struct LaunchShape {
 // (remap and blend) is a zeroed int through which the launch hands out its
 // work items
 // defer: near-tie pixels go on the list (tieCount, ties) for launchRemapFix;
-// otherwise k_remap recomputes them itself
+// otherwise k_remap recomputes them itself.  srcFmt: the format of every
+// source of the launch (PS_FMT_BGR32 selects the specialised kernel), or 0
+// when they differ
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, int* tieCount,
-                        RemapTie* ties, bool defer, cudaStream_t st);
+                        RemapTie* ties, bool defer, int srcFmt, cudaStream_t st);
 // the pixels k_remap listed as lying near a rounding tie, recomputed exactly;
 // ties has room for kRemapTiesPerTile entries per remap tile of the launch,
 // and tieCount is a zeroed int

@@ -324,8 +324,10 @@ __device__ __forceinline__ void remapFixPixel(const FrameDev& F, const RigDev& R
 // Deferred, a warp appends such pixels to the launch's list (tieCount, ties:
 // room for tieCap entries, one atomic per warp) and k_remap_fix recomputes
 // them before anything reads level 0: the remap is faster, and the short
-// extra launch costs latency only when nothing else is in flight.
-template <bool kDefer>
+// extra launch costs latency only when nothing else is in flight.  kFmt
+// fixes the sources' format at compile time (PS_FMT_BGR32, the common
+// case, saves the per-texel format test) or leaves it to the frame (0).
+template <bool kDefer, int kFmt>
 __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict__ segs, int nsegs, int total,
                                                        int* __restrict__ counter, int* __restrict__ tieCount,
                                                        RemapTie* __restrict__ ties, int tieCap)
@@ -406,8 +408,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_remap(const Segment* __restrict
             n1 = remapMapValue(*cur.R, nitem, lx, ly + 8);
         }
         bool tie0 = false, tie1 = false;
-        const uint32_t v0 = remapPixel<!kDefer>(m0, base, pitch, fmt, sw, sh, lut, tie0);
-        const uint32_t v1 = remapPixel<!kDefer>(m1, base, pitch, fmt, sw, sh, lut, tie1);
+        const uint32_t v0 = remapPixel<!kDefer>(m0, base, pitch, kFmt ? kFmt : fmt, sw, sh, lut, tie0);
+        const uint32_t v1 = remapPixel<!kDefer>(m1, base, pitch, kFmt ? kFmt : fmt, sw, sh, lut, tie1);
         const int x = item.tx * kRemapTW + lx, y0 = item.ty * kRemapTH + ly, y1 = y0 + 8;
         if (kDefer) {
             const uint32_t b0 = __ballot_sync(0xffffffffu, tie0), b1 = __ballot_sync(0xffffffffu, tie1);
@@ -2073,7 +2075,10 @@ static cudaError_t launchPdl(void (*kernel)(Args...), int grid, int block, cudaS
 int residentCtasPerSm(int kind)
 {
     switch (kind) {
-    case 0: return std::min(residentPerSm<k_remap<true>>(kThreads), residentPerSm<k_remap<false>>(kThreads));
+    case 0:
+        return std::min(std::min(residentPerSm<k_remap<true, 0>>(kThreads), residentPerSm<k_remap<false, 0>>(kThreads)),
+                        std::min(residentPerSm<k_remap<true, PS_FMT_BGR32>>(kThreads),
+                                 residentPerSm<k_remap<false, PS_FMT_BGR32>>(kThreads)));
     case 1: return residentPerSm<k_pyrdown>(kThreads);
     case 2: return residentPerSm<k_blend>(kBlendThreads);
     default: return 1;
@@ -2095,15 +2100,24 @@ static int tieListCap(int total)
 #endif
 }
 
+template <bool kDefer, int kFmt>
+static cudaError_t launchRemapAs(const Segment* segs, int nsegs, int total, int perSm, int* counter, int* tieCount,
+                                 RemapTie* ties, cudaStream_t st)
+{
+    return launchPdl(k_remap<kDefer, kFmt>, gridFor(total, residentPerSm<k_remap<kDefer, kFmt>>(kThreads), perSm),
+                     kThreads, st, segs, nsegs, total, counter, tieCount, ties, kDefer ? tieListCap(total) : 0);
+}
+
 cudaError_t launchRemap(const Segment* segs, int nsegs, int total, int perSm, int* counter, int* tieCount,
-                        RemapTie* ties, bool defer, cudaStream_t st)
+                        RemapTie* ties, bool defer, int srcFmt, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
+    const bool bgr32 = srcFmt == PS_FMT_BGR32;
     if (defer)
-        return launchPdl(k_remap<true>, gridFor(total, residentPerSm<k_remap<true>>(kThreads), perSm), kThreads, st,
-                         segs, nsegs, total, counter, tieCount, ties, tieListCap(total));
-    return launchPdl(k_remap<false>, gridFor(total, residentPerSm<k_remap<false>>(kThreads), perSm), kThreads, st,
-                     segs, nsegs, total, counter, tieCount, ties, 0);
+        return bgr32 ? launchRemapAs<true, PS_FMT_BGR32>(segs, nsegs, total, perSm, counter, tieCount, ties, st)
+                     : launchRemapAs<true, 0>(segs, nsegs, total, perSm, counter, tieCount, ties, st);
+    return bgr32 ? launchRemapAs<false, PS_FMT_BGR32>(segs, nsegs, total, perSm, counter, tieCount, ties, st)
+                 : launchRemapAs<false, 0>(segs, nsegs, total, perSm, counter, tieCount, ties, st);
 }
 
 cudaError_t launchRemapFix(const Segment* segs, int nsegs, int total, const int* tieCount, const RemapTie* ties,

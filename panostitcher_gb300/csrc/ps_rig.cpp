@@ -1454,7 +1454,7 @@ bool Plan::matches(const std::vector<Rig*>& rigs) const
     return true;
 }
 
-void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
+void Plan::launchAll(const IoSlot& slot, cudaStream_t st, int srcFmt, Profiler* prof)
 {
     const Segment* segs = reinterpret_cast<const Segment*>(static_cast<const uint8_t*>(slot.dArgs.get()) + segOff_);
     int* counters = reinterpret_cast<int*>(static_cast<uint8_t*>(slot.dArgs.get()) + counterOff_);
@@ -1473,7 +1473,7 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof)
         int* tieCount = counters + steps_.size();  // the remap's count of listed near-tie pixels
         if (s.kind == 0)
             PS_CUDA(launchRemap(p, s.nsegs, s.total, perSm_[0], counters + si, tieCount, slot.ties.as<RemapTie>(),
-                                remapDefer_, st));
+                                remapDefer_, srcFmt, st));
         else if (s.kind == 7) PS_CUDA(launchRemapFix(p, s.nsegs, s.total, tieCount, slot.ties.as<RemapTie>(), st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, perSm_[1], st));
         else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, probe_, st));
@@ -1535,6 +1535,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
     uint8_t* dArgs = S.dArgs.as<uint8_t>();
     std::vector<YuvFrames> cvt;  // decoder frames converted into the slots' BGR32 staging
     double cvtBytes = 0;
+    int srcFmt = -1;  // the format all rigs' sources share, else 0
     for (size_t r = 0; r < rigs_.size(); r++) {
         Rig* rig = rigs_[r];
         const FrameInput& f = in[r];
@@ -1665,6 +1666,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
             fd.outFmt = d.format;
         }
         fd.status = rig->statusWord();
+        srcFmt = srcFmt < 0 || srcFmt == fd.srcFmt ? fd.srcFmt : 0;
         std::memcpy(stage + sizeof(FrameDev) * r, &fd, sizeof fd);
     }
     if (!segs_.empty()) {
@@ -1698,12 +1700,19 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
             prof->record(5, 0, cvtBytes / cvt.size(), a, b);
         }
     }
+    srcFmt = srcFmt == PS_FMT_BGR32 ? PS_FMT_BGR32 : 0;  // the formats the remap is specialised for
     if (useGraph) {
+        if (S.graph && S.graphFmt != srcFmt) {  // re-record for the other format, after the slot's last run
+            if (S.used) PS_CUDA(cudaEventSynchronize(S.computed));
+            PS_CUDA(cudaGraphExecDestroy(S.graph));
+            S.graph = nullptr;
+        }
         if (!S.graph) {
+            S.graphFmt = srcFmt;
             cudaGraph_t g = nullptr;
             PS_CUDA(cudaStreamBeginCapture(capStream_, cudaStreamCaptureModeThreadLocal));
             try {
-                launchAll(S, capStream_);
+                launchAll(S, capStream_, srcFmt);
             } catch (...) {
                 cudaStreamEndCapture(capStream_, &g);
                 if (g) cudaGraphDestroy(g);
@@ -1716,7 +1725,7 @@ void Plan::run(const std::vector<FrameInput>& in, cudaStream_t st, bool useGraph
         }
         PS_CUDA(cudaGraphLaunch(S.graph, comp));
     } else {
-        launchAll(S, comp, prof);
+        launchAll(S, comp, srcFmt, prof);
     }
     PS_CUDA(cudaEventRecord(S.computed, comp));
     for (size_t r = 0; r < rigs_.size(); r++) PS_CUDA(cudaEventRecord(rigs_[r]->slotComputed(rs[r]), comp));

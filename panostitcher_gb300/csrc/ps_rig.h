@@ -284,10 +284,12 @@ private:
         HostBuf stage;  // pinned staging copy of dArgs
         DevBuf ties;    // the remap's list of tiles to recompute exactly (k_remap_fix)
         cudaGraphExec_t graph = nullptr;
+        int graphFmt = 0;  // the sources' format the graph's remap was specialised for (0: any)
         cudaEvent_t argsCopied = nullptr, computed = nullptr, downloaded = nullptr;
         bool used = false;
     };
-    void launchAll(const IoSlot& slot, cudaStream_t st, Profiler* prof = nullptr);
+    // srcFmt: the format every source of the run shares (0: mixed)
+    void launchAll(const IoSlot& slot, cudaStream_t st, int srcFmt, Profiler* prof = nullptr);
     void dropGraph();
     void ensureStreams();
     void quiesce();

@@ -147,6 +147,34 @@ def test_device_io_bgr24_bgr32_agree(cuda, oracle_lib):
     assert np.array_equal(dst24.cpu().numpy(), ref[..., :3])
 
 
+def test_alternating_source_formats(cuda, oracle_lib):
+    """The remap is specialised for BGR32 sources; a state slot whose recorded launches were made for the
+    other format records them again.  Twenty renders alternate the formats over the eight slots, and a batch
+    mixes them (the remap then takes the format from each frame)."""
+    import torch
+    cfg = _cfg("c1", 8)
+    p = Prepared(cfg)
+    W, H = cfg.dst_size
+    frames = [p.frames.frame(k) for k in (3, 4)]
+    refs = [p.oracle_render(f, p.luts)[..., :3] for f in frames]
+    dst = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    for k in range(20):
+        f = frames[k % 2]
+        src = [torch.from_numpy(np.ascontiguousarray(x if k % 3 else x[..., :3])).cuda() for x in f]
+        p.r.render(src, dst, p.luts, check=True)
+        torch.cuda.synchronize()
+        assert np.array_equal(dst.cpu().numpy()[..., :3], refs[k % 2]), k
+    q = Prepared(_cfg("c3c", 8))
+    fq = q.frames.frame(1)
+    dsts = [np.zeros((c.dst_size[1], c.dst_size[0], 4), np.uint8) for c in (cfg, q.cfg)]
+    for _ in range(2):
+        P.render_batch([p.r, q.r], [[np.ascontiguousarray(x[..., :3]) for x in frames[0]], fq], dsts,
+                       [p.luts, q.luts])
+        cuda.cuda.synchronize()
+        assert np.array_equal(dsts[0][..., :3], refs[0])
+        assert np.array_equal(dsts[1][..., :3], q.oracle_render(fq, q.luts)[..., :3])
+
+
 def test_explicit_seams(cuda, oracle_lib):
     cfg = _cfg("c2", 8)
     base = Prepared(cfg)
