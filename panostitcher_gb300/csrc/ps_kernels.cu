@@ -1303,6 +1303,13 @@ __device__ __forceinline__ void computeUnit(const Stage& S, const UnitGeo& G, co
         for (int p = 0; p < 4; p++)
 #pragma unroll
             for (int c = 0; c < 3; c++) n[p][c] = (acc.r[p][c] + 128) >> 8;
+    } else if (j == 0 && __all_sync(0xffffffffu, ((acc.wsum[0] | acc.wsum[1] | acc.wsum[2] | acc.wsum[3]) & ~256) == 0)) {
+        // Level-0 weights are the 0/256 seam masks.  Where each pixel's sum is 0 or 256 (one camera at
+        // most: always, unless custom masks overlap), R = 256 L exactly, and R / W truncated is the shift.
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) n[p][c] = acc.r[p][c] >> 8;
     } else {
 #pragma unroll
         for (int p = 0; p < 4; p++) {
