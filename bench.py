@@ -603,6 +603,13 @@ def run_batched(args, dev):
                        f"{r.num_levels} levels" for n, c, r in zip(names, cfgs, renders)},
            "ticks": steps, "ticks_in_flight": nq}
 
+    # each rig's launch shape tuned for this many ticks in flight (untimed), used by both forms
+    res["launch_shapes"] = {}
+    for n, r in zip(names, renders):
+        if not args.no_tune:
+            r.autotune(in_flight=nq)
+        res["launch_shapes"][n] = r.launch_shape()
+
     def timed(tick, nticks):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
@@ -629,9 +636,12 @@ def run_batched(args, dev):
     bms = timed(batched, steps)
     timed(plain, max(nq, args.warmup))
     pms = timed(plain, steps)
-    # the plain path one tick at a time (one stream), as a per-frame caller issues it
+    # the plain path one tick at a time (one stream), as a per-frame caller issues it, with the rigs'
+    # shapes tuned for one frame at a time
     for r in renders:
         r.set_graph(True)
+        if not args.no_tune:
+            r.autotune(in_flight=1)
     timed(lambda k, st, ds: plain(k, streams[0], dsts[0]), 3)
     sms = timed(lambda k, st, ds: plain(k, streams[0], dsts[0]), steps)
     res.update({"mpix_s": round(steps * px / (bms / 1e3) / 1e6, 1),
@@ -640,7 +650,7 @@ def run_batched(args, dev):
                 "ms_per_tick": round(bms / steps, 4), "plain_ms_per_tick": round(pms / steps, 4),
                 "speedup_vs_plain": round(pms / bms, 3),
                 "speedup_vs_plain_one_stream": round(sms / bms, 3),
-                "plain": "graph-captured renders, one per rig, same ticks in flight"})
+                "plain": "graph-captured renders, one per rig, same ticks in flight and launch shapes"})
     return res
 
 
