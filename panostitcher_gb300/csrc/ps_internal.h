@@ -201,11 +201,14 @@ cudaError_t launchPyrDown(const Segment* segs, int nsegs, int total, int perSm, 
 // Accesses the checked build's kernels refused since the last reset
 // (waits for the device); -1 in the normal build, -2 on a CUDA error.
 long long boundsViolations(bool reset);
-// probePolls > 0: the failure-path test of the bounded waits (k_blend)
+// probePolls > 0: the failure-path test of the bounded waits (k_blend).
+// early: the launch before this one wrote only C levels (a blend step after
+// the first), so the G_j, weight and G_{j+1} reads of each CTA's first unit
+// may be issued before the wait for it (k_blend, k_blend_small)
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, int probePolls,
-                        cudaStream_t st);
+                        bool early, cudaStream_t st);
 // blend of few-tile levels above 0: two work items (the 64x8 halves) per tile
-cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st);
+cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, bool early, cudaStream_t st);
 // one cluster per segment: the rig's pyrDown levels tailDown..L and blend
 // levels L..tailBlend; cluster 8 or 16 CTAs (0 or more than the GPU
 // co-schedules: the widest it does)

@@ -1085,8 +1085,12 @@ __device__ __forceinline__ void stageUnitDirect(Stage& S, const RigDev& R, const
 //     row, a lane's two columns once per unit (columns fx0 + lane and, for
 //     lanes 0 and 1, fx0 + 32 + lane).
 // Threads 0..kConsumers-1; the caller synchronises before the stage is read.
+// doG: the cameras' G_j rows, weights and G_{j+1} footprints; doC: the
+// C_{j+1} footprint (the only part the previous blend launch writes, so the
+// rest may be staged before the wait for it).
 template <bool kFresh, class Stage>
-__device__ __forceinline__ void stageUnitRows(Stage& S, const RigDev& R, const uint4& raw, int chunk, int half)
+__device__ __forceinline__ void stageUnitRows(Stage& S, const RigDev& R, const uint4& raw, int chunk, int half,
+                                              bool doG = true, bool doC = true)
 {
     constexpr int NC = Stage::kCams;
     constexpr int kWarps = kConsumers / 32;
@@ -1121,7 +1125,7 @@ __device__ __forceinline__ void stageUnitRows(Stage& S, const RigDev& R, const u
         for (int r = 0; r < 2; r++) {
             gv[q][r] = make_uint2(0, 0);
             wv[q][r] = 0;
-            if (q < nc && r < rowsPerThread && y + r < Lj.h) {  // columns up to the pitch are allocated
+            if (doG && q < nc && r < rowsPerThread && y + r < Lj.h) {  // columns up to the pitch are allocated
                 const size_t o = (size_t)cam * Lj.camStride + (size_t)(y + r) * Lj.pitch + x;
                 const uint2* gp = reinterpret_cast<const uint2*>(Lj.G + o);
                 const uint32_t* wp2 = reinterpret_cast<const uint32_t*>(Lj.Wt + o);
@@ -1130,7 +1134,7 @@ __device__ __forceinline__ void stageUnitRows(Stage& S, const RigDev& R, const u
             }
         }
     }
-    const int gTasks = hasUp ? nc * nr : 0;
+    const int gTasks = hasUp && doG ? nc * nr : 0;
 #pragma unroll
     for (int i = 0; i < kGRows; i++) {
         const int t = wp + i * kWarps;  // row task: camera t / nr, footprint row rb + t % nr
@@ -1144,7 +1148,7 @@ __device__ __forceinline__ void stageUnitRows(Stage& S, const RigDev& R, const u
             if (hasB && inside(row + colB, Lu.G, gBytes(R, Lu))) fb[i] = ldLevel<kFresh>(row + colB);
         }
     }
-    const int cTasks = hasUp && last ? nr : 0;
+    const int cTasks = hasUp && last && doC ? nr : 0;
 #pragma unroll
     for (int i = 0; i < kCRows; i++) {
         const int t = wp + i * kWarps;
@@ -1159,7 +1163,7 @@ __device__ __forceinline__ void stageUnitRows(Stage& S, const RigDev& R, const u
     for (int q = 0; q < NC; q++)
 #pragma unroll
         for (int r = 0; r < 2; r++)
-            if (q < nc && r < rowsPerThread) {
+            if (doG && q < nc && r < rowsPerThread) {
                 *reinterpret_cast<uint2*>(&S.gj[q][ly + r][lx]) = gv[q][r];
                 *reinterpret_cast<uint32_t*>(&S.w[q][ly + r][lx]) = wv[q][r];
             }
@@ -1542,7 +1546,7 @@ __device__ __forceinline__ void computeUnitRows(const Stage& S, const UnitGeo& G
 // on, so the wait runs out, and the timeout is reported as any other
 // (status bit 4 of every frame in the launch).
 __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __restrict__ gsegs, int nsegs, int total,
-                                                            int* __restrict__ counter, int probePolls)
+                                                            int* __restrict__ counter, int probePolls, int early)
 {
     __shared__ BlendStage st[kBStages];
     __shared__ UnitInfo info[kBStages];
@@ -1572,7 +1576,11 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
         // The hand-out counter, items and descriptors are written before the
         // launch sequence, not by a kernel: the first unit is worked out
         // while the previous kernel finishes, and the wait comes before its
-        // first copy of level data.
+        // first copy of level data -- or, with early set (every blend step
+        // after the first, where the launch before this one wrote only C
+        // levels), before its first copy of C_{j+1}: its G_j, weights and
+        // G_{j+1} footprint, written by launches that have completed, are
+        // copied (through L2, by the tensor copies) while it finishes.
         bool waited = false;
         auto nextItem = [&] {
             int v = 0;
@@ -1623,7 +1631,11 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
             }
             fenceProxyAsync();
             if (lane == 0) info[stg] = ui;
-            if (!waited) {
+            bool tma = false;
+#ifndef PS_CHECK_BOUNDS
+            tma = ui.staged && R->tmaps;
+#endif
+            if (!waited && !(early && tma)) {
                 waitPrevGrid();
                 allowNextGrid();
                 waited = true;
@@ -1656,7 +1668,16 @@ __global__ void __launch_bounds__(kBlendThreads, 4) k_blend(const Segment* __res
                                           &full[stg]);
                             if (hasUp) tmaLoad3d(&st[stg].fpw[q][0], tmU + kTmGfp * 128, fx0 - 3, fy0, cam, &full[stg]);
                         }
-                        if (hasUp && last) tmaLoad2d(&st[stg].cf[0][0], tmU + kTmC * 128, fx0 - 1, fy0, &full[stg]);
+                    }
+                    if (!waited) {  // C_{j+1} is the previous launch's output
+                        __syncwarp();
+                        waitPrevGrid();
+                        allowNextGrid();
+                        waited = true;
+                    }
+                    if (lane == 0 && hasUp && last) {
+                        const uint8_t* tmU = static_cast<const uint8_t*>(R->tmaps) + (size_t)(j + 1) * kTmapsPerLevel * 128;
+                        tmaLoad2d(&st[stg].cf[0][0], tmU + kTmC * 128, fx0 - 1, fy0, &full[stg]);
                     }
                     nCopies = 0;
                 }
@@ -1819,21 +1840,28 @@ __global__ void __launch_bounds__(kThreads) k_tail(const Segment* __restrict__ s
 // ============================================================================
 using SmallStage = BlendStageT<kTailCamsPerUnit>;
 
-__global__ void __launch_bounds__(kThreads) k_blend_small(const Segment* __restrict__ segs, int nsegs, int total)
+__global__ void __launch_bounds__(kThreads) k_blend_small(const Segment* __restrict__ segs, int nsegs, int total,
+                                                          int early)
 {
     extern __shared__ __align__(128) uint8_t smallSmem[];  // a SmallStage (dynamic: above the 48 KB static limit)
     SmallStage& st = *reinterpret_cast<SmallStage*>(smallSmem);
-    
+
     // Items and descriptors are written before the launch sequence, not by
     // a kernel: the first item's are read while the previous kernel finishes.
+    // With early set (every blend step after the first: the launch before
+    // this one wrote only C levels), the first unit's G_j, weights and G_{j+1}
+    // footprints, written by launches that have completed, are staged then
+    // too, through L2; only its C_{j+1} footprint waits.
     int s = 0;
     uint4 raw = make_uint4(0, 0, 0, 0);
     UnitGeo geo;
     const int first = blockIdx.x;
+    const bool pre = early && first < total;
     if (first < total) {
         s = findSegment(segs, nsegs, first, s);
         raw = __ldg(static_cast<const uint4*>(segs[s].items) + ((first - segs[s].prefix) >> 1));
         fillGeo(geo, *segs[s].rig, *segs[s].frame, raw.x & 0xFF);
+        if (pre) stageUnitRows<true>(st, *segs[s].rig, raw, 0, (first - segs[s].prefix) & 1, true, false);
     }
     waitPrevGrid();
     allowNextGrid();
@@ -1849,7 +1877,8 @@ __global__ void __launch_bounds__(kThreads) k_blend_small(const Segment* __restr
         const int half = (it - sg.prefix) & 1;
         for (int chunk = 0; chunk < unitChunks<kTailCamsPerUnit>(raw); chunk++) {
             __syncthreads();  // readers of the previous unit are done
-            stageUnitRows<false>(st, R, raw, chunk, half);
+            const bool staged = pre && it == first && chunk == 0;  // G part staged before the wait
+            stageUnitRows<false>(st, R, raw, chunk, half, !staged, true);
             __syncthreads();
             computeUnitRows(st, geo, raw, chunk, acc, half);
         }
@@ -2159,14 +2188,14 @@ cudaError_t launchLinear(const Segment* segs, int nsegs, int total, int maxCams,
 }
 
 cudaError_t launchBlend(const Segment* segs, int nsegs, int total, int perSm, int* counter, int probePolls,
-                        cudaStream_t st)
+                        bool early, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
     return launchPdl(k_blend, gridFor(total, residentPerSm<k_blend>(kBlendThreads), perSm), kBlendThreads, st, segs,
-                     nsegs, total, counter, probePolls);
+                     nsegs, total, counter, probePolls, (int)early);
 }
 
-cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStream_t st)
+cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, bool early, cudaStream_t st)
 {
     if (total <= 0) return cudaSuccess;
     static const int perSm = [] {  // the attribute is set before any launch can see perSm
@@ -2183,7 +2212,7 @@ cudaError_t launchBlendSmall(const Segment* segs, int nsegs, int total, cudaStre
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_blend_small, segs, nsegs, total);
+    return cudaLaunchKernelEx(&cfg, k_blend_small, segs, nsegs, total, (int)early);
 }
 
 int tailClusterMax()

@@ -1410,8 +1410,10 @@ void Plan::bind(const std::vector<Rig*>& rigs)
             if (j > 0 && cnt <= rigs[r]->shape().smallBlendMaxItems) small.push_back({r, {rigs[r]->blendItems(j), 2 * cnt}});
             else parts.push_back({r, {rigs[r]->blendItems(j), cnt}});
         }
+        const size_t before = steps_.size();
         addStep(6, small, s);
         addStep(2, parts, s);
+        for (size_t k = before; k < steps_.size(); k++) steps_[k].early = s > 0;
     }
     // one work counter per step after the segments, zeroed in every run's staged copy
     // and the remap's tie count after them
@@ -1476,9 +1478,9 @@ void Plan::launchAll(const IoSlot& slot, cudaStream_t st, int srcFmt, Profiler* 
                                 remapDefer_, srcFmt, st));
         else if (s.kind == 7) PS_CUDA(launchRemapFix(p, s.nsegs, s.total, tieCount, slot.ties.as<RemapTie>(), st));
         else if (s.kind == 1) PS_CUDA(launchPyrDown(p, s.nsegs, s.total, perSm_[1], st));
-        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, probe_, st));
+        else if (s.kind == 2) PS_CUDA(launchBlend(p, s.nsegs, s.total, perSm_[2], counters + si, probe_, s.early, st));
         else if (s.kind == 3) PS_CUDA(launchTail(p, s.nsegs, tailCluster_, st));
-        else if (s.kind == 6) PS_CUDA(launchBlendSmall(p, s.nsegs, s.total, st));
+        else if (s.kind == 6) PS_CUDA(launchBlendSmall(p, s.nsegs, s.total, s.early, st));
         else PS_CUDA(launchLinear(p, s.nsegs, s.total, maxCams_, st));
         if (prof) {
             PS_CUDA(cudaEventRecord(b, st));

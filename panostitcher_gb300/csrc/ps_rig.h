@@ -276,6 +276,7 @@ private:
         int segOff, nsegs, total;
         int level;      // level of the first rig in the step
         double bytes;   // algorithmic bytes of the step (all rigs)
+        bool early = false;  // a blend step after the first: only C levels were written by the launch before
     };
     // Per-run state in kIoSlots copies: run k uses slot k % kIoSlots, so while
     // run k computes, run k + 1 uploads and run k - 1 downloads.
