@@ -304,7 +304,7 @@ int ps_render_export_collapsed(const ps_render* r, int level, int16_t* host_out,
    the few-tile top levels, reported at its lowest blend level, 4 the
    linear-blend render, 5 the conversion of decoder frames, at level 0, 6
    the blend of few-tile levels in half tiles, 7 the exact recompute of the
-   remap tiles whose fp32 result lies near a rounding tie, at level 0) at
+   remap pixels whose fp32 result lies near a rounding tie, at level 0) at
    one level (-1 = all levels): launch count, summed device milliseconds
    and summed algorithmic bytes (each input and output element counted
    once).

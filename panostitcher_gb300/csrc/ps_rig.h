@@ -283,7 +283,7 @@ private:
     struct IoSlot {
         DevBuf dArgs;   // [FrameDev x nr][LUTs][Segment x nseg]
         HostBuf stage;  // pinned staging copy of dArgs
-        DevBuf ties;    // the remap's list of tiles to recompute exactly (k_remap_fix)
+        DevBuf ties;    // the remap's list of near-tie pixels for k_remap_fix
         cudaGraphExec_t graph = nullptr;
         int graphFmt = 0;  // the sources' format the graph's remap was specialised for (0: any)
         cudaEvent_t argsCopied = nullptr, computed = nullptr, downloaded = nullptr;
