@@ -1,9 +1,11 @@
 // ps_kernels.cu -- the per-frame stitch kernels (sm_103a).
 //
-// One frame of one or more rigs runs as 2L+2 launches over prepared work
-// lists:
+// One frame of one or more rigs runs as about 2L+2 launches over prepared
+// work lists:
 //   k_remap        level 0: LUT gain + bilinear remap of every covered tile,
 //                  written as uchar4 G0 (cudaTransform + cudaReprojectTo16S);
+//   k_remap_fix    (launch shapes that defer them) the near-tie pixels the
+//                  remap listed, recomputed with the double sequence;
 //   k_pyrdown      levels 1..L: masked 5x5 decimation G_j -> G_{j+1}
 //                  (pyrDown16SC4To16SC4 with alpha scale);
 //   k_blend        levels L..0: for every canvas tile, the Laplacian of each
@@ -11,7 +13,9 @@
 //                  (G_j - pyrUp(G_{j+1})), its weighted accumulation, the
 //                  normalisation, and the collapse step pyrUp(C_{j+1}) + N_j,
 //                  all in registers; level 0 writes the 8-bit output with
-//                  the uncovered pixels zeroed.
+//                  the uncovered pixels zeroed;
+//   k_blend_small, k_tail  the same for the few-tile top levels (half tiles;
+//                  one thread-block cluster running several levels).
 // The reference runs the same arithmetic as ~35 launches per camera plus
 // ~36 per frame over full-canvas int16/int32 images
 // (source/CudaAccel/CudaMultibandBlend.cpp:785-823).
